@@ -1,0 +1,341 @@
+"""Benchmark of the GB300 Poisson hot path.
+
+Workload (one "step"): 16 independent right-hand sides on a 256^3-interval
+grid (255^3 interior unknowns, the reference LaplCube needs n+1 = 2^k), built
+as manufactured solutions with k's in [1,60] plus N(0,1e-3) noise from the
+seed, solved by the mixed-precision form (FP32 DST / tridiagonal inner
+solves, FP64-accurate residual, iterative refinement to 1e-10 relative error
+vs the FP64 GPU form).  Inputs (16 x 133 MB) are larger than L2, so no L2
+flush is needed between steps.
+
+value: solves/s with inputs resident in HBM (CUDA events around K steps on
+the launching stream, barrier + synchronize both sides, max over ranks).
+e2e:   solves/s through the host-pointer C-ABI batch entry point, with the
+step's inputs copied from pinned host memory and the results copied back
+inside the timed region.
+
+--impl reference: the reference's CPU LaplCube::solve on the host cores (the
+compiled reference where it was built on this machine, otherwise the C
+restatement of it in oracle/), same metric, on a bounded sample.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import math
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+from pathlib import Path
+
+ROOT = Path(__file__).resolve().parent
+sys.path.insert(0, str(ROOT))
+
+METRIC = "256³ Poisson solves/s at ≤1e-10 rel err, mixed vs FP64 on 1 GB300; p50/p99 latency"
+UNIT = "solves/s"
+N_INT = 255
+NRHS = 16
+KMAX = 60
+NOISE = 1e-3
+TOL = 1e-10
+# algorithmic bytes per interior point of one solve: read f, write u (FP64)
+SOLVE_BYTES_PER_POINT = 16
+# per-kernel algorithmic bytes per point: its input read + output write
+KERNEL_BYTES = {
+    "sine_x_f32_84": 12, "sine_x_f32_44": 8, "sine_x_f32_48": 12, "sine_x_f32_88": 16,
+    "sine_y_f32_44": 8, "sine_x_f64_88": 16, "sine_y_f64_88": 16,
+    "tridiag_f32": 8, "tridiag_f64": 16, "residual": 16, "combine": 16,
+}
+
+
+def peaks():
+    p = ROOT / "MEASURED_PEAKS.json"
+    if p.exists():
+        d = json.loads(p.read_text())
+        return float(d["hbm_gbs"]), "measured"
+    return 6800.0, "fallback"
+
+
+class ClockSampler:
+    """nvidia-smi clock/throttle samples every 200 ms while running."""
+
+    FIELDS = ("clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,clocks_event_reasons.hw_slowdown,"
+              "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,"
+              "clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, index: int):
+        self.index = index
+        self.proc = None
+        self.lines = []
+
+    def __enter__(self):
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", "-i", str(self.index), "--query-gpu=" + self.FIELDS, "--format=csv,noheader,nounits",
+                 "-lms", "200"], stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.t = threading.Thread(target=self._read, daemon=True)
+            self.t.start()
+        except OSError:
+            self.proc = None
+        return self
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def __exit__(self, *a):
+        if self.proc:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except subprocess.TimeoutExpired:
+                self.proc.kill()
+            self.t.join(timeout=2)
+
+    def summary(self):
+        sm, smax, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for ln in self.lines:
+            parts = [p.strip() for p in ln.split(",")]
+            if len(parts) < 8:
+                continue
+            try:
+                sm.append(float(parts[0]))
+                smax.append(float(parts[1]))
+            except ValueError:
+                continue
+            for nm, v in zip(names, parts[4:8]):
+                if v.lower() == "active":
+                    reasons.add(nm)
+        if not sm:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": [], "samples": 0}
+        return {"sm_mhz": statistics.median(sm), "sm_max_mhz": max(smax), "reasons": sorted(reasons),
+                "samples": len(sm)}
+
+
+def dist_setup():
+    import torch
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    if world > 1:
+        import torch.distributed as dist
+        backend = "nccl" if torch.cuda.is_available() else "gloo"
+        dist.init_process_group(backend=backend)
+    return world, rank, local
+
+
+def barrier(world):
+    if world > 1:
+        import torch.distributed as dist
+        dist.barrier()
+
+
+def allreduce_max(world, x: float) -> float:
+    if world <= 1:
+        return x
+    import torch
+    import torch.distributed as dist
+    t = torch.tensor([x], dtype=torch.float64, device="cuda" if torch.cuda.is_available() else "cpu")
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def cpu_reference_rate(sample_solves: int, n: int = N_INT, time_budget: float = 20.0):
+    """Times the reference CPU solve (compiled reference if present, else the
+    C restatement) on a bounded sample of the workload: up to
+    `sample_solves` single-RHS 255^3 solves, stopping early once the budget
+    is spent.  Returns (solves/s, kind, cores, sample text)."""
+    from fdm_gb300 import workloads
+    from oracle.oracle import port, reference
+    import numpy as np
+    ref = reference()
+    kind = "reference" if ref is not None else "port"
+    impl = ref if ref is not None else port()
+    f, _ = workloads.manufactured(n, n, n, seed=0, kmax=KMAX, noise=NOISE)
+    args = workloads.solver_args(n, n, n)[:6]
+    impl.lapl_cube(f, *args)  # warm-up
+    times = []
+    t_start = time.perf_counter()
+    for _ in range(sample_solves):
+        t0 = time.perf_counter()
+        impl.lapl_cube(f, *args)
+        times.append(time.perf_counter() - t0)
+        if time.perf_counter() - t_start > time_budget:
+            break
+    med = statistics.median(times)
+    cores = port().threads()
+    sample = "%d single-RHS %d^3 LaplCube<double> solves (median %.3f s each), OpenMP threads=%d" % (
+        len(times), n, med, cores)
+    return 1.0 / med, kind, cores, sample
+
+
+def run_reference_arm(args, world, rank):
+    if rank != 0:
+        return
+    rate, kind, cores, sample = cpu_reference_rate(max(args.steps, 3), time_budget=60.0)
+    line = {
+        "impl": "reference", "metric": METRIC, "value": rate, "unit": UNIT, "n_gpus": args.gpus,
+        "steps": args.steps, "warmup": args.warmup, "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+        "config": {"workload": "poisson_dirichlet_255^3_x16rhs", "grid": [N_INT] * 3, "nrhs": NRHS,
+                   "kmax": KMAX, "noise": NOISE, "tol": TOL},
+        "cpu_baseline": {"value": rate, "unit": UNIT, "cores": cores, "kind": kind, "sample": sample},
+        "e2e": {"value": rate, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(line), flush=True)
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=10)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    args = ap.parse_args()
+    args.warmup = max(args.warmup, 3)
+
+    world, rank, local = dist_setup()
+    if args.impl == "reference":
+        run_reference_arm(args, world, rank)
+        return
+
+    import numpy as np
+    import torch
+    import fdm_gb300
+    from fdm_gb300 import _native, workloads
+
+    torch.cuda.set_device(local)
+    dev = torch.device("cuda", local)
+    stream = torch.cuda.Stream(device=dev)
+    n = N_INT
+    vol = n ** 3
+    sargs = workloads.solver_args(n, n, n)
+
+    # inputs: each rank gets its own seeds (replicas, no collective)
+    with torch.cuda.stream(stream):
+        f = torch.empty((NRHS, n, n, n), dtype=torch.float64, device=dev)
+        for i in range(NRHS):
+            f[i] = workloads.manufactured_torch(n, n, n, seed=1000 * rank + i, kmax=KMAX, noise=NOISE,
+                                                device=dev)[0]
+        out = torch.empty_like(f)
+        ref64 = torch.empty_like(f)
+    stream.synchronize()
+
+    mixed = fdm_gb300.LaplCube(*sargs, precision="mixed", tol=TOL)
+    plain = fdm_gb300.LaplCube(*sargs)
+
+    # accuracy of the measured form vs the FP64 GPU form, per RHS
+    plain.solve_device(ref64, f, nrhs=NRHS, stream=stream)
+    mixed.solve_device(out, f, nrhs=NRHS, stream=stream)
+    stream.synchronize()
+    errs = [(torch.linalg.norm(out[i] - ref64[i]) / torch.linalg.norm(ref64[i])).item() for i in range(NRHS)]
+    sweeps, est = mixed.last_info(NRHS)
+    del ref64
+    torch.cuda.empty_cache()
+
+    def step():
+        mixed.solve_device(out, f, nrhs=NRHS, stream=stream)
+
+    for _ in range(args.warmup):
+        step()
+    stream.synchronize()
+
+    sampler = ClockSampler(local)
+    with sampler:
+        # ---- value: device-resident inputs
+        barrier(world)
+        torch.cuda.synchronize()
+        l0 = _native.launch_count()
+        e0 = torch.cuda.Event(enable_timing=True)
+        e1 = torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        for _ in range(args.steps):
+            step()
+        e1.record(stream)
+        torch.cuda.synchronize()
+        barrier(world)
+        launches = _native.launch_count() - l0
+        ms = e0.elapsed_time(e1)
+        ms = allreduce_max(world, ms)
+
+        # ---- e2e: host-pointer batch entry point, pinned host buffers
+        hf = torch.empty((NRHS, n, n, n), dtype=torch.float64, pin_memory=True)
+        hout = torch.empty_like(hf, pin_memory=True)
+        hf.copy_(f)
+        mixed.solve_batch(hout, hf, NRHS)  # warm-up of the staging buffers
+        e2e_steps = max(2, min(args.steps, 5))
+        barrier(world)
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        for _ in range(e2e_steps):
+            mixed.solve_batch(hout, hf, NRHS)
+        torch.cuda.synchronize()
+        e2e_s = time.perf_counter() - t0
+        barrier(world)
+        e2e_s = allreduce_max(world, e2e_s)
+    clocks = sampler.summary()
+
+    # ---- per-kernel CUDA-event timing of the same step (after the timed
+    # region, so the events do not perturb it)
+    _native.profile_reset()
+    _native.profile_enable(True)
+    for _ in range(2):
+        step()
+    stream.synchronize()
+    _native.profile_enable(False)
+    prof = _native.profile_collect()
+    dominant = max(prof.items(), key=lambda kv: kv[1][1])
+    dname, (dcount, dms) = dominant
+    per_launch_ms = dms / dcount
+    bpp = KERNEL_BYTES.get(dname)
+    hbm, peak_kind = peaks()
+    achieved = (bpp * vol * NRHS / (per_launch_ms * 1e-3) / 1e9) if bpp else None
+    traffic = None
+    tfile = ROOT / "profiles" / "ncu_traffic.json"
+    if tfile.exists():
+        traffic = json.loads(tfile.read_text()).get(dname)
+
+    solves = args.steps * NRHS * world
+    value = solves / (ms * 1e-3)
+    e2e_value = e2e_steps * NRHS * world / e2e_s
+    step_ms = ms / args.steps
+    line = {
+        "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": step_ms, "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "f64 in/out; f32 inner solves", "data": "synthetic",
+        "config": {"workload": "poisson_dirichlet_255^3_x16rhs", "grid": [n, n, n], "nrhs_per_step": NRHS,
+                   "kmax": KMAX, "noise": NOISE, "tol": TOL, "precision": "mixed",
+                   "l2_flush": "inputs 2.1 GB per step > 135 MB L2", "parallelism": "replicas%d" % world},
+        "accuracy": {"rel_l2_vs_fp64_gpu_max": max(errs), "rel_l2_vs_fp64_gpu_median": statistics.median(errs),
+                     "sweeps": sweeps, "correction_estimate_max": max(est)},
+        "latency_ms_per_solve": step_ms / NRHS,
+        "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": NRHS * vol * 8,
+                "d2h_bytes_per_step": NRHS * vol * 8},
+        "gpu_launches": launches,
+        "roofline": {"bound": "hbm", "kernel": dname, "achieved": achieved, "peak": hbm, "unit": "GB/s",
+                     "frac": (achieved / hbm) if achieved else None, "traffic": traffic,
+                     "peak_source": peak_kind, "algorithmic_bytes_per_point": bpp,
+                     "launch_ms": per_launch_ms},
+        "solve_roofline": {"achieved_gbs": value / world * SOLVE_BYTES_PER_POINT * vol / 1e9, "peak": hbm,
+                           "frac": value / world * SOLVE_BYTES_PER_POINT * vol / 1e9 / hbm,
+                           "bytes_per_point": SOLVE_BYTES_PER_POINT},
+        "kernels_ms_per_step": {k: v[1] / 2 for k, v in sorted(prof.items(), key=lambda kv: -kv[1][1])},
+        "clocks": clocks,
+    }
+    if rank == 0 and not args.no_cpu_baseline:
+        rate, kind, cores, sample = cpu_reference_rate(5)
+        line["cpu_baseline"] = {"value": rate, "unit": UNIT, "cores": cores, "kind": kind, "sample": sample}
+    if rank == 0:
+        print(json.dumps(line), flush=True)
+    if world > 1:
+        import torch.distributed as dist
+        dist.destroy_process_group()
+
+
+if __name__ == "__main__":
+    main()

@@ -1,0 +1,125 @@
+"""ctypes binding of libfdmgpu.so (the C ABI of include/fdmgpu.h).
+
+The library is the only compute path: if it is missing or fails to load,
+importing anything that solves raises immediately.  There is no CPU fallback.
+"""
+from __future__ import annotations
+
+import ctypes
+from ctypes import POINTER, c_char_p, c_double, c_int, c_longlong, c_size_t, c_ulonglong, c_void_p
+from pathlib import Path
+
+LIB_PATH = Path(__file__).resolve().parent / "libfdmgpu.so"
+
+OK, EINVAL, ESIZE, ENOMEM, ECUDA, ETIMEOUT, ENOTSUP, EBUDGET = range(8)
+F64, F32 = 0, 1
+PLAIN, MIXED = 0, 1
+RECT_TRIDIAG, RECT_FFT2 = 0, 1
+MAX_N = 1023
+
+_STATUS_NAMES = {
+    OK: "OK", EINVAL: "EINVAL", ESIZE: "ESIZE", ENOMEM: "ENOMEM", ECUDA: "ECUDA",
+    ETIMEOUT: "ETIMEOUT", ENOTSUP: "ENOTSUP", EBUDGET: "EBUDGET",
+}
+
+
+class FdmError(RuntimeError):
+    """A non-zero status from libfdmgpu.  `status` is the code."""
+
+    def __init__(self, status: int, message: str):
+        super().__init__("%s: %s" % (_STATUS_NAMES.get(status, status), message))
+        self.status = status
+
+
+# (name, restype, argtypes)
+_SIGS = [
+    ("fdmgpu_last_error", c_char_p, []),
+    ("fdmgpu_version", c_int, []),
+    ("fdmgpu_launch_count", c_ulonglong, []),
+    ("fdmgpu_profile_enable", c_int, [c_int]),
+    ("fdmgpu_profile_collect", c_int, [POINTER(c_int)]),
+    ("fdmgpu_profile_entry", c_int, [c_int, c_char_p, c_int, POINTER(c_longlong), POINTER(c_double)]),
+    ("fdmgpu_profile_reset", c_int, []),
+    ("fdmgpu_lapl_cube_create", c_int,
+     [POINTER(c_void_p), c_int, c_int] + [c_double] * 6 + [c_int] * 3),
+    ("fdmgpu_lapl_cube_set_precision", c_int, [c_void_p, c_int, c_double, c_int]),
+    ("fdmgpu_lapl_cube_solve", c_int, [c_void_p, c_void_p, c_void_p]),
+    ("fdmgpu_lapl_cube_solve_host_batch", c_int, [c_void_p, c_void_p, c_void_p, c_int]),
+    ("fdmgpu_lapl_cube_solve_device", c_int, [c_void_p, c_void_p, c_void_p, c_int, c_void_p]),
+    ("fdmgpu_lapl_cube_last_info", c_int, [c_void_p, POINTER(c_int), POINTER(c_double), c_int]),
+    ("fdmgpu_lapl_cube_scratch_bytes", c_int, [c_void_p, POINTER(c_size_t)]),
+    ("fdmgpu_lapl_cube_destroy", c_int, [c_void_p]),
+    ("fdmgpu_lapl_rect_create", c_int,
+     [POINTER(c_void_p), c_int, c_int] + [c_double] * 4 + [c_int] * 2),
+    ("fdmgpu_lapl_rect_solve", c_int, [c_void_p, c_void_p, c_void_p]),
+    ("fdmgpu_lapl_rect_solve_device", c_int, [c_void_p, c_void_p, c_void_p, c_int, c_void_p]),
+    ("fdmgpu_lapl_rect_destroy", c_int, [c_void_p]),
+    ("fdmgpu_sine_device", c_int, [c_int, c_int, c_int, c_double, c_void_p, c_void_p, c_void_p]),
+    ("fdmgpu_tridiag_device", c_int, [c_int, c_int, c_int, c_void_p, c_void_p, c_void_p, c_void_p, c_void_p]),
+    ("fdmgpu_nscube_create", c_int,
+     [POINTER(c_void_p), c_int, c_int, c_int] + [c_double] * 9),
+    ("fdmgpu_nscube_step", c_int, [c_void_p, c_int]),
+    ("fdmgpu_nscube_set_stream", c_int, [c_void_p, c_void_p]),
+    ("fdmgpu_nscube_field_info", c_int, [c_void_p, c_int, POINTER(c_size_t), POINTER(c_int)]),
+    ("fdmgpu_nscube_get_field", c_int, [c_void_p, c_int, c_void_p, c_size_t]),
+    ("fdmgpu_nscube_set_field", c_int, [c_void_p, c_int, c_void_p, c_size_t]),
+    ("fdmgpu_nscube_field_device", c_int, [c_void_p, c_int, POINTER(c_void_p)]),
+    ("fdmgpu_nscube_time_index", c_int, [c_void_p, POINTER(c_int)]),
+    ("fdmgpu_nscube_destroy", c_int, [c_void_p]),
+]
+
+EXPORTED = [s[0] for s in _SIGS]
+
+_lib = None
+
+
+def load(path: Path | str | None = None):
+    """Loads libfdmgpu.so once and declares every entry point.  Raises
+    OSError when the library is missing or lacks a symbol."""
+    global _lib
+    if _lib is not None and path is None:
+        return _lib
+    p = Path(path) if path else LIB_PATH
+    if not p.exists():
+        raise OSError("libfdmgpu.so not built at %s; run __graft_entry__.build()" % p)
+    lib = ctypes.CDLL(str(p))
+    for name, res, args in _SIGS:
+        fn = getattr(lib, name)  # AttributeError -> missing export
+        fn.restype = res
+        fn.argtypes = args
+    if path is None:
+        _lib = lib
+    return lib
+
+
+def check(status: int) -> None:
+    if status != OK:
+        msg = load().fdmgpu_last_error()
+        raise FdmError(status, msg.decode() if msg else "")
+
+
+def launch_count() -> int:
+    return int(load().fdmgpu_launch_count())
+
+
+def profile_enable(on: bool = True) -> None:
+    check(load().fdmgpu_profile_enable(1 if on else 0))
+
+
+def profile_reset() -> None:
+    check(load().fdmgpu_profile_reset())
+
+
+def profile_collect() -> dict:
+    """{kernel name: (launches, total ms)} of the launches timed so far."""
+    lib = load()
+    n = c_int()
+    check(lib.fdmgpu_profile_collect(ctypes.byref(n)))
+    out = {}
+    for i in range(n.value):
+        buf = ctypes.create_string_buffer(64)
+        cnt = c_longlong()
+        ms = c_double()
+        check(lib.fdmgpu_profile_entry(i, buf, 64, ctypes.byref(cnt), ctypes.byref(ms)))
+        out[buf.value.decode()] = (cnt.value, ms.value)
+    return out

@@ -1,0 +1,92 @@
+"""Build recipe for libfdmgpu.so (and the CPU checkers under oracle/).
+
+The CUDA library is compiled in-tree for sm_103a only, one nvcc process per
+translation unit in parallel, then linked with nvcc -shared.  No torch
+extension machinery is involved: the library exposes the plain C ABI of
+include/fdmgpu.h.
+"""
+from __future__ import annotations
+
+import concurrent.futures as cf
+import os
+import shutil
+import subprocess
+import sys
+from pathlib import Path
+
+PKG = Path(__file__).resolve().parent
+ROOT = PKG.parent
+CSRC = PKG / "csrc"
+BUILD = PKG / "_build"
+LIB = PKG / "libfdmgpu.so"
+ORACLE = ROOT / "oracle"
+REF_SRC = Path(os.environ.get("FDM_REF_SRC", "/root/reference/src"))
+
+ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
+NVCC_FLAGS = ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC", "-Xcompiler", "-O2"]
+
+
+def _nvcc() -> str:
+    for cand in (shutil.which("nvcc"), "/usr/local/cuda/bin/nvcc"):
+        if cand and Path(cand).exists():
+            return cand
+    raise RuntimeError("nvcc not found")
+
+
+def _sources():
+    return sorted(CSRC.glob("*.cu"))
+
+
+def _deps():
+    return sorted(list(CSRC.glob("*.cu")) + list(CSRC.glob("*.cuh")) + list(CSRC.glob("*.h"))
+                  + list((ROOT / "include").glob("*.h")))
+
+
+def _run(cmd):
+    p = subprocess.run(cmd, stdout=subprocess.PIPE, stderr=subprocess.STDOUT, text=True)
+    if p.returncode != 0:
+        raise RuntimeError("command failed: %s\n%s" % (" ".join(cmd), p.stdout))
+    return p.stdout
+
+
+def build_cuda(force: bool = False, verbose: bool = False) -> Path:
+    """Compiles every csrc/*.cu for sm_103a and links libfdmgpu.so."""
+    BUILD.mkdir(exist_ok=True)
+    newest = max(p.stat().st_mtime for p in _deps())
+    if not force and LIB.exists() and LIB.stat().st_mtime >= newest:
+        return LIB
+    nvcc = _nvcc()
+    objs = []
+    jobs = []
+    with cf.ThreadPoolExecutor(max_workers=max(1, min(8, os.cpu_count() or 1))) as ex:
+        for src in _sources():
+            obj = BUILD / (src.stem + ".o")
+            objs.append(obj)
+            cmd = [nvcc, *ARCH, *NVCC_FLAGS, "-I", str(ROOT / "include"), "-c", str(src), "-o", str(obj)]
+            jobs.append(ex.submit(_run, cmd))
+        for j in jobs:
+            out = j.result()
+            if verbose and out.strip():
+                print(out)
+    tmp = LIB.with_suffix(".so.tmp")
+    _run([nvcc, *ARCH, "-shared", "-o", str(tmp), *map(str, objs), "-lcudart"])
+    os.replace(tmp, LIB)
+    return LIB
+
+
+def build_oracle(with_reference: bool = True) -> None:
+    """Builds oracle/liboracle.so; also oracle/_ref/libfdm_ref.so from the
+    reference sources when that tree exists on this machine."""
+    _run(["make", "-s", "-C", str(ORACLE), "liboracle.so"])
+    if with_reference and REF_SRC.is_dir():
+        _run(["make", "-s", "-C", str(ORACLE), "ref", "REF_SRC=%s" % REF_SRC])
+
+
+def build_all(force: bool = False) -> None:
+    build_cuda(force=force)
+    build_oracle()
+
+
+if __name__ == "__main__":
+    build_all(force="--force" in sys.argv)
+    print(LIB)

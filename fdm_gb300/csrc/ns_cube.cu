@@ -1,0 +1,409 @@
+// NSCube lid-driven cavity projection step on the GPU, FP64, and its C ABI.
+//
+// Restates fdm::NSCube<T,check>::step (src/ns_cube.cpp:27-62): boundary
+// ghosts (init_bound, :65-122), the F,G,H predictor (FGH, :126-200), the
+// divergence RHS plus the pressure Poisson solve (poisson, :204-238) and the
+// velocity correction with p = x (update_uvwp, :241-277).  Fields keep the
+// reference tensor layouts (src/ns_cube.h:64-75): inclusive index ranges, x
+// fastest, ghost layers included.  The arithmetic of every stencil is written
+// in the reference's order of operations.
+//
+// A step is 9 launches on the handle's stream (two boundary phases, FGH,
+// RHS, the five passes of the plain FP64 Poisson solve, update).  After the
+// first eager step the sequence is captured once into a CUDA graph and
+// replayed, which removes the host launch cost that dominates at 63^3.
+#include <cmath>
+#include <memory>
+
+#include "common.cuh"
+#include "internal.h"
+#include "poisson.h"
+
+namespace fdmgpu {
+
+struct Field {
+    double* p;
+    int z1, z2, y1, y2, x1, x2;
+    long long sy, sz, size;
+    __host__ __device__ double& operator()(int i, int k, int j) const {
+        return p[(long long)(i - z1) * sz + (long long)(k - y1) * sy + (j - x1)];
+    }
+};
+
+static Field make_field(int z1, int z2, int y1, int y2, int x1, int x2) {
+    Field f;
+    f.z1 = z1; f.z2 = z2; f.y1 = y1; f.y2 = y2; f.x1 = x1; f.x2 = x2;
+    f.sy = x2 - x1 + 1;
+    f.sz = f.sy * (y2 - y1 + 1);
+    f.size = f.sz * (z2 - z1 + 1);
+    f.p = nullptr;
+    return f;
+}
+
+struct NSParams {
+    int nx, ny, nz;
+    double U0, Re, dt, dx, dy, dz, dx2, dy2, dz2;
+};
+
+__device__ __forceinline__ double sq(double x) { return x * x; }  // asp::sq, src/asp_misc.h:295
+
+// init_bound, first phase: the lid (without the two x-ghost columns that the
+// mirror below overwrites anyway), the x-mirror of u below the lid, and the
+// y-/z-mirrors of v and w.  None of these reads what another writes.
+// Thread grid covers a (z,y,x) box of (nz+3) x (ny+3) x (nx+3).
+__global__ void k_ns_bound1(Field u, Field v, Field w, NSParams P) {
+    const int nx = P.nx, ny = P.ny, nz = P.nz;
+    const long long e = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    const int W = nx + 3, H = ny + 3, D = nz + 3;
+    if (e >= (long long)W * H * D) return;
+    const int j = (int)(e % W) - 1;
+    const int k = (int)((e / W) % H) - 1;
+    const int i = (int)(e / ((long long)W * H)) - 1;
+    // lid (src/ns_cube.cpp:67-72): u[nz+1][k][j] = 2U0 - u[nz][k][j], j in [-1, nz+1]
+    if (i == nz + 1 && k >= 0 && k <= ny + 1 && j >= 0 && j <= min(nz + 1, nx)) u(nz + 1, k, j) = 2 * P.U0 - u(nz, k, j);
+    // u x-mirror for i <= nz (:76-81)
+    if (i >= 0 && i <= nz && k >= 0 && k <= ny + 1) {
+        if (j == -1) u(i, k, -1) = u(i, k, 1);
+        if (j == nx + 1) u(i, k, nx + 1) = u(i, k, nx - 1);
+    }
+    // v y-mirror (:83-88)
+    if (i >= 0 && i <= nz + 1 && j >= 0 && j <= nx + 1) {
+        if (k == -1) v(i, -1, j) = v(i, 1, j);
+        if (k == ny + 1) v(i, ny + 1, j) = v(i, ny - 1, j);
+    }
+    // w z-mirror (:90-95)
+    if (k >= 0 && k <= ny + 1 && j >= 0 && j <= nx + 1) {
+        if (i == -1) w(-1, k, j) = w(1, k, j);
+        if (i == nz + 1) w(nz + 1, k, j) = w(nz - 1, k, j);
+    }
+}
+
+// init_bound, second phase: u x-mirror of the lid row (reads the lid values
+// written by phase one) and the Neumann pressure ghosts (:98-121).
+__global__ void k_ns_bound2(Field u, Field v, Field w, Field p, NSParams P) {
+    const int nx = P.nx, ny = P.ny, nz = P.nz;
+    const long long e = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    const int W = nx + 2, H = ny + 2, D = nz + 2;
+    if (e >= (long long)W * H * D) return;
+    const int j = (int)(e % W);
+    const int k = (int)((e / W) % H);
+    const int i = (int)(e / ((long long)W * H));
+    const double Re = P.Re, dx = P.dx, dy = P.dy, dz = P.dz;
+    if (i == nz + 1 && k <= ny + 1) {
+        if (j == 0) u(nz + 1, k, -1) = u(nz + 1, k, 1);
+        if (j == nx + 1) u(nz + 1, k, nx + 1) = u(nz + 1, k, nx - 1);
+    }
+    if (i >= 1 && i <= nz && k >= 1 && k <= ny) {
+        if (j == 0) p(i, k, 0) = p(i, k, 1) - (u(i, k, 1) - 2 * u(i, k, 0) + u(i, k, -1)) / Re / dx;
+        if (j == nx + 1)
+            p(i, k, nx + 1) = p(i, k, nx) - (u(i, k, nx + 1) - 2 * u(i, k, nx) + u(i, k, nx - 1)) / Re / dx;
+    }
+    if (i >= 1 && i <= nz && j >= 1 && j <= nx) {
+        if (k == 0) p(i, 0, j) = p(i, 1, j) - (v(i, 1, j) - 2 * v(i, 0, j) + v(i, -1, j)) / Re / dy;
+        if (k == ny + 1)
+            p(i, ny + 1, j) = p(i, ny, j) - (v(i, ny + 1, j) - 2 * v(i, ny, j) + v(i, ny - 1, j)) / Re / dy;
+    }
+    if (k >= 1 && k <= ny && j >= 1 && j <= nx) {
+        if (i == 0) p(0, k, j) = p(1, k, j) - (w(1, k, j) - 2 * w(0, k, j) + w(-1, k, j)) / Re / dz;
+        if (i == nz + 1)
+            p(nz + 1, k, j) = p(nz, k, j) - (w(nz + 1, k, j) - 2 * w(nz, k, j) + w(nz - 1, k, j)) / Re / dz;
+    }
+}
+
+// FGH (src/ns_cube.cpp:126-200), one thread per (i,k,j) of the box
+// [0,nz] x [0,ny] x [0,nx]; each thread writes whichever of F, G, H has that
+// point in its range.
+__global__ void __launch_bounds__(256) k_ns_fgh(Field u, Field v, Field w, Field F, Field G, Field H, NSParams P) {
+    const int nx = P.nx, ny = P.ny, nz = P.nz;
+    const long long e = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    const int W = nx + 1, Hh = ny + 1, D = nz + 1;
+    if (e >= (long long)W * Hh * D) return;
+    const int j = (int)(e % W);
+    const int k = (int)((e / W) % Hh);
+    const int i = (int)(e / ((long long)W * Hh));
+    const double Re = P.Re, dt = P.dt, dx = P.dx, dy = P.dy, dz = P.dz;
+    const double dx2 = P.dx2, dy2 = P.dy2, dz2 = P.dz2;
+    if (i >= 1 && k >= 1) {
+        F(i, k, j) = u(i, k, j) + dt * (
+            (u(i, k, j + 1) - 2 * u(i, k, j) + u(i, k, j - 1)) / Re / dx2 +
+            (u(i, k + 1, j) - 2 * u(i, k, j) + u(i, k - 1, j)) / Re / dy2 +
+            (u(i + 1, k, j) - 2 * u(i, k, j) + u(i - 1, k, j)) / Re / dz2 -
+            (sq(0.5 * (u(i, k, j) + u(i, k, j + 1))) - sq(0.5 * (u(i, k, j - 1) + u(i, k, j)))) / dx -
+            0.25 * ((u(i, k, j) + u(i, k + 1, j)) * (v(i, k, j + 1) + v(i, k, j)) -
+                    (u(i, k - 1, j) + u(i, k, j)) * (v(i, k - 1, j + 1) + v(i, k - 1, j))) / dy -
+            0.25 * ((u(i, k, j) + u(i + 1, k, j)) * (w(i, k, j + 1) + w(i, k, j)) -
+                    (u(i - 1, k, j) + u(i, k, j)) * (w(i - 1, k, j + 1) + w(i - 1, k, j))) / dz);
+    }
+    if (i >= 1 && j >= 1) {
+        G(i, k, j) = v(i, k, j) + dt * (
+            (v(i, k, j + 1) - 2 * v(i, k, j) + v(i, k, j - 1)) / Re / dx2 +
+            (v(i, k + 1, j) - 2 * v(i, k, j) + v(i, k - 1, j)) / Re / dy2 +
+            (v(i + 1, k, j) - 2 * v(i, k, j) + v(i - 1, k, j)) / Re / dz2 -
+            (sq(0.5 * (v(i, k, j) + v(i, k + 1, j))) - sq(0.5 * (v(i, k - 1, j) + v(i, k, j)))) / dy -
+            0.25 * ((u(i, k, j) + u(i, k + 1, j)) * (v(i, k, j + 1) + v(i, k, j)) -
+                    (u(i, k, j - 1) + u(i, k + 1, j - 1)) * (v(i, k, j) + v(i, k, j - 1))) / dx -
+            0.25 * ((w(i, k, j) + w(i, k + 1, j)) * (v(i, k, j) + v(i + 1, k, j)) -
+                    (w(i - 1, k, j) + w(i - 1, k + 1, j)) * (v(i - 1, k, j) + v(i, k, j))) / dz);
+    }
+    if (k >= 1 && j >= 1) {
+        H(i, k, j) = w(i, k, j) + dt * (
+            (w(i, k, j + 1) - 2 * w(i, k, j) + w(i, k, j - 1)) / Re / dx2 +
+            (w(i, k + 1, j) - 2 * w(i, k, j) + w(i, k - 1, j)) / Re / dy2 +
+            (w(i + 1, k, j) - 2 * w(i, k, j) + w(i - 1, k, j)) / Re / dz2 -
+            (sq(0.5 * (w(i + 1, k, j) + w(i, k, j))) - sq(0.5 * (w(i - 1, k, j) + w(i, k, j)))) / dz -
+            0.25 * ((u(i + 1, k, j) + u(i, k, j)) * (w(i, k, j + 1) + w(i, k, j)) -
+                    (u(i + 1, k, j - 1) + u(i, k, j - 1)) * (w(i, k, j) + w(i, k, j - 1))) / dx -
+            0.25 * ((w(i, k, j) + w(i, k + 1, j)) * (v(i, k, j) + v(i + 1, k, j)) -
+                    (w(i, k - 1, j) + w(i, k, j)) * (v(i, k - 1, j) + v(i + 1, k - 1, j))) / dy);
+    }
+}
+
+// Divergence RHS with the Dirichlet pressure ghosts folded in
+// (src/ns_cube.cpp:206-235).
+__global__ void k_ns_rhs(Field F, Field G, Field H, Field p, Field RHS, NSParams P) {
+    const int nx = P.nx, ny = P.ny, nz = P.nz;
+    const long long e = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (e >= (long long)nx * ny * nz) return;
+    const int j = (int)(e % nx) + 1;
+    const int k = (int)((e / nx) % ny) + 1;
+    const int i = (int)(e / ((long long)nx * ny)) + 1;
+    double r = ((F(i, k, j) - F(i, k, j - 1)) / P.dx + (G(i, k, j) - G(i, k - 1, j)) / P.dy +
+                (H(i, k, j) - H(i - 1, k, j)) / P.dz) / P.dt;
+    if (i <= 1) r -= p(i - 1, k, j) / P.dz2;
+    if (k <= 1) r -= p(i, k - 1, j) / P.dy2;
+    if (j <= 1) r -= p(i, k, j - 1) / P.dx2;
+    if (j >= nx) r -= p(i, k, j + 1) / P.dx2;
+    if (k >= ny) r -= p(i, k + 1, j) / P.dy2;
+    if (i >= nz) r -= p(i + 1, k, j) / P.dz2;
+    RHS(i, k, j) = r;
+}
+
+// update_uvwp (src/ns_cube.cpp:241-277): pressure-gradient correction of the
+// interior faces, then p = x on the interior (src/tensor.h:280-283).
+__global__ void k_ns_update(Field u, Field v, Field w, Field p, Field x, Field F, Field G, Field H, NSParams P) {
+    const int nx = P.nx, ny = P.ny, nz = P.nz;
+    const long long e = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (e >= (long long)nx * ny * nz) return;
+    const int j = (int)(e % nx) + 1;
+    const int k = (int)((e / nx) % ny) + 1;
+    const int i = (int)(e / ((long long)nx * ny)) + 1;
+    const double xc = x(i, k, j);
+    if (j < nx) u(i, k, j) = F(i, k, j) - P.dt / P.dx * (x(i, k, j + 1) - xc);
+    if (k < ny) v(i, k, j) = G(i, k, j) - P.dt / P.dy * (x(i, k + 1, j) - xc);
+    if (i < nz) w(i, k, j) = H(i, k, j) - P.dt / P.dz * (x(i + 1, k, j) - xc);
+    p(i, k, j) = xc;
+}
+
+struct NSPlan {
+    NSParams P;
+    double x1, y1, z1, x2, y2, z2;
+    Field f[9];  // u v w p x F G H RHS
+    void* mem = nullptr;
+    fdmgpu_lapl_cube* lapl = nullptr;
+    cudaStream_t st = nullptr;
+    bool own_stream = false;
+    cudaGraph_t graph = nullptr;
+    cudaGraphExec_t gexec = nullptr;
+    int time_index = 0;
+    int steps_run = 0;
+
+    ~NSPlan() {
+        if (gexec) cudaGraphExecDestroy(gexec);
+        if (graph) cudaGraphDestroy(graph);
+        if (lapl) fdmgpu_lapl_cube_destroy(lapl);
+        if (mem) cudaFree(mem);
+        if (own_stream && st) cudaStreamDestroy(st);
+    }
+
+    void init() {
+        const int nx = P.nx, ny = P.ny, nz = P.nz;
+        f[0] = make_field(0, nz + 1, 0, ny + 1, -1, nx + 1);
+        f[1] = make_field(0, nz + 1, -1, ny + 1, 0, nx + 1);
+        f[2] = make_field(-1, nz + 1, 0, ny + 1, 0, nx + 1);
+        f[3] = make_field(0, nz + 1, 0, ny + 1, 0, nx + 1);
+        f[4] = make_field(1, nz, 1, ny, 1, nx);
+        f[5] = make_field(1, nz, 1, ny, 0, nx);
+        f[6] = make_field(1, nz, 0, ny, 1, nx);
+        f[7] = make_field(0, nz, 1, ny, 1, nx);
+        f[8] = make_field(1, nz, 1, ny, 1, nx);
+        size_t total = 0;
+        for (auto& fi : f) total += (size_t)((fi.size + 31) / 32 * 32);
+        FDM_CUDA(cudaMalloc(&mem, total * sizeof(double)));
+        FDM_CUDA(cudaMemset(mem, 0, total * sizeof(double)));
+        size_t off = 0;
+        for (auto& fi : f) {
+            fi.p = (double*)mem + off;
+            off += (size_t)((fi.size + 31) / 32 * 32);
+        }
+        FDM_CUDA(cudaStreamCreateWithFlags(&st, cudaStreamNonBlocking));
+        own_stream = true;
+        // LaplCube(dx, dy, dz, x2-x1+dx, y2-y1+dy, z2-z1+dz, nx, ny, nz), src/ns_cube.h:77
+        int rc = fdmgpu_lapl_cube_create(&lapl, FDMGPU_F64, FDMGPU_DIRICHLET, P.dx, P.dy, P.dz, x2 - x1 + P.dx,
+                                         y2 - y1 + P.dy, z2 - z1 + P.dz, nx, ny, nz);
+        if (rc) throw Error{rc};
+    }
+
+    void enqueue_step() {
+        const int nx = P.nx, ny = P.ny, nz = P.nz;
+        const int B = 256;
+        auto blocks = [&](long long n) { return (unsigned)((n + B - 1) / B); };
+        const long long vol = (long long)nx * ny * nz;
+        {
+            FDM_TIMED("ns_bound1", st);
+            k_ns_bound1<<<blocks((long long)(nx + 3) * (ny + 3) * (nz + 3)), B, 0, st>>>(f[0], f[1], f[2], P);
+            FDM_LAUNCH_CHECK();
+        }
+        {
+            FDM_TIMED("ns_bound2", st);
+            k_ns_bound2<<<blocks((long long)(nx + 2) * (ny + 2) * (nz + 2)), B, 0, st>>>(f[0], f[1], f[2], f[3], P);
+            FDM_LAUNCH_CHECK();
+        }
+        {
+            FDM_TIMED("ns_fgh", st);
+            k_ns_fgh<<<blocks((long long)(nx + 1) * (ny + 1) * (nz + 1)), B, 0, st>>>(f[0], f[1], f[2], f[5], f[6],
+                                                                                      f[7], P);
+            FDM_LAUNCH_CHECK();
+        }
+        {
+            FDM_TIMED("ns_rhs", st);
+            k_ns_rhs<<<blocks(vol), B, 0, st>>>(f[5], f[6], f[7], f[3], f[8], P);
+            FDM_LAUNCH_CHECK();
+        }
+        cube_solve_device(lapl, f[4].p, f[8].p, 1, st);
+        {
+            FDM_TIMED("ns_update", st);
+            k_ns_update<<<blocks(vol), B, 0, st>>>(f[0], f[1], f[2], f[3], f[4], f[5], f[6], f[7], P);
+            FDM_LAUNCH_CHECK();
+        }
+    }
+
+    void step(int k) {
+        for (int s = 0; s < k; s++) {
+            if (steps_run == 0) {
+                enqueue_step();  // eager first step: sets kernel attributes
+            } else {
+                if (!gexec) {
+                    FDM_CUDA(cudaStreamBeginCapture(st, cudaStreamCaptureModeThreadLocal));
+                    try {
+                        enqueue_step();
+                    } catch (...) {
+                        cudaGraph_t g;
+                        cudaStreamEndCapture(st, &g);
+                        if (g) cudaGraphDestroy(g);
+                        throw;
+                    }
+                    FDM_CUDA(cudaStreamEndCapture(st, &graph));
+                    FDM_CUDA(cudaGraphInstantiate(&gexec, graph, 0));
+                }
+                FDM_CUDA(cudaGraphLaunch(gexec, st));
+            }
+            steps_run++;
+            time_index++;
+        }
+    }
+};
+
+}  // namespace fdmgpu
+
+using namespace fdmgpu;
+
+struct fdmgpu_nscube {
+    NSPlan plan;
+};
+
+extern "C" {
+
+int fdmgpu_nscube_create(fdmgpu_nscube** h, int dtype, int nx, int nz, double x1, double y1, double z1, double x2,
+                         double y2, double z2, double u0, double Re, double dt) {
+    FDM_API_BEGIN
+    if (!h) FDM_FAIL(FDMGPU_EINVAL, "null handle pointer");
+    *h = nullptr;
+    if (dtype != FDMGPU_F64) FDM_FAIL(FDMGPU_ENOTSUP, "NSCube is implemented for FP64");
+    if (nx < 2 || nz < 2 || nx > FDMGPU_MAX_N || nz > FDMGPU_MAX_N || ilog2_exact(nx + 1) < 0 ||
+        ilog2_exact(nz + 1) < 0)
+        FDM_FAIL(FDMGPU_ESIZE, "verify((1<<n) == N) failed: nx+1 and nz+1 must be powers of two (nx=%d nz=%d)", nx,
+                 nz);
+    if (!(x2 > x1 && y2 > y1 && z2 > z1 && Re > 0 && dt > 0)) FDM_FAIL(FDMGPU_EINVAL, "bad domain or parameters");
+    std::unique_ptr<fdmgpu_nscube> p(new fdmgpu_nscube());
+    NSPlan& s = p->plan;
+    s.x1 = x1; s.y1 = y1; s.z1 = z1; s.x2 = x2; s.y2 = y2; s.z2 = z2;
+    s.P.nx = nx; s.P.ny = nx; s.P.nz = nz;  // ny from key "nx", src/ns_cube.h:57-59
+    s.P.U0 = u0; s.P.Re = Re; s.P.dt = dt;
+    s.P.dx = (x2 - x1) / nx; s.P.dy = (y2 - y1) / s.P.ny; s.P.dz = (z2 - z1) / nz;
+    s.P.dx2 = s.P.dx * s.P.dx; s.P.dy2 = s.P.dy * s.P.dy; s.P.dz2 = s.P.dz * s.P.dz;
+    s.init();
+    *h = p.release();
+    FDM_API_END
+}
+
+int fdmgpu_nscube_step(fdmgpu_nscube* h, int k) {
+    FDM_API_BEGIN
+    if (!h) FDM_FAIL(FDMGPU_EINVAL, "null handle");
+    if (k < 0) FDM_FAIL(FDMGPU_EINVAL, "negative step count");
+    h->plan.step(k);
+    FDM_API_END
+}
+
+int fdmgpu_nscube_set_stream(fdmgpu_nscube* h, void* stream) {
+    FDM_API_BEGIN
+    if (!h) FDM_FAIL(FDMGPU_EINVAL, "null handle");
+    NSPlan& s = h->plan;
+    FDM_CUDA(cudaStreamSynchronize(s.st));
+    if (s.own_stream) FDM_CUDA(cudaStreamDestroy(s.st));
+    s.own_stream = false;
+    s.st = (cudaStream_t)stream;
+    FDM_API_END
+}
+
+int fdmgpu_nscube_field_info(fdmgpu_nscube* h, int field, size_t* count, int* r) {
+    FDM_API_BEGIN
+    if (!h || field < 0 || field > 8) FDM_FAIL(FDMGPU_EINVAL, "bad handle or field %d", field);
+    const Field& f = h->plan.f[field];
+    if (count) *count = (size_t)f.size;
+    if (r) {
+        r[0] = f.z1; r[1] = f.z2; r[2] = f.y1; r[3] = f.y2; r[4] = f.x1; r[5] = f.x2;
+    }
+    FDM_API_END
+}
+
+int fdmgpu_nscube_get_field(fdmgpu_nscube* h, int field, void* host, size_t count) {
+    FDM_API_BEGIN
+    if (!h || !host || field < 0 || field > 8) FDM_FAIL(FDMGPU_EINVAL, "bad argument");
+    const Field& f = h->plan.f[field];
+    if (count != (size_t)f.size) FDM_FAIL(FDMGPU_EINVAL, "field has %lld elements, got %zu", f.size, count);
+    FDM_CUDA(cudaStreamSynchronize(h->plan.st));
+    FDM_CUDA(cudaMemcpy(host, f.p, count * sizeof(double), cudaMemcpyDeviceToHost));
+    FDM_API_END
+}
+
+int fdmgpu_nscube_set_field(fdmgpu_nscube* h, int field, const void* host, size_t count) {
+    FDM_API_BEGIN
+    if (!h || !host || field < 0 || field > 8) FDM_FAIL(FDMGPU_EINVAL, "bad argument");
+    const Field& f = h->plan.f[field];
+    if (count != (size_t)f.size) FDM_FAIL(FDMGPU_EINVAL, "field has %lld elements, got %zu", f.size, count);
+    FDM_CUDA(cudaStreamSynchronize(h->plan.st));
+    FDM_CUDA(cudaMemcpy(f.p, host, count * sizeof(double), cudaMemcpyHostToDevice));
+    FDM_API_END
+}
+
+int fdmgpu_nscube_field_device(fdmgpu_nscube* h, int field, void** dptr) {
+    FDM_API_BEGIN
+    if (!h || !dptr || field < 0 || field > 8) FDM_FAIL(FDMGPU_EINVAL, "bad argument");
+    *dptr = h->plan.f[field].p;
+    FDM_API_END
+}
+
+int fdmgpu_nscube_time_index(fdmgpu_nscube* h, int* t) {
+    FDM_API_BEGIN
+    if (!h || !t) FDM_FAIL(FDMGPU_EINVAL, "bad argument");
+    *t = h->plan.time_index;
+    FDM_API_END
+}
+
+int fdmgpu_nscube_destroy(fdmgpu_nscube* h) {
+    FDM_API_BEGIN
+    delete h;
+    FDM_API_END
+}
+
+}  // extern "C"

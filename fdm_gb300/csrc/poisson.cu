@@ -1,0 +1,567 @@
+// LaplCube / LaplRect plans and their C ABI (declared in include/fdmgpu.h).
+//
+// Plain form (any dtype): DST-x, DST-y on the user's output buffer in place,
+// then one constant-coefficient tridiagonal solve per (x-mode, y-mode) along
+// z, then the inverse DST-y and DST-x.  The z-tridiagonal replaces the
+// reference's DST_z / divide / inverse DST_z (src/lapl_cube.cpp:13-30,
+// :70-84, :124-141); it inverts the same operator, so results agree to
+// round-off.  No scratch memory.
+//
+// Mixed form (FP64 arrays): the same pipeline in FP32 gives u0; then each
+// refinement sweep forms r = f - A u / S from the FP32/FP64 state in FP64,
+// solves for the correction in FP32 and accumulates.  S is the reference's
+// overall scale (prod_a h_a N_a / l_a, 1 for the usual l = (n+1)h).
+#include <cmath>
+#include <cstring>
+#include <memory>
+#include <vector>
+
+#include "internal.h"
+#include "poisson.h"
+#include "sine.cuh"
+#include "solve_kernels.cuh"
+
+namespace fdmgpu {
+
+// ---------------------------------------------------------------------------
+// per-axis tables
+// ---------------------------------------------------------------------------
+template <typename T>
+struct AxisTables {
+    int N = 0, M = 0;
+    DevBuf tw, post, wpre;
+
+    void build(int N_) {
+        N = N_;
+        M = N / 2;
+        using T2 = vec2_t<T>;
+        std::vector<T2> htw(M > 0 ? M : 1), hpost(M > 0 ? M : 1);
+        std::vector<T> hw(N);
+        for (int k = 0; k < M; k++) {
+            const double a = 2.0 * M_PI * k / M, b = 2.0 * M_PI * k / N;
+            htw[k].x = (T)std::cos(a);
+            htw[k].y = (T)(-std::sin(a));
+            hpost[k].x = (T)std::cos(b);
+            hpost[k].y = (T)(-std::sin(b));
+        }
+        for (int j = 0; j < N; j++) hw[j] = (T)std::sin(M_PI * j / N);
+        FDM_CUDA(cudaMemcpy(tw.get(htw.size() * sizeof(T2)), htw.data(), htw.size() * sizeof(T2),
+                            cudaMemcpyHostToDevice));
+        FDM_CUDA(cudaMemcpy(post.get(hpost.size() * sizeof(T2)), hpost.data(), hpost.size() * sizeof(T2),
+                            cudaMemcpyHostToDevice));
+        FDM_CUDA(cudaMemcpy(wpre.get(hw.size() * sizeof(T)), hw.data(), hw.size() * sizeof(T),
+                            cudaMemcpyHostToDevice));
+    }
+    SineTables<T> view() const {
+        SineTables<T> v;
+        v.tw = (const vec2_t<T>*)tw.p;
+        v.post = (const vec2_t<T>*)post.p;
+        v.wpre = (const T*)wpre.p;
+        v.N = N;
+        v.M = M;
+        return v;
+    }
+};
+
+// Dirichlet eigenvalues 4/h^2 sin^2(j pi / (2(n+1))), j = 1..n at [j-1]
+// (src/lapl_cube.cpp:145-172), uploaded in type T.
+template <typename T>
+static void upload_lambda(DevBuf& buf, int n, double h) {
+    std::vector<T> v(n);
+    for (int j = 1; j <= n; j++) {
+        const double s = std::sin(j * M_PI * 0.5 / (n + 1));
+        v[j - 1] = (T)(4. / (h * h) * (s * s));
+    }
+    FDM_CUDA(cudaMemcpy(buf.get(n * sizeof(T)), v.data(), n * sizeof(T), cudaMemcpyHostToDevice));
+}
+
+// ---------------------------------------------------------------------------
+// launchers
+// ---------------------------------------------------------------------------
+static const size_t kSineSmemBudget = 96 * 1024;
+
+template <typename T>
+static int pick_lines(int N) {
+    int L = 32;
+    while (L > 1 && sine_smem_bytes<T>(N, L) > kSineSmemBudget) L >>= 1;
+    return L;
+}
+
+template <typename Tin, typename T, typename Tout, int AXIS>
+static void launch_sine(const Tin* in, Tout* out, int nx, int ny, int nz, int nvol, const SineTables<T>& tb,
+                        double scale, cudaStream_t st) {
+    const int L = pick_lines<T>(tb.N);
+    int Lshift = 0;
+    while ((1 << Lshift) < L) Lshift++;
+    const size_t smem = sine_smem_bytes<T>(tb.N, L);
+    static bool attr_set = false;
+    if (!attr_set) {
+        FDM_CUDA(cudaFuncSetAttribute(k_sine_pass<Tin, T, Tout, AXIS>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                      (int)(kSineSmemBudget + 1024)));
+        attr_set = true;
+    }
+    unsigned gx;
+    if (AXIS == 0) gx = (unsigned)((ny * (long long)nz + L - 1) / L);
+    else gx = (unsigned)(nz * ((nx + L - 1) / L));
+    dim3 grid(gx, nvol);
+    const long long vstride = (long long)nx * ny * nz;
+    // name: axis, compute type, input and output element bytes
+    static const char* names[2][2][3][3] = {
+        {{{"", "", ""}, {"", "sine_x_f32_44", "sine_x_f32_48"}, {"", "sine_x_f32_84", "sine_x_f32_88"}},
+         {{"", "", ""}, {"", "sine_x_f64_44", "sine_x_f64_48"}, {"", "sine_x_f64_84", "sine_x_f64_88"}}},
+        {{{"", "", ""}, {"", "sine_y_f32_44", "sine_y_f32_48"}, {"", "sine_y_f32_84", "sine_y_f32_88"}},
+         {{"", "", ""}, {"", "sine_y_f64_44", "sine_y_f64_48"}, {"", "sine_y_f64_84", "sine_y_f64_88"}}}};
+    const char* name = names[AXIS][sizeof(T) == 8][sizeof(Tin) / 4][sizeof(Tout) / 4];
+    FDM_TIMED(name, st);
+    k_sine_pass<Tin, T, Tout, AXIS><<<grid, L * kGroup, smem, st>>>(in, out, nx, ny, nz, vstride, tb, (T)scale, L,
+                                                                   Lshift);
+    FDM_LAUNCH_CHECK();
+}
+
+template <typename T>
+static void launch_tridiag(T* W, int nlines, int n, int A, long long sa, long long sb, long long st_,
+                           long long vstride, int nvol, const T* lamA, const T* lamB, double h2, double gscale,
+                           cudaStream_t st) {
+    dim3 grid((nlines + 127) / 128, nvol);
+    FDM_TIMED(sizeof(T) == 8 ? "tridiag_f64" : "tridiag_f32", st);
+    k_tridiag_const<T><<<grid, 128, 0, st>>>(W, nlines, n, A, sa, sb, st_, vstride, lamA, lamB, (T)h2, (T)gscale);
+    FDM_LAUNCH_CHECK();
+}
+
+static void check_grid_y(int nrhs) {
+    if (nrhs < 1 || nrhs > 65535) FDM_FAIL(FDMGPU_EINVAL, "nrhs must be in [1, 65535], got %d", nrhs);
+}
+
+static bool pow2_interior(int n) { return n >= 1 && n <= FDMGPU_MAX_N && ilog2_exact(n + 1) > 0; }
+
+// ---------------------------------------------------------------------------
+// LaplCube
+// ---------------------------------------------------------------------------
+struct CubePlan {
+    int dtype, nx, ny, nz;
+    double dx, dy, dz, lx, ly, lz;
+    int precision = FDMGPU_PLAIN;
+    double tol = 1e-10;
+    int max_sweeps = 3;
+    double scx, scy, slx, sly;  // forward / inverse DST scales
+    double hx_eff, hz_eff;      // spacings whose eigenvalues the reference uses
+    double zfac, S;
+    AxisTables<double> tx64, ty64;
+    AxisTables<float> tx32, ty32;
+    DevBuf lamx64, lamy64, lamx32, lamy32;
+    DevBuf work32, uhi, ulo, corr, norms;
+    DevBuf hin, hout;
+    int last_sweeps = 0, last_nrhs = 0;
+    cudaStream_t last_stream = 0;
+
+    void init() {
+        slx = std::sqrt(2. / lx);
+        sly = std::sqrt(2. / ly);
+        const double slz = std::sqrt(2. / lz);
+        scx = dx * slx;
+        scy = dy * sly;
+        // The reference shares lm_y with x (resp. z) when the point counts
+        // match, whatever the spacing (src/lapl_cube.cpp:165, :171).
+        hx_eff = (nx == ny) ? dy : dx;
+        hz_eff = (nz == ny) ? dy : dz;
+        zfac = dz * slz * slz * (nz + 1) / 2.0;
+        S = (dx * slx * slx * (nx + 1) / 2.0) * (dy * sly * sly * (ny + 1) / 2.0) * zfac;
+        if (dtype == FDMGPU_F64) {
+            tx64.build(nx + 1);
+            ty64.build(ny + 1);
+            upload_lambda<double>(lamx64, nx, hx_eff);
+            upload_lambda<double>(lamy64, ny, dy);
+        } else {
+            tx32.build(nx + 1);
+            ty32.build(ny + 1);
+            upload_lambda<float>(lamx32, nx, hx_eff);
+            upload_lambda<float>(lamy32, ny, dy);
+        }
+    }
+
+    void ensure_mixed_tables() {
+        if (!tx32.N) {
+            tx32.build(nx + 1);
+            ty32.build(ny + 1);
+            upload_lambda<float>(lamx32, nx, hx_eff);
+            upload_lambda<float>(lamy32, ny, dy);
+        }
+    }
+
+    long long vol() const { return (long long)nx * ny * nz; }
+
+    template <typename Tin, typename T, typename Tout>
+    void forward_xy(const Tin* in, T* W, int nrhs, const AxisTables<T>& tx, const AxisTables<T>& ty,
+                    cudaStream_t st) {
+        launch_sine<Tin, T, T, 0>(in, W, nx, ny, nz, nrhs, tx.view(), scx, st);
+        launch_sine<T, T, T, 1>(W, W, nx, ny, nz, nrhs, ty.view(), scy, st);
+    }
+    template <typename T>
+    void zsolve(T* W, int nrhs, const DevBuf& lx_, const DevBuf& ly_, cudaStream_t st) {
+        launch_tridiag<T>(W, nx * ny, nz, nx, 1, nx, (long long)nx * ny, vol(), nrhs, (const T*)lx_.p,
+                          (const T*)ly_.p, hz_eff * hz_eff, zfac * hz_eff * hz_eff, st);
+    }
+
+    void solve_device(void* ans, const void* rhs, int nrhs, cudaStream_t st) {
+        check_grid_y(nrhs);
+        last_stream = st;
+        last_nrhs = nrhs;
+        if (precision == FDMGPU_PLAIN) {
+            last_sweeps = 0;
+            if (dtype == FDMGPU_F64) run_plain<double>((double*)ans, (const double*)rhs, nrhs, tx64, ty64, lamx64,
+                                                       lamy64, st);
+            else run_plain<float>((float*)ans, (const float*)rhs, nrhs, tx32, ty32, lamx32, lamy32, st);
+            return;
+        }
+        run_mixed((double*)ans, (const double*)rhs, nrhs, st);
+    }
+
+    template <typename T>
+    void run_plain(T* ans, const T* rhs, int nrhs, const AxisTables<T>& tx, const AxisTables<T>& ty,
+                   const DevBuf& lx_, const DevBuf& ly_, cudaStream_t st) {
+        forward_xy<T, T, T>(rhs, ans, nrhs, tx, ty, st);
+        zsolve<T>(ans, nrhs, lx_, ly_, st);
+        launch_sine<T, T, T, 1>(ans, ans, nx, ny, nz, nrhs, ty.view(), sly, st);
+        launch_sine<T, T, T, 0>(ans, ans, nx, ny, nz, nrhs, tx.view(), slx, st);
+    }
+
+    int sweeps_for_tol() const {
+        int s = tol >= 1e-5 ? 0 : (tol >= 1e-11 ? 1 : 2);
+        return s < max_sweeps ? s : max_sweeps;
+    }
+
+    void run_mixed(double* ans, const double* rhs, int nrhs, cudaStream_t st) {
+        ensure_mixed_tables();
+        const long long V = vol() * nrhs;
+        const int sweeps = sweeps_for_tol();
+        last_sweeps = sweeps;
+        float* W = (float*)work32.get(V * sizeof(float));
+        forward_xy<double, float, float>(rhs, W, nrhs, tx32, ty32, st);
+        zsolve<float>(W, nrhs, lamx32, lamy32, st);
+        launch_sine<float, float, float, 1>(W, W, nx, ny, nz, nrhs, ty32.view(), sly, st);
+        if (sweeps == 0) {
+            launch_sine<float, float, double, 0>(W, ans, nx, ny, nz, nrhs, tx32.view(), slx, st);
+            return;
+        }
+        float* UH = (float*)uhi.get(V * sizeof(float));
+        float* C = (float*)corr.get(V * sizeof(float));
+        float* UL = sweeps > 1 ? (float*)ulo.get(V * sizeof(float)) : nullptr;
+        double* NR = (double*)norms.get((size_t)2 * nrhs * sweeps * sizeof(double));
+        FDM_CUDA(cudaMemsetAsync(NR, 0, (size_t)2 * nrhs * sweeps * sizeof(double), st));
+        launch_sine<float, float, float, 0>(W, UH, nx, ny, nz, nrhs, tx32.view(), slx, st);
+        const double cx = 1.0 / (hx_eff * hx_eff), cy = 1.0 / (dy * dy), cz = 1.0 / (hz_eff * hz_eff);
+        const long long vstride = vol();
+        for (int s = 1; s <= sweeps; s++) {
+            const float* ul_in = s >= 2 ? UL : nullptr;
+            {
+                dim3 grid((unsigned)((vol() + 255) / 256), nrhs);
+                FDM_TIMED("residual", st);
+                k_residual_f64<<<grid, 256, 0, st>>>(rhs, UH, ul_in, W, nx, ny, nz, vstride, 1.0 / S, cx, cy, cz);
+                FDM_LAUNCH_CHECK();
+            }
+            // r = f - A u / S: the inner solve multiplies by S again, so it
+            // returns the correction S A^-1 f - u
+            forward_xy<float, float, float>(W, W, nrhs, tx32, ty32, st);
+            zsolve<float>(W, nrhs, lamx32, lamy32, st);
+            launch_sine<float, float, float, 1>(W, W, nx, ny, nz, nrhs, ty32.view(), sly, st);
+            launch_sine<float, float, float, 0>(W, C, nx, ny, nz, nrhs, tx32.view(), slx, st);
+            {
+                dim3 grid((unsigned)((vol() + 255) / 256), nrhs);
+                FDM_TIMED("combine", st);
+                k_combine<<<grid, 256, 0, st>>>(UH, ul_in, C, ans, UL, vol(), vstride, s == sweeps ? 1 : 0,
+                                                NR + (size_t)2 * nrhs * (s - 1));
+                FDM_LAUNCH_CHECK();
+            }
+        }
+    }
+
+    size_t scratch_bytes() const {
+        return work32.bytes + uhi.bytes + ulo.bytes + corr.bytes + norms.bytes + hin.bytes + hout.bytes;
+    }
+};
+
+// ---------------------------------------------------------------------------
+// LaplRect / LaplRectFFT2
+// ---------------------------------------------------------------------------
+template <typename T>
+__global__ void k_divide2d(T* W, int nx, int ny, long long vstride, const T* lamx, const T* lamy) {
+    const long long idx = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (idx >= (long long)nx * ny) return;
+    const int j = idx % nx, k = idx / nx;
+    T* p = W + (long long)blockIdx.y * vstride + idx;
+    *p = *p / (-lamy[k] * T(1) - lamx[j]);
+}
+
+struct RectPlan {
+    int dtype, method, nx, ny;
+    double dx, dy, lx, ly;
+    AxisTables<double> tx64, ty64;
+    AxisTables<float> tx32, ty32;
+    DevBuf lamx64, lamy64, lamx32, lamy32;
+    DevBuf hin, hout;
+
+    void init() {
+        if (dtype == FDMGPU_F64) {
+            ty64.build(ny + 1);
+            upload_lambda<double>(lamy64, ny, dy);
+            if (method == FDMGPU_RECT_FFT2) {
+                tx64.build(nx + 1);
+                upload_lambda<double>(lamx64, nx, nx == ny ? dy : dx);  // src/lapl_rect.cpp:40
+            }
+        } else {
+            ty32.build(ny + 1);
+            upload_lambda<float>(lamy32, ny, dy);
+            if (method == FDMGPU_RECT_FFT2) {
+                tx32.build(nx + 1);
+                upload_lambda<float>(lamx32, nx, nx == ny ? dy : dx);
+            }
+        }
+    }
+
+    template <typename T>
+    void run(T* ans, const T* rhs, int nrhs, const AxisTables<T>& tx, const AxisTables<T>& ty, const DevBuf& lamx,
+             const DevBuf& lamy, cudaStream_t st) {
+        const double sly = std::sqrt(2. / ly), slx = std::sqrt(2. / lx);
+        const long long vs = (long long)nx * ny;
+        launch_sine<T, T, T, 1>(rhs, ans, nx, ny, 1, nrhs, ty.view(), dy * sly, st);
+        if (method == FDMGPU_RECT_TRIDIAG) {
+            // per y-mode k: (u[j-1] - 2u[j] + u[j+1])/dx^2 - lm_y[k] u[j] = g[j]
+            launch_tridiag<T>(ans, ny, nx, 1, 0, nx, 1, vs, nrhs, nullptr, (const T*)lamy.p, dx * dx, dx * dx, st);
+        } else {
+            launch_sine<T, T, T, 0>(ans, ans, nx, ny, 1, nrhs, tx.view(), dx * slx, st);
+            dim3 grid((unsigned)((vs + 255) / 256), nrhs);
+            FDM_TIMED("divide2d", st);
+            k_divide2d<T><<<grid, 256, 0, st>>>(ans, nx, ny, vs, (const T*)lamx.p, (const T*)lamy.p);
+            FDM_LAUNCH_CHECK();
+            launch_sine<T, T, T, 0>(ans, ans, nx, ny, 1, nrhs, tx.view(), slx, st);
+        }
+        launch_sine<T, T, T, 1>(ans, ans, nx, ny, 1, nrhs, ty.view(), sly, st);
+    }
+
+    void solve_device(void* ans, const void* rhs, int nrhs, cudaStream_t st) {
+        check_grid_y(nrhs);
+        if (dtype == FDMGPU_F64) run<double>((double*)ans, (const double*)rhs, nrhs, tx64, ty64, lamx64, lamy64, st);
+        else run<float>((float*)ans, (const float*)rhs, nrhs, tx32, ty32, lamx32, lamy32, st);
+    }
+};
+
+}  // namespace fdmgpu
+
+using namespace fdmgpu;
+
+struct fdmgpu_lapl_cube {
+    CubePlan plan;
+};
+struct fdmgpu_lapl_rect {
+    RectPlan plan;
+};
+
+namespace fdmgpu {
+void cube_solve_device(fdmgpu_lapl_cube* h, void* ans, const void* rhs, int nrhs, cudaStream_t st) {
+    h->plan.solve_device(ans, rhs, nrhs, st);
+}
+}  // namespace fdmgpu
+
+static size_t elem_size(int dtype) { return dtype == FDMGPU_F64 ? sizeof(double) : sizeof(float); }
+
+extern "C" {
+
+int fdmgpu_lapl_cube_create(fdmgpu_lapl_cube** h, int dtype, int bc_flags, double dx, double dy, double dz,
+                            double lx, double ly, double lz, int nx, int ny, int nz) {
+    FDM_API_BEGIN
+    if (!h) FDM_FAIL(FDMGPU_EINVAL, "null handle pointer");
+    *h = nullptr;
+    if (dtype != FDMGPU_F64 && dtype != FDMGPU_F32) FDM_FAIL(FDMGPU_EINVAL, "bad dtype %d", dtype);
+    if (bc_flags != FDMGPU_DIRICHLET) FDM_FAIL(FDMGPU_ENOTSUP, "only Dirichlet boundaries are implemented");
+    if (!pow2_interior(nx) || !pow2_interior(ny) || !pow2_interior(nz))
+        FDM_FAIL(FDMGPU_ESIZE, "verify((1<<n) == N) failed: n+1 must be a power of two and n <= %d (got %d,%d,%d)",
+                 FDMGPU_MAX_N, nx, ny, nz);
+    if (!(dx > 0 && dy > 0 && dz > 0 && lx > 0 && ly > 0 && lz > 0))
+        FDM_FAIL(FDMGPU_EINVAL, "spacings and lengths must be positive");
+    std::unique_ptr<fdmgpu_lapl_cube> p(new fdmgpu_lapl_cube());
+    CubePlan& c = p->plan;
+    c.dtype = dtype; c.nx = nx; c.ny = ny; c.nz = nz;
+    c.dx = dx; c.dy = dy; c.dz = dz; c.lx = lx; c.ly = ly; c.lz = lz;
+    c.init();
+    *h = p.release();
+    FDM_API_END
+}
+
+int fdmgpu_lapl_cube_set_precision(fdmgpu_lapl_cube* h, int precision, double tol, int max_sweeps) {
+    FDM_API_BEGIN
+    if (!h) FDM_FAIL(FDMGPU_EINVAL, "null handle");
+    if (precision != FDMGPU_PLAIN && precision != FDMGPU_MIXED) FDM_FAIL(FDMGPU_EINVAL, "bad precision %d", precision);
+    if (precision == FDMGPU_MIXED && h->plan.dtype != FDMGPU_F64)
+        FDM_FAIL(FDMGPU_ENOTSUP, "mixed precision needs FP64 arrays");
+    h->plan.precision = precision;
+    h->plan.tol = tol > 0 ? tol : 1e-10;
+    h->plan.max_sweeps = max_sweeps >= 0 ? max_sweeps : 3;
+    FDM_API_END
+}
+
+int fdmgpu_lapl_cube_solve_device(fdmgpu_lapl_cube* h, void* d_ans, const void* d_rhs, int nrhs, void* stream) {
+    FDM_API_BEGIN
+    if (!h || !d_ans || !d_rhs) FDM_FAIL(FDMGPU_EINVAL, "null argument");
+    h->plan.solve_device(d_ans, d_rhs, nrhs, (cudaStream_t)stream);
+    FDM_API_END
+}
+
+int fdmgpu_lapl_cube_solve(fdmgpu_lapl_cube* h, void* ans, const void* rhs) {
+    FDM_API_BEGIN
+    if (!h || !ans || !rhs) FDM_FAIL(FDMGPU_EINVAL, "null argument");
+    CubePlan& c = h->plan;
+    const size_t bytes = (size_t)c.vol() * elem_size(c.dtype);
+    void* din = c.hin.get(bytes);
+    void* dout = c.hout.get(bytes);
+    FDM_CUDA(cudaMemcpy(din, rhs, bytes, cudaMemcpyHostToDevice));
+    c.solve_device(dout, din, 1, 0);
+    FDM_CUDA(cudaMemcpy(ans, dout, bytes, cudaMemcpyDeviceToHost));
+    FDM_API_END
+}
+
+int fdmgpu_lapl_cube_solve_host_batch(fdmgpu_lapl_cube* h, void* ans, const void* rhs, int nrhs) {
+    FDM_API_BEGIN
+    if (!h || !ans || !rhs) FDM_FAIL(FDMGPU_EINVAL, "null argument");
+    CubePlan& c = h->plan;
+    check_grid_y(nrhs);
+    const size_t bytes = (size_t)c.vol() * elem_size(c.dtype) * nrhs;
+    void* din = c.hin.get(bytes);
+    void* dout = c.hout.get(bytes);
+    FDM_CUDA(cudaMemcpyAsync(din, rhs, bytes, cudaMemcpyHostToDevice, 0));
+    c.solve_device(dout, din, nrhs, 0);
+    FDM_CUDA(cudaMemcpyAsync(ans, dout, bytes, cudaMemcpyDeviceToHost, 0));
+    FDM_CUDA(cudaStreamSynchronize(0));
+    FDM_API_END
+}
+
+int fdmgpu_lapl_cube_last_info(fdmgpu_lapl_cube* h, int* sweeps, double* est, int nrhs) {
+    FDM_API_BEGIN
+    if (!h) FDM_FAIL(FDMGPU_EINVAL, "null handle");
+    CubePlan& c = h->plan;
+    FDM_CUDA(cudaStreamSynchronize(c.last_stream));
+    if (sweeps) *sweeps = c.last_sweeps;
+    if (est) {
+        if (nrhs > c.last_nrhs) FDM_FAIL(FDMGPU_EINVAL, "asked for %d estimates, last solve had %d", nrhs, c.last_nrhs);
+        if (c.last_sweeps == 0) {
+            for (int i = 0; i < nrhs; i++) est[i] = -1.0;
+        } else {
+            std::vector<double> v((size_t)2 * c.last_nrhs);
+            FDM_CUDA(cudaMemcpy(v.data(), (double*)c.norms.p + (size_t)2 * c.last_nrhs * (c.last_sweeps - 1),
+                                v.size() * sizeof(double), cudaMemcpyDeviceToHost));
+            for (int i = 0; i < nrhs; i++) est[i] = v[2 * i + 1] > 0 ? std::sqrt(v[2 * i] / v[2 * i + 1]) : 0.0;
+        }
+    }
+    FDM_API_END
+}
+
+int fdmgpu_lapl_cube_scratch_bytes(fdmgpu_lapl_cube* h, size_t* bytes) {
+    FDM_API_BEGIN
+    if (!h || !bytes) FDM_FAIL(FDMGPU_EINVAL, "null argument");
+    *bytes = h->plan.scratch_bytes();
+    FDM_API_END
+}
+
+int fdmgpu_lapl_cube_destroy(fdmgpu_lapl_cube* h) {
+    FDM_API_BEGIN
+    delete h;
+    FDM_API_END
+}
+
+int fdmgpu_lapl_rect_create(fdmgpu_lapl_rect** h, int dtype, int method, double dx, double dy, double lx, double ly,
+                            int nx, int ny) {
+    FDM_API_BEGIN
+    if (!h) FDM_FAIL(FDMGPU_EINVAL, "null handle pointer");
+    *h = nullptr;
+    if (dtype != FDMGPU_F64 && dtype != FDMGPU_F32) FDM_FAIL(FDMGPU_EINVAL, "bad dtype %d", dtype);
+    if (method != FDMGPU_RECT_TRIDIAG && method != FDMGPU_RECT_FFT2) FDM_FAIL(FDMGPU_EINVAL, "bad method %d", method);
+    if (!pow2_interior(ny)) FDM_FAIL(FDMGPU_ESIZE, "verify((1<<n) == N) failed: ny+1 must be a power of two (ny=%d)", ny);
+    if (method == FDMGPU_RECT_FFT2 && !pow2_interior(nx))
+        FDM_FAIL(FDMGPU_ESIZE, "verify((1<<n) == N) failed: nx+1 must be a power of two (nx=%d)", nx);
+    if (nx < 1 || nx > kTriCk * kTriMaxCk) FDM_FAIL(FDMGPU_ESIZE, "nx must be in [1, %d]", kTriCk * kTriMaxCk);
+    if (!(dx > 0 && dy > 0 && lx > 0 && ly > 0)) FDM_FAIL(FDMGPU_EINVAL, "spacings and lengths must be positive");
+    std::unique_ptr<fdmgpu_lapl_rect> p(new fdmgpu_lapl_rect());
+    RectPlan& r = p->plan;
+    r.dtype = dtype; r.method = method; r.nx = nx; r.ny = ny;
+    r.dx = dx; r.dy = dy; r.lx = lx; r.ly = ly;
+    r.init();
+    *h = p.release();
+    FDM_API_END
+}
+
+int fdmgpu_lapl_rect_solve_device(fdmgpu_lapl_rect* h, void* d_ans, const void* d_rhs, int nrhs, void* stream) {
+    FDM_API_BEGIN
+    if (!h || !d_ans || !d_rhs) FDM_FAIL(FDMGPU_EINVAL, "null argument");
+    h->plan.solve_device(d_ans, d_rhs, nrhs, (cudaStream_t)stream);
+    FDM_API_END
+}
+
+int fdmgpu_lapl_rect_solve(fdmgpu_lapl_rect* h, void* ans, const void* rhs) {
+    FDM_API_BEGIN
+    if (!h || !ans || !rhs) FDM_FAIL(FDMGPU_EINVAL, "null argument");
+    RectPlan& r = h->plan;
+    const size_t bytes = (size_t)r.nx * r.ny * elem_size(r.dtype);
+    void* din = r.hin.get(bytes);
+    void* dout = r.hout.get(bytes);
+    FDM_CUDA(cudaMemcpy(din, rhs, bytes, cudaMemcpyHostToDevice));
+    r.solve_device(dout, din, 1, 0);
+    FDM_CUDA(cudaMemcpy(ans, dout, bytes, cudaMemcpyDeviceToHost));
+    FDM_API_END
+}
+
+int fdmgpu_lapl_rect_destroy(fdmgpu_lapl_rect* h) {
+    FDM_API_BEGIN
+    delete h;
+    FDM_API_END
+}
+
+int fdmgpu_sine_device(int dtype, int N, int nlines, double scale, void* d_out, const void* d_in, void* stream) {
+    FDM_API_BEGIN
+    if (!d_out || !d_in) FDM_FAIL(FDMGPU_EINVAL, "null argument");
+    if (N < 2 || N - 1 > FDMGPU_MAX_N || ilog2_exact(N) < 0)
+        FDM_FAIL(FDMGPU_ESIZE, "verify((1<<n) == N) failed: N=%d", N);
+    if (nlines < 1) FDM_FAIL(FDMGPU_EINVAL, "nlines must be positive");
+    cudaStream_t st = (cudaStream_t)stream;
+    if (dtype == FDMGPU_F64) {
+        AxisTables<double> t;
+        t.build(N);
+        launch_sine<double, double, double, 0>((const double*)d_in, (double*)d_out, N - 1, nlines, 1, 1, t.view(),
+                                               scale, st);
+        FDM_CUDA(cudaStreamSynchronize(st));
+    } else if (dtype == FDMGPU_F32) {
+        AxisTables<float> t;
+        t.build(N);
+        launch_sine<float, float, float, 0>((const float*)d_in, (float*)d_out, N - 1, nlines, 1, 1, t.view(), scale,
+                                            st);
+        FDM_CUDA(cudaStreamSynchronize(st));
+    } else {
+        FDM_FAIL(FDMGPU_EINVAL, "bad dtype %d", dtype);
+    }
+    FDM_API_END
+}
+
+int fdmgpu_tridiag_device(int dtype, int n, int nsys, const void* d_lower, const void* d_diag, const void* d_upper,
+                          void* d_b, void* stream) {
+    FDM_API_BEGIN
+    if (!d_lower || !d_diag || !d_upper || !d_b) FDM_FAIL(FDMGPU_EINVAL, "null argument");
+    if (n < 1 || nsys < 1) FDM_FAIL(FDMGPU_EINVAL, "n and nsys must be positive");
+    cudaStream_t st = (cudaStream_t)stream;
+    DevBuf work;
+    const int blocks = (nsys + 127) / 128;
+    FDM_TIMED("tridiag_general", st);
+    if (dtype == FDMGPU_F64) {
+        double* cw = (double*)work.get((size_t)n * nsys * sizeof(double));
+        k_tridiag_general<double><<<blocks, 128, 0, st>>>(n, nsys, (const double*)d_lower, (const double*)d_diag,
+                                                          (const double*)d_upper, (double*)d_b, cw);
+    } else if (dtype == FDMGPU_F32) {
+        float* cw = (float*)work.get((size_t)n * nsys * sizeof(float));
+        k_tridiag_general<float><<<blocks, 128, 0, st>>>(n, nsys, (const float*)d_lower, (const float*)d_diag,
+                                                         (const float*)d_upper, (float*)d_b, cw);
+    } else {
+        FDM_FAIL(FDMGPU_EINVAL, "bad dtype %d", dtype);
+    }
+    FDM_LAUNCH_CHECK();
+    FDM_CUDA(cudaStreamSynchronize(st));
+    FDM_API_END
+}
+
+}  // extern "C"

@@ -1,0 +1,207 @@
+"""Host-side mirror of the reference's fast Poisson solvers.
+
+`LaplCube`, `LaplRect` and `LaplRectFFT2` keep the reference constructors and
+`solve(ans, rhs)` (src/lapl_cube.h:58-102, src/lapl_rect.h:40-68, 89-105):
+arrays hold the interior points, x fastest; `ans` is overwritten; `rhs` is
+read only.  The work runs in libfdmgpu.so on the GPU; sizes the reference
+rejects with verify() raise `FdmError` with status ESIZE here.
+
+`solve_device` takes CUDA tensors (or raw device addresses) and batches
+`nrhs` volumes stored back to back.
+"""
+from __future__ import annotations
+
+import ctypes
+from ctypes import byref, c_double, c_int, c_size_t, c_void_p
+
+import numpy as np
+
+from . import _native as N
+
+
+def _dtype_code(dtype) -> int:
+    dt = np.dtype(dtype)
+    if dt == np.float64:
+        return N.F64
+    if dt == np.float32:
+        return N.F32
+    raise N.FdmError(N.EINVAL, "dtype must be float64 or float32, got %s" % dt)
+
+
+def _host_ptr(a: np.ndarray, dtype, count: int, writable: bool) -> int:
+    if not isinstance(a, np.ndarray):
+        raise N.FdmError(N.EINVAL, "expected a numpy array")
+    if a.dtype != np.dtype(dtype) or not a.flags.c_contiguous or a.size != count:
+        raise N.FdmError(N.EINVAL, "array must be C-contiguous %s with %d elements" % (np.dtype(dtype), count))
+    if writable and not a.flags.writeable:
+        raise N.FdmError(N.EINVAL, "output array is read-only")
+    return a.ctypes.data
+
+
+def _dev_ptr(t, elem_bytes: int, count: int) -> int:
+    """Device address of a CUDA tensor (checked) or a raw integer address."""
+    if isinstance(t, int):
+        return t
+    if not getattr(t, "is_cuda", False):
+        raise N.FdmError(N.EINVAL, "expected a CUDA tensor")
+    if not t.is_contiguous() or t.numel() < count or t.element_size() != elem_bytes:
+        raise N.FdmError(N.EINVAL, "tensor must be contiguous with >= %d elements of %d bytes" % (count, elem_bytes))
+    return t.data_ptr()
+
+
+def _stream_ptr(stream) -> int | None:
+    if stream is None:
+        try:
+            import torch
+            return torch.cuda.current_stream().cuda_stream or None
+        except Exception:
+            return None
+    if isinstance(stream, int):
+        return stream or None
+    return stream.cuda_stream or None
+
+
+class LaplCube:
+    """3-D Dirichlet Poisson solver, fdm::LaplCube<T,check,F> (src/lapl_cube.h:9-106).
+
+    precision: "plain" (every stage in `dtype`) or "mixed" (float64 arrays;
+    FP32 inner solves with refinement to `tol`).
+    """
+
+    def __init__(self, dx, dy, dz, lx, ly, lz, nx, ny, nz, dtype=np.float64, precision="plain",
+                 tol=1e-10, max_sweeps=3, periodic=False):
+        self._lib = N.load()
+        self.dtype = np.dtype(dtype)
+        self.nx, self.ny, self.nz = int(nx), int(ny), int(nz)
+        self.dx, self.dy, self.dz = float(dx), float(dy), float(dz)
+        self.lx, self.ly, self.lz = float(lx), float(ly), float(lz)
+        self.count = self.nx * self.ny * self.nz
+        h = c_void_p()
+        flags = 7 if periodic else 0
+        N.check(self._lib.fdmgpu_lapl_cube_create(byref(h), _dtype_code(dtype), flags, self.dx, self.dy, self.dz,
+                                                  self.lx, self.ly, self.lz, self.nx, self.ny, self.nz))
+        self._h = h
+        self.precision = precision
+        if precision not in ("plain", "mixed"):
+            raise N.FdmError(N.EINVAL, "precision must be 'plain' or 'mixed'")
+        N.check(self._lib.fdmgpu_lapl_cube_set_precision(self._h, N.MIXED if precision == "mixed" else N.PLAIN,
+                                                         float(tol), int(max_sweeps)))
+
+    def solve(self, ans: np.ndarray, rhs: np.ndarray) -> None:
+        """ans <- solution for rhs (host arrays, synchronous)."""
+        pa = _host_ptr(ans, self.dtype, self.count, True)
+        pr = _host_ptr(np.ascontiguousarray(rhs), self.dtype, self.count, False)
+        N.check(self._lib.fdmgpu_lapl_cube_solve(self._h, pa, pr))
+
+    def solve_batch(self, ans, rhs, nrhs: int) -> None:
+        """Host solve of nrhs volumes stored back to back (synchronous).
+        ans / rhs: numpy arrays or CPU tensors (pinned memory is fastest)."""
+        cnt = self.count * nrhs
+        if hasattr(ans, "data_ptr"):
+            if ans.is_cuda or rhs.is_cuda or ans.numel() != cnt or rhs.numel() != cnt:
+                raise N.FdmError(N.EINVAL, "expected CPU tensors with %d elements" % cnt)
+            pa, pr = ans.data_ptr(), rhs.data_ptr()
+        else:
+            pa = _host_ptr(ans, self.dtype, cnt, True)
+            pr = _host_ptr(rhs, self.dtype, cnt, False)
+        N.check(self._lib.fdmgpu_lapl_cube_solve_host_batch(self._h, pa, pr, int(nrhs)))
+
+    def solve_device(self, ans, rhs, nrhs: int = 1, stream=None) -> None:
+        """Device solve of nrhs volumes stored back to back (asynchronous)."""
+        eb = self.dtype.itemsize
+        N.check(self._lib.fdmgpu_lapl_cube_solve_device(self._h, _dev_ptr(ans, eb, self.count * nrhs),
+                                                        _dev_ptr(rhs, eb, self.count * nrhs), int(nrhs),
+                                                        _stream_ptr(stream)))
+
+    def last_info(self, nrhs: int = 1):
+        """(sweeps, [relative size of the last correction per RHS])."""
+        s = c_int()
+        est = (c_double * nrhs)()
+        N.check(self._lib.fdmgpu_lapl_cube_last_info(self._h, byref(s), est, int(nrhs)))
+        return s.value, list(est)
+
+    def scratch_bytes(self) -> int:
+        b = c_size_t()
+        N.check(self._lib.fdmgpu_lapl_cube_scratch_bytes(self._h, byref(b)))
+        return b.value
+
+    def close(self) -> None:
+        if getattr(self, "_h", None):
+            self._lib.fdmgpu_lapl_cube_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+class LaplRect:
+    """2-D Dirichlet Poisson solver, fdm::LaplRect<T,check,F>: DST along y,
+    tridiagonal solve along x per y-mode (src/lapl_rect.cpp:63-110)."""
+
+    _method = N.RECT_TRIDIAG
+
+    def __init__(self, dx, dy, lx, ly, nx, ny, dtype=np.float64, periodic=False):
+        if periodic:
+            raise N.FdmError(N.ENOTSUP, "periodic LaplRect is not implemented")
+        self._lib = N.load()
+        self.dtype = np.dtype(dtype)
+        self.nx, self.ny = int(nx), int(ny)
+        self.count = self.nx * self.ny
+        h = c_void_p()
+        N.check(self._lib.fdmgpu_lapl_rect_create(byref(h), _dtype_code(dtype), self._method, float(dx), float(dy),
+                                                  float(lx), float(ly), self.nx, self.ny))
+        self._h = h
+
+    def solve(self, ans: np.ndarray, rhs: np.ndarray) -> None:
+        pa = _host_ptr(ans, self.dtype, self.count, True)
+        pr = _host_ptr(np.ascontiguousarray(rhs), self.dtype, self.count, False)
+        N.check(self._lib.fdmgpu_lapl_rect_solve(self._h, pa, pr))
+
+    def solve_device(self, ans, rhs, nrhs: int = 1, stream=None) -> None:
+        eb = self.dtype.itemsize
+        N.check(self._lib.fdmgpu_lapl_rect_solve_device(self._h, _dev_ptr(ans, eb, self.count * nrhs),
+                                                        _dev_ptr(rhs, eb, self.count * nrhs), int(nrhs),
+                                                        _stream_ptr(stream)))
+
+    def close(self) -> None:
+        if getattr(self, "_h", None):
+            self._lib.fdmgpu_lapl_rect_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+class LaplRectFFT2(LaplRect):
+    """2-D Dirichlet Poisson solver with DSTs on both axes,
+    fdm::LaplRectFFT2 (src/lapl_rect.cpp:113-207)."""
+
+    _method = N.RECT_FFT2
+
+
+def sine_transform_device(out, inp, N_points: int, nlines: int, scale: float = 1.0, dtype=np.float64,
+                          stream=None) -> None:
+    """DST-I of nlines contiguous lines of N-1 values on the device
+    (FFT<T>::sFFT, src/fft.cpp:294-365, on entries 1..N-1)."""
+    lib = N.load()
+    eb = np.dtype(dtype).itemsize
+    cnt = (N_points - 1) * nlines
+    N.check(lib.fdmgpu_sine_device(_dtype_code(dtype), int(N_points), int(nlines), float(scale),
+                                   _dev_ptr(out, eb, cnt), _dev_ptr(inp, eb, cnt), _stream_ptr(stream)))
+
+
+def tridiag_device(lower, diag, upper, b, n: int, nsys: int, dtype=np.float64, stream=None) -> None:
+    """Solves nsys tridiagonal systems in place in b (system-interleaved
+    layout, element i of system s at [i*nsys + s])."""
+    lib = N.load()
+    eb = np.dtype(dtype).itemsize
+    cnt = n * nsys
+    N.check(lib.fdmgpu_tridiag_device(_dtype_code(dtype), int(n), int(nsys), _dev_ptr(lower, eb, cnt),
+                                      _dev_ptr(diag, eb, cnt), _dev_ptr(upper, eb, cnt), _dev_ptr(b, eb, cnt),
+                                      _stream_ptr(stream)))

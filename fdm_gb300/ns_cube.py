@@ -1,0 +1,122 @@
+"""Host-side mirror of fdm::NSCube<T,check> (src/ns_cube.h:14-92).
+
+Constructed from a `Config` with the reference keys ns:{x1,y1,z1,x2,y2,z2,
+u0,Re,dt,nx,nz} and defaults (src/ns_cube.h:46-78; ny is read from key "nx"
+as in the reference).  `step()` advances one projection step on the GPU
+(src/ns_cube.cpp:27-62); the state stays on the device.  The public tensors
+u, v, w, p, x, F, G, H, RHS are returned as `Tensor3` copies in the reference
+layout (inclusive index ranges, x fastest) with reference-style indexing
+`t[i, k, j]` over those ranges.
+"""
+from __future__ import annotations
+
+import math
+from ctypes import byref, c_int, c_size_t, c_void_p
+
+import numpy as np
+
+from . import _native as N
+from .config import Config
+
+FIELDS = ("u", "v", "w", "p", "x", "F", "G", "H", "RHS")
+
+
+class Tensor3:
+    """A host copy of a reference tensor: `data` (z, y, x) plus the inclusive
+    index ranges (z1, z2, y1, y2, x1, x2) of src/tensor.h:192-219."""
+
+    def __init__(self, data: np.ndarray, ranges):
+        self.data = data
+        self.ranges = tuple(ranges)
+
+    def __getitem__(self, idx):
+        i, k, j = idx
+        z1, _, y1, _, x1, _ = self.ranges
+        return self.data[i - z1, k - y1, j - x1]
+
+    def maxabs(self) -> float:
+        return float(np.abs(self.data).max()) if self.data.size else 0.0
+
+
+class NSCube:
+    def __init__(self, cfg: Config | None = None, dtype=np.float64, **overrides):
+        cfg = cfg or Config()
+        for k, v in overrides.items():
+            cfg.set("ns", k, v)
+        self.x1 = cfg.get("ns", "x1", -math.pi)
+        self.y1 = cfg.get("ns", "y1", -math.pi)
+        self.z1 = cfg.get("ns", "z1", -math.pi)
+        self.x2 = cfg.get("ns", "x2", math.pi)
+        self.y2 = cfg.get("ns", "y2", math.pi)
+        self.z2 = cfg.get("ns", "z2", math.pi)
+        self.U0 = cfg.get("ns", "u0", 1.0)
+        self.Re = cfg.get("ns", "Re", 1.0)
+        self.dt = cfg.get("ns", "dt", 0.001)
+        self.nx = cfg.get("ns", "nx", 32)
+        self.ny = cfg.get("ns", "nx", 32)
+        self.nz = cfg.get("ns", "nz", 32)
+        self.verbose = cfg.get("ns", "verbose", 0)
+        if np.dtype(dtype) != np.float64:
+            raise N.FdmError(N.ENOTSUP, "NSCube is implemented for float64")
+        self._lib = N.load()
+        h = c_void_p()
+        N.check(self._lib.fdmgpu_nscube_create(byref(h), N.F64, int(self.nx), int(self.nz), float(self.x1),
+                                               float(self.y1), float(self.z1), float(self.x2), float(self.y2),
+                                               float(self.z2), float(self.U0), float(self.Re), float(self.dt)))
+        self._h = h
+        self.dx = (self.x2 - self.x1) / self.nx
+        self.dy = (self.y2 - self.y1) / self.ny
+        self.dz = (self.z2 - self.z1) / self.nz
+
+    def step(self, k: int = 1) -> None:
+        N.check(self._lib.fdmgpu_nscube_step(self._h, int(k)))
+
+    @property
+    def time_index(self) -> int:
+        t = c_int()
+        N.check(self._lib.fdmgpu_nscube_time_index(self._h, byref(t)))
+        return t.value
+
+    def field_info(self, name: str):
+        fid = FIELDS.index(name)
+        cnt = c_size_t()
+        r = (c_int * 6)()
+        N.check(self._lib.fdmgpu_nscube_field_info(self._h, fid, byref(cnt), r))
+        return cnt.value, tuple(r)
+
+    def get(self, name: str) -> Tensor3:
+        fid = FIELDS.index(name)
+        cnt, r = self.field_info(name)
+        shape = (r[1] - r[0] + 1, r[3] - r[2] + 1, r[5] - r[4] + 1)
+        out = np.empty(shape, np.float64)
+        N.check(self._lib.fdmgpu_nscube_get_field(self._h, fid, out.ctypes.data, cnt))
+        return Tensor3(out, r)
+
+    def set(self, name: str, data: np.ndarray) -> None:
+        fid = FIELDS.index(name)
+        cnt, _ = self.field_info(name)
+        a = np.ascontiguousarray(data, np.float64)
+        if a.size != cnt:
+            raise N.FdmError(N.EINVAL, "field %s has %d elements" % (name, cnt))
+        N.check(self._lib.fdmgpu_nscube_set_field(self._h, fid, a.ctypes.data, cnt))
+
+    def device_ptr(self, name: str) -> int:
+        p = c_void_p()
+        N.check(self._lib.fdmgpu_nscube_field_device(self._h, FIELDS.index(name), byref(p)))
+        return p.value
+
+    def __getattr__(self, name):
+        if name in FIELDS:
+            return self.get(name)
+        raise AttributeError(name)
+
+    def close(self) -> None:
+        if getattr(self, "_h", None):
+            self._lib.fdmgpu_nscube_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass

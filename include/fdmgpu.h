@@ -1,0 +1,179 @@
+/*
+ * fdmgpu — GB300 (sm_103a) fast Poisson solver and NSCube projection step.
+ *
+ * C ABI of libfdmgpu.so: plain pointers, sizes and status codes, no C++ or
+ * CUDA types.  `stream` arguments are a cudaStream_t passed as void* (NULL =
+ * the legacy default stream).  Host-pointer entry points are synchronous and
+ * keep the reference's semantics; *_device entry points take device pointers
+ * and are asynchronous on `stream`.
+ *
+ * Each entry point names the reference interface it replaces (paths are
+ * within the reference project resetius/fdm).  The reference has no C ABI:
+ * its interface is the C++ templates listed here, which the header-only shims
+ * in include/fdm_gb300/ recreate on top of this ABI.
+ *
+ * Every function returns FDMGPU_OK (0) or a status code; the message of the
+ * calling thread's last error is available from fdmgpu_last_error().  The
+ * reference aborts through verify() where these functions return an error
+ * (src/verify.h:10-36, src/fft.cpp:67); the C++ shims restore that.
+ *
+ * Thread safety: a handle is used by one thread at a time (the reference's
+ * LaplCube::solve is not re-entrant per instance either, src/lapl_cube.h:55-56).
+ * Distinct handles may be used concurrently.
+ */
+#ifndef FDMGPU_H
+#define FDMGPU_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* ---- status codes ------------------------------------------------------ */
+enum {
+    FDMGPU_OK = 0,
+    FDMGPU_EINVAL = 1,    /* bad argument (null handle/pointer, bad enum)      */
+    FDMGPU_ESIZE = 2,     /* unsupported size: n+1 not a power of two, n < 1,
+                             or n above FDMGPU_MAX_N (reference: verify abort,
+                             src/fft.cpp:67)                                    */
+    FDMGPU_ENOMEM = 3,    /* device or host allocation failed                   */
+    FDMGPU_ECUDA = 4,     /* a CUDA runtime call failed                         */
+    FDMGPU_ETIMEOUT = 5,  /* a bounded device-side wait gave up                 */
+    FDMGPU_ENOTSUP = 6,   /* combination not supported (e.g. periodic flags)    */
+    FDMGPU_EBUDGET = 7    /* request exceeds the configured memory budget      */
+};
+
+/* element type of user arrays */
+enum { FDMGPU_F64 = 0, FDMGPU_F32 = 1 };
+
+/* solve precision */
+enum {
+    FDMGPU_PLAIN = 0, /* every stage in the element type (FP64 for F64)       */
+    FDMGPU_MIXED = 1  /* F64 arrays only: FP32 DST/tridiagonal inner solves,
+                         accurate residual, iterative refinement             */
+};
+
+/* boundary flags per axis (bit 0 = x, 1 = y, 2 = z); only Dirichlet (0) is
+ * implemented; periodic flags return FDMGPU_ENOTSUP. */
+enum { FDMGPU_DIRICHLET = 0 };
+
+#define FDMGPU_MAX_N 1023 /* largest interior size per axis */
+
+const char* fdmgpu_last_error(void);
+int fdmgpu_version(void);
+
+/* ---- launch accounting and timing (no reference counterpart: the reference
+ * times its phases with std::chrono, src/ns_cube.cpp:27-62) ---------------
+ * fdmgpu_launch_count: kernels launched by this library since load.
+ * fdmgpu_profile_enable(1): bracket every later launch with CUDA events on
+ * its stream; fdmgpu_profile_collect resolves them into per-kernel totals
+ * (synchronises those events) and reports the number of kernel names;
+ * fdmgpu_profile_entry reads total i. */
+unsigned long long fdmgpu_launch_count(void);
+int fdmgpu_profile_enable(int on);
+int fdmgpu_profile_collect(int* nnames);
+int fdmgpu_profile_entry(int i, char* name, int namelen, long long* count, double* total_ms);
+int fdmgpu_profile_reset(void);
+
+/* ---- LaplCube: 3-D Dirichlet Poisson --------------------------------------
+ * Replaces fdm::LaplCube<T,check,F> (src/lapl_cube.h:9-106):
+ *   ctor LaplCube(dx,dy,dz, lx,ly,lz, nx,ny,nz)   src/lapl_cube.h:58-100
+ *   void solve(T* ans, T* rhs)                    src/lapl_cube.cpp:9-142
+ * Arrays are the interior nz*ny*nx points, x fastest (the tensor view
+ * {1,nz,1,ny,1,nx}, src/lapl_cube.h:80).  The result equals the reference's
+ * DST_z DST_y DST_x / (-lambda) inverse transforms, including its scale
+ * convention (forward h*sqrt(2/l), inverse sqrt(2/l) per axis) and its use of
+ * lm_y for x and z when the point counts match (src/lapl_cube.cpp:165,171). */
+typedef struct fdmgpu_lapl_cube fdmgpu_lapl_cube;
+
+int fdmgpu_lapl_cube_create(fdmgpu_lapl_cube** h, int dtype, int bc_flags,
+                            double dx, double dy, double dz,
+                            double lx, double ly, double lz,
+                            int nx, int ny, int nz);
+/* FDMGPU_MIXED needs dtype F64.  tol: target relative error (<= 0 selects
+ * 1e-10); max_sweeps: refinement sweeps cap (< 0 selects 3). */
+int fdmgpu_lapl_cube_set_precision(fdmgpu_lapl_cube* h, int precision, double tol, int max_sweeps);
+/* host pointers, synchronous (LaplCube::solve, src/lapl_cube.cpp:9) */
+int fdmgpu_lapl_cube_solve(fdmgpu_lapl_cube* h, void* ans, const void* rhs);
+/* host pointers, nrhs volumes back to back, synchronous: copies in, solves
+ * the batch, copies out (page-locked host memory makes the copies faster) */
+int fdmgpu_lapl_cube_solve_host_batch(fdmgpu_lapl_cube* h, void* ans, const void* rhs, int nrhs);
+/* device pointers; nrhs volumes back to back (stride nz*ny*nx elements);
+ * asynchronous on stream */
+int fdmgpu_lapl_cube_solve_device(fdmgpu_lapl_cube* h, void* d_ans, const void* d_rhs,
+                                  int nrhs, void* stream);
+/* refinement report of the last solve: sweeps done and, per RHS, the
+ * relative size of the last correction ||c||_2/||u||_2 (an upper estimate of
+ * the remaining relative error).  est may be NULL; it receives nrhs values.
+ * Synchronises the handle's last stream. */
+int fdmgpu_lapl_cube_last_info(fdmgpu_lapl_cube* h, int* sweeps, double* est, int nrhs);
+/* bytes of device scratch the handle holds */
+int fdmgpu_lapl_cube_scratch_bytes(fdmgpu_lapl_cube* h, size_t* bytes);
+int fdmgpu_lapl_cube_destroy(fdmgpu_lapl_cube* h);
+
+/* ---- LaplRect / LaplRectFFT2: 2-D Dirichlet Poisson ----------------------
+ * Replaces fdm::LaplRect<T,check,F> (src/lapl_rect.h:11-73, solve
+ * src/lapl_rect.cpp:63-110: DST-y, tridiagonal solve along x per y-mode,
+ * inverse DST-y) and fdm::LaplRectFFT2 (src/lapl_rect.h:75-105, solve
+ * src/lapl_rect.cpp:113-207: DST on both axes).  ctor (dx,dy,lx,ly,nx,ny);
+ * arrays ny*nx, x fastest.  LaplRect needs ny+1 a power of two (any nx >= 1);
+ * LaplRectFFT2 needs both. */
+enum { FDMGPU_RECT_TRIDIAG = 0, FDMGPU_RECT_FFT2 = 1 };
+typedef struct fdmgpu_lapl_rect fdmgpu_lapl_rect;
+
+int fdmgpu_lapl_rect_create(fdmgpu_lapl_rect** h, int dtype, int method,
+                            double dx, double dy, double lx, double ly, int nx, int ny);
+int fdmgpu_lapl_rect_solve(fdmgpu_lapl_rect* h, void* ans, const void* rhs);
+int fdmgpu_lapl_rect_solve_device(fdmgpu_lapl_rect* h, void* d_ans, const void* d_rhs,
+                                  int nrhs, void* stream);
+int fdmgpu_lapl_rect_destroy(fdmgpu_lapl_rect* h);
+
+/* ---- 1-D building blocks (test / integration surface) --------------------
+ * fdmgpu_sine_device: S[k] = scale * sum_j s[j] sin(pi j k / N) for nlines
+ * contiguous lines of n = N-1 values (FFT<T>::sFFT, src/fft.cpp:294-365, on
+ * the 1..N-1 part of its arrays).
+ * fdmgpu_tridiag_device: nsys independent tridiagonal systems stored
+ * system-interleaved (element i of system s at [i*nsys + s]):
+ * lower[i]*x[i-1] + diag[i]*x[i] + upper[i]*x[i+1] = b[i], solved in place
+ * in b (the solve of cyclic_reduction / solve_tdiag_linear_my,
+ * src/cyclic_reduction.h:20-107, src/asp_gauss.cpp:185-207). */
+int fdmgpu_sine_device(int dtype, int N, int nlines, double scale,
+                       void* d_out, const void* d_in, void* stream);
+int fdmgpu_tridiag_device(int dtype, int n, int nsys, const void* d_lower, const void* d_diag,
+                          const void* d_upper, void* d_b, void* stream);
+
+/* ---- NSCube: lid-driven cavity projection step ---------------------------
+ * Replaces fdm::NSCube<T,check> (src/ns_cube.h:14-92): ctor from Config keys
+ * ns:{x1,y1,z1,x2,y2,z2,u0,Re,dt,nx,nz} (ny is read from key nx, as in the
+ * reference, src/ns_cube.h:57-59), step() (src/ns_cube.cpp:27-62) and the
+ * public tensors u,v,w,p,x,F,G,H,RHS in the reference layouts (inclusive
+ * index ranges, x fastest).  State lives on the device. */
+typedef struct fdmgpu_nscube fdmgpu_nscube;
+enum {
+    FDMGPU_NS_U = 0, FDMGPU_NS_V, FDMGPU_NS_W, FDMGPU_NS_P, FDMGPU_NS_X,
+    FDMGPU_NS_F, FDMGPU_NS_G, FDMGPU_NS_H, FDMGPU_NS_RHS
+};
+
+int fdmgpu_nscube_create(fdmgpu_nscube** h, int dtype, int nx, int nz,
+                         double x1, double y1, double z1, double x2, double y2, double z2,
+                         double u0, double Re, double dt);
+/* k steps; asynchronous on the handle's stream */
+int fdmgpu_nscube_step(fdmgpu_nscube* h, int k);
+int fdmgpu_nscube_set_stream(fdmgpu_nscube* h, void* stream);
+/* element count of a field's storage (ghost layers included) and its index
+ * ranges {z1,z2,y1,y2,x1,x2} */
+int fdmgpu_nscube_field_info(fdmgpu_nscube* h, int field, size_t* count, int* ranges6);
+/* copies between a field and host memory (synchronous) */
+int fdmgpu_nscube_get_field(fdmgpu_nscube* h, int field, void* host, size_t count);
+int fdmgpu_nscube_set_field(fdmgpu_nscube* h, int field, const void* host, size_t count);
+/* device pointer of a field's storage */
+int fdmgpu_nscube_field_device(fdmgpu_nscube* h, int field, void** dptr);
+int fdmgpu_nscube_time_index(fdmgpu_nscube* h, int* t);
+int fdmgpu_nscube_destroy(fdmgpu_nscube* h);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* FDMGPU_H */

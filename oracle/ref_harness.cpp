@@ -1,0 +1,180 @@
+// Test infrastructure, not product code.
+//
+// C-ABI harness around the reference fdm library's own CPU classes, compiled
+// together with the reference sources (see oracle/Makefile) into
+// oracle/_ref/libfdm_ref.so.  Only the tests, the golden-fixture generator and
+// bench.py's CPU-baseline leg load it, and only as the checker or the timed
+// CPU baseline.
+//
+// Wrapped reference interfaces:
+//   fdm::LaplCube<T,false,F>::solve      src/lapl_cube.h:58-102, src/lapl_cube.cpp:9-142
+//   fdm::LaplRect<T,false>::solve        src/lapl_rect.h:40-68,  src/lapl_rect.cpp:63-110
+//   fdm::LaplRectFFT2<T,false>::solve    src/lapl_rect.h:89-105, src/lapl_rect.cpp:113-207
+//   fdm::FFT<T>::sFFT                    src/fft.h:45-98,        src/fft.cpp:294-365
+//   fdm::cyclic_reduction(_general)      src/cyclic_reduction.h:20-107
+//   solve_tdiag_linear_my                src/asp_gauss.cpp:185-207
+//   fdm::NSCube<T,false>                 src/ns_cube.h:14-92,    src/ns_cube.cpp:27-277
+#include <cmath>
+#include <cstdio>
+#include <cstring>
+#include <string>
+#include <vector>
+
+#include "lapl_cube.h"
+#include "lapl_rect.h"
+#include "ns_cube.h"
+#include "cyclic_reduction.h"
+#include "asp_gauss.h"
+#include "config.h"
+
+using namespace fdm;
+
+// LAPACK ?gtsv_ is referenced by LaplRect::solve (src/blas.h:14,72-75) but no
+// LAPACK exists in this build.  The matrices LaplRect builds are strictly
+// diagonally dominant (|D| = 2/dx^2 + lambda > 2/dx^2 = |L|+|U|), so partial
+// pivoting never swaps rows and elimination without pivoting gives the same
+// factorisation.  The adapter therefore calls the reference's own no-pivot
+// Thomas solver, solve_tdiag_linear_my (src/asp_gauss.cpp:185-207), whose
+// argument convention (sub, diag, super) equals LAPACK's (DL, D, DU).
+extern "C" void dgtsv_(int* n, int* nrhs, double* dl, double* d, double* du,
+                       double* b, int* ldb, int* info) {
+    *info = 0;
+    if (*nrhs != 1) { *info = -2; return; }
+    solve_tdiag_linear_my(b, dl, d, du, *n);
+}
+extern "C" void sgtsv_(int* n, int* nrhs, float* dl, float* d, float* du,
+                       float* b, int* ldb, int* info) {
+    *info = 0;
+    if (*nrhs != 1) { *info = -2; return; }
+    solve_tdiag_linearf_my(b, dl, d, du, *n);
+}
+
+namespace {
+using periodic3 = tensor_flags<tensor_flag::periodic, tensor_flag::periodic, tensor_flag::periodic>;
+
+template <typename T, typename F>
+void cube_solve(int nx, int ny, int nz, double dx, double dy, double dz,
+                double lx, double ly, double lz, T* ans, const T* rhs, int reps) {
+    LaplCube<T, false, F> lapl(dx, dy, dz, lx, ly, lz, nx, ny, nz);
+    std::vector<T> r(rhs, rhs + (size_t)nx * ny * nz);
+    for (int i = 0; i < reps; i++) lapl.solve(ans, r.data());
+}
+}  // namespace
+
+extern "C" {
+
+int ref_lapl_cube_solve_d(int nx, int ny, int nz, double dx, double dy, double dz,
+                          double lx, double ly, double lz, int periodic,
+                          double* ans, const double* rhs, int reps) {
+    if (periodic) cube_solve<double, periodic3>(nx, ny, nz, dx, dy, dz, lx, ly, lz, ans, rhs, reps);
+    else cube_solve<double, tensor_flags<>>(nx, ny, nz, dx, dy, dz, lx, ly, lz, ans, rhs, reps);
+    return 0;
+}
+
+int ref_lapl_cube_solve_f(int nx, int ny, int nz, double dx, double dy, double dz,
+                          double lx, double ly, double lz, int periodic,
+                          float* ans, const float* rhs, int reps) {
+    if (periodic) cube_solve<float, periodic3>(nx, ny, nz, dx, dy, dz, lx, ly, lz, ans, rhs, reps);
+    else cube_solve<float, tensor_flags<>>(nx, ny, nz, dx, dy, dz, lx, ly, lz, ans, rhs, reps);
+    return 0;
+}
+
+int ref_lapl_rect_solve_d(int nx, int ny, double dx, double dy, double lx, double ly,
+                          int fft2, double* ans, const double* rhs) {
+    std::vector<double> r(rhs, rhs + (size_t)nx * ny);
+    if (fft2) {
+        LaplRectFFT2<double, false> l(dx, dy, lx, ly, nx, ny);
+        l.solve(ans, r.data());
+    } else {
+        LaplRect<double, false> l(dx, dy, lx, ly, nx, ny);
+        l.solve(ans, r.data());
+    }
+    return 0;
+}
+
+// S[1..N-1] = dx * sum_{j=1}^{N-1} s[j] sin(pi j k / N); s is overwritten.
+int ref_sfft_d(double* S, double* s, double dx, int N) {
+    FFTTable<double> t(N);
+    FFT<double> ft(t, N);
+    ft.sFFT(S, s, dx);
+    return 0;
+}
+int ref_sfft_f(float* S, float* s, float dx, int N) {
+    FFTTable<float> t(N);
+    FFT<float> ft(t, N);
+    ft.sFFT(S, s, dx);
+    return 0;
+}
+
+int ref_cyclic_reduction_d(double* d, double* e, double* f, double* b, int q, int n, int general) {
+    if (general) cyclic_reduction_general(d, e, f, b, q, n);
+    else cyclic_reduction(d, e, f, b, q, n);
+    return 0;
+}
+
+int ref_thomas_d(double* b, double* lower, double* diag, double* upper, int n) {
+    solve_tdiag_linear_my(b, lower, diag, upper, n);
+    return 0;
+}
+
+struct RefNS {
+    Config cfg;
+    NSCube<double, false>* ns = nullptr;
+};
+
+void* ref_nscube_create(int nx, int nz, double Re, double dt, double u0,
+                        double x1, double y1, double z1, double x2, double y2, double z2) {
+    auto* h = new RefNS();
+    char buf[16][96];
+    const char* keys[] = {"nx", "nz", "Re", "dt", "u0", "x1", "y1", "z1", "x2", "y2", "z2"};
+    double vals[] = {(double)nx, (double)nz, Re, dt, u0, x1, y1, z1, x2, y2, z2};
+    char* argv[16];
+    argv[0] = (char*)"ref";
+    for (int i = 0; i < 11; i++) {
+        if (i < 2) snprintf(buf[i], sizeof(buf[i]), "--ns:%s=%d", keys[i], (int)vals[i]);
+        else snprintf(buf[i], sizeof(buf[i]), "--ns:%s=%.17g", keys[i], vals[i]);
+        argv[i + 1] = buf[i];
+    }
+    h->cfg.rewrite(12, argv);
+    h->ns = new NSCube<double, false>(h->cfg);
+    return h;
+}
+
+int ref_nscube_step(void* hp, int k) {
+    auto* h = (RefNS*)hp;
+    for (int i = 0; i < k; i++) h->ns->step();
+    return 0;
+}
+
+// Copies a field's whole storage (ghost layers included, layout of the
+// reference tensor: row-major over its inclusive index ranges, x fastest).
+// field: 0=u 1=v 2=w 3=p 4=x 5=F 6=G 7=H 8=RHS.  Returns the element count,
+// or -1 for a bad field id.  out may be NULL to query the size.
+long ref_nscube_get(void* hp, int field, double* out) {
+    auto* h = (RefNS*)hp;
+    auto* ns = h->ns;
+    tensor<double, 3, false>* t[] = {&ns->u, &ns->v, &ns->w, &ns->p, &ns->x,
+                                     &ns->F, &ns->G, &ns->H, &ns->RHS};
+    if (field < 0 || field > 8) return -1;
+    long n = t[field]->size;
+    if (out) memcpy(out, t[field]->vec, sizeof(double) * n);
+    return n;
+}
+
+int ref_nscube_set(void* hp, int field, const double* in) {
+    auto* h = (RefNS*)hp;
+    auto* ns = h->ns;
+    tensor<double, 3, false>* t[] = {&ns->u, &ns->v, &ns->w, &ns->p, &ns->x,
+                                     &ns->F, &ns->G, &ns->H, &ns->RHS};
+    if (field < 0 || field > 8) return -1;
+    memcpy(t[field]->vec, in, sizeof(double) * t[field]->size);
+    return 0;
+}
+
+void ref_nscube_destroy(void* hp) {
+    auto* h = (RefNS*)hp;
+    delete h->ns;
+    delete h;
+}
+
+}  // extern "C"

@@ -1,0 +1,174 @@
+"""Generates the golden fixtures in tests/golden/ by running the reference's
+own CPU code (oracle/_ref/libfdm_ref.so, built by `make -C oracle ref` from
+the reference sources).  Run from the repository root:
+
+    make -C oracle ref && python tests/golden/make_golden.py
+
+Inputs are seeded (numpy default_rng) or analytic; each fixture stores the
+inputs it needs (or the seed plus checksums of the regenerated input) and the
+reference outputs.  Small cases are stored in full; 31^3 cases as checksums
+plus values at seeded sample positions.
+"""
+from __future__ import annotations
+
+import math
+import sys
+from pathlib import Path
+
+import numpy as np
+
+ROOT = Path(__file__).resolve().parents[2]
+sys.path.insert(0, str(ROOT))
+
+from fdm_gb300 import workloads  # noqa: E402
+from oracle.oracle import reference  # noqa: E402
+
+OUT = Path(__file__).resolve().parent
+
+
+def checksums(a: np.ndarray, nsamp: int = 256, seed: int = 1234):
+    rng = np.random.default_rng(seed)
+    flat = a.ravel()
+    idx = rng.choice(flat.size, size=min(nsamp, flat.size), replace=False)
+    return dict(sum=flat.sum(), l2=np.linalg.norm(flat), maxabs=np.abs(flat).max(), idx=idx, vals=flat[idx])
+
+
+def ut_lapl_cube_rhs(n: int):
+    """RHS and analytic answer of the reference's test_lapl_cube
+    (ut/ut_lapl_cube.cpp:21-92): u = sin^2 x + cos^2 y + sin^2 z at cell
+    centres of [0,1]^3, boundary values folded into the RHS."""
+    x1 = y1 = z1 = 0.0
+    x2 = y2 = z2 = 1.0
+    dx = (x2 - x1) / n
+    dy, dz = dx, dx
+
+    def c(i, h, o):
+        return o + h * i - h / 2
+
+    def ans(i, k, j):
+        return math.sin(c(j, dx, x1)) ** 2 + math.cos(c(k, dy, y1)) ** 2 + math.sin(c(i, dz, z1)) ** 2
+
+    def rp(i, k, j):
+        x, y, z = c(j, dx, x1), c(k, dy, y1), c(i, dz, z1)
+        return (2 * math.sin(y) ** 2 - 2 * math.cos(y) ** 2 - 2 * math.sin(x) ** 2 + 2 * math.cos(x) ** 2
+                - 2 * math.sin(z) ** 2 + 2 * math.cos(z) ** 2)
+
+    rhs = np.zeros((n, n, n))
+    exact = np.zeros((n, n, n))
+    for i in range(1, n + 1):
+        for k in range(1, n + 1):
+            for j in range(1, n + 1):
+                r = rp(i, k, j)
+                if i <= 1: r -= ans(i - 1, k, j) / dz / dz
+                if k <= 1: r -= ans(i, k - 1, j) / dy / dy
+                if j <= 1: r -= ans(i, k, j - 1) / dx / dx
+                if j >= n: r -= ans(i, k, j + 1) / dx / dx
+                if k >= n: r -= ans(i, k + 1, j) / dy / dy
+                if i >= n: r -= ans(i + 1, k, j) / dz / dz
+                rhs[i - 1, k - 1, j - 1] = r
+                exact[i - 1, k - 1, j - 1] = ans(i, k, j)
+    args = (dx, dy, dz, x2 - x1 + dx, y2 - y1 + dy, z2 - z1 + dz)
+    return rhs, exact, args
+
+
+def main():
+    R = reference()
+    if R is None:
+        raise SystemExit("oracle/_ref/libfdm_ref.so missing: run `make -C oracle ref` first")
+
+    # DST-I vectors (FFT<T>::sFFT)
+    d = {}
+    for N in (2, 8, 32, 256, 1024):
+        s = np.random.default_rng(N).uniform(-1, 1, N)
+        s[0] = 0.0
+        d["s_%d" % N] = s
+        d["S_%d" % N] = R.sfft(s, 1.0)
+        d["Sh_%d" % N] = R.sfft(s, 0.5)
+    np.savez_compressed(OUT / "dst.npz", **d)
+
+    # LaplCube
+    c = {}
+    f, _ = workloads.manufactured(15, 15, 15, seed=3, kmax=4)
+    a = workloads.solver_args(15, 15, 15)
+    c["m15_rhs"] = f
+    c["m15_ans"] = R.lapl_cube(f, *a[:6])
+    rng = np.random.default_rng(11)
+    rhs = rng.standard_normal((7, 15, 15))
+    h = (0.1, 0.2, 0.3)
+    args = (h[0], h[1], h[2], 16 * h[0], 16 * h[1], 8 * h[2])
+    c["aniso_rhs"], c["aniso_args"] = rhs, np.array(args)
+    c["aniso_ans"] = R.lapl_cube(rhs, *args)
+    rhs = rng.standard_normal((15, 7, 31))
+    args = (0.05, 0.3, 0.11, 32 * 0.05, 8 * 0.3, 16 * 0.11 * 1.5)  # lz not (nz+1)dz: scale convention
+    c["lz_rhs"], c["lz_args"] = rhs, np.array(args)
+    c["lz_ans"] = R.lapl_cube(rhs, *args)
+    f, _ = workloads.manufactured(31, 31, 31, seed=0, kmax=12)
+    a = workloads.solver_args(31, 31, 31)
+    for k, v in checksums(f).items():
+        c["c0_rhs_" + k] = v
+    for k, v in checksums(R.lapl_cube(f, *a[:6])).items():
+        c["c0_ans_" + k] = v
+    rhs, exact, args = ut_lapl_cube_rhs(31)
+    out = R.lapl_cube(rhs, *args)
+    for k, v in checksums(out).items():
+        c["ut31_ans_" + k] = v
+    c["ut31_err"] = np.abs(out - exact).max() / np.abs(exact).max()
+    np.savez_compressed(OUT / "lapl_cube.npz", **c)
+
+    # LaplRect / LaplRectFFT2
+    r = {}
+    rng = np.random.default_rng(5)
+    for (nx, ny) in ((31, 31), (20, 63)):
+        rhs = rng.standard_normal((ny, nx))
+        dx, dy = 0.1, 0.07
+        args = (dx, dy, (nx + 1) * dx, (ny + 1) * dy)
+        r["rhs_%dx%d" % (nx, ny)] = rhs
+        r["args_%dx%d" % (nx, ny)] = np.array(args)
+        r["tri_%dx%d" % (nx, ny)] = R.lapl_rect(rhs, *args, fft2=False)
+        if (nx + 1) & nx == 0:
+            r["fft2_%dx%d" % (nx, ny)] = R.lapl_rect(rhs, *args, fft2=True)
+    np.savez_compressed(OUT / "lapl_rect.npz", **r)
+
+    # tridiagonal: Thomas and cyclic reduction on U(-1,1) systems with a
+    # dominant diagonal
+    t = {}
+    rng = np.random.default_rng(9)
+    for n in (9, 31, 32, 63, 255):
+        lo = rng.uniform(-1, 1, n)
+        up = rng.uniform(-1, 1, n)
+        dg = rng.uniform(-1, 1, n) + np.sign(rng.uniform(-1, 1, n)) * 3.0
+        b = rng.uniform(-1, 1, n)
+        lo[0] = 0.0
+        up[-1] = 0.0
+        t["lo_%d" % n], t["dg_%d" % n], t["up_%d" % n], t["b_%d" % n] = lo, dg, up, b
+        # Thomas: lower[j] = A(j+1, j) = lo[j+1]
+        t["thomas_%d" % n] = R.thomas(np.r_[lo[1:], 0.0], dg, up, b)
+        t["crg_%d" % n] = R.cyclic_reduction(dg, lo, up, b, general=True)
+        if (n + 1) & n == 0:
+            t["cr_%d" % n] = R.cyclic_reduction(dg, lo, up, b, general=False)
+    np.savez_compressed(OUT / "tdiag.npz", **t)
+
+    # NSCube lid-driven cavity, Re=250, dt=0.01, [-pi,pi]^3
+    ns = {}
+    m = R.nscube(15, 15, 250.0, 0.01)
+    m.step(20)
+    for name in ("u", "v", "w", "p"):
+        ns["n15_s20_" + name] = m.get(name)
+    m.step(80)
+    for name in ("u", "v", "w", "p", "x"):
+        for k, v in checksums(m.get(name)).items():
+            ns["n15_s100_%s_%s" % (name, k)] = v
+    m.close()
+    m = R.nscube(31, 31, 250.0, 0.01)
+    m.step(10)
+    for name in ("u", "v", "w", "p"):
+        for k, v in checksums(m.get(name)).items():
+            ns["n31_s10_%s_%s" % (name, k)] = v
+    m.close()
+    np.savez_compressed(OUT / "ns_cube.npz", **ns)
+    for p in sorted(OUT.glob("*.npz")):
+        print(p.name, p.stat().st_size)
+
+
+if __name__ == "__main__":
+    main()

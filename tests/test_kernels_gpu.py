@@ -1,0 +1,87 @@
+"""GPU parity of the 1-D building blocks and LaplRect through the C ABI:
+the DST-I line transform (FFT<T>::sFFT), the tridiagonal solver
+(solve_tdiag_linear_my / cyclic_reduction) and LaplRect / LaplRectFFT2."""
+import numpy as np
+import pytest
+
+from tests.helpers import rel_l2
+from fdm_gb300 import LaplRect, LaplRectFFT2, sine_transform_device, tridiag_device
+
+pytestmark = pytest.mark.gpu
+
+
+@pytest.mark.parametrize("N", [2, 4, 8, 32, 64, 128, 256, 512, 1024])
+def test_sine_f64_vs_reference(cuda, golden, port, N):
+    import torch
+    g = golden("dst")
+    rng = np.random.default_rng(N)
+    lines = rng.uniform(-1, 1, (37, N - 1))
+    if "s_%d" % N in g:
+        lines[0] = g["s_%d" % N][1:]
+    x = torch.from_numpy(lines).to(cuda)
+    y = torch.empty_like(x)
+    sine_transform_device(y, x, N, 37, 0.5)
+    torch.cuda.synchronize()
+    out = y.cpu().numpy()
+    for i in range(37):
+        s = np.r_[0.0, lines[i]]
+        ref = port.sfft(s, 0.5)[1:]
+        assert np.abs(out[i] - ref).max() <= 1e-13 * max(1.0, np.abs(ref).max())
+    if "s_%d" % N in g:
+        assert np.abs(out[0] - g["Sh_%d" % N][1:]).max() <= 1e-13 * max(1.0, np.abs(g["Sh_%d" % N]).max())
+
+
+@pytest.mark.parametrize("N", [32, 256])
+def test_sine_f32_roundtrip(cuda, N):
+    import torch
+    x = torch.rand((64, N - 1), dtype=torch.float32, device=cuda) * 2 - 1
+    y = torch.empty_like(x)
+    z = torch.empty_like(x)
+    sine_transform_device(y, x, N, 64, 1.0, dtype=np.float32)
+    sine_transform_device(z, y, N, 64, 2.0 / N, dtype=np.float32)
+    torch.cuda.synchronize()
+    assert (z - x).abs().max().item() <= 1e-5  # ut/ut_fft.cpp test_sin, float tolerance
+
+
+@pytest.mark.parametrize("n", [9, 31, 32, 63, 255])
+def test_tridiag_vs_reference(cuda, golden, n):
+    import torch
+    g = golden("tdiag")
+    lo, dg, up, b = g["lo_%d" % n], g["dg_%d" % n], g["up_%d" % n], g["b_%d" % n]
+    # two systems interleaved: the golden one and its negation
+    L = torch.tensor(np.stack([lo, lo], 1).ravel(), device=cuda)
+    D = torch.tensor(np.stack([dg, dg], 1).ravel(), device=cuda)
+    U = torch.tensor(np.stack([up, up], 1).ravel(), device=cuda)
+    B = torch.tensor(np.stack([b, -b], 1).ravel(), device=cuda)
+    tridiag_device(L, D, U, B, n, 2)
+    torch.cuda.synchronize()
+    x = B.cpu().numpy().reshape(n, 2)
+    assert np.abs(x[:, 0] - g["thomas_%d" % n]).max() <= 1e-13
+    assert np.abs(x[:, 1] + g["crg_%d" % n]).max() <= 1e-13
+
+
+def test_rect_vs_reference(cuda, golden):
+    g = golden("lapl_rect")
+    for key, (nx, ny) in (("31x31", (31, 31)), ("20x63", (20, 63))):
+        rhs, args = g["rhs_" + key], tuple(g["args_" + key])
+        r = LaplRect(*args, nx, ny)
+        ans = np.zeros_like(rhs)
+        r.solve(ans, rhs)
+        assert rel_l2(ans, g["tri_" + key]) <= 1e-12
+        if "fft2_" + key in g:
+            r2 = LaplRectFFT2(*args, nx, ny)
+            ans2 = np.zeros_like(rhs)
+            r2.solve(ans2, rhs)
+            assert rel_l2(ans2, g["fft2_" + key]) <= 1e-12
+
+
+def test_rect_formulations_agree_511(cuda):
+    # ut/ut_lapl_rect.cpp:384-456
+    n = 511
+    rhs = np.random.default_rng(2).uniform(-1, 1, (n, n))
+    h = 1.0 / (n + 1)
+    a = np.zeros_like(rhs)
+    b = np.zeros_like(rhs)
+    LaplRect(h, h, 1.0, 1.0, n, n).solve(a, rhs)
+    LaplRectFFT2(h, h, 1.0, 1.0, n, n).solve(b, rhs)
+    assert np.abs(a - b).max() <= 1e-14 * max(1.0, np.abs(a).max())

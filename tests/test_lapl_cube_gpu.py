@@ -1,0 +1,179 @@
+"""GPU parity of the LaplCube path (plain and mixed precision) through the
+C ABI of libfdmgpu.so, against the reference's golden outputs, the CPU oracle
+and size-independent properties."""
+import numpy as np
+import pytest
+
+from tests.helpers import lap7, rel_l2
+from fdm_gb300 import FdmError, LaplCube, workloads
+
+pytestmark = pytest.mark.gpu
+
+# FP64 plain form vs the reference's CPU LaplCube::solve: relative L2 <= 1e-12
+TOL_PLAIN = 1e-12
+# mixed form with refinement vs the FP64 GPU form: relative L2 <= 1e-10
+TOL_MIXED = 1e-10
+
+
+def solve_host(args, rhs, **kw):
+    lc = LaplCube(*args, **kw)
+    ans = np.zeros_like(rhs)
+    lc.solve(ans, rhs)
+    return ans, lc
+
+
+def test_golden_small_cases(cuda, golden):
+    g = golden("lapl_cube")
+    a = workloads.solver_args(15, 15, 15)
+    ans, _ = solve_host(a, g["m15_rhs"])
+    assert rel_l2(ans, g["m15_ans"]) <= TOL_PLAIN
+    ans, _ = solve_host(tuple(g["aniso_args"]) + (15, 15, 7), g["aniso_rhs"])
+    assert rel_l2(ans, g["aniso_ans"]) <= TOL_PLAIN
+    ans, _ = solve_host(tuple(g["lz_args"]) + (31, 7, 15), g["lz_rhs"])
+    assert rel_l2(ans, g["lz_ans"]) <= TOL_PLAIN
+
+
+def test_config0_against_reference_checksums(cuda, golden):
+    g = golden("lapl_cube")
+    f, u = workloads.manufactured(31, 31, 31, seed=0, kmax=12)
+    ans, _ = solve_host(workloads.solver_args(31, 31, 31), f)
+    assert np.allclose(ans.ravel()[g["c0_ans_idx"]], g["c0_ans_vals"], rtol=0, atol=1e-12 * g["c0_ans_maxabs"])
+    assert rel_l2(ans, u) <= 1e-13  # manufactured solution to round-off
+
+
+def test_reference_unit_case(cuda, golden):
+    from tests.golden.make_golden import ut_lapl_cube_rhs
+    g = golden("lapl_cube")
+    rhs, exact, args = ut_lapl_cube_rhs(31)
+    ans, _ = solve_host(args + (31, 31, 31), rhs)
+    err = np.abs(ans - exact).max() / np.abs(exact).max()
+    assert err < 1e-4  # ut/ut_lapl_cube.cpp:124
+    assert abs(err - g["ut31_err"]) <= 1e-10
+    assert np.allclose(ans.ravel()[g["ut31_ans_idx"]], g["ut31_ans_vals"], rtol=0, atol=1e-12 * g["ut31_ans_maxabs"])
+
+
+@pytest.mark.parametrize("shape", [(1, 1, 1), (3, 7, 1), (7, 15, 31), (63, 31, 15), (31, 127, 63), (63, 63, 63)])
+def test_plain_f64_vs_oracle(cuda, port, shape):
+    nx, ny, nz = shape
+    rng = np.random.default_rng(nx * 7 + ny * 3 + nz)
+    rhs = rng.standard_normal((nz, ny, nx))
+    h = (0.3, 0.11, 0.07)
+    args = (h[0], h[1], h[2], (nx + 1) * h[0], (ny + 1) * h[1], (nz + 1) * h[2], nx, ny, nz)
+    ans, _ = solve_host(args, rhs)
+    ref = port.lapl_cube(rhs, *args[:6])
+    assert rel_l2(ans, ref) <= TOL_PLAIN
+
+
+def test_plain_f32_vs_oracle(cuda, port):
+    n = 31
+    f, u = workloads.manufactured(n, n, n, seed=4, kmax=8)
+    args = workloads.solver_args(n, n, n)
+    lc = LaplCube(*args, dtype=np.float32)
+    ans = np.zeros(f.shape, np.float32)
+    lc.solve(ans, f.astype(np.float32))
+    assert rel_l2(ans, port.lapl_cube(f, *args[:6])) <= 1e-5
+
+
+@pytest.mark.parametrize("n", [127, 255])
+def test_plain_large_residual_and_linearity(cuda, n):
+    """Size-independent properties at full size: the 7-point residual of the
+    answer and linearity in the right-hand side."""
+    import torch
+    f, u = workloads.manufactured_torch(n, n, n, seed=2, kmax=60 if n == 255 else 30, noise=1e-3)
+    args = workloads.solver_args(n, n, n)
+    lc = LaplCube(*args)
+    ans = torch.empty_like(f)
+    lc.solve_device(ans, f)
+    f2 = torch.roll(f, 1, 0).contiguous()
+    ans2 = torch.empty_like(f)
+    lc.solve_device(ans2, f2)
+    both = torch.empty_like(f)
+    lc.solve_device(both, (2.0 * f - 3.0 * f2).contiguous())
+    torch.cuda.synchronize()
+    a, b, c = ans.cpu().numpy(), ans2.cpu().numpy(), both.cpu().numpy()
+    h = args[0]
+    fr = f.cpu().numpy()
+    assert rel_l2(lap7(a, h, h, h), fr) <= 1e-12
+    assert rel_l2(c, 2 * a - 3 * b) <= 1e-13
+
+
+def test_batched_equals_single(cuda):
+    import torch
+    n = 63
+    fs = [workloads.manufactured_torch(n, n, n, seed=s, kmax=16)[0] for s in range(3)]
+    args = workloads.solver_args(n, n, n)
+    lc = LaplCube(*args)
+    batch = torch.stack(fs).contiguous()
+    out = torch.empty_like(batch)
+    lc.solve_device(out, batch, nrhs=3)
+    for i, f in enumerate(fs):
+        one = torch.empty_like(f)
+        lc.solve_device(one, f)
+        torch.cuda.synchronize()
+        assert torch.equal(one, out[i])
+
+
+@pytest.mark.parametrize("n,kmax", [(31, 8), (63, 16), (127, 32)])
+def test_mixed_vs_plain(cuda, n, kmax):
+    import torch
+    f, u = workloads.manufactured_torch(n, n, n, seed=n, kmax=kmax, noise=1e-3)
+    args = workloads.solver_args(n, n, n)
+    plain = LaplCube(*args)
+    mixed = LaplCube(*args, precision="mixed", tol=1e-10)
+    a = torch.empty_like(f)
+    b = torch.empty_like(f)
+    plain.solve_device(a, f)
+    mixed.solve_device(b, f)
+    sweeps, est = mixed.last_info(1)
+    err = (torch.linalg.norm(b - a) / torch.linalg.norm(a)).item()
+    assert sweeps >= 1
+    assert err <= TOL_MIXED
+    assert 0 <= est[0] < 1e-4
+
+
+def test_mixed_config2_full_size(cuda):
+    """255^3, k in [1,60], N(0,1e-3) noise: two RHS batched."""
+    import torch
+    n = 255
+    fs = [workloads.manufactured_torch(n, n, n, seed=s, kmax=60, noise=1e-3)[0] for s in (0, 1)]
+    args = workloads.solver_args(n, n, n)
+    batch = torch.stack(fs).contiguous()
+    plain = LaplCube(*args)
+    mixed = LaplCube(*args, precision="mixed", tol=1e-10)
+    a = torch.empty_like(batch)
+    b = torch.empty_like(batch)
+    plain.solve_device(a, batch, nrhs=2)
+    mixed.solve_device(b, batch, nrhs=2)
+    torch.cuda.synchronize()
+    for i in range(2):
+        err = (torch.linalg.norm(b[i] - a[i]) / torch.linalg.norm(a[i])).item()
+        assert err <= TOL_MIXED, (i, err)
+
+
+def test_mixed_tolerance_levels(cuda):
+    import torch
+    n = 63
+    f, _ = workloads.manufactured_torch(n, n, n, seed=9, kmax=16, noise=1e-3)
+    args = workloads.solver_args(n, n, n)
+    plain = LaplCube(*args)
+    a = torch.empty_like(f)
+    plain.solve_device(a, f)
+    for tol, want_sweeps in ((1e-4, 0), (1e-6, 1), (1e-10, 1), (1e-13, 2)):
+        m = LaplCube(*args, precision="mixed", tol=tol)
+        b = torch.empty_like(f)
+        m.solve_device(b, f)
+        s, _ = m.last_info(1)
+        assert s == want_sweeps
+        err = (torch.linalg.norm(b - a) / torch.linalg.norm(a)).item()
+        assert err <= max(tol, 1e-13), (tol, err)
+
+
+def test_errors_like_reference(cuda):
+    with pytest.raises(FdmError) as e:
+        LaplCube(0.1, 0.1, 0.1, 3.3, 3.3, 3.3, 32, 31, 31)
+    assert e.value.status == 2  # ESIZE: verify((1<<n) == N) in the reference
+    with pytest.raises(FdmError):
+        LaplCube(0.1, 0.1, 0.1, 3.2, 3.2, 3.2, 31, 31, 31, dtype=np.float32, precision="mixed")
+    lc = LaplCube(*workloads.solver_args(7, 7, 7))
+    with pytest.raises(FdmError):
+        lc.solve(np.zeros(10), np.zeros(343))

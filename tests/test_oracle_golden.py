@@ -1,0 +1,123 @@
+"""Pins the CPU oracle (oracle/fdm_oracle.c) to the reference's own outputs
+stored in tests/golden (generated by tests/golden/make_golden.py from the
+compiled reference), and ports the reference unit tests' assertions:
+ut/ut_fft.cpp test_sin / test_sin_new, ut/ut_lapl_cube.cpp test_lapl_cube,
+ut/ut_lapl_rect.cpp test_lapl_rect_fft1_fft2_cmp, ut/ut_tdiag.cpp."""
+import math
+
+import numpy as np
+import pytest
+
+from tests.helpers import rel_l2
+from fdm_gb300 import workloads
+
+
+@pytest.mark.parametrize("N", [2, 8, 32, 256, 1024])
+def test_sfft_matches_reference(port, golden, N):
+    g = golden("dst")
+    s = g["s_%d" % N]
+    assert np.abs(port.sfft(s, 1.0)[1:] - g["S_%d" % N][1:]).max() <= 1e-12 * max(1.0, np.abs(g["S_%d" % N]).max())
+    assert np.abs(port.sfft(s, 0.5)[1:] - g["Sh_%d" % N][1:]).max() <= 1e-12 * max(1.0, np.abs(g["Sh_%d" % N]).max())
+
+
+def test_sfft_roundtrip_and_naive(port):
+    # ut/ut_fft.cpp:190-228: S = sFFT(s); s' = sFFT(S) * 2/N recovers s
+    N = 1024
+    s = np.random.default_rng(0).uniform(-1, 1, N)
+    s[0] = 0
+    S = port.sfft(s, 1.0)
+    s1 = port.sfft(S, 2.0 / N)
+    assert np.abs(s1[1:N - 1] - s[1:N - 1]).max() <= 1e-13
+    S2 = port.sft_naive(S, 2.0 / N)
+    assert np.abs(s1[1:N - 1] - S2[1:N - 1]).max() <= 1e-12
+
+
+def test_sfft_rejects_non_power_of_two(port):
+    with pytest.raises(ValueError):
+        port.sfft(np.zeros(12))
+
+
+def test_lapl_cube_matches_reference(port, golden):
+    g = golden("lapl_cube")
+    a = workloads.solver_args(15, 15, 15)
+    assert rel_l2(port.lapl_cube(g["m15_rhs"], *a[:6]), g["m15_ans"]) <= 1e-14
+    assert rel_l2(port.lapl_cube(g["aniso_rhs"], *g["aniso_args"]), g["aniso_ans"]) <= 1e-14
+    assert rel_l2(port.lapl_cube(g["lz_rhs"], *g["lz_args"]), g["lz_ans"]) <= 1e-14
+
+
+def test_lapl_cube_config0_checksums(port, golden):
+    g = golden("lapl_cube")
+    f, u = workloads.manufactured(31, 31, 31, seed=0, kmax=12)
+    # the generator still produces the input the fixture was made from
+    assert abs(f.sum() - g["c0_rhs_sum"]) <= 1e-9 * abs(g["c0_rhs_l2"])
+    assert np.allclose(f.ravel()[g["c0_rhs_idx"]], g["c0_rhs_vals"], rtol=0, atol=1e-12 * g["c0_rhs_maxabs"])
+    ans = port.lapl_cube(f, *workloads.solver_args(31, 31, 31)[:6])
+    assert np.allclose(ans.ravel()[g["c0_ans_idx"]], g["c0_ans_vals"], rtol=0, atol=1e-13 * g["c0_ans_maxabs"])
+    assert abs(np.linalg.norm(ans) - g["c0_ans_l2"]) <= 1e-13 * g["c0_ans_l2"]
+    # manufactured solution recovered to round-off
+    assert rel_l2(ans, u) <= 1e-13
+
+
+def test_lapl_cube_reference_unit_case(port, golden):
+    from tests.golden.make_golden import ut_lapl_cube_rhs
+    g = golden("lapl_cube")
+    rhs, exact, args = ut_lapl_cube_rhs(31)
+    ans = port.lapl_cube(rhs, *args)
+    err = np.abs(ans - exact).max() / np.abs(exact).max()
+    assert err < 1e-4  # ut/ut_lapl_cube.cpp:124
+    assert abs(err - g["ut31_err"]) <= 1e-12
+    assert np.allclose(ans.ravel()[g["ut31_ans_idx"]], g["ut31_ans_vals"], rtol=0, atol=1e-13 * g["ut31_ans_maxabs"])
+
+
+def test_lapl_rect_matches_reference(port, golden):
+    g = golden("lapl_rect")
+    for key in ("31x31", "20x63"):
+        rhs, args = g["rhs_" + key], g["args_" + key]
+        assert rel_l2(port.lapl_rect(rhs, *args), g["tri_" + key]) <= 1e-14
+        if "fft2_" + key in g:
+            assert rel_l2(port.lapl_rect(rhs, *args, fft2=True), g["fft2_" + key]) <= 1e-14
+
+
+def test_lapl_rect_two_formulations_agree(port):
+    # ut/ut_lapl_rect.cpp:384-456 (511^2, |delta| <= 1e-15 absolute)
+    n = 511
+    rhs = np.random.default_rng(2).uniform(-1, 1, (n, n))
+    h = 1.0 / (n + 1)
+    a = port.lapl_rect(rhs, h, h, 1.0, 1.0)
+    b = port.lapl_rect(rhs, h, h, 1.0, 1.0, fft2=True)
+    assert np.abs(a - b).max() <= 1e-14 * max(1.0, np.abs(a).max())
+
+
+@pytest.mark.parametrize("n", [9, 31, 32, 63, 255])
+def test_tridiagonal_matches_reference(port, golden, n):
+    g = golden("tdiag")
+    lo, dg, up, b = g["lo_%d" % n], g["dg_%d" % n], g["up_%d" % n], g["b_%d" % n]
+    th = port.thomas(np.r_[lo[1:], 0.0], dg, up, b)
+    assert np.abs(th - g["thomas_%d" % n]).max() <= 1e-15 * 10
+    crg = port.cyclic_reduction(dg, lo, up, b, general=True)
+    assert np.abs(crg - g["crg_%d" % n]).max() <= 1e-15 * 10
+    assert np.abs(crg - th).max() <= 1e-13  # ut/ut_tdiag.cpp: CR vs Thomas
+    if "cr_%d" % n in g:
+        cr = port.cyclic_reduction(dg, lo, up, b, general=False)
+        assert np.abs(cr - g["cr_%d" % n]).max() <= 1e-15 * 10
+
+
+def test_nscube_matches_reference(port, golden):
+    g = golden("ns_cube")
+    m = port.nscube(15, 15, 250.0, 0.01)
+    m.step(20)
+    for name in ("u", "v", "w", "p"):
+        ref = g["n15_s20_" + name]
+        assert np.abs(m.get(name) - ref).max() <= 1e-12 * max(1.0, np.abs(ref).max()), name
+    m.step(80)
+    for name in ("u", "v", "w", "p", "x"):
+        a = m.get(name)
+        ref_vals = g["n15_s100_%s_vals" % name]
+        scale = max(1.0, float(g["n15_s100_%s_maxabs" % name]))
+        assert np.abs(a[g["n15_s100_%s_idx" % name]] - ref_vals).max() <= 1e-11 * scale, name
+    m.close()
+
+
+def test_nscube_rejects_bad_size(port):
+    with pytest.raises(ValueError):
+        port.nscube(32, 32, 250.0, 0.01)
