@@ -87,34 +87,45 @@ static int pick_lines(int N) {
     return L;
 }
 
-template <typename Tin, typename T, typename Tout, int AXIS>
+template <typename Tin, typename T, typename Tout, int AXIS, int MODE>
+constexpr const char* sine_name() {
+    return AXIS == 1 ? (sizeof(T) == 8 ? "sine_y_f64" : "sine_y_f32")
+           : MODE == kRound    ? "sine_x_round"
+           : MODE == kResidual ? "sine_x_resid"
+           : MODE == kCombine  ? "sine_x_combine"
+           : sizeof(T) == 8    ? "sine_x_f64"
+           : sizeof(Tout) == 8 ? "sine_x_f32_out64"
+                               : "sine_x_f32";
+}
+
+template <typename Tin, typename T, typename Tout, int AXIS, int MODE = kPlain>
 static void launch_sine(const Tin* in, Tout* out, int nx, int ny, int nz, int nvol, const SineTables<T>& tb,
-                        double scale, cudaStream_t st) {
+                        double scale, cudaStream_t st, const SineFused* fused = nullptr) {
     const int L = pick_lines<T>(tb.N);
     int Lshift = 0;
     while ((1 << Lshift) < L) Lshift++;
     const size_t smem = sine_smem_bytes<T>(tb.N, L);
     static bool attr_set = false;
     if (!attr_set) {
-        FDM_CUDA(cudaFuncSetAttribute(k_sine_pass<Tin, T, Tout, AXIS>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                      (int)(kSineSmemBudget + 1024)));
+        FDM_CUDA(cudaFuncSetAttribute(k_sine_pass<Tin, T, Tout, AXIS, MODE>,
+                                      cudaFuncAttributeMaxDynamicSharedMemorySize, (int)(kSineSmemBudget + 1024)));
         attr_set = true;
     }
     unsigned gx;
     if (AXIS == 0) gx = (unsigned)((ny * (long long)nz + L - 1) / L);
     else gx = (unsigned)(nz * ((nx + L - 1) / L));
     dim3 grid(gx, nvol);
-    const long long vstride = (long long)nx * ny * nz;
-    // name: axis, compute type, input and output element bytes
-    static const char* names[2][2][3][3] = {
-        {{{"", "", ""}, {"", "sine_x_f32_44", "sine_x_f32_48"}, {"", "sine_x_f32_84", "sine_x_f32_88"}},
-         {{"", "", ""}, {"", "sine_x_f64_44", "sine_x_f64_48"}, {"", "sine_x_f64_84", "sine_x_f64_88"}}},
-        {{{"", "", ""}, {"", "sine_y_f32_44", "sine_y_f32_48"}, {"", "sine_y_f32_84", "sine_y_f32_88"}},
-         {{"", "", ""}, {"", "sine_y_f64_44", "sine_y_f64_48"}, {"", "sine_y_f64_84", "sine_y_f64_88"}}}};
-    const char* name = names[AXIS][sizeof(T) == 8][sizeof(Tin) / 4][sizeof(Tout) / 4];
-    FDM_TIMED(name, st);
-    k_sine_pass<Tin, T, Tout, AXIS><<<grid, L * kGroup, smem, st>>>(in, out, nx, ny, nz, vstride, tb, (T)scale, L,
-                                                                   Lshift);
+    SineGeom geo;
+    geo.nx = nx; geo.ny = ny; geo.nz = nz;
+    geo.vstride = (long long)nx * ny * nz;
+    geo.L = L; geo.Lshift = Lshift;
+    geo.div_n = FastDiv((unsigned)(AXIS == 0 ? nx : ny));
+    geo.div_ny = FastDiv((unsigned)ny);
+    SineFused fu;
+    memset(&fu, 0, sizeof(fu));
+    if (fused) fu = *fused;
+    FDM_TIMED((sine_name<Tin, T, Tout, AXIS, MODE>()), st);
+    k_sine_pass<Tin, T, Tout, AXIS, MODE><<<grid, L * kGroup, smem, st>>>(in, out, geo, tb, (T)scale, fu);
     FDM_LAUNCH_CHECK();
 }
 
@@ -126,6 +137,43 @@ static void launch_tridiag(T* W, int nlines, int n, int A, long long sa, long lo
     FDM_TIMED(sizeof(T) == 8 ? "tridiag_f64" : "tridiag_f32", st);
     k_tridiag_const<T><<<grid, 128, 0, st>>>(W, nlines, n, A, sa, sb, st_, vstride, lamA, lamB, (T)h2, (T)gscale);
     FDM_LAUNCH_CHECK();
+}
+
+template <typename T, int m>
+static void launch_zpart(T* W, int nx, int ny, int P, long long vstride, int nvol, const T* lamx, const T* lamy,
+                         double h2, double gscale, cudaStream_t st) {
+    const size_t smem = (size_t)4 * P * 32 * sizeof(T);
+    dim3 grid((unsigned)(ny * ((nx + 31) / 32)), nvol);
+    FDM_TIMED(sizeof(T) == 8 ? "zsolve_f64" : "zsolve_f32", st);
+    k_zsolve_part<T, m><<<grid, 32 * P, smem, st>>>(W, nx, ny, P, vstride, lamx, lamy, (T)h2, (T)gscale);
+    FDM_LAUNCH_CHECK();
+}
+
+// Tridiagonal solves along z of every (x-mode, y-mode) line: the partitioned
+// kernel when the line splits into at most 16 blocks of 2^k-1 rows, the
+// one-thread-per-line kernel otherwise.
+template <typename T>
+static void zsolve_lines(T* W, int nx, int ny, int nz, int nvol, const T* lamx, const T* lamy, double h2,
+                         double gscale, cudaStream_t st) {
+    const int mmax = sizeof(T) == 4 ? 31 : 15;
+    const int m = nz < mmax ? nz : mmax;
+    const int P = (nz + 1) / (m + 1);
+    const long long vs = (long long)nx * ny * nz;
+    const int maxP = (m * (int)sizeof(T) >= 31 * 4 ? 256 : 512) / 32;
+    if (P <= maxP && (m + 1) * P == nz + 1) {
+        switch (m) {
+            case 1: return launch_zpart<T, 1>(W, nx, ny, P, vs, nvol, lamx, lamy, h2, gscale, st);
+            case 3: return launch_zpart<T, 3>(W, nx, ny, P, vs, nvol, lamx, lamy, h2, gscale, st);
+            case 7: return launch_zpart<T, 7>(W, nx, ny, P, vs, nvol, lamx, lamy, h2, gscale, st);
+            case 15: return launch_zpart<T, 15>(W, nx, ny, P, vs, nvol, lamx, lamy, h2, gscale, st);
+            case 31:
+                if (sizeof(T) == 4) return launch_zpart<T, sizeof(T) == 4 ? 31 : 15>(W, nx, ny, P, vs, nvol, lamx,
+                                                                                     lamy, h2, gscale, st);
+                break;
+            default: break;
+        }
+    }
+    launch_tridiag<T>(W, nx * ny, nz, nx, 1, nx, (long long)nx * ny, vs, nvol, lamx, lamy, h2, gscale, st);
 }
 
 static void check_grid_y(int nrhs) {
@@ -149,7 +197,7 @@ struct CubePlan {
     AxisTables<double> tx64, ty64;
     AxisTables<float> tx32, ty32;
     DevBuf lamx64, lamy64, lamx32, lamy32;
-    DevBuf work32, uhi, ulo, corr, norms;
+    DevBuf work32, uhi, ulo, norms;
     DevBuf hin, hout;
     int last_sweeps = 0, last_nrhs = 0;
     cudaStream_t last_stream = 0;
@@ -190,16 +238,16 @@ struct CubePlan {
 
     long long vol() const { return (long long)nx * ny * nz; }
 
-    template <typename Tin, typename T, typename Tout>
+    template <typename Tin, typename T, int MODE = kPlain>
     void forward_xy(const Tin* in, T* W, int nrhs, const AxisTables<T>& tx, const AxisTables<T>& ty,
-                    cudaStream_t st) {
-        launch_sine<Tin, T, T, 0>(in, W, nx, ny, nz, nrhs, tx.view(), scx, st);
+                    cudaStream_t st, const SineFused* fu = nullptr) {
+        launch_sine<Tin, T, T, 0, MODE>(in, W, nx, ny, nz, nrhs, tx.view(), scx, st, fu);
         launch_sine<T, T, T, 1>(W, W, nx, ny, nz, nrhs, ty.view(), scy, st);
     }
     template <typename T>
     void zsolve(T* W, int nrhs, const DevBuf& lx_, const DevBuf& ly_, cudaStream_t st) {
-        launch_tridiag<T>(W, nx * ny, nz, nx, 1, nx, (long long)nx * ny, vol(), nrhs, (const T*)lx_.p,
-                          (const T*)ly_.p, hz_eff * hz_eff, zfac * hz_eff * hz_eff, st);
+        zsolve_lines<T>(W, nx, ny, nz, nrhs, (const T*)lx_.p, (const T*)ly_.p, hz_eff * hz_eff,
+                        zfac * hz_eff * hz_eff, st);
     }
 
     void solve_device(void* ans, const void* rhs, int nrhs, cudaStream_t st) {
@@ -219,7 +267,7 @@ struct CubePlan {
     template <typename T>
     void run_plain(T* ans, const T* rhs, int nrhs, const AxisTables<T>& tx, const AxisTables<T>& ty,
                    const DevBuf& lx_, const DevBuf& ly_, cudaStream_t st) {
-        forward_xy<T, T, T>(rhs, ans, nrhs, tx, ty, st);
+        forward_xy<T, T>(rhs, ans, nrhs, tx, ty, st);
         zsolve<T>(ans, nrhs, lx_, ly_, st);
         launch_sine<T, T, T, 1>(ans, ans, nx, ny, nz, nrhs, ty.view(), sly, st);
         launch_sine<T, T, T, 0>(ans, ans, nx, ny, nz, nrhs, tx.view(), slx, st);
@@ -230,13 +278,18 @@ struct CubePlan {
         return s < max_sweeps ? s : max_sweeps;
     }
 
+    static ff split_host(double v) {
+        const float h = (float)v;
+        return ff{h, (float)(v - (double)h)};
+    }
+
     void run_mixed(double* ans, const double* rhs, int nrhs, cudaStream_t st) {
         ensure_mixed_tables();
         const long long V = vol() * nrhs;
         const int sweeps = sweeps_for_tol();
         last_sweeps = sweeps;
         float* W = (float*)work32.get(V * sizeof(float));
-        forward_xy<double, float, float>(rhs, W, nrhs, tx32, ty32, st);
+        forward_xy<double, float, kRound>(rhs, W, nrhs, tx32, ty32, st);
         zsolve<float>(W, nrhs, lamx32, lamy32, st);
         launch_sine<float, float, float, 1>(W, W, nx, ny, nz, nrhs, ty32.view(), sly, st);
         if (sweeps == 0) {
@@ -244,39 +297,39 @@ struct CubePlan {
             return;
         }
         float* UH = (float*)uhi.get(V * sizeof(float));
-        float* C = (float*)corr.get(V * sizeof(float));
         float* UL = sweeps > 1 ? (float*)ulo.get(V * sizeof(float)) : nullptr;
         double* NR = (double*)norms.get((size_t)2 * nrhs * sweeps * sizeof(double));
         FDM_CUDA(cudaMemsetAsync(NR, 0, (size_t)2 * nrhs * sweeps * sizeof(double), st));
         launch_sine<float, float, float, 0>(W, UH, nx, ny, nz, nrhs, tx32.view(), slx, st);
-        const double cx = 1.0 / (hx_eff * hx_eff), cy = 1.0 / (dy * dy), cz = 1.0 / (hz_eff * hz_eff);
-        const long long vstride = vol();
+        // r = f - A u / S: the inner solve multiplies by S again, so it
+        // returns the correction S A^-1 f - u
+        const double cx = 1.0 / (hx_eff * hx_eff) / S, cy = 1.0 / (dy * dy) / S, cz = 1.0 / (hz_eff * hz_eff) / S;
         for (int s = 1; s <= sweeps; s++) {
-            const float* ul_in = s >= 2 ? UL : nullptr;
-            {
-                dim3 grid((unsigned)((vol() + 255) / 256), nrhs);
-                FDM_TIMED("residual", st);
-                k_residual_f64<<<grid, 256, 0, st>>>(rhs, UH, ul_in, W, nx, ny, nz, vstride, 1.0 / S, cx, cy, cz);
-                FDM_LAUNCH_CHECK();
-            }
-            // r = f - A u / S: the inner solve multiplies by S again, so it
-            // returns the correction S A^-1 f - u
-            forward_xy<float, float, float>(W, W, nrhs, tx32, ty32, st);
+            SineFused fr;
+            memset(&fr, 0, sizeof(fr));
+            fr.f = rhs;
+            fr.uhi = UH;
+            fr.ulo = s >= 2 ? UL : nullptr;
+            fr.cx = split_host(cx); fr.cy = split_host(cy); fr.cz = split_host(cz);
+            fr.cxf = (float)cx; fr.cyf = (float)cy; fr.czf = (float)cz;
+            forward_xy<float, float, kResidual>(nullptr, W, nrhs, tx32, ty32, st, &fr);
             zsolve<float>(W, nrhs, lamx32, lamy32, st);
             launch_sine<float, float, float, 1>(W, W, nx, ny, nz, nrhs, ty32.view(), sly, st);
-            launch_sine<float, float, float, 0>(W, C, nx, ny, nz, nrhs, tx32.view(), slx, st);
-            {
-                dim3 grid((unsigned)((vol() + 255) / 256), nrhs);
-                FDM_TIMED("combine", st);
-                k_combine<<<grid, 256, 0, st>>>(UH, ul_in, C, ans, UL, vol(), vstride, s == sweeps ? 1 : 0,
-                                                NR + (size_t)2 * nrhs * (s - 1));
-                FDM_LAUNCH_CHECK();
-            }
+            SineFused fc;
+            memset(&fc, 0, sizeof(fc));
+            fc.uhi = UH;
+            fc.ulo = s >= 2 ? UL : nullptr;
+            fc.out64 = ans;
+            fc.ulo_out = UL;
+            fc.last = s == sweeps ? 1 : 0;
+            fc.norms = NR + (size_t)2 * nrhs * (s - 1);
+            launch_sine<float, float, float, 0, kCombine>(W, (float*)nullptr, nx, ny, nz, nrhs, tx32.view(), slx,
+                                                          st, &fc);
         }
     }
 
     size_t scratch_bytes() const {
-        return work32.bytes + uhi.bytes + ulo.bytes + corr.bytes + norms.bytes + hin.bytes + hout.bytes;
+        return work32.bytes + uhi.bytes + ulo.bytes + norms.bytes + hin.bytes + hout.bytes;
     }
 };
 

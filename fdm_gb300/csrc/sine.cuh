@@ -11,12 +11,17 @@
 //   2. a radix-4 (+ one radix-2) Stockham complex FFT of length M = N/2 in
 //      shared memory (the real DFT packed as y_{2m} + i y_{2m+1}),
 //   3. the real-DFT unpack, where F[2k] = -Im Y_k and the odd outputs are a
-//      prefix sum F[2k+1] = F[2k-1] + Re Y_k, done with a segmented warp scan.
+//      prefix sum F[2k+1] = F[2k-1] + Re Y_k (segmented warp scan).
 // Twiddle and weight tables are computed in FP64 on the host and rounded to
 // the compute type once.
+//
+// Shared-memory layouts are skewed (one pad slot every 16 complex / 32 real
+// entries) so that the contiguous per-thread blocks of the unpack and prefix
+// sum fall into distinct banks.
 #pragma once
 
 #include "common.cuh"
+#include "dd.cuh"
 
 namespace fdmgpu {
 
@@ -30,25 +35,47 @@ struct SineTables {
     int N, M;
 };
 
-// Complex elements per line in each of the two shared buffers.  The +8 pad
-// makes consecutive lines start 8 complex elements apart modulo 16, so the
-// two lines of a half-warp never share a bank pair.
-__host__ __device__ inline int sine_line_stride(int M) { return M + 8; }
-
-// Reals per line in the staging view of the buffers (x[0..N], F[1..N-1]).
-// N+1 is odd, so a column-wise (transposed) access by consecutive threads
-// hits distinct banks.
-__host__ __device__ inline int sine_stage_stride(int N) { return N + 1; }
+// complex slots per line of a Stockham buffer: holds M entries skewed by
+// k + k/16, and is 8 (mod 16) so the two lines of a half-warp use disjoint
+// bank pairs
+__host__ __device__ inline int sine_line_stride(int M) {
+    int S = M + M / 16 + 1;
+    while (S % 16 != 8) S++;
+    return S;
+}
+__host__ __device__ __forceinline__ int skew_c(int k) { return k + (k >> 4); }
+// reals per line of the staging view (x[0..N] / F[1..N-1], skewed by i/32);
+// odd, so transposed accesses by consecutive threads hit distinct banks
+__host__ __device__ inline int sine_stage_stride(int N) {
+    int SX = N + N / 32 + 2;
+    if (SX % 2 == 0) SX++;
+    return SX;
+}
+__host__ __device__ __forceinline__ int skew_r(int i) { return i + (i >> 5); }
 
 template <typename T>
 __host__ __device__ inline size_t sine_smem_bytes(int N, int L) {
     return 2ull * L * sine_line_stride(N / 2) * sizeof(vec2_t<T>);
 }
 
+// x / d for 0 <= x < 2^31 by multiply-high (Granlund-Montgomery round-up
+// method).
+struct FastDiv {
+    unsigned d, m, s;
+    FastDiv() : d(1), m(0), s(0) {}
+    explicit FastDiv(unsigned div) : d(div) {
+        s = 0;
+        while ((1u << s) < d) s++;
+        m = (unsigned)((((unsigned long long)1 << 32) * ((1ull << s) - d)) / d + 1);
+    }
+    __device__ __forceinline__ unsigned div(unsigned x) const { return (__umulhi(x, m) + x) >> s; }
+};
+
 // Runs the transform of every line held by this CTA.  On entry the staging
-// view of buffer B holds x[1..n] of line l at stage(B) + l*SX + 1 (entries 0
-// and N must be zero).  On exit the result F[1..n] (unscaled) sits in the
-// staging view of the buffer returned.  All threads of the CTA must call it.
+// view of buffer B holds x[1..n] of line l at stage(B) + l*SX + skew_r(j)
+// (entries 0 and N zero).  On exit the unscaled result F[1..n] sits in the
+// staging view of the buffer returned, same skewed indexing.  All threads of
+// the CTA must call it.
 template <typename T>
 __device__ T* sine_block(vec2_t<T>* A, vec2_t<T>* B, const SineTables<T>& tb, int l, int g) {
     using T2 = vec2_t<T>;
@@ -64,24 +91,25 @@ __device__ T* sine_block(vec2_t<T>* A, vec2_t<T>* B, const SineTables<T>& tb, in
             const int j0 = 2 * m, j1 = 2 * m + 1;
             T y0 = T(0);
             if (m > 0) {
-                T a = X[j0], b = X[N - j0];
+                T a = X[skew_r(j0)], b = X[skew_r(N - j0)];
                 y0 = ldg(tb.wpre + j0) * (a + b) + half * (a - b);
             }
-            T a = X[j1], b = X[N - j1];
+            T a = X[skew_r(j1)], b = X[skew_r(N - j1)];
             T y1 = ldg(tb.wpre + j1) * (a + b) + half * (a - b);
             T2 v; v.x = y0; v.y = y1;
-            Al[m] = v;
+            Al[m] = v;  // M == 1: no passes, and skew_c(0) == 0
         }
     }
     __syncthreads();
 
-    // 2. Stockham passes, A -> B -> A ...
+    // 2. Stockham passes, A -> B -> A ...; the last pass writes skewed
     T2* src = A;
     T2* dst = B;
     for (int Ns = 1; Ns < M;) {
         const int R = ((M / Ns) % 4 == 0) ? 4 : 2;
         const int MR = M / R;
         const int twstep = M / (Ns * R);
+        const bool last = Ns * R == M;
         const T2* s = src + (size_t)l * S;
         T2* d = dst + (size_t)l * S;
         for (int j = g; j < MR; j += kGroup) {
@@ -96,15 +124,24 @@ __device__ T* sine_block(vec2_t<T>* A, vec2_t<T>* B, const SineTables<T>& tb, in
                 }
                 T2 a0 = cadd<T>(v0, v2), a1 = csub<T>(v0, v2);
                 T2 b0 = cadd<T>(v1, v3), b1 = cmul_mi<T>(csub<T>(v1, v3));
-                d[base] = cadd<T>(a0, b0);
-                d[base + Ns] = cadd<T>(a1, b1);
-                d[base + 2 * Ns] = csub<T>(a0, b0);
-                d[base + 3 * Ns] = csub<T>(a1, b1);
+                if (last) {
+                    d[skew_c(base)] = cadd<T>(a0, b0);
+                    d[skew_c(base + Ns)] = cadd<T>(a1, b1);
+                    d[skew_c(base + 2 * Ns)] = csub<T>(a0, b0);
+                    d[skew_c(base + 3 * Ns)] = csub<T>(a1, b1);
+                } else {
+                    d[base] = cadd<T>(a0, b0);
+                    d[base + Ns] = cadd<T>(a1, b1);
+                    d[base + 2 * Ns] = csub<T>(a0, b0);
+                    d[base + 3 * Ns] = csub<T>(a1, b1);
+                }
             } else {
                 T2 v0 = s[j], v1 = s[j + MR];
                 if (k) v1 = cmul<T>(v1, ldg(tb.tw + k * twstep));
-                d[base] = cadd<T>(v0, v1);
-                d[base + Ns] = csub<T>(v0, v1);
+                const int o0 = last ? skew_c(base) : base;
+                const int o1 = last ? skew_c(base + Ns) : base + Ns;
+                d[o0] = cadd<T>(v0, v1);
+                d[o1] = csub<T>(v0, v1);
             }
         }
         __syncwarp();
@@ -121,16 +158,16 @@ __device__ T* sine_block(vec2_t<T>* A, vec2_t<T>* B, const SineTables<T>& tb, in
     const int k1 = min(M, k0 + kb);
     T sum = T(0);
     for (int k = k0; k < k1; k++) {
-        const T2 ck = C[k];
-        const T2 cm = C[(M - k) & (M - 1)];
+        const T2 ck = C[skew_c(k)];
+        const T2 cm = C[skew_c((M - k) & (M - 1))];
         T ex = T(0.5) * (ck.x + cm.x), ey = T(0.5) * (ck.y - cm.y);
         T ox = T(0.5) * (ck.y + cm.y), oy = T(-0.5) * (ck.x - cm.x);
         const T2 w = ldg(tb.post + k);
         T yr = ex + (w.x * ox - w.y * oy);
         T yi = ey + (w.x * oy + w.y * ox);
         if (k == 0) yr *= T(0.5);
-        else F[2 * k] = -yi;
-        F[2 * k + 1] = yr;
+        else F[skew_r(2 * k)] = -yi;
+        F[skew_r(2 * k + 1)] = yr;
         sum += yr;
     }
     T incl = sum;
@@ -141,25 +178,86 @@ __device__ T* sine_block(vec2_t<T>* A, vec2_t<T>* B, const SineTables<T>& tb, in
     }
     T run = incl - sum;
     for (int k = k0; k < k1; k++) {
-        run += F[2 * k + 1];
-        F[2 * k + 1] = run;
+        run += F[skew_r(2 * k + 1)];
+        F[skew_r(2 * k + 1)] = run;
     }
     __syncthreads();
     return reinterpret_cast<T*>(dst);
+}
+
+// What a pass does around the transform.
+enum SineMode {
+    kPlain = 0,    // load Tin -> T, store T -> Tout
+    kRound = 1,    // load FP64 -> FP32 by integer rounding (first pass of the mixed solve)
+    kResidual = 2, // load r = f - A(uhi + ulo) in float-float (first pass of a refinement sweep)
+    kCombine = 3   // store u = uhi + ulo + c to FP64, or ulo += c (last pass of a sweep)
+};
+
+struct SineFused {
+    // kResidual
+    const double* f;
+    const float* uhi;
+    const float* ulo;
+    ff cx, cy, cz;        // stencil coefficients 1/h^2 / S as float pairs
+    float cxf, cyf, czf;  // the same rounded to float (for A ulo)
+    // kCombine
+    double* out64;
+    float* ulo_out;
+    int last;
+    double* norms;  // per volume: ||c||^2, ||u||^2
+};
+
+struct SineGeom {
+    int nx, ny, nz;
+    long long vstride;
+    int L, Lshift;
+    FastDiv div_n;   // by the line length n
+    FastDiv div_ny;  // rows -> (z, y)
+};
+
+constexpr int kLoadBatch = 8;
+
+// r = f - A(uhi + ulo) at one interior point (x fastest index idx), zero
+// outside the box.  A U is formed exactly enough in float-float; A ulo in
+// FP32 (it is ~1e-7 of A U).
+__device__ __forceinline__ float residual_at(const SineFused& fu, long long idx, int x, int y, int z, int nx,
+                                             int ny, int nz) {
+    const long long sy = nx, sz = (long long)nx * ny;
+    const float* U = fu.uhi;
+    const float uc = U[idx];
+    const float xm = x > 0 ? U[idx - 1] : 0.f, xp = x < nx - 1 ? U[idx + 1] : 0.f;
+    const float ym = y > 0 ? U[idx - sy] : 0.f, yp = y < ny - 1 ? U[idx + sy] : 0.f;
+    const float zm = z > 0 ? U[idx - sz] : 0.f, zp = z < nz - 1 ? U[idx + sz] : 0.f;
+    const ff fsp = f64_split(fu.f[idx]);
+    const float u2 = uc + uc;  // exact
+    ff dx = ff_add_f(two_sum(xm, xp), -u2);
+    ff dy = ff_add_f(two_sum(ym, yp), -u2);
+    ff dz = ff_add_f(two_sum(zm, zp), -u2);
+    ff au = ff_add(ff_add(ff_mul(dx, fu.cx), ff_mul(dy, fu.cy)), ff_mul(dz, fu.cz));
+    float alo = 0.f;
+    if (fu.ulo) {
+        const float* V = fu.ulo;
+        const float vc = V[idx];
+        const float vxm = x > 0 ? V[idx - 1] : 0.f, vxp = x < nx - 1 ? V[idx + 1] : 0.f;
+        const float vym = y > 0 ? V[idx - sy] : 0.f, vyp = y < ny - 1 ? V[idx + sy] : 0.f;
+        const float vzm = z > 0 ? V[idx - sz] : 0.f, vzp = z < nz - 1 ? V[idx + sz] : 0.f;
+        alo = fu.cxf * ((vxm + vxp) - 2.f * vc) + fu.cyf * ((vym + vyp) - 2.f * vc) + fu.czf * ((vzm + vzp) - 2.f * vc);
+    }
+    ff r = ff_add(fsp, ff{-au.h, -au.l});
+    return (r.h + (r.l - alo));
 }
 
 // One DST pass over every line along x (AXIS 0, rows) or along y (AXIS 1,
 // columns) of a batch of nz*ny*nx volumes (x fastest), out-of-place or
 // in-place.  Rows: a CTA takes L consecutive rows.  Columns: a CTA takes a
 // tile of L consecutive x at one z, all y.  gridDim.y indexes the volume.
-// Loads convert Tin -> T, stores T -> Tout after multiplying by `scale`.
-template <typename Tin, typename T, typename Tout, int AXIS>
-__global__ void __launch_bounds__(256) k_sine_pass(const Tin* in, Tout* out,
-                                                   int nx, int ny, int nz, long long vstride,
-                                                   SineTables<T> tb, T scale, int L, int Lshift) {
+template <typename Tin, typename T, typename Tout, int AXIS, int MODE>
+__global__ void __launch_bounds__(256) k_sine_pass(const Tin* in, Tout* out, SineGeom geo, SineTables<T> tb,
+                                                   T scale, SineFused fu) {
     using T2 = vec2_t<T>;
     extern __shared__ __align__(16) unsigned char smem_raw[];
-    const int M = tb.M, N = tb.N;
+    const int M = tb.M, N = tb.N, L = geo.L;
+    const int nx = geo.nx, ny = geo.ny, nz = geo.nz;
     T2* A = reinterpret_cast<T2*>(smem_raw);
     T2* B = A + (size_t)L * sine_line_stride(M);
     T* XB = reinterpret_cast<T*>(B);
@@ -167,45 +265,88 @@ __global__ void __launch_bounds__(256) k_sine_pass(const Tin* in, Tout* out,
     const int tid = threadIdx.x;
     const int nthr = blockDim.x;
     const int l = tid / kGroup, g = tid % kGroup;
-    const long long voff = (long long)blockIdx.y * vstride;
-    in += voff;
-    out += voff;
+    const long long voff = (long long)blockIdx.y * geo.vstride;
 
     int n, row0 = 0, nact, x0 = 0, z = 0;
     if (AXIS == 0) {
         n = nx;
-        const int lines = ny * nz;
         row0 = blockIdx.x * L;
-        nact = min(L, lines - row0);
+        nact = min(L, ny * nz - row0);
     } else {
         n = ny;
-        const int ntx = (nx + L - 1) >> Lshift;
+        const int ntx = (nx + L - 1) >> geo.Lshift;
         z = blockIdx.x / ntx;
-        x0 = (blockIdx.x - z * ntx) << Lshift;
+        x0 = (blockIdx.x - z * ntx) << geo.Lshift;
         nact = min(L, nx - x0);
     }
 
-    // zero the ends of every staged line
     for (int i = tid; i < L; i += nthr) {
         XB[(size_t)i * SX] = T(0);
-        XB[(size_t)i * SX + N] = T(0);
+        XB[(size_t)i * SX + skew_r(N)] = T(0);
     }
     if (AXIS == 0) {
         const int total = nact * n;
-        const Tin* src = in + (long long)row0 * n;
-        for (int e = tid; e < total; e += nthr) {
-            const int r = e / n, c = e - r * n;
-            XB[(size_t)r * SX + c + 1] = T(src[e]);
+        const long long base = voff + (long long)row0 * n;
+        for (int e0 = tid; e0 < total; e0 += kLoadBatch * nthr) {
+            T v[kLoadBatch];
+            if (MODE == kResidual) {
+#pragma unroll 2
+                for (int q = 0; q < kLoadBatch; q++) {
+                    const int e = e0 + q * nthr;
+                    if (e < total) {
+                        const int r = geo.div_n.div(e), c = e - r * n;
+                        const int R = row0 + r;
+                        const int zz = geo.div_ny.div(R), yy = R - zz * ny;
+                        SineFused f2 = fu;
+                        f2.f += voff;
+                        f2.uhi += voff;
+                        if (f2.ulo) f2.ulo += voff;
+                        v[q] = T(residual_at(f2, (long long)R * n + c, c, yy, zz, nx, ny, nz));
+                    }
+                }
+            } else {
+#pragma unroll
+                for (int q = 0; q < kLoadBatch; q++) {
+                    const int e = e0 + q * nthr;
+                    if (e < total) {
+                        if (MODE == kRound) v[q] = T(f64_to_f32((double)in[base + e]));
+                        else v[q] = T(in[base + e]);
+                    }
+                }
+            }
+#pragma unroll
+            for (int q = 0; q < kLoadBatch; q++) {
+                const int e = e0 + q * nthr;
+                if (e < total) {
+                    const int r = geo.div_n.div(e), c = e - r * n;
+                    XB[(size_t)r * SX + skew_r(c + 1)] = v[q];
+                }
+            }
         }
         for (int e = nact * SX + tid; e < L * SX; e += nthr) XB[e] = T(0);
     } else {
-        const int total = n << Lshift;
-        const Tin* src = in + ((long long)z * ny) * nx + x0;
-        for (int e = tid; e < total; e += nthr) {
-            const int y = e >> Lshift, c = e & (L - 1);
-            T v = T(0);
-            if (c < nact) v = T(src[(long long)y * nx + c]);
-            XB[(size_t)c * SX + y + 1] = v;
+        const int total = n << geo.Lshift;
+        const long long base = voff + ((long long)z * ny) * nx + x0;
+        for (int e0 = tid; e0 < total; e0 += kLoadBatch * nthr) {
+            T v[kLoadBatch];
+#pragma unroll
+            for (int q = 0; q < kLoadBatch; q++) {
+                const int e = e0 + q * nthr;
+                const int y = e >> geo.Lshift, c = e & (L - 1);
+                v[q] = T(0);
+                if (e < total && c < nact) {
+                    if (MODE == kRound) v[q] = T(f64_to_f32((double)in[base + (long long)y * nx + c]));
+                    else v[q] = T(in[base + (long long)y * nx + c]);
+                }
+            }
+#pragma unroll
+            for (int q = 0; q < kLoadBatch; q++) {
+                const int e = e0 + q * nthr;
+                if (e < total) {
+                    const int y = e >> geo.Lshift, c = e & (L - 1);
+                    XB[(size_t)c * SX + skew_r(y + 1)] = v[q];
+                }
+            }
         }
     }
     __syncthreads();
@@ -214,17 +355,56 @@ __global__ void __launch_bounds__(256) k_sine_pass(const Tin* in, Tout* out,
 
     if (AXIS == 0) {
         const int total = nact * n;
-        Tout* dstp = out + (long long)row0 * n;
-        for (int e = tid; e < total; e += nthr) {
-            const int r = e / n, c = e - r * n;
-            dstp[e] = Tout(scale * F[(size_t)r * SX + c + 1]);
+        const long long base = voff + (long long)row0 * n;
+        if (MODE == kCombine) {
+            float cc = 0.f, uu = 0.f;
+            for (int e = tid; e < total; e += nthr) {
+                const int r = geo.div_n.div(e), c = e - r * n;
+                const float cv = (float)(scale * F[(size_t)r * SX + skew_r(c + 1)]);
+                const long long idx = base + e;
+                const float h = fu.uhi[idx];
+                const float lo = fu.ulo ? fu.ulo[idx] : 0.f;
+                ff s = two_sum(h, lo);
+                s = ff_add_f(s, cv);
+                if (fu.last) fu.out64[idx] = ff_to_f64(s);
+                else fu.ulo_out[idx] = lo + cv;
+                cc += cv * cv;
+                uu += s.h * s.h;
+            }
+            // per-CTA reduction, one FP64 atomic per CTA and quantity
+            for (int o = 16; o > 0; o >>= 1) {
+                cc += __shfl_down_sync(0xffffffffu, cc, o);
+                uu += __shfl_down_sync(0xffffffffu, uu, o);
+            }
+            __shared__ float red[2][32];
+            const int w = tid >> 5, ln = tid & 31;
+            if (ln == 0) { red[0][w] = cc; red[1][w] = uu; }
+            __syncthreads();
+            if (w == 0) {
+                const int nw = nthr >> 5;
+                cc = ln < nw ? red[0][ln] : 0.f;
+                uu = ln < nw ? red[1][ln] : 0.f;
+                for (int o = 16; o > 0; o >>= 1) {
+                    cc += __shfl_down_sync(0xffffffffu, cc, o);
+                    uu += __shfl_down_sync(0xffffffffu, uu, o);
+                }
+                if (ln == 0 && fu.norms) {
+                    atomicAdd(&fu.norms[2 * blockIdx.y], (double)cc);
+                    atomicAdd(&fu.norms[2 * blockIdx.y + 1], (double)uu);
+                }
+            }
+        } else {
+            for (int e = tid; e < total; e += nthr) {
+                const int r = geo.div_n.div(e), c = e - r * n;
+                out[base + e] = Tout(scale * F[(size_t)r * SX + skew_r(c + 1)]);
+            }
         }
     } else {
-        const int total = n << Lshift;
-        Tout* dstp = out + ((long long)z * ny) * nx + x0;
+        const int total = n << geo.Lshift;
+        const long long base = voff + ((long long)z * ny) * nx + x0;
         for (int e = tid; e < total; e += nthr) {
-            const int y = e >> Lshift, c = e & (L - 1);
-            if (c < nact) dstp[(long long)y * nx + c] = Tout(scale * F[(size_t)c * SX + y + 1]);
+            const int y = e >> geo.Lshift, c = e & (L - 1);
+            if (c < nact) out[base + (long long)y * nx + c] = Tout(scale * F[(size_t)c * SX + skew_r(y + 1)]);
         }
     }
 }

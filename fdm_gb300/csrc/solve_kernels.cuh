@@ -115,73 +115,97 @@ __global__ void k_tridiag_general(int n, int nsys, const T* lower, const T* diag
     }
 }
 
-// r = f - inv_s * A(uhi + ulo) for the 7-point operator
-// A u = cx(u[j-1] - 2u + u[j+1]) + cy(...) + cz(...), zero outside the box.
-// FP64 arithmetic; r rounded to FP32.  ulo may be null.
-__global__ void k_residual_f64(const double* __restrict__ f, const float* __restrict__ uhi,
-                               const float* __restrict__ ulo, float* __restrict__ r, int nx, int ny, int nz,
-                               long long vstride, double inv_s, double cx, double cy, double cz) {
-    const long long vol = (long long)nx * ny * nz;
-    const long long idx = (long long)blockIdx.x * blockDim.x + threadIdx.x;
-    if (idx >= vol) return;
-    const long long off = (long long)blockIdx.y * vstride;
-    const int j = idx % nx;
-    const long long t = idx / nx;
-    const int k = t % ny;
-    const int i = t / ny;
-    const long long sy = nx, sz = (long long)nx * ny;
-    auto U = [&](long long o) -> double {
-        double v = (double)uhi[off + o];
-        if (ulo) v += (double)ulo[off + o];
-        return v;
-    };
-    const double uc = U(idx);
-    const double xm = j > 0 ? U(idx - 1) : 0.0, xp = j < nx - 1 ? U(idx + 1) : 0.0;
-    const double ym = k > 0 ? U(idx - sy) : 0.0, yp = k < ny - 1 ? U(idx + sy) : 0.0;
-    const double zm = i > 0 ? U(idx - sz) : 0.0, zp = i < nz - 1 ? U(idx + sz) : 0.0;
-    const double au = cx * ((xm + xp) - 2.0 * uc) + cy * ((ym + yp) - 2.0 * uc) + cz * ((zm + zp) - 2.0 * uc);
-    r[off + idx] = (float)(f[off + idx] - inv_s * au);
-}
+// Partitioned tridiagonal solve along z for the (x-mode, y-mode) lines of
+// a batch of volumes (x fastest, line stride nx*ny): the same Dirichlet
+// systems as k_tridiag_const,
+//     u[i-1] + b u[i] + u[i+1] = gscale * g[i],  b = -2 - (lamx[x] + lamy[y]) h2,
+// for n = P(m+1) - 1 rows (n+1 and m+1 powers of two).  The line is cut by
+// P-1 separator rows (row c(m+1)+m) into P blocks of m rows.  Warp c of the
+// CTA owns block c for 32 consecutive x: it loads its m rows coalesced into
+// registers and solves the block with zero ends (v) and the responses to a
+// unit value at either end (beta at the right end; by persymmetry of the
+// constant-coefficient block the left-end response is beta reversed).  The
+// separator values then satisfy a constant-coefficient tridiagonal system of
+// P-1 unknowns,
+//     beta_0 s[c-1] + (b + 2 beta_{m-1}) s[c] + beta_0 s[c+1]
+//         = g(sep_c) - v^c_{m-1} - v^{c+1}_0,
+// which one lane per column solves from shared memory; each block then adds
+// the end responses and stores.  Every value is read and written once.
+template <typename T, int m>
+constexpr int zpart_max_threads() { return m * sizeof(T) >= 31 * 4 ? 256 : 512; }
 
-// Last refinement sweep: out = uhi + ulo_in + c in FP64; otherwise
-// ulo_out = ulo_in + c in FP32 (ulo_in may be null = zero).
-// Accumulates ||c||^2 and ||u||^2 per volume into norms[2*v], norms[2*v+1].
-__global__ void k_combine(const float* __restrict__ uhi, const float* ulo_in, const float* __restrict__ c,
-                          double* __restrict__ out, float* ulo_out, long long vol, long long vstride, int last,
-                          double* __restrict__ norms) {
-    const long long idx = (long long)blockIdx.x * blockDim.x + threadIdx.x;
-    const long long off = (long long)blockIdx.y * vstride;
-    double cc = 0.0, uu = 0.0;
-    if (idx < vol) {
-        const float cf = c[off + idx];
-        const float lo = ulo_in ? ulo_in[off + idx] : 0.f;
-        const double ch = (double)cf;
-        const double u = (double)uhi[off + idx] + (double)lo + ch;
-        if (last) out[off + idx] = u;
-        else ulo_out[off + idx] = lo + cf;
-        cc = ch * ch;
-        uu = u * u;
+template <typename T, int m>
+__global__ void __launch_bounds__(zpart_max_threads<T, m>()) k_zsolve_part(T* W, int nx, int ny, int P, long long vstride,
+                                                     const T* lamx, const T* lamy, T h2, T gscale) {
+    extern __shared__ __align__(16) unsigned char zsm[];
+    T* s_vf = reinterpret_cast<T*>(zsm);  // [P][32] first row of v per block
+    T* s_vl = s_vf + P * 32;               // [P][32] last row of v
+    T* s_g = s_vl + P * 32;                // [P][32] separator right-hand sides
+    T* s_u = s_g + P * 32;                 // [P][32] separator solutions
+    const int lane = threadIdx.x & 31;
+    const int c = threadIdx.x >> 5;
+    const int ntx = (nx + 31) >> 5;
+    const int y = blockIdx.x / ntx;
+    const int x = ((blockIdx.x - y * ntx) << 5) + lane;
+    const bool act = x < nx;
+    const long long st = (long long)nx * ny;
+    T* p = W + (long long)blockIdx.y * vstride + (long long)y * nx + (act ? x : 0);
+    const T b = act ? T(-2) - (lamx[x] + lamy[y]) * h2 : T(-4);
+    const int r0 = c * (m + 1);
+
+    T v[m], cp[m], be[m];
+#pragma unroll
+    for (int i = 0; i < m; i++) v[i] = act ? p[(r0 + i) * st] : T(0);
+    T gsep = T(0);
+    if (c < P - 1 && act) gsep = p[(r0 + m) * st];
+    // forward elimination
+    T prev_c = T(0), prev_d = T(0);
+#pragma unroll
+    for (int i = 0; i < m; i++) {
+        const T r = T(1) / (b - prev_c);
+        cp[i] = r;
+        prev_d = (v[i] * gscale - prev_d) * r;
+        v[i] = prev_d;
+        prev_c = r;
     }
-    for (int o = 16; o > 0; o >>= 1) {
-        cc += __shfl_down_sync(0xffffffffu, cc, o);
-        uu += __shfl_down_sync(0xffffffffu, uu, o);
+    // back substitution for v and the right-end response beta
+    T bv = -cp[m - 1];
+    be[m - 1] = bv;
+#pragma unroll
+    for (int i = m - 2; i >= 0; i--) {
+        v[i] = v[i] - cp[i] * v[i + 1];
+        bv = -cp[i] * bv;
+        be[i] = bv;
     }
-    __shared__ double red[2][32];
-    const int w = threadIdx.x >> 5, ln = threadIdx.x & 31;
-    if (ln == 0) { red[0][w] = cc; red[1][w] = uu; }
+    s_vf[c * 32 + lane] = v[0];
+    s_vl[c * 32 + lane] = v[m - 1];
+    s_g[c * 32 + lane] = gsep * gscale;
     __syncthreads();
-    if (w == 0) {
-        const int nw = blockDim.x >> 5;
-        cc = ln < nw ? red[0][ln] : 0.0;
-        uu = ln < nw ? red[1][ln] : 0.0;
-        for (int o = 16; o > 0; o >>= 1) {
-            cc += __shfl_down_sync(0xffffffffu, cc, o);
-            uu += __shfl_down_sync(0xffffffffu, uu, o);
+    if (c == 0 && P > 1) {
+        // separators: constant-coefficient Thomas, P-1 rows
+        const T lo = be[0], dg = b + T(2) * be[m - 1];
+        T pc = T(0), pd = T(0);
+        for (int k = 0; k < P - 1; k++) {
+            const T rhs = s_g[k * 32 + lane] - s_vl[k * 32 + lane] - s_vf[(k + 1) * 32 + lane];
+            const T r = T(1) / (dg - lo * pc);
+            pc = lo * r;
+            pd = (rhs - lo * pd) * r;
+            s_u[k * 32 + lane] = pd;  // d' for now
+            s_vf[k * 32 + lane] = pc;  // c' (v_first of block k is no longer needed)
         }
-        if (ln == 0) {
-            atomicAdd(&norms[2 * blockIdx.y], cc);
-            atomicAdd(&norms[2 * blockIdx.y + 1], uu);
+        T u = T(0);
+        for (int k = P - 2; k >= 0; k--) {
+            u = s_u[k * 32 + lane] - s_vf[k * 32 + lane] * u;
+            s_u[k * 32 + lane] = u;
         }
+    }
+    __syncthreads();
+    const T ul = c > 0 ? s_u[(c - 1) * 32 + lane] : T(0);
+    const T ur = c < P - 1 ? s_u[c * 32 + lane] : T(0);
+    if (act) {
+#pragma unroll
+        for (int i = 0; i < m; i++) p[(r0 + i) * st] = v[i] + be[m - 1 - i] * ul + be[i] * ur;
+        if (c < P - 1) p[(r0 + m) * st] = ur;
     }
 }
 
