@@ -71,6 +71,21 @@ struct FastDiv {
     __device__ __forceinline__ unsigned div(unsigned x) const { return (__umulhi(x, m) + x) >> s; }
 };
 
+// s + e += v with the rounding error of the addition kept in e (TwoSum);
+// plain addition for FP64.
+template <typename T>
+__device__ __forceinline__ void acc_add(T& s, T& e, T v);
+template <>
+__device__ __forceinline__ void acc_add<float>(float& s, float& e, float v) {
+    const ff t = two_sum(s, v);
+    s = t.h;
+    e = __fadd_rn(e, t.l);
+}
+template <>
+__device__ __forceinline__ void acc_add<double>(double& s, double& e, double v) {
+    s += v;
+}
+
 // Runs the transform of every line held by this CTA.  On entry the staging
 // view of buffer B holds x[1..n] of line l at stage(B) + l*SX + skew_r(j)
 // (entries 0 and N zero).  On exit the unscaled result F[1..n] sits in the
@@ -156,7 +171,10 @@ __device__ T* sine_block(vec2_t<T>* A, vec2_t<T>* B, const SineTables<T>& tb, in
     const int kb = (M + kGroup - 1) / kGroup;
     const int k0 = g * kb;
     const int k1 = min(M, k0 + kb);
-    T sum = T(0);
+    // The odd outputs are a running sum of M terms; it is accumulated with
+    // an error term (float-float for FP32) so the rounding does not grow with
+    // the line length.
+    T sum = T(0), sum_e = T(0);
     for (int k = k0; k < k1; k++) {
         const T2 ck = C[skew_c(k)];
         const T2 cm = C[skew_c((M - k) & (M - 1))];
@@ -168,18 +186,25 @@ __device__ T* sine_block(vec2_t<T>* A, vec2_t<T>* B, const SineTables<T>& tb, in
         if (k == 0) yr *= T(0.5);
         else F[skew_r(2 * k)] = -yi;
         F[skew_r(2 * k + 1)] = yr;
-        sum += yr;
+        acc_add<T>(sum, sum_e, yr);
     }
-    T incl = sum;
+    // exclusive scan of the per-thread totals across the line's group
+    T incl = sum, incl_e = sum_e;
 #pragma unroll
     for (int off = 1; off < kGroup; off <<= 1) {
         T t = __shfl_up_sync(0xffffffffu, incl, off, kGroup);
-        if (g >= off) incl += t;
+        T te = __shfl_up_sync(0xffffffffu, incl_e, off, kGroup);
+        if (g >= off) {
+            acc_add<T>(incl, incl_e, t);
+            incl_e += te;
+        }
     }
-    T run = incl - sum;
+    T run = incl, run_e = incl_e;
+    acc_add<T>(run, run_e, -sum);
+    run_e -= sum_e;
     for (int k = k0; k < k1; k++) {
-        run += F[skew_r(2 * k + 1)];
-        F[skew_r(2 * k + 1)] = run;
+        acc_add<T>(run, run_e, F[skew_r(2 * k + 1)]);
+        F[skew_r(2 * k + 1)] = run + run_e;
     }
     __syncthreads();
     return reinterpret_cast<T*>(dst);
