@@ -16,6 +16,7 @@ F64, F32 = 0, 1
 PLAIN, MIXED = 0, 1
 RECT_TRIDIAG, RECT_FFT2 = 0, 1
 MAX_N = 1023
+NOALLOC_SCRATCH_BYTES = 32 * 1024 * 1024
 
 _STATUS_NAMES = {
     OK: "OK", EINVAL: "EINVAL", ESIZE: "ESIZE", ENOMEM: "ENOMEM", ECUDA: "ECUDA",
@@ -46,6 +47,8 @@ _SIGS = [
     ("fdmgpu_lapl_cube_solve", c_int, [c_void_p, c_void_p, c_void_p]),
     ("fdmgpu_lapl_cube_solve_host_batch", c_int, [c_void_p, c_void_p, c_void_p, c_int]),
     ("fdmgpu_lapl_cube_solve_device", c_int, [c_void_p, c_void_p, c_void_p, c_int, c_void_p]),
+    ("fdmgpu_lapl_cube_solve_mixed_noalloc", c_int,
+     [c_double] * 6 + [c_int] * 3 + [c_double, c_void_p, c_void_p, c_int, c_void_p]),
     ("fdmgpu_lapl_cube_last_info", c_int, [c_void_p, POINTER(c_int), POINTER(c_double), c_int]),
     ("fdmgpu_lapl_cube_scratch_bytes", c_int, [c_void_p, POINTER(c_size_t)]),
     ("fdmgpu_lapl_cube_destroy", c_int, [c_void_p]),

@@ -14,6 +14,7 @@
 #include <cmath>
 #include <cstring>
 #include <memory>
+#include <mutex>
 #include <vector>
 
 #include "internal.h"
@@ -410,6 +411,171 @@ struct fdmgpu_lapl_rect {
 };
 
 namespace fdmgpu {
+
+// ---------------------------------------------------------------------------
+// Mixed-precision solve that allocates nothing
+//
+// Some callers cannot allocate device memory when they solve: an application
+// whose device memory is owned by its own pool or by another framework's
+// allocator (a cudaMalloc behind that allocator's back can fail or fragment
+// it), a time-stepping loop that must not stall in the allocator after
+// start-up, or a host program that forbids dynamic device allocation once it
+// is initialised.  fdmgpu_lapl_cube_solve_mixed_noalloc serves them: it runs
+// the same kernels as the mixed solve of fdmgpu_lapl_cube_solve_device, but
+// its tables, FP32 work volumes and norms live in the fixed array below,
+// which exists once per device for as long as the library is loaded.
+// ---------------------------------------------------------------------------
+static __device__ __align__(256) unsigned char g_noalloc_scratch[FDMGPU_NOALLOC_SCRATCH_BYTES];
+
+constexpr int kNoallocMaxDevices = 64;
+static std::mutex g_noalloc_mu;
+static void* g_noalloc_ptr[kNoallocMaxDevices];
+
+// Device address of the array on the current device.  The first call on a
+// device looks it up with cudaGetSymbolAddress (which also loads the module
+// there); later calls reuse the address.
+static unsigned char* noalloc_scratch() {
+    int dev = 0;
+    FDM_CUDA(cudaGetDevice(&dev));
+    if (dev < 0 || dev >= kNoallocMaxDevices) FDM_FAIL(FDMGPU_EINVAL, "device ordinal %d out of range", dev);
+    std::lock_guard<std::mutex> lk(g_noalloc_mu);
+    if (!g_noalloc_ptr[dev]) {
+        void* p = nullptr;
+        cudaError_t e = cudaGetSymbolAddress(&p, g_noalloc_scratch);
+        if (e != cudaSuccess || !p)
+            FDM_FAIL(FDMGPU_ECUDA, "cudaGetSymbolAddress of the scratch array failed: %s", cudaGetErrorString(e));
+        g_noalloc_ptr[dev] = p;
+    }
+    return (unsigned char*)g_noalloc_ptr[dev];
+}
+
+// DST tables (rounded to FP32 from FP64 values) and Dirichlet eigenvalues
+// 4/h^2 sin^2(j pi / (2(n+1))) of one axis, written into the array.
+__global__ void k_noalloc_tables(float2* tw, float2* post, float* wpre, float* lam, int N, double h) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    const int M = N / 2, n = N - 1;
+    double s, c;
+    if (i < M) {
+        sincospi(2.0 * i / M, &s, &c);
+        tw[i] = make_float2((float)c, (float)(-s));
+        sincospi(2.0 * i / N, &s, &c);
+        post[i] = make_float2((float)c, (float)(-s));
+    }
+    if (i < N) wpre[i] = (float)sinpi((double)i / N);
+    if (i < n) {
+        const double sv = sinpi((i + 1) * 0.5 / (n + 1));
+        lam[i] = (float)(4.0 / (h * h) * (sv * sv));
+    }
+}
+
+struct NoallocAxis {
+    float2 *tw, *post;
+    float *wpre, *lam;
+};
+
+static size_t noalloc_align(size_t v) { return (v + 255) & ~(size_t)255; }
+
+static size_t noalloc_axis_bytes(int N) {
+    const int M = N / 2 > 0 ? N / 2 : 1;
+    return noalloc_align(M * sizeof(float2)) * 2 + noalloc_align(N * sizeof(float)) * 2;
+}
+
+static NoallocAxis noalloc_axis(unsigned char*& p, int N) {
+    const int M = N / 2 > 0 ? N / 2 : 1;
+    NoallocAxis a;
+    a.tw = (float2*)p; p += noalloc_align(M * sizeof(float2));
+    a.post = (float2*)p; p += noalloc_align(M * sizeof(float2));
+    a.wpre = (float*)p; p += noalloc_align(N * sizeof(float));
+    a.lam = (float*)p; p += noalloc_align(N * sizeof(float));
+    return a;
+}
+
+static void noalloc_solve(double dx, double dy, double dz, double lx, double ly, double lz, int nx, int ny, int nz,
+                          double tol, double* ans, const double* rhs, int nrhs, cudaStream_t st) {
+    // geometry as CubePlan::init
+    const double slx = std::sqrt(2. / lx), sly = std::sqrt(2. / ly), slz = std::sqrt(2. / lz);
+    const double scx = dx * slx, scy = dy * sly;
+    const double hx_eff = (nx == ny) ? dy : dx;
+    const double hz_eff = (nz == ny) ? dy : dz;
+    const double zfac = dz * slz * slz * (nz + 1) / 2.0;
+    const double S = (dx * slx * slx * (nx + 1) / 2.0) * (dy * sly * sly * (ny + 1) / 2.0) * zfac;
+    int sweeps = tol >= 1e-5 ? 0 : (tol >= 1e-11 ? 1 : 2);
+
+    const long long V = (long long)nx * ny * nz * nrhs;
+    const size_t need = noalloc_axis_bytes(nx + 1) + noalloc_axis_bytes(ny + 1) +
+                        noalloc_align((size_t)2 * nrhs * (sweeps > 0 ? sweeps : 1) * sizeof(double)) +
+                        noalloc_align((size_t)V * sizeof(float)) * (sweeps == 0 ? 1 : (sweeps > 1 ? 3 : 2));
+    if (need > (size_t)FDMGPU_NOALLOC_SCRATCH_BYTES)
+        FDM_FAIL(FDMGPU_EBUDGET,
+                 "the solve needs %zu bytes of scratch; the no-allocation entry point has %u (nrhs=%d of %dx%dx%d)",
+                 need, (unsigned)FDMGPU_NOALLOC_SCRATCH_BYTES, nrhs, nx, ny, nz);
+
+    unsigned char* p = noalloc_scratch();
+    NoallocAxis ax = noalloc_axis(p, nx + 1);
+    NoallocAxis ay = noalloc_axis(p, ny + 1);
+    double* NR = (double*)p;
+    p += noalloc_align((size_t)2 * nrhs * (sweeps > 0 ? sweeps : 1) * sizeof(double));
+    float* W = (float*)p;
+    p += noalloc_align((size_t)V * sizeof(float));
+    float* UH = sweeps > 0 ? (float*)p : nullptr;
+    if (sweeps > 0) p += noalloc_align((size_t)V * sizeof(float));
+    float* UL = sweeps > 1 ? (float*)p : nullptr;
+
+    {
+        FDM_TIMED("noalloc_tables", st);
+        k_noalloc_tables<<<(nx + 1 + 255) / 256, 256, 0, st>>>(ax.tw, ax.post, ax.wpre, ax.lam, nx + 1, hx_eff);
+        FDM_LAUNCH_CHECK();
+    }
+    {
+        FDM_TIMED("noalloc_tables", st);
+        k_noalloc_tables<<<(ny + 1 + 255) / 256, 256, 0, st>>>(ay.tw, ay.post, ay.wpre, ay.lam, ny + 1, dy);
+        FDM_LAUNCH_CHECK();
+    }
+    auto view = [](const NoallocAxis& a, int N) {
+        SineTables<float> v;
+        v.tw = a.tw; v.post = a.post; v.wpre = a.wpre; v.N = N; v.M = N / 2;
+        return v;
+    };
+    const SineTables<float> tx = view(ax, nx + 1), ty = view(ay, ny + 1);
+    const double h2 = hz_eff * hz_eff, gscale = zfac * hz_eff * hz_eff;
+
+    launch_sine<double, float, float, 0, kRound>(rhs, W, nx, ny, nz, nrhs, tx, scx, st);
+    launch_sine<float, float, float, 1>(W, W, nx, ny, nz, nrhs, ty, scy, st);
+    zsolve_lines<float>(W, nx, ny, nz, nrhs, ax.lam, ay.lam, h2, gscale, st);
+    launch_sine<float, float, float, 1>(W, W, nx, ny, nz, nrhs, ty, sly, st);
+    if (sweeps == 0) {
+        launch_sine<float, float, double, 0>(W, ans, nx, ny, nz, nrhs, tx, slx, st);
+        return;
+    }
+    // the norms must start at zero on every call: the array keeps the last
+    // call's contents
+    FDM_CUDA(cudaMemsetAsync(NR, 0, (size_t)2 * nrhs * sweeps * sizeof(double), st));
+    launch_sine<float, float, float, 0>(W, UH, nx, ny, nz, nrhs, tx, slx, st);
+    const double cx = 1.0 / (hx_eff * hx_eff) / S, cy = 1.0 / (dy * dy) / S, cz = 1.0 / (hz_eff * hz_eff) / S;
+    for (int s = 1; s <= sweeps; s++) {
+        SineFused fr;
+        memset(&fr, 0, sizeof(fr));
+        fr.f = rhs;
+        fr.uhi = UH;
+        fr.ulo = s >= 2 ? UL : nullptr;
+        fr.cx = CubePlan::split_host(cx); fr.cy = CubePlan::split_host(cy); fr.cz = CubePlan::split_host(cz);
+        fr.cxf = (float)cx; fr.cyf = (float)cy; fr.czf = (float)cz;
+        launch_sine<float, float, float, 0, kResidual>(nullptr, W, nx, ny, nz, nrhs, tx, scx, st, &fr);
+        launch_sine<float, float, float, 1>(W, W, nx, ny, nz, nrhs, ty, scy, st);
+        zsolve_lines<float>(W, nx, ny, nz, nrhs, ax.lam, ay.lam, h2, gscale, st);
+        launch_sine<float, float, float, 1>(W, W, nx, ny, nz, nrhs, ty, sly, st);
+        SineFused fc;
+        memset(&fc, 0, sizeof(fc));
+        fc.uhi = UH;
+        fc.ulo = s >= 2 ? UL : nullptr;
+        fc.out64 = ans;
+        fc.ulo_out = UL;
+        fc.last = s == sweeps ? 1 : 0;
+        fc.norms = NR + (size_t)2 * nrhs * (s - 1);
+        launch_sine<float, float, float, 0, kCombine>(W, (float*)nullptr, nx, ny, nz, nrhs, tx, slx, st, &fc);
+    }
+}
+
 void cube_solve_device(fdmgpu_lapl_cube* h, void* ans, const void* rhs, int nrhs, cudaStream_t st) {
     h->plan.solve_device(ans, rhs, nrhs, st);
 }
@@ -564,6 +730,22 @@ int fdmgpu_lapl_rect_solve(fdmgpu_lapl_rect* h, void* ans, const void* rhs) {
 int fdmgpu_lapl_rect_destroy(fdmgpu_lapl_rect* h) {
     FDM_API_BEGIN
     delete h;
+    FDM_API_END
+}
+
+int fdmgpu_lapl_cube_solve_mixed_noalloc(double dx, double dy, double dz, double lx, double ly, double lz, int nx,
+                                         int ny, int nz, double tol, void* d_ans, const void* d_rhs, int nrhs,
+                                         void* stream) {
+    FDM_API_BEGIN
+    if (!d_ans || !d_rhs) FDM_FAIL(FDMGPU_EINVAL, "null argument");
+    if (!pow2_interior(nx) || !pow2_interior(ny) || !pow2_interior(nz))
+        FDM_FAIL(FDMGPU_ESIZE, "verify((1<<n) == N) failed: n+1 must be a power of two and n <= %d (got %d,%d,%d)",
+                 FDMGPU_MAX_N, nx, ny, nz);
+    if (!(dx > 0 && dy > 0 && dz > 0 && lx > 0 && ly > 0 && lz > 0))
+        FDM_FAIL(FDMGPU_EINVAL, "spacings and lengths must be positive");
+    check_grid_y(nrhs);
+    noalloc_solve(dx, dy, dz, lx, ly, lz, nx, ny, nz, tol > 0 ? tol : 1e-10, (double*)d_ans, (const double*)d_rhs,
+                  nrhs, (cudaStream_t)stream);
     FDM_API_END
 }
 

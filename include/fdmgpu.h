@@ -104,6 +104,31 @@ int fdmgpu_lapl_cube_solve_host_batch(fdmgpu_lapl_cube* h, void* ans, const void
  * asynchronous on stream */
 int fdmgpu_lapl_cube_solve_device(fdmgpu_lapl_cube* h, void* d_ans, const void* d_rhs,
                                   int nrhs, void* stream);
+/* Mixed-precision solve that allocates nothing (no counterpart in the
+ * reference, whose LaplCube owns its scratch as member vectors).  For
+ * callers that must not allocate device memory while they solve: programs
+ * whose device memory belongs to their own pool or to another framework's
+ * allocator, loops that must not wait on the allocator after start-up, and
+ * hosts that forbid device allocation once initialised.  Same arguments and
+ * result as a handle created with these sizes and set to FDMGPU_MIXED with
+ * `tol`, called through fdmgpu_lapl_cube_solve_device (FP64 device arrays,
+ * nrhs volumes back to back, asynchronous on stream), but no handle: its
+ * tables, FP32 work volumes and norms live in one array of
+ * FDMGPU_NOALLOC_SCRATCH_BYTES that the library holds on every device it is
+ * loaded on, until the process exits.  A solve needs about
+ * 4*nx*ny*nz*nrhs bytes per FP32 volume (2 volumes for one refinement sweep,
+ * 3 for two) plus a few KB; larger requests return FDMGPU_EBUDGET with the
+ * byte counts in the message.  The first call on a device looks up the
+ * array's device address (and loads the module there); make that first call
+ * before any stream capture.  All calls on a device share the array: calls
+ * that overlap on the GPU (other streams, other host threads) race on it, so
+ * serialise them.  No cudaMalloc, cudaFree or other allocating routine is
+ * called (with fdmgpu_profile_enable(1) the library creates timing events for
+ * every launch, this entry point's included). */
+#define FDMGPU_NOALLOC_SCRATCH_BYTES (32u * 1024u * 1024u)
+int fdmgpu_lapl_cube_solve_mixed_noalloc(double dx, double dy, double dz, double lx, double ly, double lz,
+                                         int nx, int ny, int nz, double tol, void* d_ans, const void* d_rhs,
+                                         int nrhs, void* stream);
 /* refinement report of the last solve: sweeps done and, per RHS, the
  * relative size of the last correction ||c||_2/||u||_2 (an upper estimate of
  * the remaining relative error).  est may be NULL; it receives nrhs values.

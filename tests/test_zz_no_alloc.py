@@ -1,0 +1,102 @@
+"""GPU test of fdmgpu_lapl_cube_solve_mixed_noalloc, the mixed-precision
+solve for callers that must not allocate device memory while solving (their
+device memory belongs to their own pool or another framework's allocator, or
+they may not wait on an allocator after start-up).  It keeps its scratch in a
+fixed array inside libfdmgpu.so instead of allocating.
+
+Called through the C ABI; its result must match the existing mixed entry
+point (fdmgpu_lapl_cube_solve_device on a FDMGPU_MIXED handle) within the
+mixed-precision tolerance, on two calls in a row with different inputs (the
+second call must not see the first call's leftovers).  This file is named to
+be collected last."""
+import ctypes
+
+import numpy as np
+import pytest
+
+from fdm_gb300 import _native as N
+from fdm_gb300 import LaplCube, workloads
+
+pytestmark = pytest.mark.gpu
+
+TOL_MIXED = 1e-10  # relative L2, the tolerance of the mixed-precision tests
+
+
+def _noalloc(lib, args, ans, rhs, nrhs, tol=1e-10, stream=None):
+    dx, dy, dz, lx, ly, lz, nx, ny, nz = args
+    return lib.fdmgpu_lapl_cube_solve_mixed_noalloc(dx, dy, dz, lx, ly, lz, nx, ny, nz, tol, ans.data_ptr(),
+                                                    rhs.data_ptr(), nrhs, stream)
+
+
+def _rel(a, b):
+    import torch
+    return (torch.linalg.norm(a - b) / torch.linalg.norm(b)).item()
+
+
+def test_noalloc_matches_mixed_entry_point_twice(cuda):
+    import torch
+    lib = N.load()
+    nx, ny, nz = 63, 31, 63
+    args = workloads.solver_args(nx, ny, nz)
+    batch1 = torch.stack([workloads.manufactured_torch(nx, ny, nz, seed=s, kmax=(16, 8, 16), noise=1e-3)[0]
+                          for s in (1, 2)]).contiguous()
+    batch2 = torch.stack([workloads.manufactured_torch(nx, ny, nz, seed=s, kmax=(12, 6, 12), noise=1e-3)[0]
+                          for s in (3, 4)]).contiguous()
+
+    mixed = LaplCube(*args, precision="mixed", tol=1e-10)
+    plain = LaplCube(*args)
+    refs, exact = [], []
+    for b in (batch1, batch2):
+        r = torch.empty_like(b)
+        mixed.solve_device(r, b, nrhs=2)
+        p = torch.empty_like(b)
+        plain.solve_device(p, b, nrhs=2)
+        refs.append(r)
+        exact.append(p)
+    torch.cuda.synchronize()
+
+    outs = []
+    for b in (batch1, batch2):
+        o = torch.full_like(b, float("nan"))
+        assert _noalloc(lib, args, o, b, 2) == N.OK, lib.fdmgpu_last_error()
+        outs.append(o)
+    torch.cuda.synchronize()
+    for o, r, p in zip(outs, refs, exact):
+        for i in range(2):
+            assert torch.isfinite(o[i]).all()
+            assert _rel(o[i], r[i]) <= TOL_MIXED
+            assert _rel(o[i], p[i]) <= TOL_MIXED
+
+
+def test_noalloc_allocates_nothing_and_rejects_oversize(cuda):
+    import torch
+    lib = N.load()
+    n = 127
+    args = workloads.solver_args(n, n, n)
+    f = workloads.manufactured_torch(n, n, n, seed=5, kmax=32, noise=1e-3)[0].contiguous()
+    out = torch.empty_like(f)
+    assert _noalloc(lib, args, out, f, 1) == N.OK, lib.fdmgpu_last_error()  # first call: set-up on this device
+    torch.cuda.synchronize()
+    free0, _ = torch.cuda.mem_get_info()
+    out2 = torch.empty_like(f)
+    torch.cuda.synchronize()
+    free1, _ = torch.cuda.mem_get_info()
+    assert _noalloc(lib, args, out2, f, 1) == N.OK, lib.fdmgpu_last_error()
+    torch.cuda.synchronize()
+    free2, _ = torch.cuda.mem_get_info()
+    assert free2 == free1  # the call itself took no device memory
+    assert free1 <= free0
+    assert torch.equal(out, out2)
+    plain = LaplCube(*args)
+    p = torch.empty_like(f)
+    plain.solve_device(p, f)
+    torch.cuda.synchronize()
+    assert _rel(out2, p) <= TOL_MIXED
+
+    # 255^3 needs ~133 MB of scratch: refused with a clear status, nothing run
+    n = 255
+    big = workloads.solver_args(n, n, n)
+    dummy = torch.empty(1, dtype=torch.float64, device=cuda)
+    rc = _noalloc(lib, big, dummy, dummy, 1)
+    assert rc == N.EBUDGET
+    assert b"scratch" in lib.fdmgpu_last_error()
