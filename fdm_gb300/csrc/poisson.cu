@@ -20,6 +20,7 @@
 #include "internal.h"
 #include "poisson.h"
 #include "sine.cuh"
+#include "sine_rg.cuh"
 #include "solve_kernels.cuh"
 
 namespace fdmgpu {
@@ -99,9 +100,47 @@ constexpr const char* sine_name() {
                                : "sine_x_f32";
 }
 
+template <typename Tin, typename T, typename Tout, int AXIS, int MODE, int N>
+static void launch_rg(const Tin* in, Tout* out, int nx, int ny, int nz, int nvol, const SineTables<T>& tb,
+                      double scale, cudaStream_t st, const SineFused& fu, SineGeom geo) {
+    constexpr int L = RgGeom<N>::L;
+    constexpr size_t smem = rg_smem_bytes<T, N>();
+    static bool attr_set = false;
+    if (!attr_set) {
+        FDM_CUDA(cudaFuncSetAttribute(k_sine_rg<Tin, T, Tout, AXIS, MODE, N>,
+                                      cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+        attr_set = true;
+    }
+    unsigned gx;
+    if (AXIS == 0) gx = (unsigned)((ny * (long long)nz + L - 1) / L);
+    else gx = (unsigned)(nz * ((nx + L - 1) / L));
+    dim3 grid(gx, nvol);
+    FDM_TIMED((sine_name<Tin, T, Tout, AXIS, MODE>()), st);
+    k_sine_rg<Tin, T, Tout, AXIS, MODE, N><<<grid, 256, smem, st>>>(in, out, geo, tb, (T)scale, fu);
+    FDM_LAUNCH_CHECK();
+}
+
 template <typename Tin, typename T, typename Tout, int AXIS, int MODE = kPlain>
 static void launch_sine(const Tin* in, Tout* out, int nx, int ny, int nz, int nvol, const SineTables<T>& tb,
                         double scale, cudaStream_t st, const SineFused* fused = nullptr) {
+    SineGeom geo;
+    geo.nx = nx; geo.ny = ny; geo.nz = nz;
+    geo.vstride = (long long)nx * ny * nz;
+    geo.div_n = FastDiv((unsigned)(AXIS == 0 ? nx : ny));
+    geo.div_ny = FastDiv((unsigned)ny);
+    SineFused fu;
+    memset(&fu, 0, sizeof(fu));
+    if (fused) fu = *fused;
+    switch (tb.N) {
+        case 16: return launch_rg<Tin, T, Tout, AXIS, MODE, 16>(in, out, nx, ny, nz, nvol, tb, scale, st, fu, geo);
+        case 32: return launch_rg<Tin, T, Tout, AXIS, MODE, 32>(in, out, nx, ny, nz, nvol, tb, scale, st, fu, geo);
+        case 64: return launch_rg<Tin, T, Tout, AXIS, MODE, 64>(in, out, nx, ny, nz, nvol, tb, scale, st, fu, geo);
+        case 128: return launch_rg<Tin, T, Tout, AXIS, MODE, 128>(in, out, nx, ny, nz, nvol, tb, scale, st, fu, geo);
+        case 256: return launch_rg<Tin, T, Tout, AXIS, MODE, 256>(in, out, nx, ny, nz, nvol, tb, scale, st, fu, geo);
+        case 512: return launch_rg<Tin, T, Tout, AXIS, MODE, 512>(in, out, nx, ny, nz, nvol, tb, scale, st, fu, geo);
+        default: break;
+    }
+    // other lengths: the shared-memory Stockham kernel
     const int L = pick_lines<T>(tb.N);
     int Lshift = 0;
     while ((1 << Lshift) < L) Lshift++;
@@ -116,15 +155,8 @@ static void launch_sine(const Tin* in, Tout* out, int nx, int ny, int nz, int nv
     if (AXIS == 0) gx = (unsigned)((ny * (long long)nz + L - 1) / L);
     else gx = (unsigned)(nz * ((nx + L - 1) / L));
     dim3 grid(gx, nvol);
-    SineGeom geo;
-    geo.nx = nx; geo.ny = ny; geo.nz = nz;
-    geo.vstride = (long long)nx * ny * nz;
-    geo.L = L; geo.Lshift = Lshift;
-    geo.div_n = FastDiv((unsigned)(AXIS == 0 ? nx : ny));
-    geo.div_ny = FastDiv((unsigned)ny);
-    SineFused fu;
-    memset(&fu, 0, sizeof(fu));
-    if (fused) fu = *fused;
+    geo.L = L;
+    geo.Lshift = Lshift;
     FDM_TIMED((sine_name<Tin, T, Tout, AXIS, MODE>()), st);
     k_sine_pass<Tin, T, Tout, AXIS, MODE><<<grid, L * kGroup, smem, st>>>(in, out, geo, tb, (T)scale, fu);
     FDM_LAUNCH_CHECK();
