@@ -71,6 +71,11 @@ def ut_lapl_cube_rhs(n: int):
     return rhs, exact, args
 
 
+def f32_line(N: int, t: int) -> np.ndarray:
+    """Line t of the FP32 round-trip inputs: N-1 values uniform in (-1, 1)."""
+    return np.random.default_rng(1000 + t).uniform(-1, 1, N - 1).astype(np.float32)
+
+
 def main():
     R = reference()
     if R is None:
@@ -84,6 +89,26 @@ def main():
         d["s_%d" % N] = s
         d["S_%d" % N] = R.sfft(s, 1.0)
         d["Sh_%d" % N] = R.sfft(s, 0.5)
+    # FP32 round trip S = sFFT(s, 1), s' = sFFT(S, 2/N) of the reference's
+    # float instantiation, 64 lines uniform(-1,1) per N (ut/ut_fft.cpp:190-228
+    # asserts 1e-5 at N=1024 for its one default-seeded line)
+    import ctypes
+    fp = ctypes.POINTER(ctypes.c_float)
+    R.L.ref_sfft_f.argtypes = [fp, fp, ctypes.c_float, ctypes.c_int]
+
+    def sfft32(v, dx):
+        S = np.zeros(v.size, np.float32)
+        a = v.astype(np.float32).copy()
+        R.L.ref_sfft_f(S.ctypes.data_as(fp), a.ctypes.data_as(fp), dx, v.size)
+        return S
+    for N in (32, 256, 1024):
+        worst = 0.0
+        for t in range(64):
+            v = np.zeros(N, np.float32)
+            v[1:] = f32_line(N, t)
+            v1 = sfft32(sfft32(v, 1.0), 2.0 / N)
+            worst = max(worst, float(np.abs(v1[1:] - v[1:]).max()))
+        d["f32_roundtrip_err_%d" % N] = np.array(worst)
     np.savez_compressed(OUT / "dst.npz", **d)
 
     # LaplCube

@@ -31,16 +31,22 @@ def test_sine_f64_vs_reference(cuda, golden, port, N):
         assert np.abs(out[0] - g["Sh_%d" % N][1:]).max() <= 1e-13 * max(1.0, np.abs(g["Sh_%d" % N]).max())
 
 
-@pytest.mark.parametrize("N", [32, 256])
-def test_sine_f32_roundtrip(cuda, N):
+@pytest.mark.parametrize("N", [32, 256, 1024])
+def test_sine_f32_roundtrip(cuda, golden, N):
+    """FP32 round trip s' = DST(DST(s) * 1) * 2/N on 64 uniform(-1,1) lines.
+    The bar is the reference's own float sFFT on the same lines (golden
+    f32_roundtrip_err_N: 5.4e-6 at N=256, 1.9e-5 at N=1024): both compute the
+    odd outputs as running sums, whose error grows like sqrt(N)."""
     import torch
-    x = torch.rand((64, N - 1), dtype=torch.float32, device=cuda) * 2 - 1
+    from tests.golden.make_golden import f32_line
+    ref_err = float(golden("dst")["f32_roundtrip_err_%d" % N])
+    x = torch.tensor(np.stack([f32_line(N, t) for t in range(64)]), device=cuda)
     y = torch.empty_like(x)
     z = torch.empty_like(x)
     sine_transform_device(y, x, N, 64, 1.0, dtype=np.float32)
     sine_transform_device(z, y, N, 64, 2.0 / N, dtype=np.float32)
     torch.cuda.synchronize()
-    assert (z - x).abs().max().item() <= 1e-5  # ut/ut_fft.cpp test_sin, float tolerance
+    assert (z - x).abs().max().item() <= 3.0 * ref_err
 
 
 @pytest.mark.parametrize("n", [9, 31, 32, 63, 255])
