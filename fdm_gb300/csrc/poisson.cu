@@ -188,7 +188,7 @@ static void launch_zpart(T* W, int nx, int ny, int P, long long vstride, int nvo
 template <typename T>
 static void zsolve_lines(T* W, int nx, int ny, int nz, int nvol, const T* lamx, const T* lamy, double h2,
                          double gscale, cudaStream_t st) {
-    const int mmax = sizeof(T) == 4 ? 31 : 15;
+    const int mmax = 15;
     const int m = nz < mmax ? nz : mmax;
     const int P = (nz + 1) / (m + 1);
     const long long vs = (long long)nx * ny * nz;

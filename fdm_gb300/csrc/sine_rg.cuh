@@ -13,10 +13,10 @@
 //     pass 2: each thread does R1/G DFTs of length R2 in registers, giving
 //             C[k1 + R1*k2].
 // Every line uses one shared region: the staged input, the transpose, C and
-// the staged output reuse it in turn.  The staged view is XOR-swizzled per
-// line (position ((i + i/32) ^ (line % 32))) so that both row-wise and
-// column-wise (transposed) accesses by consecutive threads hit distinct
-// banks.
+// the staged output reuse it in turn.  Staged entry i sits at i + i/32 (one
+// pad slot per 32, so the per-thread blocks of the unpack fall into distinct
+// banks); in the column pass it is also XOR-swizzled with the line index so
+// that consecutive threads walking across lines hit distinct banks.
 #pragma once
 
 #include "sine.cuh"
@@ -105,9 +105,12 @@ __device__ __forceinline__ void dft_reg(vec2_t<T>* v) {
     }
 }
 
-template <int N>
+// staged position of entry i of line l; the XOR swizzle is needed only
+// when consecutive threads walk across lines (the column pass)
+template <int N, int AXIS>
 __device__ __forceinline__ int rg_pos(int l, int i) {
-    return l * RgGeom<N>::LS + ((i + (i >> 5)) ^ (l & 31));
+    if (AXIS == 1) return l * RgGeom<N>::LS + ((i + (i >> 5)) ^ (l & 31));
+    return l * RgGeom<N>::LS + i + (i >> 5);
 }
 
 template <typename Tin, typename T, typename Tout, int AXIS, int MODE, int N>
@@ -138,8 +141,8 @@ __global__ void __launch_bounds__(256) k_sine_rg(const Tin* in, Tout* out, SineG
 
     // ---- load phase: staged lines x[1..n], x[0] = x[N] = 0
     for (int i = tid; i < L; i += nthr) {
-        S[rg_pos<N>(i, 0)] = T(0);
-        S[rg_pos<N>(i, N)] = T(0);
+        S[rg_pos<N, AXIS>(i, 0)] = T(0);
+        S[rg_pos<N, AXIS>(i, N)] = T(0);
     }
     if (AXIS == 0) {
         const int total = nact * n;
@@ -176,13 +179,13 @@ __global__ void __launch_bounds__(256) k_sine_rg(const Tin* in, Tout* out, SineG
                 const int e = e0 + q * nthr;
                 if (e < total) {
                     const int r = e / n, c = e - r * n;
-                    S[rg_pos<N>(r, c + 1)] = v[q];
+                    S[rg_pos<N, AXIS>(r, c + 1)] = v[q];
                 }
             }
         }
         for (int e = nact * n + tid; e < L * n; e += nthr) {
             const int r = e / n, c = e - r * n;
-            S[rg_pos<N>(r, c + 1)] = T(0);
+            S[rg_pos<N, AXIS>(r, c + 1)] = T(0);
         }
     } else {
         const int total = n * L;
@@ -204,7 +207,7 @@ __global__ void __launch_bounds__(256) k_sine_rg(const Tin* in, Tout* out, SineG
                 const int e = e0 + q * nthr;
                 if (e < total) {
                     const int y = e / L, c = e - y * L;
-                    S[rg_pos<N>(c, y + 1)] = v[q];
+                    S[rg_pos<N, AXIS>(c, y + 1)] = v[q];
                 }
             }
         }
@@ -221,10 +224,10 @@ __global__ void __launch_bounds__(256) k_sine_rg(const Tin* in, Tout* out, SineG
             const int a0 = 2 * m, a1 = 2 * m + 1;
             T y0 = T(0);
             if (m > 0) {
-                const T a = S[rg_pos<N>(l, a0)], b = S[rg_pos<N>(l, N - a0)];
+                const T a = S[rg_pos<N, AXIS>(l, a0)], b = S[rg_pos<N, AXIS>(l, N - a0)];
                 y0 = ldg(tb.wpre + a0) * (a + b) + half * (a - b);
             }
-            const T a = S[rg_pos<N>(l, a1)], b = S[rg_pos<N>(l, N - a1)];
+            const T a = S[rg_pos<N, AXIS>(l, a1)], b = S[rg_pos<N, AXIS>(l, N - a1)];
             const T y1 = ldg(tb.wpre + a1) * (a + b) + half * (a - b);
             v[j1].x = y0;
             v[j1].y = y1;
@@ -262,7 +265,6 @@ __global__ void __launch_bounds__(256) k_sine_rg(const Tin* in, Tout* out, SineG
 
     // ---- unpack + prefix sum over this thread's block of R1 consecutive k
     T ev[R1], od[R1];
-    T sum = T(0), sum_e = T(0);
 #pragma unroll
     for (int t = 0; t < R1; t++) {
         const int k = g * R1 + t;
@@ -275,33 +277,27 @@ __global__ void __launch_bounds__(256) k_sine_rg(const Tin* in, Tout* out, SineG
         const T yi = ey + (w.x * oy + w.y * ox);
         if (k == 0) yr *= T(0.5);
         ev[t] = -yi;
-        acc_add<T>(sum, sum_e, yr);
         od[t] = yr;
     }
-    T incl = sum, incl_e = sum_e;
+    // running sum of the odd terms: local inclusive prefix, then the
+    // exclusive offset from the lanes before (segmented shuffle scan)
+#pragma unroll
+    for (int t = 1; t < R1; t++) od[t] += od[t - 1];
+    T incl = od[R1 - 1];
 #pragma unroll
     for (int off = 1; off < G; off <<= 1) {
         const T t = __shfl_up_sync(0xffffffffu, incl, off, G);
-        const T te = __shfl_up_sync(0xffffffffu, incl_e, off, G);
-        if (g >= off) {
-            acc_add<T>(incl, incl_e, t);
-            incl_e += te;
-        }
+        if (g >= off) incl += t;
     }
-    T run = incl, run_e = incl_e;
-    acc_add<T>(run, run_e, -sum);
-    run_e -= sum_e;
+    const T excl = incl - od[R1 - 1];
 #pragma unroll
-    for (int t = 0; t < R1; t++) {
-        acc_add<T>(run, run_e, od[t]);
-        od[t] = run + run_e;
-    }
+    for (int t = 0; t < R1; t++) od[t] += excl;
     __syncthreads();  // every line has read its C; staged outputs overwrite the regions
 #pragma unroll
     for (int t = 0; t < R1; t++) {
         const int k = g * R1 + t;
-        if (k > 0) S[rg_pos<N>(l, 2 * k)] = ev[t];
-        S[rg_pos<N>(l, 2 * k + 1)] = od[t];
+        if (k > 0) S[rg_pos<N, AXIS>(l, 2 * k)] = ev[t];
+        S[rg_pos<N, AXIS>(l, 2 * k + 1)] = od[t];
     }
     __syncthreads();
 
@@ -313,7 +309,7 @@ __global__ void __launch_bounds__(256) k_sine_rg(const Tin* in, Tout* out, SineG
             float cc = 0.f, uu = 0.f;
             for (int e = tid; e < total; e += nthr) {
                 const int r = e / n, c = e - r * n;
-                const float cv = (float)(scale * S[rg_pos<N>(r, c + 1)]);
+                const float cv = (float)(scale * S[rg_pos<N, AXIS>(r, c + 1)]);
                 const long long idx = base + e;
                 const float h = fu.uhi[idx];
                 const float lo = fu.ulo ? fu.ulo[idx] : 0.f;
@@ -348,7 +344,7 @@ __global__ void __launch_bounds__(256) k_sine_rg(const Tin* in, Tout* out, SineG
         } else {
             for (int e = tid; e < total; e += nthr) {
                 const int r = e / n, c = e - r * n;
-                out[base + e] = Tout(scale * S[rg_pos<N>(r, c + 1)]);
+                out[base + e] = Tout(scale * S[rg_pos<N, AXIS>(r, c + 1)]);
             }
         }
     } else {
@@ -356,7 +352,7 @@ __global__ void __launch_bounds__(256) k_sine_rg(const Tin* in, Tout* out, SineG
         const long long base = voff + ((long long)z * ny) * nx + x0;
         for (int e = tid; e < total; e += nthr) {
             const int y = e / L, c = e - y * L;
-            if (c < nact) out[base + (long long)y * nx + c] = Tout(scale * S[rg_pos<N>(c, y + 1)]);
+            if (c < nact) out[base + (long long)y * nx + c] = Tout(scale * S[rg_pos<N, AXIS>(c, y + 1)]);
         }
     }
 }
