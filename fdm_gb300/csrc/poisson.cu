@@ -103,8 +103,8 @@ constexpr const char* sine_name() {
 template <typename Tin, typename T, typename Tout, int AXIS, int MODE, int N>
 static void launch_rg(const Tin* in, Tout* out, int nx, int ny, int nz, int nvol, const SineTables<T>& tb,
                       double scale, cudaStream_t st, const SineFused& fu, SineGeom geo) {
-    constexpr int L = RgGeom<N>::L;
-    constexpr size_t smem = rg_smem_bytes<T, N>();
+    constexpr int L = RgGeom<N, AXIS>::L;
+    constexpr size_t smem = rg_smem_bytes<T, N, AXIS>();
     static bool attr_set = false;
     if (!attr_set) {
         FDM_CUDA(cudaFuncSetAttribute(k_sine_rg<Tin, T, Tout, AXIS, MODE, N>,

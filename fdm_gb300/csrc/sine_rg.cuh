@@ -3,20 +3,25 @@
 // Same transform and contract as k_sine_pass (sine.cuh): for every line
 // x[1..n] (N = n+1), F[k] = scale * sum_j x[j] sin(pi j k / N), with the
 // fold -> complex FFT of M = N/2 -> real unpack + prefix sum formulation.
-// The complex FFT is done as two register passes instead of log4(M)
-// shared-memory passes:
-//     M = R1 * R2, G = R2 threads per line;
-//     pass 1: thread g loads c[j1*R2 + g] (folded on the fly from the staged
-//             line), does a DFT of length R1 in registers and multiplies by
-//             w_M^(g*k1);
-//     one transpose through shared memory;
-//     pass 2: each thread does R1/G DFTs of length R2 in registers, giving
-//             C[k1 + R1*k2].
-// Every line uses one shared region: the staged input, the transpose, C and
-// the staged output reuse it in turn.  Staged entry i sits at i + i/32 (one
-// pad slot per 32, so the per-thread blocks of the unpack fall into distinct
-// banks); in the column pass it is also XOR-swizzled with the line index so
-// that consecutive threads walking across lines hit distinct banks.
+//
+//   load:   the thread that loads x_j also loads x_{N-j} and writes the two
+//           folded values y_j, y_{N-j}; lines are stored as M complex slots
+//           c_m = (y_{2m}, y_{2m+1});
+//   pass 1: M = R1 * R2, G = R2 threads per line; thread g takes
+//           c[j1*R2 + g], does a DFT of length R1 in registers and multiplies
+//           by w_M^(g*k1);
+//   one transpose through shared memory;
+//   pass 2: each thread does R1/G DFTs of length R2 in registers, giving
+//           C[k1 + R1*k2];
+//   unpack: Y_k and Y_{M-k} both come from the pair (C_k, C_{M-k})
+//           (Y_{M-k} = conj(E_k - w_k O_k)), so each C is read once; thread
+//           g owns k in [g*E, (g+1)*E) of the first half and their mirrors;
+//           the odd outputs are a running sum over k, done as a local prefix
+//           plus a forward shuffle scan for the first half and a backward one
+//           for the mirrored blocks of the second half.
+// Each line owns one region of complex slots used in turn by the packed
+// input, the transpose, C and the packed output (F_{2k}, F_{2k+1}), so the
+// phases inside a line need only warp-level synchronisation.
 #pragma once
 
 #include "sine.cuh"
@@ -31,19 +36,21 @@ template <> struct RgCfg<128> { static constexpr int R1 = 8, R2 = 8; };
 template <> struct RgCfg<256> { static constexpr int R1 = 16, R2 = 8; };
 template <> struct RgCfg<512> { static constexpr int R1 = 16, R2 = 16; };
 
-template <int N>
+template <int N, int AXIS>
 struct RgGeom {
     static constexpr int M = N / 2;
     static constexpr int R1 = RgCfg<N>::R1, R2 = RgCfg<N>::R2;
-    static constexpr int G = R2;           // threads per line
-    static constexpr int L = 256 / G;      // lines per CTA
-    static constexpr int D2 = R1 / G;      // length-R2 DFTs per thread in pass 2
-    static constexpr int STAGE = N + N / 32 + 32;
-    static constexpr int TR = R1 * (R2 + 1);
-    static constexpr int CB = M + M / 16 + 1;
-    static constexpr int CPLX = (TR > CB ? TR : CB) + 8;
-    static constexpr int LS0 = STAGE > 2 * CPLX ? STAGE : 2 * CPLX;
-    static constexpr int LS = (LS0 + 31) / 32 * 32;  // reals per line region
+    static constexpr int G = R2;              // threads per line
+    static constexpr int L = 256 / G;         // lines per CTA
+    static constexpr int D2 = R1 / G;         // length-R2 DFTs per thread in pass 2
+    static constexpr int E = M / (2 * G);     // unpack pairs per thread
+    static constexpr int TR = R1 * (R2 + 1);  // transpose slots
+    static constexpr int CS = M + M / 16 + 1; // skewed C / packed-output slots
+    static constexpr int RS0 = TR > CS ? (TR > M ? TR : M) : (CS > M ? CS : M);
+    // line stride in slots: 8 (mod 16) for the row pass so the two lines of
+    // a half-warp use disjoint bank pairs; odd for the column pass, whose
+    // load and store walk across lines
+    static constexpr int LS2 = AXIS == 0 ? ((RS0 + 7) / 16 * 16 + 8) : (RS0 | 1);
 };
 
 // cos / sin of 2 pi m / 16
@@ -105,23 +112,21 @@ __device__ __forceinline__ void dft_reg(vec2_t<T>* v) {
     }
 }
 
-// staged position of entry i of line l; the XOR swizzle is needed only
-// when consecutive threads walk across lines (the column pass)
-template <int N, int AXIS>
-__device__ __forceinline__ int rg_pos(int l, int i) {
-    if (AXIS == 1) return l * RgGeom<N>::LS + ((i + (i >> 5)) ^ (l & 31));
-    return l * RgGeom<N>::LS + i + (i >> 5);
-}
+// skewed slot of entry k of C / the packed output: one pad slot per 16
+__device__ __forceinline__ int sk(int k) { return k + (k >> 4); }
 
 template <typename Tin, typename T, typename Tout, int AXIS, int MODE, int N>
 __global__ void __launch_bounds__(256) k_sine_rg(const Tin* in, Tout* out, SineGeom geo, SineTables<T> tb, T scale,
                                                  SineFused fu) {
     using T2 = vec2_t<T>;
-    using Gm = RgGeom<N>;
-    constexpr int M = Gm::M, R1 = Gm::R1, R2 = Gm::R2, G = Gm::G, L = Gm::L, D2 = Gm::D2, LS = Gm::LS;
+    using Gm = RgGeom<N, AXIS>;
+    constexpr int M = Gm::M, R1 = Gm::R1, R2 = Gm::R2, G = Gm::G, L = Gm::L, D2 = Gm::D2, E = Gm::E;
+    constexpr int LS2 = Gm::LS2;
     constexpr int n = N - 1;
+    constexpr int ITEMS = M + 1;  // fold items per line: j = 0..M
     extern __shared__ __align__(16) unsigned char smem_raw[];
-    T* S = reinterpret_cast<T*>(smem_raw);
+    T2* S = reinterpret_cast<T2*>(smem_raw);
+    T* Sr = reinterpret_cast<T*>(smem_raw);
     const int nx = geo.nx, ny = geo.ny, nz = geo.nz;
     const int tid = threadIdx.x;
     constexpr int nthr = L * G;
@@ -139,110 +144,98 @@ __global__ void __launch_bounds__(256) k_sine_rg(const Tin* in, Tout* out, SineG
         nact = min(L, nx - x0);
     }
 
-    // ---- load phase: staged lines x[1..n], x[0] = x[N] = 0
-    for (int i = tid; i < L; i += nthr) {
-        S[rg_pos<N, AXIS>(i, 0)] = T(0);
-        S[rg_pos<N, AXIS>(i, N)] = T(0);
-    }
-    if (AXIS == 0) {
-        const int total = nact * n;
-        const long long base = voff + (long long)row0 * n;
-        for (int e0 = tid; e0 < total; e0 += kLoadBatch * nthr) {
-            T v[kLoadBatch];
-            if (MODE == kResidual) {
-#pragma unroll 2
-                for (int q = 0; q < kLoadBatch; q++) {
-                    const int e = e0 + q * nthr;
-                    if (e < total) {
-                        const int r = e / n, c = e - r * n;
-                        const int R = row0 + r;
-                        const int zz = geo.div_ny.div(R), yy = R - zz * ny;
-                        SineFused f2 = fu;
-                        f2.f += voff;
-                        f2.uhi += voff;
-                        if (f2.ulo) f2.ulo += voff;
-                        v[q] = T(residual_at(f2, (long long)R * n + c, c, yy, zz, nx, ny, nz));
+    // ---- load + fold: item (line, j) reads x_j and x_{N-j} and writes
+    // y_j = w_j (a+b) + (a-b)/2 and y_{N-j} = w_j (a+b) - (a-b)/2
+    {
+        const T half = T(0.5);
+        constexpr int total = L * ITEMS;
+        for (int e0 = tid; e0 < total; e0 += 4 * nthr) {
+            T av[4], bv[4];
+            int lv[4], jv[4];
+#pragma unroll
+            for (int q = 0; q < 4; q++) {
+                const int e = e0 + q * nthr;
+                int line, j;
+                if (AXIS == 0) {
+                    line = e / ITEMS;
+                    j = e - line * ITEMS;
+                } else {
+                    j = e / L;
+                    line = e - j * L;
+                }
+                lv[q] = line;
+                jv[q] = j;
+                T a = T(0), b = T(0);
+                if (e < total && line < nact && j >= 1) {
+                    if (AXIS == 0) {
+                        const int R = row0 + line;
+                        if (MODE == kResidual) {
+                            const int zz = geo.div_ny.div(R), yy = R - zz * ny;
+                            SineFused f2 = fu;
+                            f2.f += voff;
+                            f2.uhi += voff;
+                            if (f2.ulo) f2.ulo += voff;
+                            const long long rb = (long long)R * n;
+                            a = T(residual_at(f2, rb + j - 1, j - 1, yy, zz, nx, ny, nz));
+                            b = T(residual_at(f2, rb + n - j, n - j, yy, zz, nx, ny, nz));
+                        } else {
+                            const Tin* p = in + voff + (long long)R * n;
+                            if (MODE == kRound) {
+                                a = T(f64_to_f32((double)p[j - 1]));
+                                b = T(f64_to_f32((double)p[n - j]));
+                            } else {
+                                a = T(p[j - 1]);
+                                b = T(p[n - j]);
+                            }
+                        }
+                    } else {
+                        const Tin* p = in + voff + ((long long)z * ny) * nx + x0 + line;
+                        if (MODE == kRound) {
+                            a = T(f64_to_f32((double)p[(long long)(j - 1) * nx]));
+                            b = T(f64_to_f32((double)p[(long long)(n - j) * nx]));
+                        } else {
+                            a = T(p[(long long)(j - 1) * nx]);
+                            b = T(p[(long long)(n - j) * nx]);
+                        }
                     }
                 }
-            } else {
+                av[q] = a;
+                bv[q] = b;
+            }
 #pragma unroll
-                for (int q = 0; q < kLoadBatch; q++) {
-                    const int e = e0 + q * nthr;
-                    if (e < total) {
-                        if (MODE == kRound) v[q] = T(f64_to_f32((double)in[base + e]));
-                        else v[q] = T(in[base + e]);
+            for (int q = 0; q < 4; q++) {
+                const int e = e0 + q * nthr;
+                if (e < total) {
+                    const int line = lv[q], j = jv[q];
+                    T* base = Sr + 2 * (size_t)line * LS2;
+                    if (j == 0) {
+                        base[0] = T(0);
+                    } else {
+                        const T w = ldg(tb.wpre + j);
+                        const T sm = w * (av[q] + bv[q]), df = half * (av[q] - bv[q]);
+                        base[j] = sm + df;
+                        if (j != M) base[N - j] = sm - df;
                     }
-                }
-            }
-#pragma unroll
-            for (int q = 0; q < kLoadBatch; q++) {
-                const int e = e0 + q * nthr;
-                if (e < total) {
-                    const int r = e / n, c = e - r * n;
-                    S[rg_pos<N, AXIS>(r, c + 1)] = v[q];
-                }
-            }
-        }
-        for (int e = nact * n + tid; e < L * n; e += nthr) {
-            const int r = e / n, c = e - r * n;
-            S[rg_pos<N, AXIS>(r, c + 1)] = T(0);
-        }
-    } else {
-        const int total = n * L;
-        const long long base = voff + ((long long)z * ny) * nx + x0;
-        for (int e0 = tid; e0 < total; e0 += kLoadBatch * nthr) {
-            T v[kLoadBatch];
-#pragma unroll
-            for (int q = 0; q < kLoadBatch; q++) {
-                const int e = e0 + q * nthr;
-                const int y = e / L, c = e - y * L;
-                v[q] = T(0);
-                if (e < total && c < nact) {
-                    if (MODE == kRound) v[q] = T(f64_to_f32((double)in[base + (long long)y * nx + c]));
-                    else v[q] = T(in[base + (long long)y * nx + c]);
-                }
-            }
-#pragma unroll
-            for (int q = 0; q < kLoadBatch; q++) {
-                const int e = e0 + q * nthr;
-                if (e < total) {
-                    const int y = e / L, c = e - y * L;
-                    S[rg_pos<N, AXIS>(c, y + 1)] = v[q];
                 }
             }
         }
     }
     __syncthreads();
 
-    // ---- pass 1: fold + DFT_R1 + twiddle
-    T2 v[R1];
-    {
-        const T half = T(0.5);
-#pragma unroll
-        for (int j1 = 0; j1 < R1; j1++) {
-            const int m = j1 * R2 + g;
-            const int a0 = 2 * m, a1 = 2 * m + 1;
-            T y0 = T(0);
-            if (m > 0) {
-                const T a = S[rg_pos<N, AXIS>(l, a0)], b = S[rg_pos<N, AXIS>(l, N - a0)];
-                y0 = ldg(tb.wpre + a0) * (a + b) + half * (a - b);
-            }
-            const T a = S[rg_pos<N, AXIS>(l, a1)], b = S[rg_pos<N, AXIS>(l, N - a1)];
-            const T y1 = ldg(tb.wpre + a1) * (a + b) + half * (a - b);
-            v[j1].x = y0;
-            v[j1].y = y1;
-        }
-        dft_reg<T, R1>(v);
-        if (g) {
-#pragma unroll
-            for (int k1 = 1; k1 < R1; k1++) v[k1] = cmul<T>(v[k1], ldg(tb.tw + ((g * k1) & (M - 1))));
-        }
-    }
-    __syncthreads();  // every line has read its staged input; the regions are reused below
+    T2* Ls = S + (size_t)l * LS2;  // this line's slots
 
-    T2* Cl = reinterpret_cast<T2*>(S + (size_t)l * LS) + 8 * (l & 1);
+    // ---- pass 1: DFT_R1 + twiddle
+    T2 v[R1];
 #pragma unroll
-    for (int k1 = 0; k1 < R1; k1++) Cl[k1 * (R2 + 1) + g] = v[k1];
+    for (int j1 = 0; j1 < R1; j1++) v[j1] = Ls[j1 * R2 + g];
+    dft_reg<T, R1>(v);
+    if (g) {
+#pragma unroll
+        for (int k1 = 1; k1 < R1; k1++) v[k1] = cmul<T>(v[k1], ldg(tb.tw + ((g * k1) & (M - 1))));
+    }
+    __syncwarp();
+#pragma unroll
+    for (int k1 = 0; k1 < R1; k1++) Ls[k1 * (R2 + 1) + g] = v[k1];
     __syncwarp();
 
     // ---- pass 2: D2 DFTs of length R2 per thread
@@ -251,7 +244,7 @@ __global__ void __launch_bounds__(256) k_sine_rg(const Tin* in, Tout* out, SineG
     for (int d = 0; d < D2; d++) {
         const int k1 = g * D2 + d;
 #pragma unroll
-        for (int j2 = 0; j2 < R2; j2++) u[d][j2] = Cl[k1 * (R2 + 1) + j2];
+        for (int j2 = 0; j2 < R2; j2++) u[d][j2] = Ls[k1 * (R2 + 1) + j2];
         dft_reg<T, R2>(u[d]);
     }
     __syncwarp();
@@ -259,57 +252,96 @@ __global__ void __launch_bounds__(256) k_sine_rg(const Tin* in, Tout* out, SineG
     for (int d = 0; d < D2; d++) {
         const int k1 = g * D2 + d;
 #pragma unroll
-        for (int k2 = 0; k2 < R2; k2++) Cl[skew_c(k1 + R1 * k2)] = u[d][k2];
+        for (int k2 = 0; k2 < R2; k2++) Ls[sk(k1 + R1 * k2)] = u[d][k2];
     }
     __syncwarp();
 
-    // ---- unpack + prefix sum over this thread's block of R1 consecutive k
-    T ev[R1], od[R1];
+    // ---- unpack: pairs (k, M-k) for k in [g*E, g*E + E)
+    T ra[E], ia[E], rb[E], ib[E];
+    T rmid = T(0), imid = T(0);
 #pragma unroll
-    for (int t = 0; t < R1; t++) {
-        const int k = g * R1 + t;
-        const T2 ck = Cl[skew_c(k)];
-        const T2 cm = Cl[skew_c((M - k) & (M - 1))];
-        const T ex = T(0.5) * (ck.x + cm.x), ey = T(0.5) * (ck.y - cm.y);
-        const T ox = T(0.5) * (ck.y + cm.y), oy = T(-0.5) * (ck.x - cm.x);
-        const T2 w = ldg(tb.post + k);
-        T yr = ex + (w.x * ox - w.y * oy);
-        const T yi = ey + (w.x * oy + w.y * ox);
-        if (k == 0) yr *= T(0.5);
-        ev[t] = -yi;
-        od[t] = yr;
+    for (int t = 0; t < E; t++) {
+        const int k = g * E + t;
+        const T2 ck = Ls[sk(k)];
+        if (k == 0) {
+            ra[t] = T(0.5) * (ck.x + ck.y);  // Re Y_0, halved in the running sum
+            ia[t] = T(0);
+            const T2 cmid = Ls[sk(M / 2)];
+            rmid = cmid.x;
+            imid = -cmid.y;
+            rb[t] = T(0);
+            ib[t] = T(0);
+        } else {
+            const T2 cm = Ls[sk(M - k)];
+            const T ex = T(0.5) * (ck.x + cm.x), ey = T(0.5) * (ck.y - cm.y);
+            const T ox = T(0.5) * (ck.y + cm.y), oy = T(-0.5) * (ck.x - cm.x);
+            const T2 w = ldg(tb.post + k);
+            const T wx = w.x * ox - w.y * oy, wy = w.x * oy + w.y * ox;
+            ra[t] = ex + wx;
+            ia[t] = ey + wy;
+            rb[t] = ex - wx;    // Re Y_{M-k}
+            ib[t] = wy - ey;    // Im Y_{M-k}
+        }
     }
-    // running sum of the odd terms: local inclusive prefix, then the
-    // exclusive offset from the lanes before (segmented shuffle scan)
+    // running sums: first half in ascending k (blocks g = 0..G-1), then
+    // Y_{M/2}, then the mirrored blocks in ascending k (g = G-1..0, each
+    // walked from t = E-1 down to t = 0)
+    T pa[E], pb[E];
+    pa[0] = ra[0];
 #pragma unroll
-    for (int t = 1; t < R1; t++) od[t] += od[t - 1];
-    T incl = od[R1 - 1];
+    for (int t = 1; t < E; t++) pa[t] = pa[t - 1] + ra[t];
+    pb[E - 1] = rb[E - 1];
+#pragma unroll
+    for (int t = E - 2; t >= 0; t--) pb[t] = pb[t + 1] + rb[t];
+    const T ta = pa[E - 1], tbk = pb[0];
+    T inca = ta;
 #pragma unroll
     for (int off = 1; off < G; off <<= 1) {
-        const T t = __shfl_up_sync(0xffffffffu, incl, off, G);
-        if (g >= off) incl += t;
+        const T x = __shfl_up_sync(0xffffffffu, inca, off, G);
+        if (g >= off) inca += x;
     }
-    const T excl = incl - od[R1 - 1];
+    T incb = tbk;
 #pragma unroll
-    for (int t = 0; t < R1; t++) od[t] += excl;
-    __syncthreads();  // every line has read its C; staged outputs overwrite the regions
+    for (int off = 1; off < G; off <<= 1) {
+        const T x = __shfl_down_sync(0xffffffffu, incb, off, G);
+        if (g + off < G) incb += x;
+    }
+    const T s1 = __shfl_sync(0xffffffffu, inca, G - 1, G);
+    const T rm = __shfl_sync(0xffffffffu, rmid, 0, G);
+    const T exa = inca - ta, exb = incb - tbk;
+    const T bbase = s1 + rm + exb;
+    __syncwarp();
 #pragma unroll
-    for (int t = 0; t < R1; t++) {
-        const int k = g * R1 + t;
-        if (k > 0) S[rg_pos<N, AXIS>(l, 2 * k)] = ev[t];
-        S[rg_pos<N, AXIS>(l, 2 * k + 1)] = od[t];
+    for (int t = 0; t < E; t++) {
+        const int k = g * E + t;
+        T2 fa;
+        fa.x = -ia[t];
+        fa.y = exa + pa[t];
+        Ls[sk(k)] = fa;
+        if (k > 0) {
+            T2 fb;
+            fb.x = -ib[t];
+            fb.y = bbase + pb[t];
+            Ls[sk(M - k)] = fb;
+        }
+    }
+    if (g == 0) {
+        T2 fm;
+        fm.x = -imid;
+        fm.y = s1 + rmid;
+        Ls[sk(M / 2)] = fm;
     }
     __syncthreads();
 
-    // ---- store phase
+    // ---- store phase: entry i of line l is component i&1 of slot sk(i>>1)
     if (AXIS == 0) {
         const int total = nact * n;
         const long long base = voff + (long long)row0 * n;
         if (MODE == kCombine) {
             float cc = 0.f, uu = 0.f;
             for (int e = tid; e < total; e += nthr) {
-                const int r = e / n, c = e - r * n;
-                const float cv = (float)(scale * S[rg_pos<N, AXIS>(r, c + 1)]);
+                const int r = e / n, i = e - r * n + 1;
+                const float cv = (float)(scale * Sr[2 * ((size_t)r * LS2 + sk(i >> 1)) + (i & 1)]);
                 const long long idx = base + e;
                 const float h = fu.uhi[idx];
                 const float lo = fu.ulo ? fu.ulo[idx] : 0.f;
@@ -343,23 +375,24 @@ __global__ void __launch_bounds__(256) k_sine_rg(const Tin* in, Tout* out, SineG
             }
         } else {
             for (int e = tid; e < total; e += nthr) {
-                const int r = e / n, c = e - r * n;
-                out[base + e] = Tout(scale * S[rg_pos<N, AXIS>(r, c + 1)]);
+                const int r = e / n, i = e - r * n + 1;
+                out[base + e] = Tout(scale * Sr[2 * ((size_t)r * LS2 + sk(i >> 1)) + (i & 1)]);
             }
         }
     } else {
         const int total = n * L;
         const long long base = voff + ((long long)z * ny) * nx + x0;
         for (int e = tid; e < total; e += nthr) {
-            const int y = e / L, c = e - y * L;
-            if (c < nact) out[base + (long long)y * nx + c] = Tout(scale * S[rg_pos<N, AXIS>(c, y + 1)]);
+            const int y = e / L, c = e - y * L, i = y + 1;
+            if (c < nact)
+                out[base + (long long)y * nx + c] = Tout(scale * Sr[2 * ((size_t)c * LS2 + sk(i >> 1)) + (i & 1)]);
         }
     }
 }
 
-template <typename T, int N>
+template <typename T, int N, int AXIS>
 constexpr size_t rg_smem_bytes() {
-    return (size_t)RgGeom<N>::L * RgGeom<N>::LS * sizeof(T);
+    return (size_t)RgGeom<N, AXIS>::L * RgGeom<N, AXIS>::LS2 * sizeof(vec2_t<T>);
 }
 
 }  // namespace fdmgpu
