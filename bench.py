@@ -47,7 +47,7 @@ SOLVE_BYTES_PER_POINT = 16
 KERNEL_BYTES = {
     "sine_x_round": 12, "sine_x_resid": 16, "sine_x_combine": 16, "sine_x_f32": 8, "sine_x_f32_out64": 12,
     "sine_y_f32": 8, "sine_x_f64": 16, "sine_y_f64": 16, "zsolve_f32": 8, "zsolve_f64": 16,
-    "tridiag_f32": 8, "tridiag_f64": 16,
+    "tridiag_f32": 8, "tridiag_f64": 16, "residual_ff": 16,
 }
 
 

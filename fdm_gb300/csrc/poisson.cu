@@ -209,6 +209,14 @@ static void zsolve_lines(T* W, int nx, int ny, int nz, int nvol, const T* lamx, 
     launch_tridiag<T>(W, nx * ny, nz, nx, 1, nx, (long long)nx * ny, vs, nvol, lamx, lamy, h2, gscale, st);
 }
 
+static void launch_residual(const SineFused& fr, float* W, int nx, int ny, int nz, int nvol, cudaStream_t st) {
+    const long long vol = (long long)nx * ny * nz;
+    dim3 grid((unsigned)((vol + 255) / 256), nvol);
+    FDM_TIMED("residual_ff", st);
+    k_residual<<<grid, 256, 0, st>>>(fr, W, nx, ny, nz, vol, FastDiv((unsigned)nx), FastDiv((unsigned)ny));
+    FDM_LAUNCH_CHECK();
+}
+
 static void check_grid_y(int nrhs) {
     if (nrhs < 1 || nrhs > 65535) FDM_FAIL(FDMGPU_EINVAL, "nrhs must be in [1, 65535], got %d", nrhs);
 }
@@ -234,6 +242,62 @@ struct CubePlan {
     DevBuf hin, hout;
     int last_sweeps = 0, last_nrhs = 0;
     cudaStream_t last_stream = 0;
+    // host-batch pipeline: copy-in, compute and copy-out streams, a ring of
+    // device slots and the events that order their reuse
+    static constexpr int kRing = 3;
+    cudaStream_t pst[3] = {nullptr, nullptr, nullptr};
+    cudaEvent_t ev_in[kRing] = {}, ev_comp[kRing] = {}, ev_out[kRing] = {};
+    DevBuf ring_in, ring_out;
+
+    ~CubePlan() {
+        for (int i = 0; i < kRing; i++) {
+            if (ev_in[i]) cudaEventDestroy(ev_in[i]);
+            if (ev_comp[i]) cudaEventDestroy(ev_comp[i]);
+            if (ev_out[i]) cudaEventDestroy(ev_out[i]);
+        }
+        for (auto& q : pst)
+            if (q) cudaStreamDestroy(q);
+    }
+
+    // nrhs host volumes: chunk i is copied in on stream 0 while chunk i-1 is
+    // solved on stream 1 and chunk i-2 is copied out on stream 2.
+    void solve_host_pipelined(void* ans, const void* rhs, int nrhs) {
+        if (!pst[0]) {
+            for (auto& q : pst) FDM_CUDA(cudaStreamCreateWithFlags(&q, cudaStreamNonBlocking));
+            for (int i = 0; i < kRing; i++) {
+                FDM_CUDA(cudaEventCreateWithFlags(&ev_in[i], cudaEventDisableTiming));
+                FDM_CUDA(cudaEventCreateWithFlags(&ev_comp[i], cudaEventDisableTiming));
+                FDM_CUDA(cudaEventCreateWithFlags(&ev_out[i], cudaEventDisableTiming));
+            }
+        }
+        const size_t eb = dtype == FDMGPU_F64 ? sizeof(double) : sizeof(float);
+        const size_t vb = (size_t)vol() * eb;
+        char* din = (char*)ring_in.get(vb * kRing);
+        char* dout = (char*)ring_out.get(vb * kRing);
+        // the slots may still be in use by a previous call on these streams
+        for (auto& q : pst) FDM_CUDA(cudaStreamSynchronize(q));
+        bool used[kRing] = {false, false, false};
+        for (int i = 0; i < nrhs; i++) {
+            const int s = i % kRing;
+            char* si = din + s * vb;
+            char* so = dout + s * vb;
+            if (used[s]) FDM_CUDA(cudaStreamWaitEvent(pst[0], ev_comp[s], 0));
+            FDM_CUDA(cudaMemcpyAsync(si, (const char*)rhs + (size_t)i * vb, vb, cudaMemcpyHostToDevice, pst[0]));
+            FDM_CUDA(cudaEventRecord(ev_in[s], pst[0]));
+            FDM_CUDA(cudaStreamWaitEvent(pst[1], ev_in[s], 0));
+            if (used[s]) FDM_CUDA(cudaStreamWaitEvent(pst[1], ev_out[s], 0));
+            solve_device(so, si, 1, pst[1]);
+            FDM_CUDA(cudaEventRecord(ev_comp[s], pst[1]));
+            FDM_CUDA(cudaStreamWaitEvent(pst[2], ev_comp[s], 0));
+            FDM_CUDA(cudaMemcpyAsync((char*)ans + (size_t)i * vb, so, vb, cudaMemcpyDeviceToHost, pst[2]));
+            FDM_CUDA(cudaEventRecord(ev_out[s], pst[2]));
+            used[s] = true;
+        }
+        FDM_CUDA(cudaStreamSynchronize(pst[2]));
+        FDM_CUDA(cudaStreamSynchronize(pst[1]));
+        last_stream = pst[1];
+        last_nrhs = 1;
+    }
 
     void init() {
         slx = std::sqrt(2. / lx);
@@ -345,7 +409,8 @@ struct CubePlan {
             fr.ulo = s >= 2 ? UL : nullptr;
             fr.cx = split_host(cx); fr.cy = split_host(cy); fr.cz = split_host(cz);
             fr.cxf = (float)cx; fr.cyf = (float)cy; fr.czf = (float)cz;
-            forward_xy<float, float, kResidual>(nullptr, W, nrhs, tx32, ty32, st, &fr);
+            launch_residual(fr, W, nx, ny, nz, nrhs, st);
+            forward_xy<float, float>(W, W, nrhs, tx32, ty32, st);
             zsolve<float>(W, nrhs, lamx32, lamy32, st);
             launch_sine<float, float, float, 1>(W, W, nx, ny, nz, nrhs, ty32.view(), sly, st);
             SineFused fc;
@@ -592,7 +657,8 @@ static void noalloc_solve(double dx, double dy, double dz, double lx, double ly,
         fr.ulo = s >= 2 ? UL : nullptr;
         fr.cx = CubePlan::split_host(cx); fr.cy = CubePlan::split_host(cy); fr.cz = CubePlan::split_host(cz);
         fr.cxf = (float)cx; fr.cyf = (float)cy; fr.czf = (float)cz;
-        launch_sine<float, float, float, 0, kResidual>(nullptr, W, nx, ny, nz, nrhs, tx, scx, st, &fr);
+        launch_residual(fr, W, nx, ny, nz, nrhs, st);
+        launch_sine<float, float, float, 0>(W, W, nx, ny, nz, nrhs, tx, scx, st);
         launch_sine<float, float, float, 1>(W, W, nx, ny, nz, nrhs, ty, scy, st);
         zsolve_lines<float>(W, nx, ny, nz, nrhs, ax.lam, ay.lam, h2, gscale, st);
         launch_sine<float, float, float, 1>(W, W, nx, ny, nz, nrhs, ty, sly, st);
@@ -673,15 +739,8 @@ int fdmgpu_lapl_cube_solve(fdmgpu_lapl_cube* h, void* ans, const void* rhs) {
 int fdmgpu_lapl_cube_solve_host_batch(fdmgpu_lapl_cube* h, void* ans, const void* rhs, int nrhs) {
     FDM_API_BEGIN
     if (!h || !ans || !rhs) FDM_FAIL(FDMGPU_EINVAL, "null argument");
-    CubePlan& c = h->plan;
-    check_grid_y(nrhs);
-    const size_t bytes = (size_t)c.vol() * elem_size(c.dtype) * nrhs;
-    void* din = c.hin.get(bytes);
-    void* dout = c.hout.get(bytes);
-    FDM_CUDA(cudaMemcpyAsync(din, rhs, bytes, cudaMemcpyHostToDevice, 0));
-    c.solve_device(dout, din, nrhs, 0);
-    FDM_CUDA(cudaMemcpyAsync(ans, dout, bytes, cudaMemcpyDeviceToHost, 0));
-    FDM_CUDA(cudaStreamSynchronize(0));
+    if (nrhs < 1) FDM_FAIL(FDMGPU_EINVAL, "nrhs must be positive");
+    h->plan.solve_host_pipelined(ans, rhs, nrhs);
     FDM_API_END
 }
 

@@ -272,6 +272,25 @@ __device__ __forceinline__ float residual_at(const SineFused& fu, long long idx,
     return (r.h + (r.l - alo));
 }
 
+// r = f - A(uhi + ulo) for every interior point of a batch of volumes,
+// float-float as residual_at, written as FP32.  One thread per point, x
+// fastest: the stencil's neighbour loads are coalesced along x and served by
+// L1/L2 across y and z.  gridDim.y indexes the volume.
+__global__ void __launch_bounds__(256) k_residual(SineFused fu, float* __restrict__ r, int nx, int ny, int nz,
+                                                  long long vstride, FastDiv div_nx, FastDiv div_ny) {
+    const long long vol = (long long)nx * ny * nz;
+    const int e = blockIdx.x * blockDim.x + threadIdx.x;
+    if (e >= vol) return;
+    const long long voff = (long long)blockIdx.y * vstride;
+    const int row = div_nx.div(e), x = e - row * nx;
+    const int z = div_ny.div(row), y = row - z * ny;
+    SineFused f2 = fu;
+    f2.f += voff;
+    f2.uhi += voff;
+    if (f2.ulo) f2.ulo += voff;
+    r[voff + e] = residual_at(f2, e, x, y, z, nx, ny, nz);
+}
+
 // One DST pass over every line along x (AXIS 0, rows) or along y (AXIS 1,
 // columns) of a batch of nz*ny*nx volumes (x fastest), out-of-place or
 // in-place.  Rows: a CTA takes L consecutive rows.  Columns: a CTA takes a

@@ -97,8 +97,11 @@ int fdmgpu_lapl_cube_create(fdmgpu_lapl_cube** h, int dtype, int bc_flags,
 int fdmgpu_lapl_cube_set_precision(fdmgpu_lapl_cube* h, int precision, double tol, int max_sweeps);
 /* host pointers, synchronous (LaplCube::solve, src/lapl_cube.cpp:9) */
 int fdmgpu_lapl_cube_solve(fdmgpu_lapl_cube* h, void* ans, const void* rhs);
-/* host pointers, nrhs volumes back to back, synchronous: copies in, solves
- * the batch, copies out (page-locked host memory makes the copies faster) */
+/* host pointers, nrhs volumes back to back, synchronous.  The volumes are
+ * pipelined one at a time through a ring of three device slots: the copy-in
+ * of one volume, the solve of the previous one and the copy-out of the one
+ * before overlap on three streams (page-locked host memory is needed for the
+ * copies to overlap).  last_info afterwards reports the last volume. */
 int fdmgpu_lapl_cube_solve_host_batch(fdmgpu_lapl_cube* h, void* ans, const void* rhs, int nrhs);
 /* device pointers; nrhs volumes back to back (stride nz*ny*nx elements);
  * asynchronous on stream */

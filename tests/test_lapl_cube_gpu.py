@@ -168,6 +168,29 @@ def test_mixed_tolerance_levels(cuda):
         assert err <= max(tol, 1e-13), (tol, err)
 
 
+@pytest.mark.parametrize("pinned", [True, False])
+def test_host_batch_pipeline_equals_device(cuda, pinned):
+    """The pipelined host-pointer batch (ring of 3 device slots) gives the
+    same answers as device-pointer solves, for more volumes than slots."""
+    import torch
+    n = 63
+    args = workloads.solver_args(n, n, n)
+    fs = torch.stack([workloads.manufactured_torch(n, n, n, seed=s, kmax=16, noise=1e-3)[0] for s in range(5)])
+    for prec in ("plain", "mixed"):
+        lc = LaplCube(*args, precision=prec)
+        dev_out = torch.empty_like(fs)
+        for i in range(5):
+            lc.solve_device(dev_out[i], fs[i].contiguous())
+        hin = fs.cpu().pin_memory() if pinned else fs.cpu()
+        hout = torch.empty_like(hin)
+        if pinned:
+            hout = hout.pin_memory()
+        lc.solve_batch(hout, hin, 5)
+        lc.solve_batch(hout, hin, 5)  # a second call reuses the ring
+        torch.cuda.synchronize()
+        assert torch.equal(hout, dev_out.cpu()), prec
+
+
 def test_errors_like_reference(cuda):
     with pytest.raises(FdmError) as e:
         LaplCube(0.1, 0.1, 0.1, 3.3, 3.3, 3.3, 32, 31, 31)
