@@ -211,10 +211,81 @@ static void zsolve_lines(T* W, int nx, int ny, int nz, int nvol, const T* lamx, 
 
 static void launch_residual(const SineFused& fr, float* W, int nx, int ny, int nz, int nvol, cudaStream_t st) {
     const long long vol = (long long)nx * ny * nz;
-    dim3 grid((unsigned)((vol + 255) / 256), nvol);
+    const int segs = (nx + kResX - 1) / kResX;
+    const long long threads = (long long)ny * nz * segs;
+    dim3 grid((unsigned)((threads + 255) / 256), nvol);
     FDM_TIMED("residual_ff", st);
-    k_residual<<<grid, 256, 0, st>>>(fr, W, nx, ny, nz, vol, FastDiv((unsigned)nx), FastDiv((unsigned)ny));
+    k_residual<<<grid, 256, 0, st>>>(fr, W, nx, ny, nz, vol, segs, FastDiv((unsigned)segs), FastDiv((unsigned)ny));
     FDM_LAUNCH_CHECK();
+}
+
+// Block / separator factors of the partitioned z-solve for every
+// (x-mode, y-mode), computed in FP64 and stored in T (layout: k_zsolve_tab).
+// Returns false when the line length does not split (the kernel without a
+// table is used then).
+template <typename T>
+static bool zsolve_table_host(DevBuf& buf, int nx, int ny, int nz, const std::vector<double>& lamx,
+                              const std::vector<double>& lamy, double h2, int* m_out, int* P_out) {
+    const int m = nz < 15 ? nz : 15;
+    const int P = (nz + 1) / (m + 1);
+    if ((m + 1) * P != nz + 1 || P > 16) return false;
+    const int modes = nx * ny;
+    const int nv = 2 * m + 2 * (P - 1);
+    std::vector<T> t((size_t)nv * modes);
+    std::vector<double> cp(m), be(m);
+    for (int k = 0; k < ny; k++)
+        for (int j = 0; j < nx; j++) {
+            const int mode = k * nx + j;
+            const double b = -2.0 - (lamx[j] + lamy[k]) * h2;
+            double c = 0.0;
+            for (int i = 0; i < m; i++) {
+                c = 1.0 / (b - c);
+                cp[i] = c;
+            }
+            be[m - 1] = -cp[m - 1];
+            for (int i = m - 2; i >= 0; i--) be[i] = -cp[i] * be[i + 1];
+            for (int i = 0; i < m; i++) {
+                t[(size_t)i * modes + mode] = (T)cp[i];
+                t[(size_t)(m + i) * modes + mode] = (T)be[i];
+            }
+            const double lo = be[0], dg = b + 2.0 * be[m - 1];
+            double pc = 0.0;
+            for (int q = 0; q < P - 1; q++) {
+                const double r = 1.0 / (dg - lo * pc);
+                pc = lo * r;
+                t[(size_t)(2 * m + q) * modes + mode] = (T)r;
+                t[(size_t)(2 * m + P - 1 + q) * modes + mode] = (T)pc;
+            }
+        }
+    FDM_CUDA(cudaMemcpy(buf.get(t.size() * sizeof(T)), t.data(), t.size() * sizeof(T), cudaMemcpyHostToDevice));
+    *m_out = m;
+    *P_out = P;
+    return true;
+}
+
+template <typename T>
+static void zsolve_tab_launch(T* W, int nx, int ny, int nz, int nvol, const T* tab, int m, int P, double gscale,
+                              cudaStream_t st) {
+    const size_t smem = (size_t)4 * P * 32 * sizeof(T);
+    dim3 grid((unsigned)(ny * ((nx + 31) / 32)), nvol);
+    const long long vs = (long long)nx * ny * nz;
+    FDM_TIMED(sizeof(T) == 8 ? "zsolve_f64" : "zsolve_f32", st);
+    switch (m) {
+        case 1: k_zsolve_tab<T, 1><<<grid, 32 * P, smem, st>>>(W, nx, ny, P, vs, tab, (T)gscale); break;
+        case 3: k_zsolve_tab<T, 3><<<grid, 32 * P, smem, st>>>(W, nx, ny, P, vs, tab, (T)gscale); break;
+        case 7: k_zsolve_tab<T, 7><<<grid, 32 * P, smem, st>>>(W, nx, ny, P, vs, tab, (T)gscale); break;
+        default: k_zsolve_tab<T, 15><<<grid, 32 * P, smem, st>>>(W, nx, ny, P, vs, tab, (T)gscale); break;
+    }
+    FDM_LAUNCH_CHECK();
+}
+
+static std::vector<double> lambda_host(int n, double h) {
+    std::vector<double> v(n);
+    for (int j = 1; j <= n; j++) {
+        const double s = std::sin(j * M_PI * 0.5 / (n + 1));
+        v[j - 1] = 4. / (h * h) * (s * s);
+    }
+    return v;
 }
 
 static void check_grid_y(int nrhs) {
@@ -239,6 +310,8 @@ struct CubePlan {
     AxisTables<float> tx32, ty32;
     DevBuf lamx64, lamy64, lamx32, lamy32;
     DevBuf work32, uhi, ulo, norms;
+    DevBuf ztab64, ztab32;  // partitioned z-solve factors per mode
+    int zm64 = 0, zP64 = 0, zm32 = 0, zP32 = 0;
     DevBuf hin, hout;
     int last_sweeps = 0, last_nrhs = 0;
     cudaStream_t last_stream = 0;
@@ -343,6 +416,18 @@ struct CubePlan {
     }
     template <typename T>
     void zsolve(T* W, int nrhs, const DevBuf& lx_, const DevBuf& ly_, cudaStream_t st) {
+        DevBuf& tab = sizeof(T) == 8 ? ztab64 : ztab32;
+        int& zm = sizeof(T) == 8 ? zm64 : zm32;
+        int& zP = sizeof(T) == 8 ? zP64 : zP32;
+        if (!tab.p && zm == 0) {
+            if (!zsolve_table_host<T>(tab, nx, ny, nz, lambda_host(nx, hx_eff), lambda_host(ny, dy), hz_eff * hz_eff,
+                                      &zm, &zP))
+                zm = -1;
+        }
+        if (zm > 0) {
+            zsolve_tab_launch<T>(W, nx, ny, nz, nrhs, (const T*)tab.p, zm, zP, zfac * hz_eff * hz_eff, st);
+            return;
+        }
         zsolve_lines<T>(W, nx, ny, nz, nrhs, (const T*)lx_.p, (const T*)ly_.p, hz_eff * hz_eff,
                         zfac * hz_eff * hz_eff, st);
     }
@@ -427,7 +512,8 @@ struct CubePlan {
     }
 
     size_t scratch_bytes() const {
-        return work32.bytes + uhi.bytes + ulo.bytes + norms.bytes + hin.bytes + hout.bytes;
+        return work32.bytes + uhi.bytes + ulo.bytes + norms.bytes + hin.bytes + hout.bytes + ztab32.bytes +
+               ztab64.bytes + ring_in.bytes + ring_out.bytes;
     }
 };
 

@@ -273,22 +273,72 @@ __device__ __forceinline__ float residual_at(const SineFused& fu, long long idx,
 }
 
 // r = f - A(uhi + ulo) for every interior point of a batch of volumes,
-// float-float as residual_at, written as FP32.  One thread per point, x
-// fastest: the stencil's neighbour loads are coalesced along x and served by
-// L1/L2 across y and z.  gridDim.y indexes the volume.
+// float-float as residual_at, written as FP32.  A thread takes kResX
+// consecutive x of one row: the row's values (with one halo on each side)
+// are loaded once and shared for the x-neighbours; the y and z neighbours
+// are coalesced along x and served by L1/L2.  gridDim.y indexes the volume.
+constexpr int kResX = 4;
+
+__device__ __forceinline__ float ff_residual(const ff& fsp, float uc, float xm, float xp, float ym, float yp,
+                                             float zm, float zp, const SineFused& fu, float alo) {
+    const float u2 = uc + uc;
+    ff dx = ff_add_f(two_sum(xm, xp), -u2);
+    ff dy = ff_add_f(two_sum(ym, yp), -u2);
+    ff dz = ff_add_f(two_sum(zm, zp), -u2);
+    ff au = ff_add(ff_add(ff_mul(dx, fu.cx), ff_mul(dy, fu.cy)), ff_mul(dz, fu.cz));
+    ff r = ff_add(fsp, ff{-au.h, -au.l});
+    return r.h + (r.l - alo);
+}
+
 __global__ void __launch_bounds__(256) k_residual(SineFused fu, float* __restrict__ r, int nx, int ny, int nz,
-                                                  long long vstride, FastDiv div_nx, FastDiv div_ny) {
-    const long long vol = (long long)nx * ny * nz;
-    const int e = blockIdx.x * blockDim.x + threadIdx.x;
-    if (e >= vol) return;
+                                                  long long vstride, int segs, FastDiv div_segs, FastDiv div_ny) {
+    const int t = blockIdx.x * blockDim.x + threadIdx.x;
+    const int rows = ny * nz;
+    if (t >= rows * segs) return;
     const long long voff = (long long)blockIdx.y * vstride;
-    const int row = div_nx.div(e), x = e - row * nx;
+    const int row = div_segs.div(t), seg = t - row * segs;
     const int z = div_ny.div(row), y = row - z * ny;
-    SineFused f2 = fu;
-    f2.f += voff;
-    f2.uhi += voff;
-    if (f2.ulo) f2.ulo += voff;
-    r[voff + e] = residual_at(f2, e, x, y, z, nx, ny, nz);
+    const int x0 = seg * kResX;
+    const long long rb = (long long)row * nx;
+    const long long sy = nx, sz = (long long)nx * ny;
+    const float* U = fu.uhi + voff;
+    const float* V = fu.ulo ? fu.ulo + voff : nullptr;
+    const double* F = fu.f + voff;
+    float c[kResX + 2];
+#pragma unroll
+    for (int q = 0; q < kResX + 2; q++) {
+        const int x = x0 - 1 + q;
+        c[q] = (x >= 0 && x < nx) ? U[rb + x] : 0.f;
+    }
+    float ym[kResX], yp[kResX], zm[kResX], zp[kResX];
+    double fv[kResX];
+#pragma unroll
+    for (int q = 0; q < kResX; q++) {
+        const int x = x0 + q;
+        const bool in = x < nx;
+        const long long i = rb + x;
+        ym[q] = (in && y > 0) ? U[i - sy] : 0.f;
+        yp[q] = (in && y < ny - 1) ? U[i + sy] : 0.f;
+        zm[q] = (in && z > 0) ? U[i - sz] : 0.f;
+        zp[q] = (in && z < nz - 1) ? U[i + sz] : 0.f;
+        fv[q] = in ? F[i] : 0.0;
+    }
+#pragma unroll
+    for (int q = 0; q < kResX; q++) {
+        const int x = x0 + q;
+        if (x >= nx) break;
+        const long long i = rb + x;
+        float alo = 0.f;
+        if (V) {
+            const float vc = V[i];
+            const float vxm = x > 0 ? V[i - 1] : 0.f, vxp = x < nx - 1 ? V[i + 1] : 0.f;
+            const float vym = y > 0 ? V[i - sy] : 0.f, vyp = y < ny - 1 ? V[i + sy] : 0.f;
+            const float vzm = z > 0 ? V[i - sz] : 0.f, vzp = z < nz - 1 ? V[i + sz] : 0.f;
+            alo = fu.cxf * ((vxm + vxp) - 2.f * vc) + fu.cyf * ((vym + vyp) - 2.f * vc) +
+                  fu.czf * ((vzm + vzp) - 2.f * vc);
+        }
+        r[voff + i] = ff_residual(f64_split(fv[q]), c[q + 1], c[q], c[q + 2], ym[q], yp[q], zm[q], zp[q], fu, alo);
+    }
 }
 
 // One DST pass over every line along x (AXIS 0, rows) or along y (AXIS 1,

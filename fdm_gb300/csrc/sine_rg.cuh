@@ -339,18 +339,35 @@ __global__ void __launch_bounds__(256) k_sine_rg(const Tin* in, Tout* out, SineG
         const long long base = voff + (long long)row0 * n;
         if (MODE == kCombine) {
             float cc = 0.f, uu = 0.f;
-            for (int e = tid; e < total; e += nthr) {
-                const int r = e / n, i = e - r * n + 1;
-                const float cv = (float)(scale * Sr[2 * ((size_t)r * LS2 + sk(i >> 1)) + (i & 1)]);
-                const long long idx = base + e;
-                const float h = fu.uhi[idx];
-                const float lo = fu.ulo ? fu.ulo[idx] : 0.f;
-                ff s2 = two_sum(h, lo);
-                s2 = ff_add_f(s2, cv);
-                if (fu.last) fu.out64[idx] = ff_to_f64(s2);
-                else fu.ulo_out[idx] = lo + cv;
-                cc += cv * cv;
-                uu += s2.h * s2.h;
+            // batches of 4 elements per thread: the uhi / ulo loads of a
+            // batch are issued before any of them is used
+            for (int e0 = tid; e0 < total; e0 += 4 * nthr) {
+                float hv[4], lv[4];
+#pragma unroll
+                for (int q = 0; q < 4; q++) {
+                    const int e = e0 + q * nthr;
+                    hv[q] = 0.f;
+                    lv[q] = 0.f;
+                    if (e < total) {
+                        hv[q] = fu.uhi[base + e];
+                        if (fu.ulo) lv[q] = fu.ulo[base + e];
+                    }
+                }
+#pragma unroll
+                for (int q = 0; q < 4; q++) {
+                    const int e = e0 + q * nthr;
+                    if (e < total) {
+                        const int r = e / n, i = e - r * n + 1;
+                        const float cv = (float)(scale * Sr[2 * ((size_t)r * LS2 + sk(i >> 1)) + (i & 1)]);
+                        const long long idx = base + e;
+                        ff s2 = two_sum(hv[q], lv[q]);
+                        s2 = ff_add_f(s2, cv);
+                        if (fu.last) fu.out64[idx] = ff_to_f64(s2);
+                        else fu.ulo_out[idx] = lv[q] + cv;
+                        cc += cv * cv;
+                        uu += s2.h * s2.h;
+                    }
+                }
             }
             for (int o = 16; o > 0; o >>= 1) {
                 cc += __shfl_down_sync(0xffffffffu, cc, o);

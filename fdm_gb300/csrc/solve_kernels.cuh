@@ -209,4 +209,79 @@ __global__ void __launch_bounds__(zpart_max_threads<T, m>()) k_zsolve_part(T* W,
     }
 }
 
+// The same partitioned solve with every mode-dependent factor read from a
+// table built once per plan (zsolve_table_host): for mode (x, y) the block
+// pivot reciprocals cp[0..m-1], the right-end response beta[0..m-1] and the
+// separator system's pivot reciprocals rc[0..P-2] and multipliers
+// pc[0..P-2], stored value-major (tab[v * modes + mode]) so lanes read
+// consecutive modes.  With no divisions left the kernel is FMA chains plus
+// coalesced loads; at 255^2 modes the FP32 table is 15.6 MB and stays in L2.
+template <typename T, int m>
+__global__ void __launch_bounds__(512) k_zsolve_tab(T* W, int nx, int ny, int P, long long vstride,
+                                                    const T* __restrict__ tab, T gscale) {
+    extern __shared__ __align__(16) unsigned char zsm[];
+    T* s_vf = reinterpret_cast<T*>(zsm);
+    T* s_vl = s_vf + P * 32;
+    T* s_g = s_vl + P * 32;
+    T* s_u = s_g + P * 32;
+    const int lane = threadIdx.x & 31;
+    const int c = threadIdx.x >> 5;
+    const int ntx = (nx + 31) >> 5;
+    const int y = blockIdx.x / ntx;
+    const int x = ((blockIdx.x - y * ntx) << 5) + lane;
+    const bool act = x < nx;
+    const int modes = nx * ny;
+    const int mode = y * nx + (act ? x : 0);
+    const long long st = (long long)nx * ny;
+    T* p = W + (long long)blockIdx.y * vstride + (long long)y * nx + (act ? x : 0);
+    const int r0 = c * (m + 1);
+
+    T v[m], cp[m];
+#pragma unroll
+    for (int i = 0; i < m; i++) v[i] = act ? p[(r0 + i) * st] : T(0);
+#pragma unroll
+    for (int i = 0; i < m; i++) cp[i] = tab[(size_t)i * modes + mode];
+    T gsep = T(0);
+    if (c < P - 1 && act) gsep = p[(r0 + m) * st];
+    T prev = T(0);
+#pragma unroll
+    for (int i = 0; i < m; i++) {
+        prev = (v[i] * gscale - prev) * cp[i];
+        v[i] = prev;
+    }
+#pragma unroll
+    for (int i = m - 2; i >= 0; i--) v[i] = v[i] - cp[i] * v[i + 1];
+    s_vf[c * 32 + lane] = v[0];
+    s_vl[c * 32 + lane] = v[m - 1];
+    s_g[c * 32 + lane] = gsep * gscale;
+    const T* be = tab + (size_t)m * modes + mode;
+    __syncthreads();
+    if (c == 0 && P > 1) {
+        const T lo = be[0];
+        const T* rc = tab + (size_t)(2 * m) * modes + mode;
+        const T* pc = tab + (size_t)(2 * m + P - 1) * modes + mode;
+        T d = T(0);
+        for (int k = 0; k < P - 1; k++) {
+            const T rhs = s_g[k * 32 + lane] - s_vl[k * 32 + lane] - s_vf[(k + 1) * 32 + lane];
+            d = (rhs - lo * d) * rc[(size_t)k * modes];
+            s_u[k * 32 + lane] = d;
+        }
+        T u = T(0);
+        for (int k = P - 2; k >= 0; k--) {
+            u = s_u[k * 32 + lane] - pc[(size_t)k * modes] * u;
+            s_u[k * 32 + lane] = u;
+        }
+    }
+    __syncthreads();
+    const T ul = c > 0 ? s_u[(c - 1) * 32 + lane] : T(0);
+    const T ur = c < P - 1 ? s_u[c * 32 + lane] : T(0);
+    if (act) {
+#pragma unroll
+        for (int i = 0; i < m; i++) cp[i] = be[(size_t)i * modes];
+#pragma unroll
+        for (int i = 0; i < m; i++) p[(r0 + i) * st] = v[i] + cp[m - 1 - i] * ul + cp[i] * ur;
+        if (c < P - 1) p[(r0 + m) * st] = ur;
+    }
+}
+
 }  // namespace fdmgpu
