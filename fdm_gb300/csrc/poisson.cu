@@ -266,7 +266,7 @@ static bool zsolve_table_host(DevBuf& buf, int nx, int ny, int nz, const std::ve
 template <typename T>
 static void zsolve_tab_launch(T* W, int nx, int ny, int nz, int nvol, const T* tab, int m, int P, double gscale,
                               cudaStream_t st) {
-    const size_t smem = (size_t)4 * P * 32 * sizeof(T);
+    const size_t smem = (size_t)6 * P * 32 * sizeof(T);
     dim3 grid((unsigned)(ny * ((nx + 31) / 32)), nvol);
     const long long vs = (long long)nx * ny * nz;
     FDM_TIMED(sizeof(T) == 8 ? "zsolve_f64" : "zsolve_f32", st);

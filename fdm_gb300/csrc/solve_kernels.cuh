@@ -217,7 +217,7 @@ __global__ void __launch_bounds__(zpart_max_threads<T, m>()) k_zsolve_part(T* W,
 // consecutive modes.  With no divisions left the kernel is FMA chains plus
 // coalesced loads; at 255^2 modes the FP32 table is 15.6 MB and stays in L2.
 template <typename T, int m>
-__global__ void __launch_bounds__(512) k_zsolve_tab(T* W, int nx, int ny, int P, long long vstride,
+__global__ void __launch_bounds__(512, 2) k_zsolve_tab(T* W, int nx, int ny, int P, long long vstride,
                                                     const T* __restrict__ tab, T gscale) {
     extern __shared__ __align__(16) unsigned char zsm[];
     T* s_vf = reinterpret_cast<T*>(zsm);
@@ -232,17 +232,17 @@ __global__ void __launch_bounds__(512) k_zsolve_tab(T* W, int nx, int ny, int P,
     const bool act = x < nx;
     const int modes = nx * ny;
     const int mode = y * nx + (act ? x : 0);
-    const long long st = (long long)nx * ny;
-    T* p = W + (long long)blockIdx.y * vstride + (long long)y * nx + (act ? x : 0);
+    const int st = nx * ny;
     const int r0 = c * (m + 1);
+    T* p = W + (long long)blockIdx.y * vstride + (long long)r0 * st + (long long)y * nx + (act ? x : 0);
 
     T v[m], cp[m];
 #pragma unroll
-    for (int i = 0; i < m; i++) v[i] = act ? p[(r0 + i) * st] : T(0);
+    for (int i = 0; i < m; i++) v[i] = act ? p[i * st] : T(0);
 #pragma unroll
     for (int i = 0; i < m; i++) cp[i] = tab[(size_t)i * modes + mode];
     T gsep = T(0);
-    if (c < P - 1 && act) gsep = p[(r0 + m) * st];
+    if (c < P - 1 && act) gsep = p[m * st];
     T prev = T(0);
 #pragma unroll
     for (int i = 0; i < m; i++) {
@@ -255,20 +255,26 @@ __global__ void __launch_bounds__(512) k_zsolve_tab(T* W, int nx, int ny, int P,
     s_vl[c * 32 + lane] = v[m - 1];
     s_g[c * 32 + lane] = gsep * gscale;
     const T* be = tab + (size_t)m * modes + mode;
+    // warp c copies separator row c's factors into shared memory before the
+    // barrier, so their latency overlaps the block solves
+    T* s_rc = s_u + P * 32;
+    T* s_pc = s_rc + P * 32;
+    if (c < P - 1) {
+        s_rc[c * 32 + lane] = tab[(size_t)(2 * m + c) * modes + mode];
+        s_pc[c * 32 + lane] = tab[(size_t)(2 * m + P - 1 + c) * modes + mode];
+    }
     __syncthreads();
     if (c == 0 && P > 1) {
         const T lo = be[0];
-        const T* rc = tab + (size_t)(2 * m) * modes + mode;
-        const T* pc = tab + (size_t)(2 * m + P - 1) * modes + mode;
         T d = T(0);
         for (int k = 0; k < P - 1; k++) {
             const T rhs = s_g[k * 32 + lane] - s_vl[k * 32 + lane] - s_vf[(k + 1) * 32 + lane];
-            d = (rhs - lo * d) * rc[(size_t)k * modes];
+            d = (rhs - lo * d) * s_rc[k * 32 + lane];
             s_u[k * 32 + lane] = d;
         }
         T u = T(0);
         for (int k = P - 2; k >= 0; k--) {
-            u = s_u[k * 32 + lane] - pc[(size_t)k * modes] * u;
+            u = s_u[k * 32 + lane] - s_pc[k * 32 + lane] * u;
             s_u[k * 32 + lane] = u;
         }
     }
@@ -279,8 +285,8 @@ __global__ void __launch_bounds__(512) k_zsolve_tab(T* W, int nx, int ny, int P,
 #pragma unroll
         for (int i = 0; i < m; i++) cp[i] = be[(size_t)i * modes];
 #pragma unroll
-        for (int i = 0; i < m; i++) p[(r0 + i) * st] = v[i] + cp[m - 1 - i] * ul + cp[i] * ur;
-        if (c < P - 1) p[(r0 + m) * st] = ur;
+        for (int i = 0; i < m; i++) p[i * st] = v[i] + cp[m - 1 - i] * ul + cp[i] * ur;
+        if (c < P - 1) p[m * st] = ur;
     }
 }
 
