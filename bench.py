@@ -189,6 +189,23 @@ def run_reference_arm(args, world, rank):
     print(json.dumps(line), flush=True)
 
 
+def run_ncu_case():
+    """Two mixed solves of 2 RHS at 255^3 (266 MB of FP64 input, larger than
+    L2) with nothing else on the GPU: the case the committed ncu summaries
+    capture."""
+    import torch
+    import fdm_gb300
+    from fdm_gb300 import workloads
+    n = N_INT
+    f = torch.stack([workloads.manufactured_torch(n, n, n, seed=s, kmax=KMAX, noise=NOISE)[0] for s in (0, 1)])
+    out = torch.empty_like(f)
+    m = fdm_gb300.LaplCube(*workloads.solver_args(n, n, n), precision="mixed", tol=TOL)
+    for _ in range(2):
+        m.solve_device(out, f.contiguous(), nrhs=2)
+    torch.cuda.synchronize()
+    print("ncu case done")
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -196,12 +213,17 @@ def main():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--ncu-case", action="store_true",
+                    help="run only two mixed solves of 2 RHS at 255^3 (a small case for profiler captures)")
     ap.add_argument("--chunk", type=int, default=NRHS,
                     help="right-hand sides per solve call within a step (divides 16)")
     args = ap.parse_args()
     args.warmup = max(args.warmup, 3)
 
     world, rank, local = dist_setup()
+    if args.ncu_case:
+        run_ncu_case()
+        return
     if args.impl == "reference":
         run_reference_arm(args, world, rank)
         return

@@ -494,6 +494,7 @@ struct CubePlan {
             fr.ulo = s >= 2 ? UL : nullptr;
             fr.cx = split_host(cx); fr.cy = split_host(cy); fr.cz = split_host(cz);
             fr.cxf = (float)cx; fr.cyf = (float)cy; fr.czf = (float)cz;
+            fr.iso = (cx == cy && cy == cz) ? 1 : 0;
             launch_residual(fr, W, nx, ny, nz, nrhs, st);
             forward_xy<float, float>(W, W, nrhs, tx32, ty32, st);
             zsolve<float>(W, nrhs, lamx32, lamy32, st);
@@ -743,6 +744,7 @@ static void noalloc_solve(double dx, double dy, double dz, double lx, double ly,
         fr.ulo = s >= 2 ? UL : nullptr;
         fr.cx = CubePlan::split_host(cx); fr.cy = CubePlan::split_host(cy); fr.cz = CubePlan::split_host(cz);
         fr.cxf = (float)cx; fr.cyf = (float)cy; fr.czf = (float)cz;
+        fr.iso = (cx == cy && cy == cz) ? 1 : 0;
         launch_residual(fr, W, nx, ny, nz, nrhs, st);
         launch_sine<float, float, float, 0>(W, W, nx, ny, nz, nrhs, tx, scx, st);
         launch_sine<float, float, float, 1>(W, W, nx, ny, nz, nrhs, ty, scy, st);

@@ -225,6 +225,7 @@ struct SineFused {
     const float* ulo;
     ff cx, cy, cz;        // stencil coefficients 1/h^2 / S as float pairs
     float cxf, cyf, czf;  // the same rounded to float (for A ulo)
+    int iso;              // cx == cy == cz: one coefficient times the 6-neighbour sum
     // kCombine
     double* out64;
     float* ulo_out;
@@ -290,6 +291,30 @@ __device__ __forceinline__ float ff_residual(const ff& fsp, float uc, float xm, 
     return r.h + (r.l - alo);
 }
 
+// Isotropic stencil: A u = c (sum of the 6 neighbours - 6 u).  The sum is
+// accumulated as a float plus a float error term (TwoSum per addition), then
+// joined with -6u and multiplied by c in float-float.
+__device__ __forceinline__ float ff_residual_iso(const ff& fsp, float uc, float xm, float xp, float ym, float yp,
+                                                 float zm, float zp, const ff& c, float alo) {
+    ff t = two_sum(xm, xp);
+    float e = t.l;
+    t = two_sum(t.h, ym);
+    e = __fadd_rn(e, t.l);
+    t = two_sum(t.h, yp);
+    e = __fadd_rn(e, t.l);
+    t = two_sum(t.h, zm);
+    e = __fadd_rn(e, t.l);
+    t = two_sum(t.h, zp);
+    e = __fadd_rn(e, t.l);
+    const ff u6 = two_prod(6.f, uc);
+    t = two_sum(t.h, -u6.h);
+    e = __fadd_rn(e, __fsub_rn(t.l, u6.l));
+    const ff sg = fast_two_sum(t.h, e);
+    const ff au = ff_mul(sg, c);
+    const ff r = ff_add(fsp, ff{-au.h, -au.l});
+    return r.h + (r.l - alo);
+}
+
 __global__ void __launch_bounds__(256) k_residual(SineFused fu, float* __restrict__ r, int nx, int ny, int nz,
                                                   long long vstride, int segs, FastDiv div_segs, FastDiv div_ny) {
     const int t = blockIdx.x * blockDim.x + threadIdx.x;
@@ -337,7 +362,10 @@ __global__ void __launch_bounds__(256) k_residual(SineFused fu, float* __restric
             alo = fu.cxf * ((vxm + vxp) - 2.f * vc) + fu.cyf * ((vym + vyp) - 2.f * vc) +
                   fu.czf * ((vzm + vzp) - 2.f * vc);
         }
-        r[voff + i] = ff_residual(f64_split(fv[q]), c[q + 1], c[q], c[q + 2], ym[q], yp[q], zm[q], zp[q], fu, alo);
+        r[voff + i] = fu.iso ? ff_residual_iso(f64_split(fv[q]), c[q + 1], c[q], c[q + 2], ym[q], yp[q], zm[q], zp[q],
+                                               fu.cx, alo)
+                             : ff_residual(f64_split(fv[q]), c[q + 1], c[q], c[q + 2], ym[q], yp[q], zm[q], zp[q], fu,
+                                           alo);
     }
 }
 

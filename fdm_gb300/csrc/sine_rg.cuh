@@ -47,11 +47,18 @@ struct RgGeom {
     static constexpr int TR = R1 * (R2 + 1);  // transpose slots
     static constexpr int CS = M + M / 16 + 1; // skewed C / packed-output slots
     static constexpr int RS0 = TR > CS ? (TR > M ? TR : M) : (CS > M ? CS : M);
-    // line stride in slots: 8 (mod 16) for the row pass so the two lines of
-    // a half-warp use disjoint bank pairs; odd for the column pass, whose
-    // load and store walk across lines
-    static constexpr int LS2 = AXIS == 0 ? ((RS0 + 7) / 16 * 16 + 8) : (RS0 | 1);
+    // line stride in slots, 8 (mod 16): the two lines of a half-warp use
+    // disjoint bank pairs in the float2 phases
+    static constexpr int LS2 = (RS0 + 7) / 16 * 16 + 8;
 };
+
+// Slot swizzle of line l.  The column pass loads and stores one float of 32
+// consecutive lines per warp instruction; XOR-ing the low three bits of the
+// slot index with (l/2) mod 8 spreads those lines over 16 banks (the floor
+// for 4-byte accesses of one parity), and as a permutation inside aligned
+// groups of 8 slots it keeps every float2 access of a line conflict-free.
+template <int AXIS>
+__device__ __forceinline__ int swz(int l) { return AXIS == 1 ? ((l >> 1) & 7) : 0; }
 
 // cos / sin of 2 pi m / 16
 __device__ __forceinline__ constexpr double c16(int m) {
@@ -208,13 +215,15 @@ __global__ void __launch_bounds__(256) k_sine_rg(const Tin* in, Tout* out, SineG
                 if (e < total) {
                     const int line = lv[q], j = jv[q];
                     T* base = Sr + 2 * (size_t)line * LS2;
+                    const int key = swz<AXIS>(line);
                     if (j == 0) {
-                        base[0] = T(0);
+                        base[2 * key] = T(0);
                     } else {
                         const T w = ldg(tb.wpre + j);
                         const T sm = w * (av[q] + bv[q]), df = half * (av[q] - bv[q]);
-                        base[j] = sm + df;
-                        if (j != M) base[N - j] = sm - df;
+                        base[2 * ((j >> 1) ^ key) + (j & 1)] = sm + df;
+                        const int jm = N - j;
+                        if (j != M) base[2 * ((jm >> 1) ^ key) + (jm & 1)] = sm - df;
                     }
                 }
             }
@@ -223,11 +232,12 @@ __global__ void __launch_bounds__(256) k_sine_rg(const Tin* in, Tout* out, SineG
     __syncthreads();
 
     T2* Ls = S + (size_t)l * LS2;  // this line's slots
+    const int key = swz<AXIS>(l);
 
     // ---- pass 1: DFT_R1 + twiddle
     T2 v[R1];
 #pragma unroll
-    for (int j1 = 0; j1 < R1; j1++) v[j1] = Ls[j1 * R2 + g];
+    for (int j1 = 0; j1 < R1; j1++) v[j1] = Ls[(j1 * R2 + g) ^ key];
     dft_reg<T, R1>(v);
     if (g) {
 #pragma unroll
@@ -235,7 +245,7 @@ __global__ void __launch_bounds__(256) k_sine_rg(const Tin* in, Tout* out, SineG
     }
     __syncwarp();
 #pragma unroll
-    for (int k1 = 0; k1 < R1; k1++) Ls[k1 * (R2 + 1) + g] = v[k1];
+    for (int k1 = 0; k1 < R1; k1++) Ls[(k1 * (R2 + 1) + g) ^ key] = v[k1];
     __syncwarp();
 
     // ---- pass 2: D2 DFTs of length R2 per thread
@@ -244,7 +254,7 @@ __global__ void __launch_bounds__(256) k_sine_rg(const Tin* in, Tout* out, SineG
     for (int d = 0; d < D2; d++) {
         const int k1 = g * D2 + d;
 #pragma unroll
-        for (int j2 = 0; j2 < R2; j2++) u[d][j2] = Ls[k1 * (R2 + 1) + j2];
+        for (int j2 = 0; j2 < R2; j2++) u[d][j2] = Ls[(k1 * (R2 + 1) + j2) ^ key];
         dft_reg<T, R2>(u[d]);
     }
     __syncwarp();
@@ -252,7 +262,7 @@ __global__ void __launch_bounds__(256) k_sine_rg(const Tin* in, Tout* out, SineG
     for (int d = 0; d < D2; d++) {
         const int k1 = g * D2 + d;
 #pragma unroll
-        for (int k2 = 0; k2 < R2; k2++) Ls[sk(k1 + R1 * k2)] = u[d][k2];
+        for (int k2 = 0; k2 < R2; k2++) Ls[sk(k1 + R1 * k2) ^ key] = u[d][k2];
     }
     __syncwarp();
 
@@ -262,17 +272,17 @@ __global__ void __launch_bounds__(256) k_sine_rg(const Tin* in, Tout* out, SineG
 #pragma unroll
     for (int t = 0; t < E; t++) {
         const int k = g * E + t;
-        const T2 ck = Ls[sk(k)];
+        const T2 ck = Ls[sk(k) ^ key];
         if (k == 0) {
             ra[t] = T(0.5) * (ck.x + ck.y);  // Re Y_0, halved in the running sum
             ia[t] = T(0);
-            const T2 cmid = Ls[sk(M / 2)];
+            const T2 cmid = Ls[sk(M / 2) ^ key];
             rmid = cmid.x;
             imid = -cmid.y;
             rb[t] = T(0);
             ib[t] = T(0);
         } else {
-            const T2 cm = Ls[sk(M - k)];
+            const T2 cm = Ls[sk(M - k) ^ key];
             const T ex = T(0.5) * (ck.x + cm.x), ey = T(0.5) * (ck.y - cm.y);
             const T ox = T(0.5) * (ck.y + cm.y), oy = T(-0.5) * (ck.x - cm.x);
             const T2 w = ldg(tb.post + k);
@@ -317,19 +327,19 @@ __global__ void __launch_bounds__(256) k_sine_rg(const Tin* in, Tout* out, SineG
         T2 fa;
         fa.x = -ia[t];
         fa.y = exa + pa[t];
-        Ls[sk(k)] = fa;
+        Ls[sk(k) ^ key] = fa;
         if (k > 0) {
             T2 fb;
             fb.x = -ib[t];
             fb.y = bbase + pb[t];
-            Ls[sk(M - k)] = fb;
+            Ls[sk(M - k) ^ key] = fb;
         }
     }
     if (g == 0) {
         T2 fm;
         fm.x = -imid;
         fm.y = s1 + rmid;
-        Ls[sk(M / 2)] = fm;
+        Ls[sk(M / 2) ^ key] = fm;
     }
     __syncthreads();
 
@@ -402,7 +412,8 @@ __global__ void __launch_bounds__(256) k_sine_rg(const Tin* in, Tout* out, SineG
         for (int e = tid; e < total; e += nthr) {
             const int y = e / L, c = e - y * L, i = y + 1;
             if (c < nact)
-                out[base + (long long)y * nx + c] = Tout(scale * Sr[2 * ((size_t)c * LS2 + sk(i >> 1)) + (i & 1)]);
+                out[base + (long long)y * nx + c] =
+                    Tout(scale * Sr[2 * ((size_t)c * LS2 + (sk(i >> 1) ^ swz<AXIS>(c))) + (i & 1)]);
         }
     }
 }
