@@ -47,18 +47,20 @@ struct RgGeom {
     static constexpr int TR = R1 * (R2 + 1);  // transpose slots
     static constexpr int CS = M + M / 16 + 1; // skewed C / packed-output slots
     static constexpr int RS0 = TR > CS ? (TR > M ? TR : M) : (CS > M ? CS : M);
-    // line stride in slots, 8 (mod 16): the two lines of a half-warp use
-    // disjoint bank pairs in the float2 phases
-    static constexpr int LS2 = (RS0 + 7) / 16 * 16 + 8;
+    // line stride in slots, 4 (mod 16): with up to four lines per warp the
+    // float2 phases of the lines land on bank pairs shifted by 4, which
+    // spreads every per-line access pattern used below evenly (each bank pair
+    // twice per warp instruction, the minimum for 256 bytes)
+    static constexpr int LS2 = (RS0 + 11) / 16 * 16 + 4;
 };
 
 // Slot swizzle of line l.  The column pass loads and stores one float of 32
-// consecutive lines per warp instruction; XOR-ing the low three bits of the
-// slot index with (l/2) mod 8 spreads those lines over 16 banks (the floor
-// for 4-byte accesses of one parity), and as a permutation inside aligned
-// groups of 8 slots it keeps every float2 access of a line conflict-free.
+// consecutive lines per warp instruction; the line stride alone (8 floats
+// mod 32) would put them on 4 banks.  XOR-ing the low two bits of the slot
+// index with (l/4) mod 4 spreads 16 lines over 16 banks (the floor for
+// 4-byte accesses of one parity is 2-way for 32 lines).
 template <int AXIS>
-__device__ __forceinline__ int swz(int l) { return AXIS == 1 ? ((l >> 1) & 7) : 0; }
+__device__ __forceinline__ int swz(int l) { return AXIS == 1 ? ((l >> 2) & 3) : 0; }
 
 // cos / sin of 2 pi m / 16
 __device__ __forceinline__ constexpr double c16(int m) {
@@ -252,7 +254,7 @@ __global__ void __launch_bounds__(256) k_sine_rg(const Tin* in, Tout* out, SineG
     T2 u[D2][R2];
 #pragma unroll
     for (int d = 0; d < D2; d++) {
-        const int k1 = g * D2 + d;
+        const int k1 = g + G * d;  // interleaved: the lines' slot sets stay disjoint
 #pragma unroll
         for (int j2 = 0; j2 < R2; j2++) u[d][j2] = Ls[(k1 * (R2 + 1) + j2) ^ key];
         dft_reg<T, R2>(u[d]);
@@ -260,7 +262,7 @@ __global__ void __launch_bounds__(256) k_sine_rg(const Tin* in, Tout* out, SineG
     __syncwarp();
 #pragma unroll
     for (int d = 0; d < D2; d++) {
-        const int k1 = g * D2 + d;
+        const int k1 = g + G * d;
 #pragma unroll
         for (int k2 = 0; k2 < R2; k2++) Ls[sk(k1 + R1 * k2) ^ key] = u[d][k2];
     }
