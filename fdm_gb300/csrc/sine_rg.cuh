@@ -47,17 +47,11 @@ struct RgGeom {
     static constexpr int TR = R1 * (R2 + 1);  // transpose slots
     static constexpr int CS = M + M / 16 + 1; // skewed C / packed-output slots
     static constexpr int RS0 = TR > CS ? (TR > M ? TR : M) : (CS > M ? CS : M);
-    // line stride in slots.  Row pass: 4 (mod 16), so with up to four lines
-    // per warp the float2 phases land on bank pairs shifted by 4 and every
-    // per-line pattern below uses each bank pair twice per warp instruction
-    // (the minimum for 256 bytes).  Column pass: odd, because its load and
-    // store touch one float of 32 consecutive lines per instruction, which an
-    // odd stride spreads over 16 banks (2-way, the floor for one parity).
-    static constexpr int LS2 = AXIS == 0 ? (RS0 + 11) / 16 * 16 + 4 : (RS0 | 1);
-    static constexpr int TAB = 2 * M + N / 2;  // shared copy of the tables, in slots
+    // line stride in slots: 8 (mod 16) for the row pass so the two lines of
+    // a half-warp use disjoint bank pairs; odd for the column pass, whose
+    // load and store walk across lines
+    static constexpr int LS2 = AXIS == 0 ? ((RS0 + 7) / 16 * 16 + 8) : (RS0 | 1);
 };
-
-
 
 // cos / sin of 2 pi m / 16
 __device__ __forceinline__ constexpr double c16(int m) {
@@ -122,7 +116,7 @@ __device__ __forceinline__ void dft_reg(vec2_t<T>* v) {
 __device__ __forceinline__ int sk(int k) { return k + (k >> 4); }
 
 template <typename Tin, typename T, typename Tout, int AXIS, int MODE, int N>
-__global__ void __launch_bounds__(256, sizeof(T) == 4 ? (AXIS == 1 ? 4 : 3) : 1) k_sine_rg(const Tin* in, Tout* out, SineGeom geo, SineTables<T> tb, T scale,
+__global__ void __launch_bounds__(256) k_sine_rg(const Tin* in, Tout* out, SineGeom geo, SineTables<T> tb, T scale,
                                                  SineFused fu) {
     using T2 = vec2_t<T>;
     using Gm = RgGeom<N, AXIS>;
@@ -130,9 +124,6 @@ __global__ void __launch_bounds__(256, sizeof(T) == 4 ? (AXIS == 1 ? 4 : 3) : 1)
     constexpr int LS2 = Gm::LS2;
     constexpr int n = N - 1;
     constexpr int ITEMS = M + 1;  // fold items per line: j = 0..M
-    // fold items per thread per batch of loads (the column pass fits 8 in the
-    // register budget of 4 CTAs per SM)
-    constexpr int kFold = (AXIS == 1 && sizeof(T) == 4) ? 8 : 4;
     extern __shared__ __align__(16) unsigned char smem_raw[];
     T2* S = reinterpret_cast<T2*>(smem_raw);
     T* Sr = reinterpret_cast<T*>(smem_raw);
@@ -153,28 +144,16 @@ __global__ void __launch_bounds__(256, sizeof(T) == 4 ? (AXIS == 1 ? 4 : 3) : 1)
         nact = min(L, nx - x0);
     }
 
-    // shared copies of the twiddles w_M^k, the unpack twiddles w_N^k and
-    // the fold weights sin(pi j / N), after the line regions
-    T2* twc_s = S + (size_t)L * LS2;
-    T2* post_s = twc_s + M;
-    T* tw_s = reinterpret_cast<T*>(post_s + M);
-    for (int i = tid; i < M; i += nthr) {
-        twc_s[i] = ldg(tb.tw + i);
-        post_s[i] = ldg(tb.post + i);
-    }
-    for (int i = tid; i < N; i += nthr) tw_s[i] = ldg(tb.wpre + i);
-    __syncthreads();
-
     // ---- load + fold: item (line, j) reads x_j and x_{N-j} and writes
     // y_j = w_j (a+b) + (a-b)/2 and y_{N-j} = w_j (a+b) - (a-b)/2
     {
         const T half = T(0.5);
         constexpr int total = L * ITEMS;
-        for (int e0 = tid; e0 < total; e0 += kFold * nthr) {
-            T av[kFold], bv[kFold];
-            int lv[kFold], jv[kFold];
+        for (int e0 = tid; e0 < total; e0 += 4 * nthr) {
+            T av[4], bv[4];
+            int lv[4], jv[4];
 #pragma unroll
-            for (int q = 0; q < kFold; q++) {
+            for (int q = 0; q < 4; q++) {
                 const int e = e0 + q * nthr;
                 int line, j;
                 if (AXIS == 0) {
@@ -224,7 +203,7 @@ __global__ void __launch_bounds__(256, sizeof(T) == 4 ? (AXIS == 1 ? 4 : 3) : 1)
                 bv[q] = b;
             }
 #pragma unroll
-            for (int q = 0; q < kFold; q++) {
+            for (int q = 0; q < 4; q++) {
                 const int e = e0 + q * nthr;
                 if (e < total) {
                     const int line = lv[q], j = jv[q];
@@ -232,7 +211,7 @@ __global__ void __launch_bounds__(256, sizeof(T) == 4 ? (AXIS == 1 ? 4 : 3) : 1)
                     if (j == 0) {
                         base[0] = T(0);
                     } else {
-                        const T w = tw_s[j];
+                        const T w = ldg(tb.wpre + j);
                         const T sm = w * (av[q] + bv[q]), df = half * (av[q] - bv[q]);
                         base[j] = sm + df;
                         if (j != M) base[N - j] = sm - df;
@@ -252,7 +231,7 @@ __global__ void __launch_bounds__(256, sizeof(T) == 4 ? (AXIS == 1 ? 4 : 3) : 1)
     dft_reg<T, R1>(v);
     if (g) {
 #pragma unroll
-        for (int k1 = 1; k1 < R1; k1++) v[k1] = cmul<T>(v[k1], twc_s[(g * k1) & (M - 1)]);
+        for (int k1 = 1; k1 < R1; k1++) v[k1] = cmul<T>(v[k1], ldg(tb.tw + ((g * k1) & (M - 1))));
     }
     __syncwarp();
 #pragma unroll
@@ -263,7 +242,7 @@ __global__ void __launch_bounds__(256, sizeof(T) == 4 ? (AXIS == 1 ? 4 : 3) : 1)
     T2 u[D2][R2];
 #pragma unroll
     for (int d = 0; d < D2; d++) {
-        const int k1 = g + G * d;  // interleaved: the lines' slot sets stay disjoint
+        const int k1 = g * D2 + d;
 #pragma unroll
         for (int j2 = 0; j2 < R2; j2++) u[d][j2] = Ls[k1 * (R2 + 1) + j2];
         dft_reg<T, R2>(u[d]);
@@ -271,7 +250,7 @@ __global__ void __launch_bounds__(256, sizeof(T) == 4 ? (AXIS == 1 ? 4 : 3) : 1)
     __syncwarp();
 #pragma unroll
     for (int d = 0; d < D2; d++) {
-        const int k1 = g + G * d;
+        const int k1 = g * D2 + d;
 #pragma unroll
         for (int k2 = 0; k2 < R2; k2++) Ls[sk(k1 + R1 * k2)] = u[d][k2];
     }
@@ -296,7 +275,7 @@ __global__ void __launch_bounds__(256, sizeof(T) == 4 ? (AXIS == 1 ? 4 : 3) : 1)
             const T2 cm = Ls[sk(M - k)];
             const T ex = T(0.5) * (ck.x + cm.x), ey = T(0.5) * (ck.y - cm.y);
             const T ox = T(0.5) * (ck.y + cm.y), oy = T(-0.5) * (ck.x - cm.x);
-            const T2 w = post_s[k];
+            const T2 w = ldg(tb.post + k);
             const T wx = w.x * ox - w.y * oy, wy = w.x * oy + w.y * ox;
             ra[t] = ex + wx;
             ia[t] = ey + wy;
@@ -423,15 +402,14 @@ __global__ void __launch_bounds__(256, sizeof(T) == 4 ? (AXIS == 1 ? 4 : 3) : 1)
         for (int e = tid; e < total; e += nthr) {
             const int y = e / L, c = e - y * L, i = y + 1;
             if (c < nact)
-                out[base + (long long)y * nx + c] =
-                    Tout(scale * Sr[2 * ((size_t)c * LS2 + sk(i >> 1)) + (i & 1)]);
+                out[base + (long long)y * nx + c] = Tout(scale * Sr[2 * ((size_t)c * LS2 + sk(i >> 1)) + (i & 1)]);
         }
     }
 }
 
 template <typename T, int N, int AXIS>
 constexpr size_t rg_smem_bytes() {
-    return ((size_t)RgGeom<N, AXIS>::L * RgGeom<N, AXIS>::LS2 + RgGeom<N, AXIS>::TAB) * sizeof(vec2_t<T>);
+    return (size_t)RgGeom<N, AXIS>::L * RgGeom<N, AXIS>::LS2 * sizeof(vec2_t<T>);
 }
 
 }  // namespace fdmgpu
