@@ -189,6 +189,70 @@ def run_reference_arm(args, world, rank):
     print(json.dumps(line), flush=True)
 
 
+def measure_uneven_batch(torch, fdm_gb300, workloads, stream, dev, count=512, tol=1e-8, reps=5):
+    """Uneven batch: count right-hand sides, each axis drawn from {31, 63, 127},
+    N(0,1) entries, mixed precision to tol, solved by one tuned graph launch
+    per step; against the same right-hand sides solved one at a time by the
+    FP64 LaplCube form (one plan per size)."""
+    shapes = workloads.random_sizes(count, seed=2024)
+    rhs, ans, ref = [], [], []
+    with torch.cuda.stream(stream):
+        for i, (nx, ny, nz) in enumerate(shapes):
+            g = torch.Generator(device=dev).manual_seed(7000 + i)
+            rhs.append(torch.randn((nz, ny, nx), dtype=torch.float64, device=dev, generator=g))
+            ans.append(torch.empty_like(rhs[-1]))
+            ref.append(torch.empty_like(rhs[-1]))
+    stream.synchronize()
+    points = sum(nx * ny * nz for nx, ny, nz in shapes)
+    geo = [workloads.solver_args(*sh) for sh in shapes]
+    b = fdm_gb300.BatchSolver(shapes, [g[0:3] for g in geo], [g[3:6] for g in geo], precision="mixed", tol=tol)
+    t0 = time.perf_counter()
+    b.tune(ans, rhs)
+    tune_s = time.perf_counter() - t0
+    for _ in range(2):
+        b.solve(ans, rhs, stream=stream)
+    stream.synchronize()
+    e0 = torch.cuda.Event(enable_timing=True)
+    e1 = torch.cuda.Event(enable_timing=True)
+    e0.record(stream)
+    for _ in range(reps):
+        b.solve(ans, rhs, stream=stream)
+    e1.record(stream)
+    stream.synchronize()
+    batch_s = e0.elapsed_time(e1) * 1e-3 / reps
+    # the per-size FP64 loop: one solve_device call per right-hand side
+    plans = {}
+    for nx, ny, nz in shapes:
+        if (nx, ny, nz) not in plans:
+            plans[(nx, ny, nz)] = fdm_gb300.LaplCube(*workloads.solver_args(nx, ny, nz))
+
+    def loop():
+        for i, s in enumerate(shapes):
+            plans[s].solve_device(ref[i], rhs[i], stream=stream)
+    loop()
+    stream.synchronize()
+    e0.record(stream)
+    for _ in range(2):
+        loop()
+    e1.record(stream)
+    stream.synchronize()
+    loop_s = e0.elapsed_time(e1) * 1e-3 / 2
+    errs = [(torch.linalg.norm(ans[i] - ref[i]) / torch.linalg.norm(ref[i])).item() for i in range(count)]
+    groups, launches = b.info()
+    sched = b.schedule()
+    return {
+        "workload": "%d RHS, each axis from {31,63,127}, tol %g" % (count, tol),
+        "points": points, "groups": groups, "kernel_launches_per_graph": launches,
+        "solves_per_s": count / batch_s, "ms_per_batch": batch_s * 1e3,
+        "hbm_gbs_fp64_in_out": 16.0 * points / batch_s / 1e9,
+        "fp64_per_size_loop": {"solves_per_s": count / loop_s, "ms_per_batch": loop_s * 1e3},
+        "speedup_vs_fp64_loop": loop_s / batch_s,
+        "rel_l2_vs_fp64_max": max(errs), "tune_s": tune_s,
+        "chunks": sorted(set(g["chunk"] for g in sched)),
+        "ztable_groups": sum(g["ztable"] for g in sched),
+    }
+
+
 def run_ncu_case():
     """Two mixed solves of 2 RHS at 255^3 (266 MB of FP64 input, larger than
     L2) with nothing else on the GPU: the case the committed ncu summaries
@@ -327,6 +391,27 @@ def main():
     if tfile.exists():
         traffic = json.loads(tfile.read_text()).get(dname)
 
+    # ---- context numbers (untimed for the headline): the plain FP64 GPU form
+    # on the same inputs, and the NSCube cavity step at 63^3
+    e0.record(stream)
+    for _ in range(2):
+        plain.solve_device(out, f, nrhs=NRHS, stream=stream)
+    e1.record(stream)
+    stream.synchronize()
+    plain_rate = 2 * NRHS / (e0.elapsed_time(e1) * 1e-3)
+    ns = fdm_gb300.NSCube(nx=63, nz=63, Re=250.0, dt=0.01, u0=1.0)
+    ns.step(20)
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    ns.step(200)
+    torch.cuda.synchronize()
+    ns_ms = (time.perf_counter() - t0) * 1e3 / 200
+    ns.close()
+
+    del out, f
+    torch.cuda.empty_cache()
+    uneven = measure_uneven_batch(torch, fdm_gb300, workloads, stream, dev)
+
     solves = args.steps * NRHS * world
     value = solves / (ms * 1e-3)
     e2e_value = e2e_steps * NRHS * world / e2e_s
@@ -353,11 +438,21 @@ def main():
                            "frac": value / world * SOLVE_BYTES_PER_POINT * vol / 1e9 / hbm,
                            "bytes_per_point": SOLVE_BYTES_PER_POINT},
         "kernels_ms_per_step": {k: v[1] / 2 for k, v in sorted(prof.items(), key=lambda kv: -kv[1][1])},
+        "plain_fp64_gpu": {"value": plain_rate, "unit": UNIT},
+        "nscube_63cubed": {"ms_per_step": ns_ms, "steps_timed": 200, "Re": 250.0, "dt": 0.01},
+        "uneven_batch": uneven,
         "clocks": clocks,
     }
     if rank == 0 and not args.no_cpu_baseline:
         rate, kind, cores, sample = cpu_reference_rate(5)
         line["cpu_baseline"] = {"value": rate, "unit": UNIT, "cores": cores, "kind": kind, "sample": sample}
+        from oracle.oracle import port
+        o = port().nscube(63, 63, 250.0, 0.01)
+        o.step(2)
+        t0 = time.perf_counter()
+        o.step(10)
+        line["cpu_baseline"]["nscube_63cubed_ms_per_step"] = (time.perf_counter() - t0) * 1e3 / 10
+        o.close()
     if rank == 0:
         print(json.dumps(line), flush=True)
     if world > 1:

@@ -52,6 +52,14 @@ _SIGS = [
     ("fdmgpu_lapl_cube_last_info", c_int, [c_void_p, POINTER(c_int), POINTER(c_double), c_int]),
     ("fdmgpu_lapl_cube_scratch_bytes", c_int, [c_void_p, POINTER(c_size_t)]),
     ("fdmgpu_lapl_cube_destroy", c_int, [c_void_p]),
+    ("fdmgpu_batch_create", c_int,
+     [POINTER(c_void_p), c_int, POINTER(c_int), POINTER(c_double), POINTER(c_double), c_int, c_double]),
+    ("fdmgpu_batch_tune", c_int, [c_void_p, POINTER(c_void_p), POINTER(c_void_p)]),
+    ("fdmgpu_batch_solve", c_int, [c_void_p, POINTER(c_void_p), POINTER(c_void_p), c_void_p]),
+    ("fdmgpu_batch_info", c_int, [c_void_p, POINTER(c_int), POINTER(c_int)]),
+    ("fdmgpu_batch_schedule", c_int,
+     [c_void_p, c_int, POINTER(c_int), POINTER(c_int), POINTER(c_int), POINTER(c_int), POINTER(c_double)]),
+    ("fdmgpu_batch_destroy", c_int, [c_void_p]),
     ("fdmgpu_lapl_rect_create", c_int,
      [POINTER(c_void_p), c_int, c_int] + [c_double] * 4 + [c_int] * 2),
     ("fdmgpu_lapl_rect_solve", c_int, [c_void_p, c_void_p, c_void_p]),

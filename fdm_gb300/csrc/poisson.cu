@@ -11,10 +11,12 @@
 // refinement sweep forms r = f - A u / S from the FP32/FP64 state in FP64,
 // solves for the correction in FP32 and accumulates.  S is the reference's
 // overall scale (prod_a h_a N_a / l_a, 1 for the usual l = (n+1)h).
+#include <algorithm>
 #include <cmath>
 #include <cstring>
 #include <memory>
 #include <mutex>
+#include <deque>
 #include <vector>
 
 #include "internal.h"
@@ -309,8 +311,9 @@ struct CubePlan {
     AxisTables<double> tx64, ty64;
     AxisTables<float> tx32, ty32;
     DevBuf lamx64, lamy64, lamx32, lamy32;
-    DevBuf work32, uhi, ulo, norms;
+    DevBuf work32, uhi, ulo, norms, work64;
     DevBuf ztab64, ztab32;  // partitioned z-solve factors per mode
+    int zmode = 1;          // 1: table-driven z-solve when the line splits, 0: factors computed per solve
     int zm64 = 0, zP64 = 0, zm32 = 0, zP32 = 0;
     DevBuf hin, hout;
     int last_sweeps = 0, last_nrhs = 0;
@@ -424,7 +427,7 @@ struct CubePlan {
                                       &zm, &zP))
                 zm = -1;
         }
-        if (zm > 0) {
+        if (zm > 0 && zmode == 1) {
             zsolve_tab_launch<T>(W, nx, ny, nz, nrhs, (const T*)tab.p, zm, zP, zfac * hz_eff * hz_eff, st);
             return;
         }
@@ -465,17 +468,28 @@ struct CubePlan {
         return ff{h, (float)(v - (double)h)};
     }
 
-    void run_mixed(double* ans, const double* rhs, int nrhs, cudaStream_t st) {
+    // Mixed solve of nrhs volumes.  With vin / vout (device arrays of nrhs
+    // user pointers) the FP64 input and output volumes are addressed through
+    // them and rhs / ans are not used; the FP32 scratch stays contiguous.
+    void run_mixed(double* ans, const double* rhs, int nrhs, cudaStream_t st, const void* const* vin = nullptr,
+                   void* const* vout = nullptr) {
         ensure_mixed_tables();
         const long long V = vol() * nrhs;
         const int sweeps = sweeps_for_tol();
         last_sweeps = sweeps;
         float* W = (float*)work32.get(V * sizeof(float));
-        forward_xy<double, float, kRound>(rhs, W, nrhs, tx32, ty32, st);
+        SineFused fin;
+        memset(&fin, 0, sizeof(fin));
+        fin.vin = vin;
+        launch_sine<double, float, float, 0, kRound>(rhs, W, nx, ny, nz, nrhs, tx32.view(), scx, st, &fin);
+        launch_sine<float, float, float, 1>(W, W, nx, ny, nz, nrhs, ty32.view(), scy, st);
         zsolve<float>(W, nrhs, lamx32, lamy32, st);
         launch_sine<float, float, float, 1>(W, W, nx, ny, nz, nrhs, ty32.view(), sly, st);
         if (sweeps == 0) {
-            launch_sine<float, float, double, 0>(W, ans, nx, ny, nz, nrhs, tx32.view(), slx, st);
+            SineFused fo;
+            memset(&fo, 0, sizeof(fo));
+            fo.vout = vout;
+            launch_sine<float, float, double, 0>(W, ans, nx, ny, nz, nrhs, tx32.view(), slx, st, &fo);
             return;
         }
         float* UH = (float*)uhi.get(V * sizeof(float));
@@ -490,6 +504,7 @@ struct CubePlan {
             SineFused fr;
             memset(&fr, 0, sizeof(fr));
             fr.f = rhs;
+            fr.vin = vin;
             fr.uhi = UH;
             fr.ulo = s >= 2 ? UL : nullptr;
             fr.cx = split_host(cx); fr.cy = split_host(cy); fr.cz = split_host(cz);
@@ -504,6 +519,7 @@ struct CubePlan {
             fc.uhi = UH;
             fc.ulo = s >= 2 ? UL : nullptr;
             fc.out64 = ans;
+            fc.vout = vout;
             fc.ulo_out = UL;
             fc.last = s == sweeps ? 1 : 0;
             fc.norms = NR + (size_t)2 * nrhs * (s - 1);
@@ -512,8 +528,40 @@ struct CubePlan {
         }
     }
 
+    // Plain FP64 solve through pointer tables: first pass from the user
+    // volumes into contiguous FP64 scratch, last pass back out.
+    void run_plain_ptrs(const void* const* vin, void* const* vout, int nrhs, cudaStream_t st) {
+        const long long V = vol() * nrhs;
+        double* W = (double*)work64.get(V * sizeof(double));
+        SineFused fin;
+        memset(&fin, 0, sizeof(fin));
+        fin.vin = vin;
+        launch_sine<double, double, double, 0>(nullptr, W, nx, ny, nz, nrhs, tx64.view(), scx, st, &fin);
+        launch_sine<double, double, double, 1>(W, W, nx, ny, nz, nrhs, ty64.view(), scy, st);
+        zsolve<double>(W, nrhs, lamx64, lamy64, st);
+        launch_sine<double, double, double, 1>(W, W, nx, ny, nz, nrhs, ty64.view(), sly, st);
+        SineFused fo;
+        memset(&fo, 0, sizeof(fo));
+        fo.vout = vout;
+        launch_sine<double, double, double, 0>(W, nullptr, nx, ny, nz, nrhs, tx64.view(), slx, st, &fo);
+    }
+
+    // Largest first-sweep correction estimate ||c||/||u|| over the nrhs
+    // volumes of the last mixed solve on st (synchronises st): the relative
+    // error of the FP32 inner solve.  0 when the last solve ran no sweep.
+    double first_sweep_est(int nrhs, cudaStream_t st) {
+        if (last_sweeps == 0 || !norms.p) return 0.0;
+        FDM_CUDA(cudaStreamSynchronize(st));
+        std::vector<double> v((size_t)2 * nrhs);
+        FDM_CUDA(cudaMemcpy(v.data(), norms.p, v.size() * sizeof(double), cudaMemcpyDeviceToHost));
+        double e = 0.0;
+        for (int i = 0; i < nrhs; i++)
+            if (v[2 * i + 1] > 0) e = std::max(e, std::sqrt(v[2 * i] / v[2 * i + 1]));
+        return e;
+    }
+
     size_t scratch_bytes() const {
-        return work32.bytes + uhi.bytes + ulo.bytes + norms.bytes + hin.bytes + hout.bytes + ztab32.bytes +
+        return work32.bytes + work64.bytes + uhi.bytes + ulo.bytes + norms.bytes + hin.bytes + hout.bytes + ztab32.bytes +
                ztab64.bytes + ring_in.bytes + ring_out.bytes;
     }
 };
@@ -589,6 +637,243 @@ using namespace fdmgpu;
 
 struct fdmgpu_lapl_cube {
     CubePlan plan;
+};
+
+namespace fdmgpu {
+
+// ---------------------------------------------------------------------------
+// Batched solves of uneven sizes
+//
+// Right-hand sides are grouped by geometry; each group owns a CubePlan (its
+// tables and contiguous FP32 scratch) and reads / writes the user volumes
+// through device arrays of pointers, so nothing is gathered or scattered.
+// A group's schedule -- right-hand sides per pipeline launch (chunk) and the
+// z-solve variant -- is picked by timing the candidates on the group's own
+// data (tune).  The first solve after tuning captures every group's
+// pipeline, each on its own stream forked from one origin stream, into a
+// single CUDA graph; later solves are one graph launch.
+// ---------------------------------------------------------------------------
+struct BatchGroup {
+    int nx, ny, nz;
+    double g[6];
+    std::vector<int> members;
+    std::unique_ptr<CubePlan> plan;
+    int chunk = 0;  // right-hand sides per pipeline launch (0: all)
+    int zmode = 1;
+    DevBuf ptr_in, ptr_out;  // device arrays of the members' user pointers
+    cudaStream_t st = nullptr;
+    cudaEvent_t done = nullptr;
+    double tuned_ms = 0.0;
+};
+
+struct BatchPlan {
+    int count = 0, precision = FDMGPU_MIXED;
+    double tol = 1e-10;
+    std::deque<BatchGroup> groups;  // never relocates its elements
+    cudaStream_t origin = nullptr;
+    cudaEvent_t fork = nullptr;
+    cudaGraph_t graph = nullptr;
+    cudaGraphExec_t exec = nullptr;
+    int launches_per_solve = 0;
+    std::vector<const void*> in_host;
+    std::vector<void*> out_host;
+
+    ~BatchPlan() {
+        if (exec) cudaGraphExecDestroy(exec);
+        if (graph) cudaGraphDestroy(graph);
+        for (auto& gr : groups) {
+            if (gr.done) cudaEventDestroy(gr.done);
+            if (gr.st) cudaStreamDestroy(gr.st);
+        }
+        if (fork) cudaEventDestroy(fork);
+        if (origin) cudaStreamDestroy(origin);
+    }
+
+    void init(const int* n3, const double* h3, const double* l3) {
+        for (int i = 0; i < count; i++) {
+            const int nx = n3[3 * i], ny = n3[3 * i + 1], nz = n3[3 * i + 2];
+            int found = -1;
+            for (size_t k = 0; k < groups.size(); k++) {
+                const BatchGroup& gr = groups[k];
+                if (gr.nx == nx && gr.ny == ny && gr.nz == nz && gr.g[0] == h3[3 * i] && gr.g[1] == h3[3 * i + 1] &&
+                    gr.g[2] == h3[3 * i + 2] && gr.g[3] == l3[3 * i] && gr.g[4] == l3[3 * i + 1] &&
+                    gr.g[5] == l3[3 * i + 2]) {
+                    found = (int)k;
+                    break;
+                }
+            }
+            if (found < 0) {
+                groups.emplace_back();
+                BatchGroup& gr = groups.back();
+                gr.nx = nx; gr.ny = ny; gr.nz = nz;
+                for (int a = 0; a < 3; a++) {
+                    gr.g[a] = h3[3 * i + a];
+                    gr.g[3 + a] = l3[3 * i + a];
+                }
+                found = (int)groups.size() - 1;
+            }
+            groups[found].members.push_back(i);
+        }
+        FDM_CUDA(cudaStreamCreateWithFlags(&origin, cudaStreamNonBlocking));
+        FDM_CUDA(cudaEventCreateWithFlags(&fork, cudaEventDisableTiming));
+        for (auto& gr : groups) {
+            gr.plan.reset(new CubePlan());
+            CubePlan& c = *gr.plan;
+            c.dtype = FDMGPU_F64;
+            c.nx = gr.nx; c.ny = gr.ny; c.nz = gr.nz;
+            c.dx = gr.g[0]; c.dy = gr.g[1]; c.dz = gr.g[2];
+            c.lx = gr.g[3]; c.ly = gr.g[4]; c.lz = gr.g[5];
+            c.precision = precision;
+            c.tol = tol;
+            c.init();
+            gr.chunk = (int)gr.members.size();
+            gr.ptr_in.get(gr.members.size() * sizeof(void*));
+            gr.ptr_out.get(gr.members.size() * sizeof(void*));
+            FDM_CUDA(cudaStreamCreateWithFlags(&gr.st, cudaStreamNonBlocking));
+            FDM_CUDA(cudaEventCreateWithFlags(&gr.done, cudaEventDisableTiming));
+        }
+    }
+
+    // copies the members' user pointers into each group's device arrays
+    void upload_pointers(void* const* ans, const void* const* rhs, cudaStream_t st) {
+        if ((int)in_host.size() == count && std::equal(in_host.begin(), in_host.end(), rhs) &&
+            std::equal(out_host.begin(), out_host.end(), ans))
+            return;  // the device arrays already hold these pointers
+        in_host.clear();
+        out_host.clear();
+        for (auto& gr : groups) {
+            std::vector<const void*> pin(gr.members.size());
+            std::vector<void*> pout(gr.members.size());
+            for (size_t k = 0; k < gr.members.size(); k++) {
+                pin[k] = rhs[gr.members[k]];
+                pout[k] = ans[gr.members[k]];
+                if (!pin[k] || !pout[k]) FDM_FAIL(FDMGPU_EINVAL, "null volume pointer for right-hand side %d", gr.members[k]);
+            }
+            FDM_CUDA(cudaMemcpyAsync(gr.ptr_in.p, pin.data(), pin.size() * sizeof(void*), cudaMemcpyHostToDevice, st));
+            FDM_CUDA(cudaMemcpyAsync(gr.ptr_out.p, pout.data(), pout.size() * sizeof(void*), cudaMemcpyHostToDevice,
+                                     st));
+        }
+        FDM_CUDA(cudaStreamSynchronize(st));  // host vectors go out of scope
+        in_host.assign(rhs, rhs + count);
+        out_host.assign(ans, ans + count);
+    }
+
+    // enqueues group gr's pipeline on stream st with its current schedule
+    void enqueue_group(BatchGroup& gr, cudaStream_t st) {
+        CubePlan& c = *gr.plan;
+        c.zmode = gr.zmode;
+        const int m = (int)gr.members.size();
+        const int ch = gr.chunk > 0 ? gr.chunk : m;
+        const void* const* vin = (const void* const*)gr.ptr_in.p;
+        void* const* vout = (void* const*)gr.ptr_out.p;
+        for (int s0 = 0; s0 < m; s0 += ch) {
+            const int k = std::min(ch, m - s0);
+            if (precision == FDMGPU_MIXED) c.run_mixed(nullptr, nullptr, k, st, vin + s0, vout + s0);
+            else c.run_plain_ptrs(vin + s0, vout + s0, k, st);
+        }
+    }
+
+    // time each schedule candidate of every group on its data; keep the best
+    void tune() {
+        cudaEvent_t a, b;
+        FDM_CUDA(cudaEventCreate(&a));
+        FDM_CUDA(cudaEventCreate(&b));
+        for (auto& gr : groups) {
+            const int m = (int)gr.members.size();
+            int chunks[4] = {m, 8, 2, 1};
+            double best = 1e30, est_table = 0.0;
+            int bc = m, bz = 1;
+            const bool mixed = precision == FDMGPU_MIXED;
+            for (int zm = 1; zm >= 0; zm--) {
+                // the per-solve FP32 z factors are less accurate than the
+                // table's (built in FP64): without a refinement sweep to
+                // absorb that they are not a candidate
+                if (zm == 0 && mixed && gr.plan->sweeps_for_tol() == 0) continue;
+                for (int ci = 0; ci < 4; ci++) {
+                    const int ch = chunks[ci];
+                    if (ch > m || (ci > 0 && ch == chunks[ci - 1])) continue;
+                    gr.chunk = ch;
+                    gr.zmode = zm;
+                    enqueue_group(gr, gr.st);  // warm-up: allocates scratch and tables
+                    FDM_CUDA(cudaEventRecord(a, gr.st));
+                    enqueue_group(gr, gr.st);
+                    FDM_CUDA(cudaEventRecord(b, gr.st));
+                    FDM_CUDA(cudaEventSynchronize(b));
+                    float ms = 0.f;
+                    FDM_CUDA(cudaEventElapsedTime(&ms, a, b));
+                    if (mixed && ci == 0) {
+                        // whole group in one launch sequence: the norms
+                        // cover every member
+                        const double e = gr.plan->first_sweep_est(m, gr.st);
+                        if (zm == 1) est_table = e;
+                        else if (e > 2.0 * est_table) break;  // less accurate: keep the table variant
+                    }
+                    if (ms < best) {
+                        best = ms;
+                        bc = ch;
+                        bz = zm;
+                    }
+                }
+            }
+            gr.chunk = bc;
+            gr.zmode = bz;
+            gr.tuned_ms = best;
+            enqueue_group(gr, gr.st);  // scratch for the chosen schedule exists before capture
+        }
+        FDM_CUDA(cudaDeviceSynchronize());
+        cudaEventDestroy(a);
+        cudaEventDestroy(b);
+        drop_graph();
+    }
+
+    void drop_graph() {
+        if (exec) cudaGraphExecDestroy(exec);
+        if (graph) cudaGraphDestroy(graph);
+        exec = nullptr;
+        graph = nullptr;
+    }
+
+    void capture() {
+        // eager pass first: every scratch buffer and table of the chosen
+        // schedules is allocated outside the capture
+        for (auto& gr : groups) enqueue_group(gr, gr.st);
+        FDM_CUDA(cudaDeviceSynchronize());
+        const unsigned long long l0 = fdmgpu_launch_count();
+        FDM_CUDA(cudaStreamBeginCapture(origin, cudaStreamCaptureModeThreadLocal));
+        try {
+            FDM_CUDA(cudaEventRecord(fork, origin));
+            for (auto& gr : groups) {
+                FDM_CUDA(cudaStreamWaitEvent(gr.st, fork, 0));
+                enqueue_group(gr, gr.st);
+                FDM_CUDA(cudaEventRecord(gr.done, gr.st));
+                FDM_CUDA(cudaStreamWaitEvent(origin, gr.done, 0));
+            }
+        } catch (...) {
+            cudaGraph_t g = nullptr;
+            cudaStreamEndCapture(origin, &g);
+            if (g) cudaGraphDestroy(g);
+            throw;
+        }
+        FDM_CUDA(cudaStreamEndCapture(origin, &graph));
+        FDM_CUDA(cudaGraphInstantiate(&exec, graph, 0));
+        launches_per_solve = (int)(fdmgpu_launch_count() - l0);
+    }
+
+    void solve(void* const* ans, const void* const* rhs, cudaStream_t st) {
+        upload_pointers(ans, rhs, origin);
+        if (!exec) capture();
+        FDM_CUDA(cudaEventRecord(fork, st));
+        FDM_CUDA(cudaStreamWaitEvent(origin, fork, 0));
+        FDM_CUDA(cudaGraphLaunch(exec, origin));
+        FDM_CUDA(cudaEventRecord(fork, origin));
+        FDM_CUDA(cudaStreamWaitEvent(st, fork, 0));
+    }
+};
+
+}  // namespace fdmgpu
+
+struct fdmgpu_batch {
+    BatchPlan plan;
 };
 struct fdmgpu_lapl_rect {
     RectPlan plan;
@@ -860,6 +1145,71 @@ int fdmgpu_lapl_cube_scratch_bytes(fdmgpu_lapl_cube* h, size_t* bytes) {
 }
 
 int fdmgpu_lapl_cube_destroy(fdmgpu_lapl_cube* h) {
+    FDM_API_BEGIN
+    delete h;
+    FDM_API_END
+}
+
+int fdmgpu_batch_create(fdmgpu_batch** h, int count, const int* n3, const double* h3, const double* l3,
+                        int precision, double tol) {
+    FDM_API_BEGIN
+    if (!h || !n3 || !h3 || !l3) FDM_FAIL(FDMGPU_EINVAL, "null argument");
+    *h = nullptr;
+    if (count < 1) FDM_FAIL(FDMGPU_EINVAL, "count must be positive");
+    if (precision != FDMGPU_PLAIN && precision != FDMGPU_MIXED) FDM_FAIL(FDMGPU_EINVAL, "bad precision %d", precision);
+    for (int i = 0; i < count; i++) {
+        for (int a = 0; a < 3; a++) {
+            if (!pow2_interior(n3[3 * i + a]))
+                FDM_FAIL(FDMGPU_ESIZE, "verify((1<<n) == N) failed: right-hand side %d has n=%d", i, n3[3 * i + a]);
+            if (!(h3[3 * i + a] > 0 && l3[3 * i + a] > 0))
+                FDM_FAIL(FDMGPU_EINVAL, "right-hand side %d: spacings and lengths must be positive", i);
+        }
+    }
+    std::unique_ptr<fdmgpu_batch> p(new fdmgpu_batch());
+    p->plan.count = count;
+    p->plan.precision = precision;
+    p->plan.tol = tol > 0 ? tol : 1e-10;
+    p->plan.init(n3, h3, l3);
+    *h = p.release();
+    FDM_API_END
+}
+
+int fdmgpu_batch_tune(fdmgpu_batch* h, void* const* d_ans, const void* const* d_rhs) {
+    FDM_API_BEGIN
+    if (!h || !d_ans || !d_rhs) FDM_FAIL(FDMGPU_EINVAL, "null argument");
+    h->plan.upload_pointers(d_ans, d_rhs, h->plan.origin);
+    h->plan.tune();
+    FDM_API_END
+}
+
+int fdmgpu_batch_solve(fdmgpu_batch* h, void* const* d_ans, const void* const* d_rhs, void* stream) {
+    FDM_API_BEGIN
+    if (!h || !d_ans || !d_rhs) FDM_FAIL(FDMGPU_EINVAL, "null argument");
+    h->plan.solve(d_ans, d_rhs, (cudaStream_t)stream);
+    FDM_API_END
+}
+
+int fdmgpu_batch_info(fdmgpu_batch* h, int* groups, int* launches_per_solve) {
+    FDM_API_BEGIN
+    if (!h) FDM_FAIL(FDMGPU_EINVAL, "null handle");
+    if (groups) *groups = (int)h->plan.groups.size();
+    if (launches_per_solve) *launches_per_solve = h->plan.launches_per_solve;
+    FDM_API_END
+}
+
+int fdmgpu_batch_schedule(fdmgpu_batch* h, int group, int* n3, int* members, int* chunk, int* ztable, double* tuned_ms) {
+    FDM_API_BEGIN
+    if (!h || group < 0 || group >= (int)h->plan.groups.size()) FDM_FAIL(FDMGPU_EINVAL, "bad handle or group");
+    const BatchGroup& gr = h->plan.groups[group];
+    if (n3) { n3[0] = gr.nx; n3[1] = gr.ny; n3[2] = gr.nz; }
+    if (members) *members = (int)gr.members.size();
+    if (chunk) *chunk = gr.chunk;
+    if (ztable) *ztable = gr.zmode;
+    if (tuned_ms) *tuned_ms = gr.tuned_ms;
+    FDM_API_END
+}
+
+int fdmgpu_batch_destroy(fdmgpu_batch* h) {
     FDM_API_BEGIN
     delete h;
     FDM_API_END

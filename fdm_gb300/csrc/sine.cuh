@@ -231,6 +231,12 @@ struct SineFused {
     float* ulo_out;
     int last;
     double* norms;  // per volume: ||c||^2, ||u||^2
+    // optional per-volume pointers (device arrays indexed by blockIdx.y) for
+    // the user-facing input (kRound / kPlain loads, the residual's f) and
+    // output (kPlain stores, kCombine's FP64 result); null = volumes back to
+    // back from the kernel's base pointer
+    const void* const* vin;
+    void* const* vout;
 };
 
 struct SineGeom {
@@ -328,7 +334,7 @@ __global__ void __launch_bounds__(256) k_residual(SineFused fu, float* __restric
     const long long sy = nx, sz = (long long)nx * ny;
     const float* U = fu.uhi + voff;
     const float* V = fu.ulo ? fu.ulo + voff : nullptr;
-    const double* F = fu.f + voff;
+    const double* F = fu.vin ? (const double*)fu.vin[blockIdx.y] : fu.f + voff;
     float c[kResX + 2];
 #pragma unroll
     for (int q = 0; q < kResX + 2; q++) {
@@ -406,6 +412,8 @@ __global__ void __launch_bounds__(256) k_sine_pass(const Tin* in, Tout* out, Sin
         XB[(size_t)i * SX] = T(0);
         XB[(size_t)i * SX + skew_r(N)] = T(0);
     }
+    // per-volume user pointers, when given, replace base + volume offset
+    const Tin* inv = fu.vin ? (const Tin*)fu.vin[blockIdx.y] - voff : in;
     if (AXIS == 0) {
         const int total = nact * n;
         const long long base = voff + (long long)row0 * n;
@@ -431,8 +439,8 @@ __global__ void __launch_bounds__(256) k_sine_pass(const Tin* in, Tout* out, Sin
                 for (int q = 0; q < kLoadBatch; q++) {
                     const int e = e0 + q * nthr;
                     if (e < total) {
-                        if (MODE == kRound) v[q] = T(f64_to_f32((double)in[base + e]));
-                        else v[q] = T(in[base + e]);
+                        if (MODE == kRound) v[q] = T(f64_to_f32((double)inv[base + e]));
+                        else v[q] = T(inv[base + e]);
                     }
                 }
             }
@@ -457,8 +465,8 @@ __global__ void __launch_bounds__(256) k_sine_pass(const Tin* in, Tout* out, Sin
                 const int y = e >> geo.Lshift, c = e & (L - 1);
                 v[q] = T(0);
                 if (e < total && c < nact) {
-                    if (MODE == kRound) v[q] = T(f64_to_f32((double)in[base + (long long)y * nx + c]));
-                    else v[q] = T(in[base + (long long)y * nx + c]);
+                    if (MODE == kRound) v[q] = T(f64_to_f32((double)inv[base + (long long)y * nx + c]));
+                    else v[q] = T(inv[base + (long long)y * nx + c]);
                 }
             }
 #pragma unroll
@@ -488,7 +496,7 @@ __global__ void __launch_bounds__(256) k_sine_pass(const Tin* in, Tout* out, Sin
                 const float lo = fu.ulo ? fu.ulo[idx] : 0.f;
                 ff s = two_sum(h, lo);
                 s = ff_add_f(s, cv);
-                if (fu.last) fu.out64[idx] = ff_to_f64(s);
+                if (fu.last) (fu.vout ? (double*)fu.vout[blockIdx.y] - voff : fu.out64)[idx] = ff_to_f64(s);
                 else fu.ulo_out[idx] = lo + cv;
                 cc += cv * cv;
                 uu += s.h * s.h;
@@ -516,9 +524,10 @@ __global__ void __launch_bounds__(256) k_sine_pass(const Tin* in, Tout* out, Sin
                 }
             }
         } else {
+            Tout* ov = fu.vout ? (Tout*)fu.vout[blockIdx.y] - voff : out;
             for (int e = tid; e < total; e += nthr) {
                 const int r = geo.div_n.div(e), c = e - r * n;
-                out[base + e] = Tout(scale * F[(size_t)r * SX + skew_r(c + 1)]);
+                ov[base + e] = Tout(scale * F[(size_t)r * SX + skew_r(c + 1)]);
             }
         }
     } else {

@@ -172,14 +172,14 @@ __global__ void __launch_bounds__(256) k_sine_rg(const Tin* in, Tout* out, SineG
                         if (MODE == kResidual) {
                             const int zz = geo.div_ny.div(R), yy = R - zz * ny;
                             SineFused f2 = fu;
-                            f2.f += voff;
+                            f2.f = fu.vin ? (const double*)fu.vin[blockIdx.y] : fu.f + voff;
                             f2.uhi += voff;
                             if (f2.ulo) f2.ulo += voff;
                             const long long rb = (long long)R * n;
                             a = T(residual_at(f2, rb + j - 1, j - 1, yy, zz, nx, ny, nz));
                             b = T(residual_at(f2, rb + n - j, n - j, yy, zz, nx, ny, nz));
                         } else {
-                            const Tin* p = in + voff + (long long)R * n;
+                            const Tin* p = (fu.vin ? (const Tin*)fu.vin[blockIdx.y] : in + voff) + (long long)R * n;
                             if (MODE == kRound) {
                                 a = T(f64_to_f32((double)p[j - 1]));
                                 b = T(f64_to_f32((double)p[n - j]));
@@ -189,7 +189,8 @@ __global__ void __launch_bounds__(256) k_sine_rg(const Tin* in, Tout* out, SineG
                             }
                         }
                     } else {
-                        const Tin* p = in + voff + ((long long)z * ny) * nx + x0 + line;
+                        const Tin* p = (fu.vin ? (const Tin*)fu.vin[blockIdx.y] : in + voff) + ((long long)z * ny) * nx + x0 +
+                                       line;
                         if (MODE == kRound) {
                             a = T(f64_to_f32((double)p[(long long)(j - 1) * nx]));
                             b = T(f64_to_f32((double)p[(long long)(n - j) * nx]));
@@ -362,7 +363,10 @@ __global__ void __launch_bounds__(256) k_sine_rg(const Tin* in, Tout* out, SineG
                         const long long idx = base + e;
                         ff s2 = two_sum(hv[q], lv[q]);
                         s2 = ff_add_f(s2, cv);
-                        if (fu.last) fu.out64[idx] = ff_to_f64(s2);
+                        if (fu.last) {
+                            double* o64 = fu.vout ? (double*)fu.vout[blockIdx.y] : fu.out64 + voff;
+                            o64[idx - voff] = ff_to_f64(s2);
+                        }
                         else fu.ulo_out[idx] = lv[q] + cv;
                         cc += cv * cv;
                         uu += s2.h * s2.h;
@@ -391,9 +395,10 @@ __global__ void __launch_bounds__(256) k_sine_rg(const Tin* in, Tout* out, SineG
                 }
             }
         } else {
+            Tout* ob = (fu.vout ? (Tout*)fu.vout[blockIdx.y] : out + voff) + (long long)row0 * n;
             for (int e = tid; e < total; e += nthr) {
                 const int r = e / n, i = e - r * n + 1;
-                out[base + e] = Tout(scale * Sr[2 * ((size_t)r * LS2 + sk(i >> 1)) + (i & 1)]);
+                ob[e] = Tout(scale * Sr[2 * ((size_t)r * LS2 + sk(i >> 1)) + (i & 1)]);
             }
         }
     } else {

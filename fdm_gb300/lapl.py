@@ -137,6 +137,87 @@ class LaplCube:
             pass
 
 
+class BatchSolver:
+    """Many right-hand sides of uneven sizes solved by one graph launch.
+
+    shapes: one (nx, ny, nz) per right-hand side; spacings / lengths: one
+    (dx, dy, dz) / (lx, ly, lz) per right-hand side, or None for h = 1/(n+1),
+    l = 1 on every axis.  Right-hand sides of equal geometry share a plan;
+    each group's schedule is timed on the caller's data by `tune` and every
+    `solve` after that replays one captured CUDA graph.  The reference solves
+    these one LaplCube at a time (src/lapl_cube.h:58-102).
+    """
+
+    def __init__(self, shapes, spacings=None, lengths=None, precision="mixed", tol=1e-10):
+        self._lib = N.load()
+        self.shapes = [tuple(int(v) for v in s) for s in shapes]
+        self.count = len(self.shapes)
+        if spacings is None:
+            spacings = [tuple(1.0 / (n + 1) for n in s) for s in self.shapes]
+        if lengths is None:
+            lengths = [(1.0, 1.0, 1.0)] * self.count
+        if len(spacings) != self.count or len(lengths) != self.count:
+            raise N.FdmError(N.EINVAL, "one spacing and one length triple per right-hand side")
+        if precision not in ("plain", "mixed"):
+            raise N.FdmError(N.EINVAL, "precision must be 'plain' or 'mixed'")
+        n3 = (c_int * (3 * self.count))(*[v for s in self.shapes for v in s])
+        h3 = (c_double * (3 * self.count))(*[float(v) for s in spacings for v in s])
+        l3 = (c_double * (3 * self.count))(*[float(v) for s in lengths for v in s])
+        h = c_void_p()
+        N.check(self._lib.fdmgpu_batch_create(byref(h), self.count, n3, h3, l3,
+                                              N.MIXED if precision == "mixed" else N.PLAIN, float(tol)))
+        self._h = h
+
+    def _ptrs(self, ans, rhs):
+        if len(ans) != self.count or len(rhs) != self.count:
+            raise N.FdmError(N.EINVAL, "expected %d volumes" % self.count)
+        pa = (c_void_p * self.count)()
+        pr = (c_void_p * self.count)()
+        for i, (nx, ny, nz) in enumerate(self.shapes):
+            pa[i] = _dev_ptr(ans[i], 8, nx * ny * nz)
+            pr[i] = _dev_ptr(rhs[i], 8, nx * ny * nz)
+        return pa, pr
+
+    def tune(self, ans, rhs) -> None:
+        """Times each group's schedules on these volumes (device FP64) and
+        keeps the fastest; overwrites ans."""
+        pa, pr = self._ptrs(ans, rhs)
+        N.check(self._lib.fdmgpu_batch_tune(self._h, pa, pr))
+
+    def solve(self, ans, rhs, stream=None) -> None:
+        """ans[i] <- solution for rhs[i], all i (device FP64, asynchronous)."""
+        pa, pr = self._ptrs(ans, rhs)
+        N.check(self._lib.fdmgpu_batch_solve(self._h, pa, pr, _stream_ptr(stream)))
+
+    def info(self):
+        """(groups, kernel launches replayed per solve)."""
+        g, l = c_int(), c_int()
+        N.check(self._lib.fdmgpu_batch_info(self._h, byref(g), byref(l)))
+        return g.value, l.value
+
+    def schedule(self):
+        """Per group: dict(shape, members, chunk, ztable, tuned_ms)."""
+        out = []
+        for k in range(self.info()[0]):
+            n3 = (c_int * 3)()
+            m, ch, zt = c_int(), c_int(), c_int()
+            ms = c_double()
+            N.check(self._lib.fdmgpu_batch_schedule(self._h, k, n3, byref(m), byref(ch), byref(zt), byref(ms)))
+            out.append(dict(shape=tuple(n3), members=m.value, chunk=ch.value, ztable=zt.value, tuned_ms=ms.value))
+        return out
+
+    def close(self) -> None:
+        if getattr(self, "_h", None):
+            self._lib.fdmgpu_batch_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
 class LaplRect:
     """2-D Dirichlet Poisson solver, fdm::LaplRect<T,check,F>: DST along y,
     tridiagonal solve along x per y-mode (src/lapl_rect.cpp:63-110)."""

@@ -141,6 +141,32 @@ int fdmgpu_lapl_cube_last_info(fdmgpu_lapl_cube* h, int* sweeps, double* est, in
 int fdmgpu_lapl_cube_scratch_bytes(fdmgpu_lapl_cube* h, size_t* bytes);
 int fdmgpu_lapl_cube_destroy(fdmgpu_lapl_cube* h);
 
+/* ---- Batched solves of uneven sizes (no counterpart in the reference,
+ * which solves one LaplCube at a time) -------------------------------------
+ * count right-hand sides, right-hand side i with sizes n3[3i..3i+2]
+ * (nx,ny,nz), spacings h3[3i..] and lengths l3[3i..] as in
+ * fdmgpu_lapl_cube_create.  Right-hand sides of equal geometry form a group
+ * with one plan.  d_ans / d_rhs are host arrays of count device pointers
+ * (FP64 volumes).  fdmgpu_batch_tune times each group's schedule candidates
+ * (right-hand sides per pipeline launch, z-solve variant) on the given data
+ * and keeps the fastest.  The first fdmgpu_batch_solve after creation or
+ * tuning captures all groups, on concurrent streams, into one CUDA graph;
+ * every solve is then one graph launch, ordered after prior work on
+ * `stream` and before later work on it.  Volume pointers may change
+ * between solves. */
+typedef struct fdmgpu_batch fdmgpu_batch;
+int fdmgpu_batch_create(fdmgpu_batch** h, int count, const int* n3, const double* h3, const double* l3,
+                        int precision, double tol);
+int fdmgpu_batch_tune(fdmgpu_batch* h, void* const* d_ans, const void* const* d_rhs);
+int fdmgpu_batch_solve(fdmgpu_batch* h, void* const* d_ans, const void* const* d_rhs, void* stream);
+/* groups formed and kernel launches one graph launch replays */
+int fdmgpu_batch_info(fdmgpu_batch* h, int* groups, int* launches_per_solve);
+/* schedule of one group: sizes, members, chunk, 1 = table-driven z-solve,
+ * and its tuned time in ms (0 before tuning) */
+int fdmgpu_batch_schedule(fdmgpu_batch* h, int group, int* n3, int* members, int* chunk, int* ztable,
+                          double* tuned_ms);
+int fdmgpu_batch_destroy(fdmgpu_batch* h);
+
 /* ---- LaplRect / LaplRectFFT2: 2-D Dirichlet Poisson ----------------------
  * Replaces fdm::LaplRect<T,check,F> (src/lapl_rect.h:11-73, solve
  * src/lapl_rect.cpp:63-110: DST-y, tridiagonal solve along x per y-mode,
