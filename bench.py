@@ -253,6 +253,143 @@ def measure_uneven_batch(torch, fdm_gb300, workloads, stream, dev, count=512, to
     }
 
 
+SERVE_RATES = (100, 300, 1000, 3000, 5000)
+
+
+def measure_serving(torch, fdm_gb300, workloads, dev, rates=SERVE_RATES, seconds=4.0, max_requests=20000,
+                    max_outstanding=1024, lanes=16, max_batch=8):
+    """Serving loop under Poisson arrivals at each rate: 70% single solves
+    (each axis from {31,63,127}, 5% at 255^3, tol 1e-6 or 1e-10 half and
+    half), 30% advances of k ~ U{1..50} steps on 64 resident 63^3 cavity
+    sessions (Re in {100,250,400}, dt 0.01), 150 GB budget.  Each rate runs
+    min(20000, rate x seconds) requests; at most max_outstanding are held by
+    the client, later arrivals wait and that wait counts in their latency.
+    Every solve's answer is checked against the FP64 form."""
+    import concurrent.futures as cf
+    import numpy as np
+    from fdm_gb300.serve import Server
+    rng = np.random.default_rng(4242)
+    small = [(a, b, c) for a in (31, 63, 127) for b in (31, 63, 127) for c in (31, 63, 127)]
+    big = (255, 255, 255)
+    geo = {}
+    rhs = {}
+    ref = {}
+    for k, sh in enumerate(small + [big]):
+        nx, ny, nz = sh
+        args = workloads.solver_args(nx, ny, nz)
+        geo[sh] = (args[0:3], args[3:6])
+        f = workloads.manufactured_torch(nx, ny, nz, seed=500 + k, kmax=(min(sh) + 1) // 4, device=dev)[0]
+        u = torch.empty_like(f)
+        fdm_gb300.LaplCube(*args).solve_device(u, f)
+        torch.cuda.synchronize()
+        rhs[sh] = f.cpu().pin_memory()
+        ref[sh] = u.cpu().numpy()
+    free = {sh: [] for sh in rhs}
+
+    def out_buf(sh):
+        return free[sh].pop() if free[sh] else torch.empty_like(rhs[sh]).pin_memory()
+
+    def check(sh, buf):
+        a = buf.numpy()
+        return sh, buf, float(np.linalg.norm(a - ref[sh]) / np.linalg.norm(ref[sh]))
+
+    srv = Server(150e9, lanes=lanes, max_batch=max_batch)
+    sess = [srv.session_create(63, 63, Re=(100.0, 250.0, 400.0)[i % 3], dt=0.01) for i in range(64)]
+    # warm-up: every plan and every session graph exists before timing
+    ids = []
+    for sh in rhs:
+        for tol in (1e-6, 1e-10):
+            b = out_buf(sh)
+            ids.append((srv.submit_solve(b, rhs[sh], sh, *geo[sh], tol=tol), sh, b))
+    for sid in sess:
+        ids.append((srv.submit_advance(sid, 2), None, None))
+    for rid, sh, b in ids:
+        srv.wait(rid)
+        if sh:
+            free[sh].append(b)
+    pool = cf.ThreadPoolExecutor(8)
+    out = []
+    for lam in rates:
+        n = int(min(max_requests, max(200, lam * seconds)))
+        arrive = np.cumsum(rng.exponential(1.0 / lam, n))
+        is_solve = rng.random(n) < 0.7
+        is_big = rng.random(n) < 0.05
+        axes = rng.choice((31, 63, 127), size=(n, 3))
+        tols = np.where(rng.random(n) < 0.5, 1e-6, 1e-10)
+        sids = rng.integers(0, 64, n)
+        ks = rng.integers(1, 51, n)
+        srv.stats_reset()
+        live = {}
+        lat, lat_solve, lat_adv, errs, futs = [], [], [], [], []
+        i = 0
+        t0 = time.perf_counter()
+        t_last = t0
+        while i < n or live:
+            now = time.perf_counter() - t0
+            while i < n and arrive[i] <= now and len(live) < max_outstanding:
+                ts = time.perf_counter() - t0
+                if is_solve[i]:
+                    sh = big if is_big[i] else tuple(int(v) for v in axes[i])
+                    b = out_buf(sh)
+                    rid = srv.submit_solve(b, rhs[sh], sh, *geo[sh], tol=float(tols[i]))
+                    live[rid] = (arrive[i], ts, sh, b)
+                else:
+                    rid = srv.submit_advance(sess[sids[i]], int(ks[i]))
+                    live[rid] = (arrive[i], ts, None, None)
+                i += 1
+            wait_ms = 2.0 if i >= n else max(0.0, min(2.0, (arrive[i] - (time.perf_counter() - t0)) * 1e3))
+            rec = srv.next_done(wait_ms) if live else None
+            while rec is not None:
+                a_t, s_t, sh, b = live.pop(rec["id"])
+                if rec["state"] != "done":
+                    raise RuntimeError("request failed: %s" % rec)
+                l_ms = rec["latency_ms"] + (s_t - a_t) * 1e3
+                lat.append(l_ms)
+                t_last = time.perf_counter()
+                if sh:
+                    lat_solve.append(l_ms)
+                    futs.append(pool.submit(check, sh, b))
+                else:
+                    lat_adv.append(l_ms)
+                rec = srv.next_done(0.0) if live else None
+            keep = []
+            for fu in futs:
+                if fu.done():
+                    sh, b, e = fu.result()
+                    errs.append(e)
+                    free[sh].append(b)
+                else:
+                    keep.append(fu)
+            futs = keep
+        for fu in futs:
+            sh, b, e = fu.result()
+            errs.append(e)
+            free[sh].append(b)
+        wall = t_last - t0
+        st = srv.stats()
+
+        def pct(v, q):
+            return float(np.percentile(v, q)) if v else None
+        out.append({
+            "offered_req_per_s": lam, "requests": n, "achieved_req_per_s": n / wall,
+            "p50_ms": pct(lat, 50), "p99_ms": pct(lat, 99),
+            "p50_solve_ms": pct(lat_solve, 50), "p99_solve_ms": pct(lat_solve, 99),
+            "p50_advance_ms": pct(lat_adv, 50), "p99_advance_ms": pct(lat_adv, 99),
+            "solve_err_vs_fp64_max": max(errs) if errs else None,
+            "solve_err_vs_fp64_median": pct(errs, 50), "solves_checked": len(errs),
+            "solve_launches": st["batches"], "solves_batched": st["batched_requests"],
+            "peak_device_gb": st["peak_bytes"] / 1e9, "mean_queue_ms": st["mean_queue_ms"],
+        })
+    pool.shutdown()
+    srv.close()
+    return {"workload": "70% solves {31,63,127}^3 + 5% 255^3, tol 1e-6/1e-10; 30% advance k~U[1,50] on 64 "
+                        "resident 63^3 sessions; Poisson arrivals; 150 GB budget",
+            "lanes": lanes, "max_batch": max_batch, "max_outstanding": max_outstanding,
+            "latency": "arrival to answer in pinned host memory (server clock from submit, plus client wait)",
+            "advance_error": "sessions are the plain FP64 NSCube (bit-identical to a lone NSCube)",
+            "rates": out}
+
+
 def run_ncu_case():
     """Two mixed solves of 2 RHS at 255^3 (266 MB of FP64 input, larger than
     L2) with nothing else on the GPU: the case the committed ncu summaries
@@ -277,6 +414,7 @@ def main():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-serving", action="store_true", help="skip the serving-loop sweep")
     ap.add_argument("--ncu-case", action="store_true",
                     help="run only two mixed solves of 2 RHS at 255^3 (a small case for profiler captures)")
     ap.add_argument("--chunk", type=int, default=NRHS,
@@ -411,6 +549,7 @@ def main():
     del out, f
     torch.cuda.empty_cache()
     uneven = measure_uneven_batch(torch, fdm_gb300, workloads, stream, dev)
+    serving = measure_serving(torch, fdm_gb300, workloads, dev) if not args.no_serving else None
 
     solves = args.steps * NRHS * world
     value = solves / (ms * 1e-3)
@@ -441,6 +580,7 @@ def main():
         "plain_fp64_gpu": {"value": plain_rate, "unit": UNIT},
         "nscube_63cubed": {"ms_per_step": ns_ms, "steps_timed": 200, "Re": 250.0, "dt": 0.01},
         "uneven_batch": uneven,
+        "serving": serving,
         "clocks": clocks,
     }
     if rank == 0 and not args.no_cpu_baseline:

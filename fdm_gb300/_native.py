@@ -24,6 +24,22 @@ _STATUS_NAMES = {
 }
 
 
+REQ_SOLVE, REQ_ADVANCE = 0, 1
+REQ_QUEUED, REQ_RUNNING, REQ_DONE, REQ_FAILED, REQ_CANCELLED = range(5)
+
+
+class ServerStats(ctypes.Structure):
+    """fdmgpu_server_stats_t."""
+    _fields_ = [(n, c_ulonglong) for n in ("submitted", "completed", "failed", "cancelled", "rejected")] + \
+        [("queued", c_int), ("running", c_int), ("batches", c_ulonglong), ("batched_requests", c_ulonglong)] + \
+        [(n, c_double) for n in ("used_bytes", "peak_bytes", "budget_bytes", "plan_bytes", "session_bytes",
+                                 "p50_ms", "p99_ms", "p50_solve_ms", "p99_solve_ms", "p50_advance_ms",
+                                 "p99_advance_ms", "mean_queue_ms")]
+
+    def as_dict(self) -> dict:
+        return {n: getattr(self, n) for n, _ in self._fields_}
+
+
 class FdmError(RuntimeError):
     """A non-zero status from libfdmgpu.  `status` is the code."""
 
@@ -77,6 +93,27 @@ _SIGS = [
     ("fdmgpu_nscube_field_device", c_int, [c_void_p, c_int, POINTER(c_void_p)]),
     ("fdmgpu_nscube_time_index", c_int, [c_void_p, POINTER(c_int)]),
     ("fdmgpu_nscube_destroy", c_int, [c_void_p]),
+    ("fdmgpu_server_create", c_int, [POINTER(c_void_p), c_double, c_int, c_int]),
+    ("fdmgpu_server_submit_solve", c_int,
+     [c_void_p, POINTER(c_ulonglong), POINTER(c_int), POINTER(c_double), POINTER(c_double), c_double, c_void_p,
+      c_void_p]),
+    ("fdmgpu_server_session_create", c_int, [c_void_p, POINTER(c_int), c_int, c_int] + [c_double] * 9),
+    ("fdmgpu_server_submit_advance", c_int, [c_void_p, POINTER(c_ulonglong), c_int, c_int]),
+    ("fdmgpu_server_poll", c_int,
+     [c_void_p, c_ulonglong, POINTER(c_int), POINTER(c_int), POINTER(c_double), POINTER(c_double), POINTER(c_int)]),
+    ("fdmgpu_server_wait", c_int,
+     [c_void_p, c_ulonglong, c_double, POINTER(c_int), POINTER(c_int), POINTER(c_double), POINTER(c_double),
+      POINTER(c_int)]),
+    ("fdmgpu_server_next_done", c_int,
+     [c_void_p, c_double, POINTER(c_ulonglong), POINTER(c_int), POINTER(c_int), POINTER(c_double),
+      POINTER(c_double), POINTER(c_int)]),
+    ("fdmgpu_server_cancel", c_int, [c_void_p, c_ulonglong]),
+    ("fdmgpu_server_session_get_field", c_int,
+     [c_void_p, c_int, c_int, c_void_p, c_size_t, POINTER(c_longlong), c_double]),
+    ("fdmgpu_server_session_close", c_int, [c_void_p, c_int, c_double]),
+    ("fdmgpu_server_stats", c_int, [c_void_p, c_void_p]),
+    ("fdmgpu_server_stats_reset", c_int, [c_void_p]),
+    ("fdmgpu_server_destroy", c_int, [c_void_p]),
 ]
 
 EXPORTED = [s[0] for s in _SIGS]

@@ -227,6 +227,69 @@ int fdmgpu_nscube_field_device(fdmgpu_nscube* h, int field, void** dptr);
 int fdmgpu_nscube_time_index(fdmgpu_nscube* h, int* t);
 int fdmgpu_nscube_destroy(fdmgpu_nscube* h);
 
+/* ---- Serving loop (no counterpart in the reference, which runs one
+ * solve or one NSCube on the caller's thread) ------------------------------
+ * Requests are Poisson solves (host buffers, FP64, page-locked) and
+ * k-step advances of resident NSCube sessions.  One scheduler thread admits
+ * them first come first served while their device memory fits under
+ * budget_bytes (staging of requests in flight + pooled solver plans +
+ * session state), runs up to `lanes` launches concurrently on separate CUDA
+ * streams, and merges waiting solves of the same geometry and refinement
+ * class into one launch of up to max_batch right-hand sides (continuous
+ * batching).  A solve's answer does not depend on the company it keeps.
+ * Latency is submit to completion on the device, copies included.
+ * Solve tolerance: tol <= 0 selects the plain FP64 form; otherwise the
+ * mixed form with the refinement sweeps tol asks for. */
+typedef struct fdmgpu_server fdmgpu_server;
+enum { FDMGPU_REQ_SOLVE = 0, FDMGPU_REQ_ADVANCE = 1 };
+enum {
+    FDMGPU_REQ_QUEUED = 0, FDMGPU_REQ_RUNNING = 1, FDMGPU_REQ_DONE = 2,
+    FDMGPU_REQ_FAILED = 3, FDMGPU_REQ_CANCELLED = 4
+};
+typedef struct {
+    unsigned long long submitted, completed, failed, cancelled, rejected;
+    int queued, running;
+    unsigned long long batches, batched_requests; /* solve launches, solves they carried */
+    double used_bytes, peak_bytes, budget_bytes, plan_bytes, session_bytes;
+    double p50_ms, p99_ms, p50_solve_ms, p99_solve_ms, p50_advance_ms, p99_advance_ms;
+    double mean_queue_ms;
+} fdmgpu_server_stats_t;
+
+int fdmgpu_server_create(fdmgpu_server** h, double budget_bytes, int lanes, int max_batch);
+/* n3 = (nx,ny,nz), h3 = (dx,dy,dz), l3 = (lx,ly,lz) as fdmgpu_lapl_cube_create;
+ * FDMGPU_EBUDGET when the request alone can never fit */
+int fdmgpu_server_submit_solve(fdmgpu_server* h, unsigned long long* id, const int* n3, const double* h3,
+                               const double* l3, double tol, const double* rhs, double* ans);
+/* a resident lid-driven cavity (parameters of fdmgpu_nscube_create, FP64) */
+int fdmgpu_server_session_create(fdmgpu_server* h, int* session, int nx, int nz, double x1, double y1,
+                                 double z1, double x2, double y2, double z2, double u0, double Re, double dt);
+/* advances run in submission order per session */
+int fdmgpu_server_submit_advance(fdmgpu_server* h, unsigned long long* id, int session, int steps);
+/* state of a request; a finished (done, failed, cancelled) request is
+ * reported once and then forgotten.  latency_ms: submit to completion
+ * (-1 while unfinished); queue_ms: submit to launch; batch: requests in its
+ * launch.  A failed request's message is left in fdmgpu_last_error(). */
+int fdmgpu_server_poll(fdmgpu_server* h, unsigned long long id, int* state, int* status, double* latency_ms,
+                       double* queue_ms, int* batch);
+/* as poll, blocking until the request finishes or timeout_ms passes
+ * (FDMGPU_ETIMEOUT) */
+int fdmgpu_server_wait(fdmgpu_server* h, unsigned long long id, double timeout_ms, int* state, int* status,
+                       double* latency_ms, double* queue_ms, int* batch);
+/* the next finished request (any), reported as poll does; FDMGPU_ETIMEOUT
+ * when none finishes within timeout_ms */
+int fdmgpu_server_next_done(fdmgpu_server* h, double timeout_ms, unsigned long long* id, int* state,
+                            int* status, double* latency_ms, double* queue_ms, int* batch);
+/* cancels a queued request (FDMGPU_EINVAL once it has started) */
+int fdmgpu_server_cancel(fdmgpu_server* h, unsigned long long id);
+/* copies a session field (FDMGPU_NS_*) once its queued advances are done */
+int fdmgpu_server_session_get_field(fdmgpu_server* h, int session, int field, double* out, size_t count,
+                                    long long* steps_done, double timeout_ms);
+int fdmgpu_server_session_close(fdmgpu_server* h, int session, double timeout_ms);
+int fdmgpu_server_stats(fdmgpu_server* h, fdmgpu_server_stats_t* out);
+int fdmgpu_server_stats_reset(fdmgpu_server* h);
+/* cancels queued requests, waits for running ones, frees everything */
+int fdmgpu_server_destroy(fdmgpu_server* h);
+
 #ifdef __cplusplus
 }
 #endif

@@ -59,3 +59,35 @@ def test_python_errors_carry_status(native):
     with pytest.raises(FdmError) as e:
         LaplCube(0.1, 0.1, 0.1, 3.2, 3.2, 3.2, 32, 31, 31)
     assert e.value.status == 2
+
+
+def test_server_stats_struct_layout(tmp_path):
+    """ctypes' ServerStats has the C struct's size and field offsets."""
+    import shutil
+    import subprocess
+    from fdm_gb300 import _native as N
+    if not shutil.which("gcc"):
+        pytest.skip("gcc not found")
+    names = [n for n, _ in N.ServerStats._fields_]
+    src = tmp_path / "layout.c"
+    src.write_text("#include <stdio.h>\n#include <stddef.h>\n#include \"fdmgpu.h\"\nint main(void){\n"
+                   "printf(\"%zu\\n\", sizeof(fdmgpu_server_stats_t));\n"
+                   + "".join("printf(\"%%zu\\n\", offsetof(fdmgpu_server_stats_t, %s));\n" % n for n in names)
+                   + "return 0;}\n")
+    exe = tmp_path / "layout"
+    subprocess.run(["gcc", "-I", str(ROOT / "include"), str(src), "-o", str(exe)], check=True)
+    vals = [int(v) for v in subprocess.run([str(exe)], check=True, capture_output=True, text=True).stdout.split()]
+    assert vals[0] == ctypes.sizeof(N.ServerStats)
+    assert vals[1:] == [getattr(N.ServerStats, n).offset for n in names]
+
+
+def test_server_arguments_without_gpu(native):
+    from fdm_gb300 import _native as N
+    lib = N.load()
+    h = c_void_p()
+    assert lib.fdmgpu_server_create(byref(h), 0.0, 8, 8) == N.EINVAL
+    assert lib.fdmgpu_server_create(byref(h), 1e9, 0, 8) == N.EINVAL
+    assert lib.fdmgpu_server_create(byref(h), 1e9, 8, 65) == N.EINVAL
+    assert lib.fdmgpu_server_create(None, 1e9, 8, 8) == N.EINVAL
+    assert lib.fdmgpu_server_destroy(None) == N.OK
+    assert lib.fdmgpu_server_cancel(None, 1) == N.EINVAL

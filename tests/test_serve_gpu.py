@@ -1,0 +1,176 @@
+"""GPU tests of the serving loop (fdmgpu_server_*) through the C ABI: each
+result is the same alone and in a mix of concurrent, batched requests;
+per-request accuracy against the FP64 form; admission under a memory
+budget; cancellation, timeouts and rejected buffers."""
+import math
+
+import numpy as np
+import pytest
+
+from fdm_gb300 import FdmError, LaplCube, NSCube, workloads
+from fdm_gb300 import _native as N
+from fdm_gb300.serve import Server
+
+pytestmark = pytest.mark.gpu
+
+SHAPES = [(31, 31, 31), (63, 31, 127), (31, 63, 63), (127, 127, 31), (63, 63, 63), (31, 31, 31), (63, 63, 63),
+          (31, 31, 31)]
+TOLS = [1e-6, 1e-10, 1e-10, 1e-6, 1e-10, 1e-10, 1e-6, 0.0]
+
+
+def _pinned_rhs(shape, seed):
+    import torch
+    nx, ny, nz = shape
+    g = torch.Generator().manual_seed(seed)
+    return torch.randn((nz, ny, nx), dtype=torch.float64, generator=g).pin_memory()
+
+
+def _pinned_like(t):
+    import torch
+    return torch.empty_like(t).pin_memory()
+
+
+def _fp64(shape, rhs):
+    """The plain FP64 LaplCube answer (h = 1/(n+1), l = 1)."""
+    nx, ny, nz = shape
+    lc = LaplCube(1 / (nx + 1), 1 / (ny + 1), 1 / (nz + 1), 1.0, 1.0, 1.0, nx, ny, nz)
+    out = np.zeros(rhs.shape)
+    lc.solve(out, rhs.numpy())
+    return out
+
+
+def _rel(a, b):
+    return float(np.linalg.norm(a - b) / np.linalg.norm(b))
+
+
+def test_results_same_alone_and_in_the_mix(cuda):
+    rhs = [_pinned_rhs(s, i) for i, s in enumerate(SHAPES)]
+    # alone: one lane, one request per launch, each waited for in turn
+    alone = []
+    with Server(budget_bytes=8e9, lanes=1, max_batch=1) as srv:
+        sid = srv.session_create(31, 31, Re=250.0, dt=0.01)
+        for s, t, r in zip(SHAPES, TOLS, rhs):
+            a = _pinned_like(r)
+            rec = srv.wait(srv.submit_solve(a, r, s, tol=t))
+            assert rec["state"] == "done" and rec["batch"] == 1
+            alone.append(a)
+        srv.wait(srv.submit_advance(sid, 12))
+        u_alone, steps = srv.session_field(sid, "u")
+        assert steps == 12
+    # in the mix: eight lanes, batching on, two sessions advancing in
+    # between, every request submitted before any finishes
+    with Server(budget_bytes=8e9, lanes=8, max_batch=8) as srv:
+        sids = [srv.session_create(31, 31, Re=250.0, dt=0.01), srv.session_create(31, 31, Re=100.0, dt=0.01)]
+        mix = [_pinned_like(r) for r in rhs]
+        ids = []
+        for k, (s, t, r, a) in enumerate(zip(SHAPES, TOLS, rhs, mix)):
+            ids.append(srv.submit_solve(a, r, s, tol=t))
+            ids.append(srv.submit_advance(sids[k % 2], 3))
+        done = 0
+        while done < len(ids):
+            rec = srv.next_done(10000.0)
+            assert rec is not None and rec["state"] == "done", rec
+            done += 1
+        u_mix, steps = srv.session_field(sids[0], "u")
+        assert steps == 12
+        st = srv.stats()
+        assert st["completed"] == len(ids) and st["failed"] == 0
+    import torch
+    for i in range(len(SHAPES)):
+        assert torch.equal(alone[i], mix[i]), (i, SHAPES[i])
+    assert np.array_equal(u_alone, u_mix)
+    # and the session matches a standalone NSCube advanced as far
+    ns = NSCube(nx=31, nz=31, Re=250.0, dt=0.01, u0=1.0, x1=-math.pi, y1=-math.pi, z1=-math.pi, x2=math.pi,
+                y2=math.pi, z2=math.pi)
+    ns.step(12)
+    assert np.array_equal(ns.get("u").data.ravel(), u_mix.ravel())
+    ns.close()
+
+
+def test_waiting_solves_share_a_launch(cuda):
+    """Solves of one geometry that wait behind a busy lane go out as one
+    launch; their answers equal the ones they get alone."""
+    shape = (63, 63, 63)
+    rhs = [_pinned_rhs(shape, 100 + i) for i in range(6)]
+    outs = [_pinned_like(r) for r in rhs]
+    with Server(budget_bytes=8e9, lanes=1, max_batch=8) as srv:
+        sid = srv.session_create(63, 63)
+        busy = srv.submit_advance(sid, 50)
+        ids = [srv.submit_solve(a, r, shape, tol=1e-10) for a, r in zip(outs, rhs)]
+        srv.wait(busy)
+        recs = [srv.wait(i) for i in ids]
+        assert max(r["batch"] for r in recs) >= 2
+        st = srv.stats()
+        assert st["batched_requests"] > st["batches"]
+    with Server(budget_bytes=8e9, lanes=1, max_batch=1) as srv:
+        for a, r in zip(outs, rhs):
+            one = _pinned_like(r)
+            srv.wait(srv.submit_solve(one, r, shape, tol=1e-10))
+            import torch
+            assert torch.equal(one, a)
+
+
+def test_per_request_error_vs_fp64(cuda):
+    with Server(budget_bytes=8e9, lanes=4, max_batch=4) as srv:
+        cases = []
+        for i, (s, t) in enumerate(zip(SHAPES, TOLS)):
+            r = _pinned_rhs(s, 50 + i)
+            a = _pinned_like(r)
+            cases.append((s, t, r, a, srv.submit_solve(a, r, s, tol=t)))
+        for s, t, r, a, rid in cases:
+            assert srv.wait(rid)["state"] == "done"
+            err = _rel(a.numpy(), _fp64(s, r))
+            assert err <= max(t, 1e-13), (s, t, err)
+
+
+def test_admission_under_budget(cuda):
+    """A budget that holds a few 63^3 solves at a time: everything still
+    completes and the accounted peak stays under the budget."""
+    shape = (63, 63, 63)
+    budget = 100e6
+    rhs = [_pinned_rhs(shape, 200 + i) for i in range(12)]
+    outs = [_pinned_like(r) for r in rhs]
+    with Server(budget_bytes=budget, lanes=8, max_batch=8) as srv:
+        ids = [srv.submit_solve(a, r, shape, tol=1e-10) for a, r in zip(outs, rhs)]
+        for i in ids:
+            assert srv.wait(i)["state"] == "done"
+        st = srv.stats()
+        assert 0 < st["peak_bytes"] <= budget
+        assert st["plan_bytes"] > 0
+    ref = _fp64(shape, rhs[0])
+    assert _rel(outs[0].numpy(), ref) <= 1e-10
+
+
+def test_rejections_cancel_and_timeout(cuda):
+    import torch
+    shape = (63, 63, 63)
+    r = _pinned_rhs(shape, 1)
+    a = _pinned_like(r)
+    with Server(budget_bytes=10e6, lanes=1, max_batch=1) as srv:
+        with pytest.raises(FdmError) as e:
+            srv.submit_solve(a, r, shape)
+        assert e.value.status == N.EBUDGET
+    with Server(budget_bytes=8e9, lanes=1, max_batch=1) as srv:
+        with pytest.raises(FdmError) as e:  # pageable buffers are refused
+            srv.submit_solve(np.zeros(63 ** 3), r.numpy().ravel().copy(), shape)
+        assert e.value.status == N.EINVAL
+        odd = torch.zeros(64 * 63 * 63, dtype=torch.float64).pin_memory()
+        with pytest.raises(FdmError) as e:  # n+1 = 65 is not a power of two
+            srv.submit_solve(odd, odd, (64, 63, 63))
+        assert e.value.status == N.ESIZE
+        sid = srv.session_create(63, 63)
+        busy = srv.submit_advance(sid, 50)
+        queued = srv.submit_solve(a, r, shape)
+        srv.cancel(queued)
+        assert srv.poll(queued)["state"] == "cancelled"
+        with pytest.raises(FdmError) as e:
+            srv.wait(busy, timeout_ms=0.01)
+        assert e.value.status == N.ETIMEOUT
+        assert srv.wait(busy)["state"] == "done"
+        with pytest.raises(FdmError):
+            srv.submit_advance(sid + 5, 1)
+        srv.session_close(sid)
+        with pytest.raises(FdmError):
+            srv.submit_advance(sid, 1)
+        st = srv.stats()
+        assert st["cancelled"] == 1 and st["completed"] == 1
