@@ -390,13 +390,21 @@ def measure_serving(torch, fdm_gb300, workloads, dev, rates=SERVE_RATES, seconds
             "rates": out}
 
 
-def run_ncu_case():
-    """Two mixed solves of 2 RHS at 255^3 (266 MB of FP64 input, larger than
-    L2) with nothing else on the GPU: the case the committed ncu summaries
-    capture."""
+def run_ncu_case(which: str = "solve"):
+    """solve: two mixed solves of 2 RHS at 255^3 (266 MB of FP64 input,
+    larger than L2) with nothing else on the GPU.  nscube: a 63^3 cavity,
+    Re 250, dt 0.01, stepped 4 times (the first eager, then one captured
+    graph replayed).  The cases the committed ncu summaries capture."""
     import torch
     import fdm_gb300
     from fdm_gb300 import workloads
+    if which == "nscube":
+        ns = fdm_gb300.NSCube(nx=63, nz=63, Re=250.0, dt=0.01, u0=1.0)
+        ns.step(4)
+        torch.cuda.synchronize()
+        ns.close()
+        print("ncu case done")
+        return
     n = N_INT
     f = torch.stack([workloads.manufactured_torch(n, n, n, seed=s, kmax=KMAX, noise=NOISE)[0] for s in (0, 1)])
     out = torch.empty_like(f)
@@ -415,8 +423,9 @@ def main():
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-serving", action="store_true", help="skip the serving-loop sweep")
-    ap.add_argument("--ncu-case", action="store_true",
-                    help="run only two mixed solves of 2 RHS at 255^3 (a small case for profiler captures)")
+    ap.add_argument("--ncu-case", nargs="?", const="solve", default=None, choices=["solve", "nscube"],
+                    help="run only a small case for profiler captures: 'solve' (two mixed solves of 2 RHS at "
+                         "255^3) or 'nscube' (four 63^3 cavity steps)")
     ap.add_argument("--chunk", type=int, default=NRHS,
                     help="right-hand sides per solve call within a step (divides 16)")
     args = ap.parse_args()
@@ -424,7 +433,7 @@ def main():
 
     world, rank, local = dist_setup()
     if args.ncu_case:
-        run_ncu_case()
+        run_ncu_case(args.ncu_case)
         return
     if args.impl == "reference":
         run_reference_arm(args, world, rank)

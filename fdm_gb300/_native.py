@@ -93,6 +93,7 @@ _SIGS = [
     ("fdmgpu_nscube_field_device", c_int, [c_void_p, c_int, POINTER(c_void_p)]),
     ("fdmgpu_nscube_time_index", c_int, [c_void_p, POINTER(c_int)]),
     ("fdmgpu_nscube_destroy", c_int, [c_void_p]),
+    ("fdmgpu_check_const_division", c_int, [c_longlong, c_void_p, c_void_p, c_void_p, c_void_p, c_void_p]),
     ("fdmgpu_server_create", c_int, [POINTER(c_void_p), c_double, c_int, c_int]),
     ("fdmgpu_server_submit_solve", c_int,
      [c_void_p, POINTER(c_ulonglong), POINTER(c_int), POINTER(c_double), POINTER(c_double), c_double, c_void_p,

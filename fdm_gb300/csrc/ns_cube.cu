@@ -40,10 +40,36 @@ static Field make_field(int z1, int z2, int y1, int y2, int x1, int x2) {
     return f;
 }
 
+// A divisor fixed for the whole run and its correctly rounded reciprocal
+// (computed on the host).
+struct CDiv {
+    double b, y;
+};
+
+static CDiv cdiv_of(double b) { return CDiv{b, 1.0 / b}; }
+
 struct NSParams {
     int nx, ny, nz;
     double U0, Re, dt, dx, dy, dz, dx2, dy2, dz2;
+    CDiv dRe, ddx, ddy, ddz, ddx2, ddy2, ddz2, ddt;
+    double dt_dx, dt_dy, dt_dz;  // dt/dx etc., correctly rounded on the host
 };
+
+// a / d.b correctly rounded, for finite a and quotients and remainders in
+// the normal range: q0 = a*y within two ulps, then two remainder
+// corrections r = a - b q (exact through the fused multiply-add) and
+// q <- q + r y.  After the first q is faithful, and a faithful q with
+// y = RN(1/b) corrects to RN(a/b) (P. Markstein, "Computation of elementary
+// functions on the IBM RISC System/6000 processor", IBM J. Res. Dev. 34,
+// 1990; the correction theorem as stated in J.-M. Muller et al., Handbook
+// of Floating-Point Arithmetic, ch. on division).  Five FP64 operations and
+// no data-dependent slow path; a zero dividend returns its signed zero.
+__device__ __forceinline__ double cdiv(double a, CDiv d) {
+    const double q0 = a * d.y;
+    double q = fma(fma(-q0, d.b, a), d.y, q0);
+    q = fma(fma(-q, d.b, a), d.y, q);
+    return (__double_as_longlong(a) << 1) == 0 ? q0 : q;
+}
 
 __device__ __forceinline__ double sq(double x) { return x * x; }  // asp::sq, src/asp_misc.h:295
 
@@ -88,25 +114,24 @@ __global__ void k_ns_bound2(Field u, Field v, Field w, Field p, NSParams P) {
     const int j = (int)(e % W);
     const int k = (int)((e / W) % H);
     const int i = (int)(e / ((long long)W * H));
-    const double Re = P.Re, dx = P.dx, dy = P.dy, dz = P.dz;
     if (i == nz + 1 && k <= ny + 1) {
         if (j == 0) u(nz + 1, k, -1) = u(nz + 1, k, 1);
         if (j == nx + 1) u(nz + 1, k, nx + 1) = u(nz + 1, k, nx - 1);
     }
     if (i >= 1 && i <= nz && k >= 1 && k <= ny) {
-        if (j == 0) p(i, k, 0) = p(i, k, 1) - (u(i, k, 1) - 2 * u(i, k, 0) + u(i, k, -1)) / Re / dx;
+        if (j == 0) p(i, k, 0) = p(i, k, 1) - cdiv(cdiv(u(i, k, 1) - 2 * u(i, k, 0) + u(i, k, -1), P.dRe), P.ddx);
         if (j == nx + 1)
-            p(i, k, nx + 1) = p(i, k, nx) - (u(i, k, nx + 1) - 2 * u(i, k, nx) + u(i, k, nx - 1)) / Re / dx;
+            p(i, k, nx + 1) = p(i, k, nx) - cdiv(cdiv(u(i, k, nx + 1) - 2 * u(i, k, nx) + u(i, k, nx - 1), P.dRe), P.ddx);
     }
     if (i >= 1 && i <= nz && j >= 1 && j <= nx) {
-        if (k == 0) p(i, 0, j) = p(i, 1, j) - (v(i, 1, j) - 2 * v(i, 0, j) + v(i, -1, j)) / Re / dy;
+        if (k == 0) p(i, 0, j) = p(i, 1, j) - cdiv(cdiv(v(i, 1, j) - 2 * v(i, 0, j) + v(i, -1, j), P.dRe), P.ddy);
         if (k == ny + 1)
-            p(i, ny + 1, j) = p(i, ny, j) - (v(i, ny + 1, j) - 2 * v(i, ny, j) + v(i, ny - 1, j)) / Re / dy;
+            p(i, ny + 1, j) = p(i, ny, j) - cdiv(cdiv(v(i, ny + 1, j) - 2 * v(i, ny, j) + v(i, ny - 1, j), P.dRe), P.ddy);
     }
     if (k >= 1 && k <= ny && j >= 1 && j <= nx) {
-        if (i == 0) p(0, k, j) = p(1, k, j) - (w(1, k, j) - 2 * w(0, k, j) + w(-1, k, j)) / Re / dz;
+        if (i == 0) p(0, k, j) = p(1, k, j) - cdiv(cdiv(w(1, k, j) - 2 * w(0, k, j) + w(-1, k, j), P.dRe), P.ddz);
         if (i == nz + 1)
-            p(nz + 1, k, j) = p(nz, k, j) - (w(nz + 1, k, j) - 2 * w(nz, k, j) + w(nz - 1, k, j)) / Re / dz;
+            p(nz + 1, k, j) = p(nz, k, j) - cdiv(cdiv(w(nz + 1, k, j) - 2 * w(nz, k, j) + w(nz - 1, k, j), P.dRe), P.ddz);
     }
 }
 
@@ -121,40 +146,41 @@ __global__ void __launch_bounds__(256) k_ns_fgh(Field u, Field v, Field w, Field
     const int j = (int)(e % W);
     const int k = (int)((e / W) % Hh);
     const int i = (int)(e / ((long long)W * Hh));
-    const double Re = P.Re, dt = P.dt, dx = P.dx, dy = P.dy, dz = P.dz;
-    const double dx2 = P.dx2, dy2 = P.dy2, dz2 = P.dz2;
+    const double dt = P.dt;
+    // x / Re / h^2 and x / h, each quotient rounded as the reference's
+    auto dif = [&](double x, CDiv d2) { return cdiv(cdiv(x, P.dRe), d2); };
     if (i >= 1 && k >= 1) {
         F(i, k, j) = u(i, k, j) + dt * (
-            (u(i, k, j + 1) - 2 * u(i, k, j) + u(i, k, j - 1)) / Re / dx2 +
-            (u(i, k + 1, j) - 2 * u(i, k, j) + u(i, k - 1, j)) / Re / dy2 +
-            (u(i + 1, k, j) - 2 * u(i, k, j) + u(i - 1, k, j)) / Re / dz2 -
-            (sq(0.5 * (u(i, k, j) + u(i, k, j + 1))) - sq(0.5 * (u(i, k, j - 1) + u(i, k, j)))) / dx -
-            0.25 * ((u(i, k, j) + u(i, k + 1, j)) * (v(i, k, j + 1) + v(i, k, j)) -
-                    (u(i, k - 1, j) + u(i, k, j)) * (v(i, k - 1, j + 1) + v(i, k - 1, j))) / dy -
-            0.25 * ((u(i, k, j) + u(i + 1, k, j)) * (w(i, k, j + 1) + w(i, k, j)) -
-                    (u(i - 1, k, j) + u(i, k, j)) * (w(i - 1, k, j + 1) + w(i - 1, k, j))) / dz);
+            dif(u(i, k, j + 1) - 2 * u(i, k, j) + u(i, k, j - 1), P.ddx2) +
+            dif(u(i, k + 1, j) - 2 * u(i, k, j) + u(i, k - 1, j), P.ddy2) +
+            dif(u(i + 1, k, j) - 2 * u(i, k, j) + u(i - 1, k, j), P.ddz2) -
+            cdiv(sq(0.5 * (u(i, k, j) + u(i, k, j + 1))) - sq(0.5 * (u(i, k, j - 1) + u(i, k, j))), P.ddx) -
+            cdiv(0.25 * ((u(i, k, j) + u(i, k + 1, j)) * (v(i, k, j + 1) + v(i, k, j)) -
+                         (u(i, k - 1, j) + u(i, k, j)) * (v(i, k - 1, j + 1) + v(i, k - 1, j))), P.ddy) -
+            cdiv(0.25 * ((u(i, k, j) + u(i + 1, k, j)) * (w(i, k, j + 1) + w(i, k, j)) -
+                         (u(i - 1, k, j) + u(i, k, j)) * (w(i - 1, k, j + 1) + w(i - 1, k, j))), P.ddz));
     }
     if (i >= 1 && j >= 1) {
         G(i, k, j) = v(i, k, j) + dt * (
-            (v(i, k, j + 1) - 2 * v(i, k, j) + v(i, k, j - 1)) / Re / dx2 +
-            (v(i, k + 1, j) - 2 * v(i, k, j) + v(i, k - 1, j)) / Re / dy2 +
-            (v(i + 1, k, j) - 2 * v(i, k, j) + v(i - 1, k, j)) / Re / dz2 -
-            (sq(0.5 * (v(i, k, j) + v(i, k + 1, j))) - sq(0.5 * (v(i, k - 1, j) + v(i, k, j)))) / dy -
-            0.25 * ((u(i, k, j) + u(i, k + 1, j)) * (v(i, k, j + 1) + v(i, k, j)) -
-                    (u(i, k, j - 1) + u(i, k + 1, j - 1)) * (v(i, k, j) + v(i, k, j - 1))) / dx -
-            0.25 * ((w(i, k, j) + w(i, k + 1, j)) * (v(i, k, j) + v(i + 1, k, j)) -
-                    (w(i - 1, k, j) + w(i - 1, k + 1, j)) * (v(i - 1, k, j) + v(i, k, j))) / dz);
+            dif(v(i, k, j + 1) - 2 * v(i, k, j) + v(i, k, j - 1), P.ddx2) +
+            dif(v(i, k + 1, j) - 2 * v(i, k, j) + v(i, k - 1, j), P.ddy2) +
+            dif(v(i + 1, k, j) - 2 * v(i, k, j) + v(i - 1, k, j), P.ddz2) -
+            cdiv(sq(0.5 * (v(i, k, j) + v(i, k + 1, j))) - sq(0.5 * (v(i, k - 1, j) + v(i, k, j))), P.ddy) -
+            cdiv(0.25 * ((u(i, k, j) + u(i, k + 1, j)) * (v(i, k, j + 1) + v(i, k, j)) -
+                         (u(i, k, j - 1) + u(i, k + 1, j - 1)) * (v(i, k, j) + v(i, k, j - 1))), P.ddx) -
+            cdiv(0.25 * ((w(i, k, j) + w(i, k + 1, j)) * (v(i, k, j) + v(i + 1, k, j)) -
+                         (w(i - 1, k, j) + w(i - 1, k + 1, j)) * (v(i - 1, k, j) + v(i, k, j))), P.ddz));
     }
     if (k >= 1 && j >= 1) {
         H(i, k, j) = w(i, k, j) + dt * (
-            (w(i, k, j + 1) - 2 * w(i, k, j) + w(i, k, j - 1)) / Re / dx2 +
-            (w(i, k + 1, j) - 2 * w(i, k, j) + w(i, k - 1, j)) / Re / dy2 +
-            (w(i + 1, k, j) - 2 * w(i, k, j) + w(i - 1, k, j)) / Re / dz2 -
-            (sq(0.5 * (w(i + 1, k, j) + w(i, k, j))) - sq(0.5 * (w(i - 1, k, j) + w(i, k, j)))) / dz -
-            0.25 * ((u(i + 1, k, j) + u(i, k, j)) * (w(i, k, j + 1) + w(i, k, j)) -
-                    (u(i + 1, k, j - 1) + u(i, k, j - 1)) * (w(i, k, j) + w(i, k, j - 1))) / dx -
-            0.25 * ((w(i, k, j) + w(i, k + 1, j)) * (v(i, k, j) + v(i + 1, k, j)) -
-                    (w(i, k - 1, j) + w(i, k, j)) * (v(i, k - 1, j) + v(i + 1, k - 1, j))) / dy);
+            dif(w(i, k, j + 1) - 2 * w(i, k, j) + w(i, k, j - 1), P.ddx2) +
+            dif(w(i, k + 1, j) - 2 * w(i, k, j) + w(i, k - 1, j), P.ddy2) +
+            dif(w(i + 1, k, j) - 2 * w(i, k, j) + w(i - 1, k, j), P.ddz2) -
+            cdiv(sq(0.5 * (w(i + 1, k, j) + w(i, k, j))) - sq(0.5 * (w(i - 1, k, j) + w(i, k, j))), P.ddz) -
+            cdiv(0.25 * ((u(i + 1, k, j) + u(i, k, j)) * (w(i, k, j + 1) + w(i, k, j)) -
+                         (u(i + 1, k, j - 1) + u(i, k, j - 1)) * (w(i, k, j) + w(i, k, j - 1))), P.ddx) -
+            cdiv(0.25 * ((w(i, k, j) + w(i, k + 1, j)) * (v(i, k, j) + v(i + 1, k, j)) -
+                         (w(i, k - 1, j) + w(i, k, j)) * (v(i, k - 1, j) + v(i + 1, k - 1, j))), P.ddy));
     }
 }
 
@@ -167,14 +193,14 @@ __global__ void k_ns_rhs(Field F, Field G, Field H, Field p, Field RHS, NSParams
     const int j = (int)(e % nx) + 1;
     const int k = (int)((e / nx) % ny) + 1;
     const int i = (int)(e / ((long long)nx * ny)) + 1;
-    double r = ((F(i, k, j) - F(i, k, j - 1)) / P.dx + (G(i, k, j) - G(i, k - 1, j)) / P.dy +
-                (H(i, k, j) - H(i - 1, k, j)) / P.dz) / P.dt;
-    if (i <= 1) r -= p(i - 1, k, j) / P.dz2;
-    if (k <= 1) r -= p(i, k - 1, j) / P.dy2;
-    if (j <= 1) r -= p(i, k, j - 1) / P.dx2;
-    if (j >= nx) r -= p(i, k, j + 1) / P.dx2;
-    if (k >= ny) r -= p(i, k + 1, j) / P.dy2;
-    if (i >= nz) r -= p(i + 1, k, j) / P.dz2;
+    double r = cdiv(cdiv(F(i, k, j) - F(i, k, j - 1), P.ddx) + cdiv(G(i, k, j) - G(i, k - 1, j), P.ddy) +
+                    cdiv(H(i, k, j) - H(i - 1, k, j), P.ddz), P.ddt);
+    if (i <= 1) r -= cdiv(p(i - 1, k, j), P.ddz2);
+    if (k <= 1) r -= cdiv(p(i, k - 1, j), P.ddy2);
+    if (j <= 1) r -= cdiv(p(i, k, j - 1), P.ddx2);
+    if (j >= nx) r -= cdiv(p(i, k, j + 1), P.ddx2);
+    if (k >= ny) r -= cdiv(p(i, k + 1, j), P.ddy2);
+    if (i >= nz) r -= cdiv(p(i + 1, k, j), P.ddz2);
     RHS(i, k, j) = r;
 }
 
@@ -188,10 +214,19 @@ __global__ void k_ns_update(Field u, Field v, Field w, Field p, Field x, Field F
     const int k = (int)((e / nx) % ny) + 1;
     const int i = (int)(e / ((long long)nx * ny)) + 1;
     const double xc = x(i, k, j);
-    if (j < nx) u(i, k, j) = F(i, k, j) - P.dt / P.dx * (x(i, k, j + 1) - xc);
-    if (k < ny) v(i, k, j) = G(i, k, j) - P.dt / P.dy * (x(i, k + 1, j) - xc);
-    if (i < nz) w(i, k, j) = H(i, k, j) - P.dt / P.dz * (x(i + 1, k, j) - xc);
+    if (j < nx) u(i, k, j) = F(i, k, j) - P.dt_dx * (x(i, k, j + 1) - xc);
+    if (k < ny) v(i, k, j) = G(i, k, j) - P.dt_dy * (x(i, k + 1, j) - xc);
+    if (i < nz) w(i, k, j) = H(i, k, j) - P.dt_dz * (x(i + 1, k, j) - xc);
     p(i, k, j) = xc;
+}
+
+// Diagnostic: IEEE a/b and the constant-divisor quotient side by side.
+__global__ void k_cdiv_check(const double* a, const double* b, double* q_ieee, double* q_c, long long n) {
+    const long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    const double bi = b[i];
+    q_ieee[i] = a[i] / bi;
+    q_c[i] = cdiv(a[i], CDiv{bi, 1.0 / bi});
 }
 
 struct NSPlan {
@@ -331,6 +366,11 @@ int fdmgpu_nscube_create(fdmgpu_nscube** h, int dtype, int nx, int nz, double x1
     s.P.U0 = u0; s.P.Re = Re; s.P.dt = dt;
     s.P.dx = (x2 - x1) / nx; s.P.dy = (y2 - y1) / s.P.ny; s.P.dz = (z2 - z1) / nz;
     s.P.dx2 = s.P.dx * s.P.dx; s.P.dy2 = s.P.dy * s.P.dy; s.P.dz2 = s.P.dz * s.P.dz;
+    s.P.dRe = cdiv_of(Re);
+    s.P.ddx = cdiv_of(s.P.dx); s.P.ddy = cdiv_of(s.P.dy); s.P.ddz = cdiv_of(s.P.dz);
+    s.P.ddx2 = cdiv_of(s.P.dx2); s.P.ddy2 = cdiv_of(s.P.dy2); s.P.ddz2 = cdiv_of(s.P.dz2);
+    s.P.ddt = cdiv_of(dt);
+    s.P.dt_dx = dt / s.P.dx; s.P.dt_dy = dt / s.P.dy; s.P.dt_dz = dt / s.P.dz;
     s.init();
     *h = p.release();
     FDM_API_END
@@ -341,6 +381,16 @@ int fdmgpu_nscube_step(fdmgpu_nscube* h, int k) {
     if (!h) FDM_FAIL(FDMGPU_EINVAL, "null handle");
     if (k < 0) FDM_FAIL(FDMGPU_EINVAL, "negative step count");
     h->plan.step(k);
+    FDM_API_END
+}
+
+int fdmgpu_check_const_division(long long n, const double* d_a, const double* d_b, double* d_q_ieee,
+                                double* d_q_const, void* stream) {
+    FDM_API_BEGIN
+    if (n < 0 || (n > 0 && (!d_a || !d_b || !d_q_ieee || !d_q_const))) FDM_FAIL(FDMGPU_EINVAL, "bad argument");
+    if (n == 0) return FDMGPU_OK;
+    k_cdiv_check<<<(unsigned)((n + 255) / 256), 256, 0, (cudaStream_t)stream>>>(d_a, d_b, d_q_ieee, d_q_const, n);
+    FDM_LAUNCH_CHECK();
     FDM_API_END
 }
 

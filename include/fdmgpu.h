@@ -226,6 +226,12 @@ int fdmgpu_nscube_set_field(fdmgpu_nscube* h, int field, const void* host, size_
 int fdmgpu_nscube_field_device(fdmgpu_nscube* h, int field, void** dptr);
 int fdmgpu_nscube_time_index(fdmgpu_nscube* h, int* t);
 int fdmgpu_nscube_destroy(fdmgpu_nscube* h);
+/* Diagnostic of the NSCube stencils' division by run constants (h, h^2, Re,
+ * dt): writes the IEEE quotient a/b and the library's constant-divisor
+ * quotient (precomputed reciprocal plus remainder corrections) for n device
+ * pairs, so a test can check they agree bit for bit. */
+int fdmgpu_check_const_division(long long n, const double* d_a, const double* d_b, double* d_q_ieee,
+                                double* d_q_const, void* stream);
 
 /* ---- Serving loop (no counterpart in the reference, which runs one
  * solve or one NSCube on the caller's thread) ------------------------------

@@ -91,3 +91,33 @@ def test_reference_field_layout(cuda):
 def test_bad_size(cuda):
     with pytest.raises(FdmError):
         make(64)
+
+
+def test_constant_division_matches_ieee(cuda):
+    """The stencils divide by run constants through a precomputed reciprocal
+    and two remainder corrections; on dividends and divisors spread over the
+    normal range (quotients normal too), zeros, the cavity's own constants
+    and divisors with all-ones significands it equals IEEE a/b bit for bit."""
+    import torch
+    from fdm_gb300 import _native as N
+    rng = np.random.default_rng(17)
+    n = 1 << 22
+    a = rng.uniform(1, 2, n) * np.exp2(rng.integers(-500, 500, n)) * rng.choice((-1, 1), n)
+    b = rng.uniform(1, 2, n) * np.exp2(rng.integers(-500, 500, n)) * rng.choice((-1, 1), n)
+    h = 2 * math.pi / 64
+    consts = np.array([100.0, 250.0, 400.0, 0.01, h, h * h, 2 * math.pi / 32, (2 * math.pi / 32) ** 2,
+                       np.nextafter(2.0, 0.0), np.nextafter(1.0, 0.0) * 2.0 ** 7, 3.0, 10.0])
+    b[: 1 << 20] = np.resize(consts, 1 << 20) * rng.choice((-1, 1), 1 << 20)
+    a[: 1 << 16] = rng.uniform(-1, 1, 1 << 16)
+    a[1 << 16: (1 << 16) + 64] = 0.0
+    a[(1 << 16) + 64: (1 << 16) + 128] = -0.0
+    a[(1 << 17): (1 << 17) + 4096] = np.exp2(rng.integers(-60, 60, 4096))  # powers of two
+    ta, tb = torch.tensor(a, device=cuda), torch.tensor(b, device=cuda)
+    q1, q2 = torch.empty_like(ta), torch.empty_like(ta)
+    N.check(N.load().fdmgpu_check_const_division(n, ta.data_ptr(), tb.data_ptr(), q1.data_ptr(), q2.data_ptr(),
+                                                 None))
+    torch.cuda.synchronize()
+    x, y = q1.cpu().numpy(), q2.cpu().numpy()
+    assert np.array_equal(x.view(np.int64), (a / b).view(np.int64))  # the device's IEEE division
+    bad = np.flatnonzero(x.view(np.int64) != y.view(np.int64))
+    assert bad.size == 0, (bad.size, a[bad[:4]], b[bad[:4]])
