@@ -250,6 +250,7 @@ def measure_uneven_batch(torch, fdm_gb300, workloads, stream, dev, count=512, to
         "rel_l2_vs_fp64_max": max(errs), "tune_s": tune_s,
         "chunks": sorted(set(g["chunk"] for g in sched)),
         "ztable_groups": sum(g["ztable"] for g in sched),
+        "tensor_core_dst_groups": sum(g["dst_tc"] for g in sched),
     }
 
 
@@ -289,9 +290,13 @@ def measure_serving(torch, fdm_gb300, workloads, dev, rates=SERVE_RATES, seconds
     def out_buf(sh):
         return free[sh].pop() if free[sh] else torch.empty_like(rhs[sh]).pin_memory()
 
+    ref_sq = {sh: float(np.sum(np.square(r))) for sh, r in ref.items()}
+
     def check(sh, buf):
-        a = buf.numpy()
-        return sh, buf, float(np.linalg.norm(a - ref[sh]) / np.linalg.norm(ref[sh]))
+        # numpy's own reductions: BLAS-backed norms are not safe to call from
+        # several threads of this pool at once
+        d = buf.numpy() - ref[sh]
+        return sh, buf, math.sqrt(float(np.sum(d * d)) / ref_sq[sh])
 
     srv = Server(150e9, lanes=lanes, max_batch=max_batch)
     sess = [srv.session_create(63, 63, Re=(100.0, 250.0, 400.0)[i % 3], dt=0.01) for i in range(64)]
@@ -394,10 +399,23 @@ def run_ncu_case(which: str = "solve"):
     """solve: two mixed solves of 2 RHS at 255^3 (266 MB of FP64 input,
     larger than L2) with nothing else on the GPU.  nscube: a 63^3 cavity,
     Re 250, dt 0.01, stepped 4 times (the first eager, then one captured
-    graph replayed).  The cases the committed ncu summaries capture."""
+    graph replayed).  tc: two mixed solves of 16 RHS at 63^3 (32 MB of FP64
+    input per RHS, 512 MB in all) with the tensor-core DST passes.  The
+    cases the committed ncu summaries capture."""
     import torch
     import fdm_gb300
     from fdm_gb300 import workloads
+    if which == "tc":
+        n = 63
+        f = torch.stack([workloads.manufactured_torch(n, n, n, seed=s, kmax=16, noise=NOISE)[0] for s in range(16)])
+        out = torch.empty_like(f)
+        m = fdm_gb300.LaplCube(*workloads.solver_args(n, n, n), precision="mixed", tol=TOL)
+        m.set_schedule(ztable=True, dst_tc=True)
+        for _ in range(2):
+            m.solve_device(out, f, nrhs=16)
+        torch.cuda.synchronize()
+        print("ncu case done")
+        return
     if which == "nscube":
         ns = fdm_gb300.NSCube(nx=63, nz=63, Re=250.0, dt=0.01, u0=1.0)
         ns.step(4)
@@ -423,9 +441,12 @@ def main():
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-serving", action="store_true", help="skip the serving-loop sweep")
-    ap.add_argument("--ncu-case", nargs="?", const="solve", default=None, choices=["solve", "nscube"],
+    ap.add_argument("--serve-rates", default=None,
+                    help="comma-separated arrival rates (req/s) of the serving sweep (default 100,300,1000,3000,5000)")
+    ap.add_argument("--ncu-case", nargs="?", const="solve", default=None, choices=["solve", "nscube", "tc"],
                     help="run only a small case for profiler captures: 'solve' (two mixed solves of 2 RHS at "
-                         "255^3) or 'nscube' (four 63^3 cavity steps)")
+                         "255^3), 'nscube' (four 63^3 cavity steps) or 'tc' (two mixed solves of 16 RHS at 63^3 "
+                         "with the tensor-core DST passes)")
     ap.add_argument("--chunk", type=int, default=NRHS,
                     help="right-hand sides per solve call within a step (divides 16)")
     args = ap.parse_args()
@@ -558,7 +579,8 @@ def main():
     del out, f
     torch.cuda.empty_cache()
     uneven = measure_uneven_batch(torch, fdm_gb300, workloads, stream, dev)
-    serving = measure_serving(torch, fdm_gb300, workloads, dev) if not args.no_serving else None
+    rates = tuple(int(x) for x in args.serve_rates.split(",")) if args.serve_rates else SERVE_RATES
+    serving = measure_serving(torch, fdm_gb300, workloads, dev, rates=rates) if not args.no_serving else None
 
     solves = args.steps * NRHS * world
     value = solves / (ms * 1e-3)

@@ -67,6 +67,8 @@ _SIGS = [
      [c_double] * 6 + [c_int] * 3 + [c_double, c_void_p, c_void_p, c_int, c_void_p]),
     ("fdmgpu_lapl_cube_last_info", c_int, [c_void_p, POINTER(c_int), POINTER(c_double), c_int]),
     ("fdmgpu_lapl_cube_scratch_bytes", c_int, [c_void_p, POINTER(c_size_t)]),
+    ("fdmgpu_lapl_cube_set_schedule", c_int, [c_void_p, c_int, c_int]),
+    ("fdmgpu_lapl_cube_device_status", c_int, [c_void_p, POINTER(c_int)]),
     ("fdmgpu_lapl_cube_destroy", c_int, [c_void_p]),
     ("fdmgpu_batch_create", c_int,
      [POINTER(c_void_p), c_int, POINTER(c_int), POINTER(c_double), POINTER(c_double), c_int, c_double]),
@@ -74,7 +76,8 @@ _SIGS = [
     ("fdmgpu_batch_solve", c_int, [c_void_p, POINTER(c_void_p), POINTER(c_void_p), c_void_p]),
     ("fdmgpu_batch_info", c_int, [c_void_p, POINTER(c_int), POINTER(c_int)]),
     ("fdmgpu_batch_schedule", c_int,
-     [c_void_p, c_int, POINTER(c_int), POINTER(c_int), POINTER(c_int), POINTER(c_int), POINTER(c_double)]),
+     [c_void_p, c_int, POINTER(c_int), POINTER(c_int), POINTER(c_int), POINTER(c_int), POINTER(c_int),
+      POINTER(c_double)]),
     ("fdmgpu_batch_destroy", c_int, [c_void_p]),
     ("fdmgpu_lapl_rect_create", c_int,
      [POINTER(c_void_p), c_int, c_int] + [c_double] * 4 + [c_int] * 2),
@@ -82,6 +85,7 @@ _SIGS = [
     ("fdmgpu_lapl_rect_solve_device", c_int, [c_void_p, c_void_p, c_void_p, c_int, c_void_p]),
     ("fdmgpu_lapl_rect_destroy", c_int, [c_void_p]),
     ("fdmgpu_sine_device", c_int, [c_int, c_int, c_int, c_double, c_void_p, c_void_p, c_void_p]),
+    ("fdmgpu_sine_tc_device", c_int, [c_int, c_int, c_int, c_longlong, c_double, c_void_p, c_void_p, c_void_p]),
     ("fdmgpu_tridiag_device", c_int, [c_int, c_int, c_int, c_void_p, c_void_p, c_void_p, c_void_p, c_void_p]),
     ("fdmgpu_nscube_create", c_int,
      [POINTER(c_void_p), c_int, c_int, c_int] + [c_double] * 9),

@@ -23,6 +23,7 @@
 #include "poisson.h"
 #include "sine.cuh"
 #include "sine_rg.cuh"
+#include "sine_tc.cuh"
 #include "solve_kernels.cuh"
 
 namespace fdmgpu {
@@ -120,6 +121,78 @@ static void launch_rg(const Tin* in, Tout* out, int nx, int ny, int nz, int nvol
     FDM_TIMED((sine_name<Tin, T, Tout, AXIS, MODE>()), st);
     k_sine_rg<Tin, T, Tout, AXIS, MODE, N><<<grid, 256, smem, st>>>(in, out, geo, tb, (T)scale, fu);
     FDM_LAUNCH_CHECK();
+}
+
+// ---------------------------------------------------------------------------
+// Tensor-core DST (N = 32, 64): the pre-swizzled TF32 high / low image of
+// the zero-padded sine matrix, and the launcher
+// ---------------------------------------------------------------------------
+static std::vector<float> tc_sine_image(int N) {
+    const int n = N - 1;
+    std::vector<float> img((size_t)2 * N * N, 0.f);
+    float* hi = img.data();
+    float* lo = img.data() + (size_t)N * N;
+    for (int r = 0; r < n; r++)
+        for (int k = 0; k < n; k++) {
+            // sin(pi m / N) with m = (r+1)(k+1) reduced mod 2N
+            const int m = ((r + 1) * (k + 1)) % (2 * N);
+            const double v = std::sin(M_PI * (double)m / (double)N);
+            const float h = tc_tf32((float)v);
+            const uint32_t o = tc_sw128(N, r, k) / 4;
+            hi[o] = h;
+            lo[o] = tc_tf32((float)(v - (double)h));
+        }
+    return img;
+}
+
+static bool tc_supported(int N) { return N == 32 || N == 64; }
+
+template <int N, int AXIS>
+static void launch_tc_n(const float* in, float* out, const SineTcGeom& g, const float* img, float scale, int* err,
+                        cudaStream_t st) {
+    using C = TcCfg<N>;
+    static int grid_cap = 0;
+    if (!grid_cap) {
+        FDM_CUDA(cudaFuncSetAttribute(k_sine_tc<N, AXIS>, cudaFuncAttributeMaxDynamicSharedMemorySize, C::kSmem));
+        FDM_CUDA(cudaFuncSetAttribute(k_sine_tc<N, AXIS>, cudaFuncAttributePreferredSharedMemoryCarveout, 100));
+        // resident CTAs per SM from the kernel's own registers and shared
+        // memory, and tensor memory (512 columns per SM across CTAs)
+        int dev = 0, sms = 0, smem_sm = 0, regs_sm = 0;
+        FDM_CUDA(cudaGetDevice(&dev));
+        FDM_CUDA(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
+        FDM_CUDA(cudaDeviceGetAttribute(&smem_sm, cudaDevAttrMaxSharedMemoryPerMultiprocessor, dev));
+        FDM_CUDA(cudaDeviceGetAttribute(&regs_sm, cudaDevAttrMaxRegistersPerMultiprocessor, dev));
+        cudaFuncAttributes fa;
+        FDM_CUDA(cudaFuncGetAttributes(&fa, k_sine_tc<N, AXIS>));
+        const int smem_cta = C::kSmem + (int)fa.sharedSizeBytes + 1024;  // + the per-CTA reservation
+        const int regs_cta = ((fa.numRegs + 7) / 8 * 8) * kTcThreads;
+        int per_sm = std::min(smem_sm / smem_cta, regs_sm / std::max(regs_cta, 1));
+        per_sm = std::max(1, std::min(per_sm, 512 / N));
+        grid_cap = per_sm * sms;
+    }
+    // as many CTAs as the tiles need in the fewest rounds, spread evenly
+    const long long tiles = (g.lines + C::M - 1) / C::M;
+    const long long rounds = (tiles + grid_cap - 1) / grid_cap;
+    const unsigned grid = (unsigned)((tiles + rounds - 1) / std::max<long long>(rounds, 1));
+    if (grid == 0) return;
+    FDM_TIMED(AXIS == 0 ? "sine_x_tc" : "sine_y_tc", st);
+    k_sine_tc<N, AXIS><<<grid, kTcThreads, C::kSmem, st>>>(in, out, g, img, scale, err);
+    FDM_LAUNCH_CHECK();
+}
+
+// DST of lines of N-1 FP32 values on the tensor cores.  AXIS 0: `lines`
+// contiguous lines; AXIS 1: lines along y of planes of (N-1) x nx values,
+// `lines` = planes * nx.
+template <int AXIS>
+static void launch_sine_tc(int N, const float* in, float* out, long long lines, int nx, const float* img,
+                           double scale, int* err, cudaStream_t st) {
+    SineTcGeom g;
+    g.lines = lines;
+    g.nx = AXIS == 0 ? N - 1 : nx;
+    g.plane = (long long)nx * (N - 1);
+    if (N == 32) return launch_tc_n<32, AXIS>(in, out, g, img, (float)scale, err, st);
+    if (N == 64) return launch_tc_n<64, AXIS>(in, out, g, img, (float)scale, err, st);
+    FDM_FAIL(FDMGPU_ESIZE, "tensor-core DST supports N = 32, 64 (got %d)", N);
 }
 
 template <typename Tin, typename T, typename Tout, int AXIS, int MODE = kPlain>
@@ -314,6 +387,8 @@ struct CubePlan {
     DevBuf work32, uhi, ulo, norms, work64;
     DevBuf ztab64, ztab32;  // partitioned z-solve factors per mode
     int zmode = 1;          // 1: table-driven z-solve when the line splits, 0: factors computed per solve
+    int dst_tc = 0;         // 1: plain FP32 DST passes of 32- or 64-point axes on the tensor cores
+    DevBuf tc_img_x, tc_img_y, tc_err;
     int zm64 = 0, zP64 = 0, zm32 = 0, zP32 = 0;
     DevBuf hin, hout;
     int last_sweeps = 0, last_nrhs = 0;
@@ -411,6 +486,29 @@ struct CubePlan {
 
     long long vol() const { return (long long)nx * ny * nz; }
 
+    // plain FP32 DST pass along AXIS, on the tensor cores when enabled and
+    // the axis has 32 or 64 points
+    template <int AXIS>
+    void sine32(const float* in, float* out, int nrhs, double scale, cudaStream_t st) {
+        const int N = (AXIS == 0 ? nx : ny) + 1;
+        if (dst_tc && tc_supported(N)) {
+            DevBuf& img = AXIS == 0 ? tc_img_x : tc_img_y;
+            if (!img.p) {
+                std::vector<float> h = tc_sine_image(N);
+                img.get(h.size() * sizeof(float));
+                FDM_CUDA(cudaMemcpy(img.p, h.data(), h.size() * sizeof(float), cudaMemcpyHostToDevice));
+            }
+            if (!tc_err.p) {
+                tc_err.get(sizeof(int));
+                FDM_CUDA(cudaMemset(tc_err.p, 0, sizeof(int)));
+            }
+            const long long lines = (long long)nrhs * nz * (AXIS == 0 ? ny : nx);
+            launch_sine_tc<AXIS>(N, in, out, lines, nx, (const float*)img.p, scale, (int*)tc_err.p, st);
+            return;
+        }
+        launch_sine<float, float, float, AXIS>(in, out, nx, ny, nz, nrhs, (AXIS == 0 ? tx32 : ty32).view(), scale, st);
+    }
+
     template <typename Tin, typename T, int MODE = kPlain>
     void forward_xy(const Tin* in, T* W, int nrhs, const AxisTables<T>& tx, const AxisTables<T>& ty,
                     cudaStream_t st, const SineFused* fu = nullptr) {
@@ -482,9 +580,9 @@ struct CubePlan {
         memset(&fin, 0, sizeof(fin));
         fin.vin = vin;
         launch_sine<double, float, float, 0, kRound>(rhs, W, nx, ny, nz, nrhs, tx32.view(), scx, st, &fin);
-        launch_sine<float, float, float, 1>(W, W, nx, ny, nz, nrhs, ty32.view(), scy, st);
+        sine32<1>(W, W, nrhs, scy, st);
         zsolve<float>(W, nrhs, lamx32, lamy32, st);
-        launch_sine<float, float, float, 1>(W, W, nx, ny, nz, nrhs, ty32.view(), sly, st);
+        sine32<1>(W, W, nrhs, sly, st);
         if (sweeps == 0) {
             SineFused fo;
             memset(&fo, 0, sizeof(fo));
@@ -496,7 +594,7 @@ struct CubePlan {
         float* UL = sweeps > 1 ? (float*)ulo.get(V * sizeof(float)) : nullptr;
         double* NR = (double*)norms.get((size_t)2 * nrhs * sweeps * sizeof(double));
         FDM_CUDA(cudaMemsetAsync(NR, 0, (size_t)2 * nrhs * sweeps * sizeof(double), st));
-        launch_sine<float, float, float, 0>(W, UH, nx, ny, nz, nrhs, tx32.view(), slx, st);
+        sine32<0>(W, UH, nrhs, slx, st);
         // r = f - A u / S: the inner solve multiplies by S again, so it
         // returns the correction S A^-1 f - u
         const double cx = 1.0 / (hx_eff * hx_eff) / S, cy = 1.0 / (dy * dy) / S, cz = 1.0 / (hz_eff * hz_eff) / S;
@@ -511,9 +609,10 @@ struct CubePlan {
             fr.cxf = (float)cx; fr.cyf = (float)cy; fr.czf = (float)cz;
             fr.iso = (cx == cy && cy == cz) ? 1 : 0;
             launch_residual(fr, W, nx, ny, nz, nrhs, st);
-            forward_xy<float, float>(W, W, nrhs, tx32, ty32, st);
+            sine32<0>(W, W, nrhs, scx, st);
+            sine32<1>(W, W, nrhs, scy, st);
             zsolve<float>(W, nrhs, lamx32, lamy32, st);
-            launch_sine<float, float, float, 1>(W, W, nx, ny, nz, nrhs, ty32.view(), sly, st);
+            sine32<1>(W, W, nrhs, sly, st);
             SineFused fc;
             memset(&fc, 0, sizeof(fc));
             fc.uhi = UH;
@@ -774,6 +873,12 @@ struct BatchPlan {
     }
 
     // time each schedule candidate of every group on its data; keep the best
+    // that keeps the tolerance.  Candidates: right-hand sides per launch
+    // sequence x z-solve variant (factor table / per-solve factors) x DST
+    // passes (FFT / tensor cores, for 32- and 64-point axes).  A variant is
+    // accurate enough when its first-sweep correction estimate e (the FP32
+    // solve's relative error) predicts 10 e^(sweeps+1) <= tol; with no sweep
+    // only the default variants qualify.
     void tune() {
         cudaEvent_t a, b;
         FDM_CUDA(cudaEventCreate(&a));
@@ -781,42 +886,46 @@ struct BatchPlan {
         for (auto& gr : groups) {
             const int m = (int)gr.members.size();
             int chunks[4] = {m, 8, 2, 1};
-            double best = 1e30, est_table = 0.0;
-            int bc = m, bz = 1;
+            double best = 1e30;
+            int bc = m, bz = 1, bt = 0;
             const bool mixed = precision == FDMGPU_MIXED;
-            for (int zm = 1; zm >= 0; zm--) {
-                // the per-solve FP32 z factors are less accurate than the
-                // table's (built in FP64): without a refinement sweep to
-                // absorb that they are not a candidate
-                if (zm == 0 && mixed && gr.plan->sweeps_for_tol() == 0) continue;
-                for (int ci = 0; ci < 4; ci++) {
-                    const int ch = chunks[ci];
-                    if (ch > m || (ci > 0 && ch == chunks[ci - 1])) continue;
-                    gr.chunk = ch;
-                    gr.zmode = zm;
-                    enqueue_group(gr, gr.st);  // warm-up: allocates scratch and tables
-                    FDM_CUDA(cudaEventRecord(a, gr.st));
-                    enqueue_group(gr, gr.st);
-                    FDM_CUDA(cudaEventRecord(b, gr.st));
-                    FDM_CUDA(cudaEventSynchronize(b));
-                    float ms = 0.f;
-                    FDM_CUDA(cudaEventElapsedTime(&ms, a, b));
-                    if (mixed && ci == 0) {
-                        // whole group in one launch sequence: the norms
-                        // cover every member
-                        const double e = gr.plan->first_sweep_est(m, gr.st);
-                        if (zm == 1) est_table = e;
-                        else if (e > 2.0 * est_table) break;  // less accurate: keep the table variant
-                    }
-                    if (ms < best) {
-                        best = ms;
-                        bc = ch;
-                        bz = zm;
+            const int sweeps = mixed ? gr.plan->sweeps_for_tol() : -1;
+            const bool tc_ok = mixed && (tc_supported(gr.nx + 1) || tc_supported(gr.ny + 1));
+            for (int tc = 0; tc <= (tc_ok ? 1 : 0); tc++) {
+                for (int zm = 1; zm >= 0; zm--) {
+                    const bool is_default = zm == 1 && tc == 0;
+                    if (!is_default && mixed && sweeps == 0) continue;
+                    for (int ci = 0; ci < 4; ci++) {
+                        const int ch = chunks[ci];
+                        if (ch > m || (ci > 0 && ch == chunks[ci - 1])) continue;
+                        gr.chunk = ch;
+                        gr.zmode = zm;
+                        gr.plan->dst_tc = tc;
+                        enqueue_group(gr, gr.st);  // warm-up: allocates scratch and tables
+                        FDM_CUDA(cudaEventRecord(a, gr.st));
+                        enqueue_group(gr, gr.st);
+                        FDM_CUDA(cudaEventRecord(b, gr.st));
+                        FDM_CUDA(cudaEventSynchronize(b));
+                        float ms = 0.f;
+                        FDM_CUDA(cudaEventElapsedTime(&ms, a, b));
+                        if (!is_default && mixed && ci == 0) {
+                            // whole group in one launch sequence: the norms
+                            // cover every member
+                            const double e = gr.plan->first_sweep_est(m, gr.st);
+                            if (10.0 * std::pow(e, sweeps + 1) > tol) break;
+                        }
+                        if (ms < best) {
+                            best = ms;
+                            bc = ch;
+                            bz = zm;
+                            bt = tc;
+                        }
                     }
                 }
             }
             gr.chunk = bc;
             gr.zmode = bz;
+            gr.plan->dst_tc = bt;
             gr.tuned_ms = best;
             enqueue_group(gr, gr.st);  // scratch for the chosen schedule exists before capture
         }
@@ -1197,7 +1306,8 @@ int fdmgpu_batch_info(fdmgpu_batch* h, int* groups, int* launches_per_solve) {
     FDM_API_END
 }
 
-int fdmgpu_batch_schedule(fdmgpu_batch* h, int group, int* n3, int* members, int* chunk, int* ztable, double* tuned_ms) {
+int fdmgpu_batch_schedule(fdmgpu_batch* h, int group, int* n3, int* members, int* chunk, int* ztable, int* dst_tc,
+                          double* tuned_ms) {
     FDM_API_BEGIN
     if (!h || group < 0 || group >= (int)h->plan.groups.size()) FDM_FAIL(FDMGPU_EINVAL, "bad handle or group");
     const BatchGroup& gr = h->plan.groups[group];
@@ -1205,6 +1315,7 @@ int fdmgpu_batch_schedule(fdmgpu_batch* h, int group, int* n3, int* members, int
     if (members) *members = (int)gr.members.size();
     if (chunk) *chunk = gr.chunk;
     if (ztable) *ztable = gr.zmode;
+    if (dst_tc) *dst_tc = gr.plan->dst_tc;
     if (tuned_ms) *tuned_ms = gr.tuned_ms;
     FDM_API_END
 }
@@ -1299,6 +1410,53 @@ int fdmgpu_sine_device(int dtype, int N, int nlines, double scale, void* d_out, 
         FDM_CUDA(cudaStreamSynchronize(st));
     } else {
         FDM_FAIL(FDMGPU_EINVAL, "bad dtype %d", dtype);
+    }
+    FDM_API_END
+}
+
+int fdmgpu_sine_tc_device(int N, int axis, int nx, long long count, double scale, void* d_out, const void* d_in,
+                          void* stream) {
+    FDM_API_BEGIN
+    if (!d_out || !d_in) FDM_FAIL(FDMGPU_EINVAL, "null argument");
+    if (!tc_supported(N)) FDM_FAIL(FDMGPU_ESIZE, "tensor-core DST supports N = 32, 64 (got %d)", N);
+    if (count < 1 || (axis != 0 && axis != 1) || (axis == 1 && nx < 1))
+        FDM_FAIL(FDMGPU_EINVAL, "bad axis, nx or count");
+    cudaStream_t st = (cudaStream_t)stream;
+    std::vector<float> h = tc_sine_image(N);
+    DevBuf img, err;
+    img.get(h.size() * sizeof(float));
+    err.get(sizeof(int));
+    FDM_CUDA(cudaMemcpy(img.p, h.data(), h.size() * sizeof(float), cudaMemcpyHostToDevice));
+    FDM_CUDA(cudaMemset(err.p, 0, sizeof(int)));
+    if (axis == 0)
+        launch_sine_tc<0>(N, (const float*)d_in, (float*)d_out, count, N - 1, (const float*)img.p, scale,
+                          (int*)err.p, st);
+    else
+        launch_sine_tc<1>(N, (const float*)d_in, (float*)d_out, count * nx, nx, (const float*)img.p, scale,
+                          (int*)err.p, st);
+    FDM_CUDA(cudaStreamSynchronize(st));
+    int failed = 0;
+    FDM_CUDA(cudaMemcpy(&failed, err.p, sizeof(int), cudaMemcpyDeviceToHost));
+    if (failed) FDM_FAIL(FDMGPU_ETIMEOUT, "tensor-core DST: the wait for the MMAs gave up");
+    FDM_API_END
+}
+
+int fdmgpu_lapl_cube_set_schedule(fdmgpu_lapl_cube* h, int ztable, int dst_tc) {
+    FDM_API_BEGIN
+    if (!h) FDM_FAIL(FDMGPU_EINVAL, "null handle");
+    if ((ztable != 0 && ztable != 1) || (dst_tc != 0 && dst_tc != 1)) FDM_FAIL(FDMGPU_EINVAL, "flags must be 0 or 1");
+    h->plan.zmode = ztable;
+    h->plan.dst_tc = dst_tc;
+    FDM_API_END
+}
+
+int fdmgpu_lapl_cube_device_status(fdmgpu_lapl_cube* h, int* failed) {
+    FDM_API_BEGIN
+    if (!h || !failed) FDM_FAIL(FDMGPU_EINVAL, "null argument");
+    *failed = 0;
+    if (h->plan.tc_err.p) {
+        FDM_CUDA(cudaDeviceSynchronize());
+        FDM_CUDA(cudaMemcpy(failed, h->plan.tc_err.p, sizeof(int), cudaMemcpyDeviceToHost));
     }
     FDM_API_END
 }

@@ -113,6 +113,19 @@ class LaplCube:
                                                         _dev_ptr(rhs, eb, self.count * nrhs), int(nrhs),
                                                         _stream_ptr(stream)))
 
+    def set_schedule(self, ztable: bool = True, dst_tc: bool = False) -> None:
+        """Mixed-form schedule: per-mode z factor table (default) or factors
+        per solve; plain FP32 DST passes of 32/64-point axes on the tensor
+        cores (dst_tc) or as FFTs (default)."""
+        N.check(self._lib.fdmgpu_lapl_cube_set_schedule(self._h, int(bool(ztable)), int(bool(dst_tc))))
+
+    def device_failed(self) -> bool:
+        """True if a tensor-core pass of this solver gave up waiting for its
+        MMAs (synchronises the device)."""
+        f = c_int()
+        N.check(self._lib.fdmgpu_lapl_cube_device_status(self._h, byref(f)))
+        return bool(f.value)
+
     def last_info(self, nrhs: int = 1):
         """(sweeps, [relative size of the last correction per RHS])."""
         s = c_int()
@@ -196,14 +209,16 @@ class BatchSolver:
         return g.value, l.value
 
     def schedule(self):
-        """Per group: dict(shape, members, chunk, ztable, tuned_ms)."""
+        """Per group: dict(shape, members, chunk, ztable, dst_tc, tuned_ms)."""
         out = []
         for k in range(self.info()[0]):
             n3 = (c_int * 3)()
-            m, ch, zt = c_int(), c_int(), c_int()
+            m, ch, zt, tc = c_int(), c_int(), c_int(), c_int()
             ms = c_double()
-            N.check(self._lib.fdmgpu_batch_schedule(self._h, k, n3, byref(m), byref(ch), byref(zt), byref(ms)))
-            out.append(dict(shape=tuple(n3), members=m.value, chunk=ch.value, ztable=zt.value, tuned_ms=ms.value))
+            N.check(self._lib.fdmgpu_batch_schedule(self._h, k, n3, byref(m), byref(ch), byref(zt), byref(tc),
+                                                    byref(ms)))
+            out.append(dict(shape=tuple(n3), members=m.value, chunk=ch.value, ztable=zt.value, dst_tc=tc.value,
+                            tuned_ms=ms.value))
         return out
 
     def close(self) -> None:
@@ -275,6 +290,17 @@ def sine_transform_device(out, inp, N_points: int, nlines: int, scale: float = 1
     cnt = (N_points - 1) * nlines
     N.check(lib.fdmgpu_sine_device(_dtype_code(dtype), int(N_points), int(nlines), float(scale),
                                    _dev_ptr(out, eb, cnt), _dev_ptr(inp, eb, cnt), _stream_ptr(stream)))
+
+
+def sine_transform_tc_device(out, inp, N_points: int, count: int, scale: float = 1.0, axis: int = 0, nx: int = 1,
+                             stream=None) -> None:
+    """FP32 DST-I on the tensor cores (N_points = 32 or 64).  axis 0: `count`
+    contiguous lines of N-1 values; axis 1: `count` planes of (N-1) x nx
+    values transformed along their rows (stride nx).  Synchronous."""
+    lib = N.load()
+    cnt = (N_points - 1) * count * (nx if axis == 1 else 1)
+    N.check(lib.fdmgpu_sine_tc_device(int(N_points), int(axis), int(nx), int(count), float(scale),
+                                      _dev_ptr(out, 4, cnt), _dev_ptr(inp, 4, cnt), _stream_ptr(stream)))
 
 
 def tridiag_device(lower, diag, upper, b, n: int, nsys: int, dtype=np.float64, stream=None) -> None:

@@ -139,6 +139,13 @@ int fdmgpu_lapl_cube_solve_mixed_noalloc(double dx, double dy, double dz, double
 int fdmgpu_lapl_cube_last_info(fdmgpu_lapl_cube* h, int* sweeps, double* est, int nrhs);
 /* bytes of device scratch the handle holds */
 int fdmgpu_lapl_cube_scratch_bytes(fdmgpu_lapl_cube* h, size_t* bytes);
+/* schedule of the mixed form: ztable = 1 uses the per-mode z factor table
+ * (default), 0 computes the factors per solve; dst_tc = 1 runs the plain
+ * FP32 DST passes of 32- and 64-point axes on the tensor cores (default 0) */
+int fdmgpu_lapl_cube_set_schedule(fdmgpu_lapl_cube* h, int ztable, int dst_tc);
+/* 1 in *failed if a tensor-core pass of this handle gave up waiting for its
+ * MMAs (synchronises the device) */
+int fdmgpu_lapl_cube_device_status(fdmgpu_lapl_cube* h, int* failed);
 int fdmgpu_lapl_cube_destroy(fdmgpu_lapl_cube* h);
 
 /* ---- Batched solves of uneven sizes (no counterpart in the reference,
@@ -162,9 +169,10 @@ int fdmgpu_batch_solve(fdmgpu_batch* h, void* const* d_ans, const void* const* d
 /* groups formed and kernel launches one graph launch replays */
 int fdmgpu_batch_info(fdmgpu_batch* h, int* groups, int* launches_per_solve);
 /* schedule of one group: sizes, members, chunk, 1 = table-driven z-solve,
- * and its tuned time in ms (0 before tuning) */
+ * 1 = DST passes on the tensor cores, and its tuned time in ms (0 before
+ * tuning) */
 int fdmgpu_batch_schedule(fdmgpu_batch* h, int group, int* n3, int* members, int* chunk, int* ztable,
-                          double* tuned_ms);
+                          int* dst_tc, double* tuned_ms);
 int fdmgpu_batch_destroy(fdmgpu_batch* h);
 
 /* ---- LaplRect / LaplRectFFT2: 2-D Dirichlet Poisson ----------------------
@@ -195,6 +203,14 @@ int fdmgpu_lapl_rect_destroy(fdmgpu_lapl_rect* h);
  * src/cyclic_reduction.h:20-107, src/asp_gauss.cpp:185-207). */
 int fdmgpu_sine_device(int dtype, int N, int nlines, double scale,
                        void* d_out, const void* d_in, void* stream);
+/* DST-I of FP32 lines of N-1 points (N = 32 or 64) as a dense contraction
+ * with the sine matrix on the tensor cores (split TF32, FP32 accumulation;
+ * no counterpart in the reference).  axis 0: `count` contiguous lines;
+ * axis 1: `count` planes of (N-1) rows x nx, transformed along the rows.
+ * Synchronous; FDMGPU_ETIMEOUT if the kernel's bounded wait for its MMAs
+ * gave up. */
+int fdmgpu_sine_tc_device(int N, int axis, int nx, long long count, double scale, void* d_out,
+                          const void* d_in, void* stream);
 int fdmgpu_tridiag_device(int dtype, int n, int nsys, const void* d_lower, const void* d_diag,
                           const void* d_upper, void* d_b, void* stream);
 

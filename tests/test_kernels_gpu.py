@@ -91,3 +91,46 @@ def test_rect_formulations_agree_511(cuda):
     LaplRect(h, h, 1.0, 1.0, n, n).solve(a, rhs)
     LaplRectFFT2(h, h, 1.0, 1.0, n, n).solve(b, rhs)
     assert np.abs(a - b).max() <= 1e-14 * max(1.0, np.abs(a).max())
+
+
+def _dst_matrix(N):
+    j = np.arange(1, N)
+    return np.sin(np.pi * np.outer(j, j) / N)
+
+
+@pytest.mark.parametrize("N", [32, 64])
+def test_sine_tc_lines_vs_fp64(cuda, N):
+    """Tensor-core DST (split TF32, FP32 accumulation) of contiguous lines,
+    including a ragged last tile, against the FP64 matrix product."""
+    import torch
+    from fdm_gb300 import sine_transform_tc_device
+    rng = np.random.default_rng(N + 1)
+    nl = 1000  # 7 full tiles of 128 lines and a ragged one
+    x = rng.uniform(-1, 1, (nl, N - 1)).astype(np.float32)
+    ref = 0.37 * x.astype(np.float64) @ _dst_matrix(N)
+    tx = torch.tensor(x, device=cuda)
+    ty = torch.full_like(tx, np.nan)
+    sine_transform_tc_device(ty, tx, N, nl, 0.37)
+    y = ty.cpu().numpy().astype(np.float64)
+    assert np.isfinite(y).all()
+    assert np.linalg.norm(y - ref) / np.linalg.norm(ref) <= 2e-6
+    assert np.abs(y - ref).max() <= 5e-6 * np.abs(ref).max()
+    # in place, as the solver uses it
+    sine_transform_tc_device(tx, tx, N, nl, 0.37)
+    assert torch.equal(tx, torch.tensor(y.astype(np.float32), device=cuda))
+
+
+@pytest.mark.parametrize("N,nx", [(32, 37), (64, 63)])
+def test_sine_tc_columns_vs_fp64(cuda, N, nx):
+    """Along y: planes of (N-1) x nx, transformed along the stride-nx rows."""
+    import torch
+    from fdm_gb300 import sine_transform_tc_device
+    rng = np.random.default_rng(N * nx)
+    planes = 9
+    x = rng.uniform(-1, 1, (planes, N - 1, nx)).astype(np.float32)
+    ref = np.einsum("jk,pjx->pkx", _dst_matrix(N), x.astype(np.float64)) * 1.5
+    tx = torch.tensor(x, device=cuda)
+    ty = torch.empty_like(tx)
+    sine_transform_tc_device(ty, tx, N, planes, 1.5, axis=1, nx=nx)
+    y = ty.cpu().numpy().astype(np.float64)
+    assert np.linalg.norm(y - ref) / np.linalg.norm(ref) <= 2e-6

@@ -200,3 +200,25 @@ def test_errors_like_reference(cuda):
     lc = LaplCube(*workloads.solver_args(7, 7, 7))
     with pytest.raises(FdmError):
         lc.solve(np.zeros(10), np.zeros(343))
+
+
+@pytest.mark.parametrize("shape", [(31, 31, 31), (63, 63, 63), (31, 63, 127), (63, 127, 31), (127, 31, 63)])
+def test_mixed_tensor_core_dst_vs_plain(cuda, shape):
+    """The mixed form with its 32-/64-point DST passes on the tensor cores
+    meets the same tolerance against the FP64 form, and the table / per-solve
+    z variants agree with it."""
+    import torch
+    nx, ny, nz = shape
+    f, _ = workloads.manufactured_torch(nx, ny, nz, seed=7, kmax=min(shape) // 4, noise=1e-3)
+    args = workloads.solver_args(nx, ny, nz)
+    plain = LaplCube(*args)
+    a = torch.empty_like(f)
+    plain.solve_device(a, f)
+    for tol in (1e-10, 1e-8):
+        m = LaplCube(*args, precision="mixed", tol=tol)
+        m.set_schedule(ztable=True, dst_tc=True)
+        b = torch.empty_like(f)
+        m.solve_device(b, f)
+        assert not m.device_failed()
+        err = (torch.linalg.norm(b - a) / torch.linalg.norm(a)).item()
+        assert err <= tol, (shape, tol, err)
