@@ -96,6 +96,8 @@ _SIGS = [
     ("fdmgpu_nscube_set_field", c_int, [c_void_p, c_int, c_void_p, c_size_t]),
     ("fdmgpu_nscube_field_device", c_int, [c_void_p, c_int, POINTER(c_void_p)]),
     ("fdmgpu_nscube_time_index", c_int, [c_void_p, POINTER(c_int)]),
+    ("fdmgpu_nscube_vtk_out", c_int, [c_void_p, c_char_p]),
+    ("fdmgpu_nscube_dtype", c_int, [c_void_p, POINTER(c_int)]),
     ("fdmgpu_nscube_destroy", c_int, [c_void_p]),
     ("fdmgpu_check_const_division", c_int, [c_longlong, c_void_p, c_void_p, c_void_p, c_void_p, c_void_p]),
     ("fdmgpu_server_create", c_int, [POINTER(c_void_p), c_double, c_int, c_int]),

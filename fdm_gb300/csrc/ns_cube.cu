@@ -13,7 +13,10 @@
 // first eager step the sequence is captured once into a CUDA graph and
 // replayed, which removes the host launch cost that dominates at 63^3.
 #include <cmath>
+#include <cstdio>
 #include <memory>
+#include <type_traits>
+#include <vector>
 
 #include "common.cuh"
 #include "internal.h"
@@ -21,17 +24,19 @@
 
 namespace fdmgpu {
 
-struct Field {
-    double* p;
+template <typename T>
+struct FieldT {
+    T* p;
     int z1, z2, y1, y2, x1, x2;
     long long sy, sz, size;
-    __host__ __device__ double& operator()(int i, int k, int j) const {
+    __host__ __device__ T& operator()(int i, int k, int j) const {
         return p[(long long)(i - z1) * sz + (long long)(k - y1) * sy + (j - x1)];
     }
 };
 
-static Field make_field(int z1, int z2, int y1, int y2, int x1, int x2) {
-    Field f;
+template <typename T>
+static FieldT<T> make_field(int z1, int z2, int y1, int y2, int x1, int x2) {
+    FieldT<T> f;
     f.z1 = z1; f.z2 = z2; f.y1 = y1; f.y2 = y2; f.x1 = x1; f.x2 = x2;
     f.sy = x2 - x1 + 1;
     f.sz = f.sy * (y2 - y1 + 1);
@@ -77,7 +82,8 @@ __device__ __forceinline__ double sq(double x) { return x * x; }  // asp::sq, sr
 // mirror below overwrites anyway), the x-mirror of u below the lid, and the
 // y-/z-mirrors of v and w.  None of these reads what another writes.
 // Thread grid covers a (z,y,x) box of (nz+3) x (ny+3) x (nx+3).
-__global__ void k_ns_bound1(Field u, Field v, Field w, NSParams P) {
+template <typename T>
+__global__ void k_ns_bound1(FieldT<T> u, FieldT<T> v, FieldT<T> w, NSParams P) {
     const int nx = P.nx, ny = P.ny, nz = P.nz;
     const long long e = (long long)blockIdx.x * blockDim.x + threadIdx.x;
     const int W = nx + 3, H = ny + 3, D = nz + 3;
@@ -106,7 +112,8 @@ __global__ void k_ns_bound1(Field u, Field v, Field w, NSParams P) {
 
 // init_bound, second phase: u x-mirror of the lid row (reads the lid values
 // written by phase one) and the Neumann pressure ghosts (:98-121).
-__global__ void k_ns_bound2(Field u, Field v, Field w, Field p, NSParams P) {
+template <typename T>
+__global__ void k_ns_bound2(FieldT<T> u, FieldT<T> v, FieldT<T> w, FieldT<T> p, NSParams P) {
     const int nx = P.nx, ny = P.ny, nz = P.nz;
     const long long e = (long long)blockIdx.x * blockDim.x + threadIdx.x;
     const int W = nx + 2, H = ny + 2, D = nz + 2;
@@ -138,7 +145,9 @@ __global__ void k_ns_bound2(Field u, Field v, Field w, Field p, NSParams P) {
 // FGH (src/ns_cube.cpp:126-200), one thread per (i,k,j) of the box
 // [0,nz] x [0,ny] x [0,nx]; each thread writes whichever of F, G, H has that
 // point in its range.
-__global__ void __launch_bounds__(256) k_ns_fgh(Field u, Field v, Field w, Field F, Field G, Field H, NSParams P) {
+template <typename T>
+__global__ void __launch_bounds__(256)
+    k_ns_fgh(FieldT<T> u, FieldT<T> v, FieldT<T> w, FieldT<T> F, FieldT<T> G, FieldT<T> H, NSParams P) {
     const int nx = P.nx, ny = P.ny, nz = P.nz;
     const long long e = (long long)blockIdx.x * blockDim.x + threadIdx.x;
     const int W = nx + 1, Hh = ny + 1, D = nz + 1;
@@ -186,14 +195,16 @@ __global__ void __launch_bounds__(256) k_ns_fgh(Field u, Field v, Field w, Field
 
 // Divergence RHS with the Dirichlet pressure ghosts folded in
 // (src/ns_cube.cpp:206-235).
-__global__ void k_ns_rhs(Field F, Field G, Field H, Field p, Field RHS, NSParams P) {
+template <typename T>
+__global__ void k_ns_rhs(FieldT<T> F, FieldT<T> G, FieldT<T> H, FieldT<T> p, FieldT<T> RHS, NSParams P) {
     const int nx = P.nx, ny = P.ny, nz = P.nz;
     const long long e = (long long)blockIdx.x * blockDim.x + threadIdx.x;
     if (e >= (long long)nx * ny * nz) return;
     const int j = (int)(e % nx) + 1;
     const int k = (int)((e / nx) % ny) + 1;
     const int i = (int)(e / ((long long)nx * ny)) + 1;
-    double r = cdiv(cdiv(F(i, k, j) - F(i, k, j - 1), P.ddx) + cdiv(G(i, k, j) - G(i, k - 1, j), P.ddy) +
+    // T-typed like the reference RHS element: rounded after each update
+    T r = cdiv(cdiv(F(i, k, j) - F(i, k, j - 1), P.ddx) + cdiv(G(i, k, j) - G(i, k - 1, j), P.ddy) +
                     cdiv(H(i, k, j) - H(i - 1, k, j), P.ddz), P.ddt);
     if (i <= 1) r -= cdiv(p(i - 1, k, j), P.ddz2);
     if (k <= 1) r -= cdiv(p(i, k - 1, j), P.ddy2);
@@ -206,18 +217,36 @@ __global__ void k_ns_rhs(Field F, Field G, Field H, Field p, Field RHS, NSParams
 
 // update_uvwp (src/ns_cube.cpp:241-277): pressure-gradient correction of the
 // interior faces, then p = x on the interior (src/tensor.h:280-283).
-__global__ void k_ns_update(Field u, Field v, Field w, Field p, Field x, Field F, Field G, Field H, NSParams P) {
+template <typename T>
+__global__ void k_ns_update(FieldT<T> u, FieldT<T> v, FieldT<T> w, FieldT<T> p, FieldT<T> x, FieldT<T> F, FieldT<T> G,
+                            FieldT<T> H, NSParams P) {
     const int nx = P.nx, ny = P.ny, nz = P.nz;
     const long long e = (long long)blockIdx.x * blockDim.x + threadIdx.x;
     if (e >= (long long)nx * ny * nz) return;
     const int j = (int)(e % nx) + 1;
     const int k = (int)((e / nx) % ny) + 1;
     const int i = (int)(e / ((long long)nx * ny)) + 1;
-    const double xc = x(i, k, j);
+    const T xc = x(i, k, j);
     if (j < nx) u(i, k, j) = F(i, k, j) - P.dt_dx * (x(i, k, j + 1) - xc);
     if (k < ny) v(i, k, j) = G(i, k, j) - P.dt_dy * (x(i, k + 1, j) - xc);
     if (i < nz) w(i, k, j) = H(i, k, j) - P.dt_dz * (x(i + 1, k, j) - xc);
     p(i, k, j) = xc;
+}
+
+// Cell-centred velocity of the interior cells for the VTK snapshot
+// (velocity_plotter::vtk_out, src/velocity_plot.cpp:200-217): out[cell*3+c]
+// with cell = ((i-1)*ny + (k-1))*nx + (j-1).
+template <typename T>
+__global__ void k_ns_cell_velocity(FieldT<T> u, FieldT<T> v, FieldT<T> w, NSParams P, double* out) {
+    const int nx = P.nx, ny = P.ny, nz = P.nz;
+    const long long e = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (e >= (long long)nx * ny * nz) return;
+    const int j = (int)(e % nx) + 1;
+    const int k = (int)((e / nx) % ny) + 1;
+    const int i = (int)(e / ((long long)nx * ny)) + 1;
+    out[3 * e] = 0.5 * (u(i, k, j) + u(i, k, j - 1));
+    out[3 * e + 1] = 0.5 * (v(i, k, j) + v(i, k - 1, j));
+    out[3 * e + 2] = 0.5 * (w(i, k, j) + w(i - 1, k, j));
 }
 
 // Diagnostic: IEEE a/b and the constant-divisor quotient side by side.
@@ -229,10 +258,11 @@ __global__ void k_cdiv_check(const double* a, const double* b, double* q_ieee, d
     q_c[i] = cdiv(a[i], CDiv{bi, 1.0 / bi});
 }
 
-struct NSPlan {
+template <typename T>
+struct NSPlanT {
     NSParams P;
     double x1, y1, z1, x2, y2, z2;
-    Field f[9];  // u v w p x F G H RHS
+    FieldT<T> f[9];  // u v w p x F G H RHS
     void* mem = nullptr;
     fdmgpu_lapl_cube* lapl = nullptr;
     cudaStream_t st = nullptr;
@@ -242,7 +272,7 @@ struct NSPlan {
     int time_index = 0;
     int steps_run = 0;
 
-    ~NSPlan() {
+    ~NSPlanT() {
         if (gexec) cudaGraphExecDestroy(gexec);
         if (graph) cudaGraphDestroy(graph);
         if (lapl) fdmgpu_lapl_cube_destroy(lapl);
@@ -252,28 +282,28 @@ struct NSPlan {
 
     void init() {
         const int nx = P.nx, ny = P.ny, nz = P.nz;
-        f[0] = make_field(0, nz + 1, 0, ny + 1, -1, nx + 1);
-        f[1] = make_field(0, nz + 1, -1, ny + 1, 0, nx + 1);
-        f[2] = make_field(-1, nz + 1, 0, ny + 1, 0, nx + 1);
-        f[3] = make_field(0, nz + 1, 0, ny + 1, 0, nx + 1);
-        f[4] = make_field(1, nz, 1, ny, 1, nx);
-        f[5] = make_field(1, nz, 1, ny, 0, nx);
-        f[6] = make_field(1, nz, 0, ny, 1, nx);
-        f[7] = make_field(0, nz, 1, ny, 1, nx);
-        f[8] = make_field(1, nz, 1, ny, 1, nx);
+        f[0] = make_field<T>(0, nz + 1, 0, ny + 1, -1, nx + 1);
+        f[1] = make_field<T>(0, nz + 1, -1, ny + 1, 0, nx + 1);
+        f[2] = make_field<T>(-1, nz + 1, 0, ny + 1, 0, nx + 1);
+        f[3] = make_field<T>(0, nz + 1, 0, ny + 1, 0, nx + 1);
+        f[4] = make_field<T>(1, nz, 1, ny, 1, nx);
+        f[5] = make_field<T>(1, nz, 1, ny, 0, nx);
+        f[6] = make_field<T>(1, nz, 0, ny, 1, nx);
+        f[7] = make_field<T>(0, nz, 1, ny, 1, nx);
+        f[8] = make_field<T>(1, nz, 1, ny, 1, nx);
         size_t total = 0;
         for (auto& fi : f) total += (size_t)((fi.size + 31) / 32 * 32);
-        FDM_CUDA(cudaMalloc(&mem, total * sizeof(double)));
-        FDM_CUDA(cudaMemset(mem, 0, total * sizeof(double)));
+        FDM_CUDA(cudaMalloc(&mem, total * sizeof(T)));
+        FDM_CUDA(cudaMemset(mem, 0, total * sizeof(T)));
         size_t off = 0;
         for (auto& fi : f) {
-            fi.p = (double*)mem + off;
+            fi.p = (T*)mem + off;
             off += (size_t)((fi.size + 31) / 32 * 32);
         }
         FDM_CUDA(cudaStreamCreateWithFlags(&st, cudaStreamNonBlocking));
         own_stream = true;
         // LaplCube(dx, dy, dz, x2-x1+dx, y2-y1+dy, z2-z1+dz, nx, ny, nz), src/ns_cube.h:77
-        int rc = fdmgpu_lapl_cube_create(&lapl, FDMGPU_F64, FDMGPU_DIRICHLET, P.dx, P.dy, P.dz, x2 - x1 + P.dx,
+        int rc = fdmgpu_lapl_cube_create(&lapl, sizeof(T) == 8 ? FDMGPU_F64 : FDMGPU_F32, FDMGPU_DIRICHLET, P.dx, P.dy, P.dz, x2 - x1 + P.dx,
                                          y2 - y1 + P.dy, z2 - z1 + P.dz, nx, ny, nz);
         if (rc) throw Error{rc};
     }
@@ -285,29 +315,29 @@ struct NSPlan {
         const long long vol = (long long)nx * ny * nz;
         {
             FDM_TIMED("ns_bound1", st);
-            k_ns_bound1<<<blocks((long long)(nx + 3) * (ny + 3) * (nz + 3)), B, 0, st>>>(f[0], f[1], f[2], P);
+            k_ns_bound1<T><<<blocks((long long)(nx + 3) * (ny + 3) * (nz + 3)), B, 0, st>>>(f[0], f[1], f[2], P);
             FDM_LAUNCH_CHECK();
         }
         {
             FDM_TIMED("ns_bound2", st);
-            k_ns_bound2<<<blocks((long long)(nx + 2) * (ny + 2) * (nz + 2)), B, 0, st>>>(f[0], f[1], f[2], f[3], P);
+            k_ns_bound2<T><<<blocks((long long)(nx + 2) * (ny + 2) * (nz + 2)), B, 0, st>>>(f[0], f[1], f[2], f[3], P);
             FDM_LAUNCH_CHECK();
         }
         {
             FDM_TIMED("ns_fgh", st);
-            k_ns_fgh<<<blocks((long long)(nx + 1) * (ny + 1) * (nz + 1)), B, 0, st>>>(f[0], f[1], f[2], f[5], f[6],
+            k_ns_fgh<T><<<blocks((long long)(nx + 1) * (ny + 1) * (nz + 1)), B, 0, st>>>(f[0], f[1], f[2], f[5], f[6],
                                                                                       f[7], P);
             FDM_LAUNCH_CHECK();
         }
         {
             FDM_TIMED("ns_rhs", st);
-            k_ns_rhs<<<blocks(vol), B, 0, st>>>(f[5], f[6], f[7], f[3], f[8], P);
+            k_ns_rhs<T><<<blocks(vol), B, 0, st>>>(f[5], f[6], f[7], f[3], f[8], P);
             FDM_LAUNCH_CHECK();
         }
         cube_solve_device(lapl, f[4].p, f[8].p, 1, st);
         {
             FDM_TIMED("ns_update", st);
-            k_ns_update<<<blocks(vol), B, 0, st>>>(f[0], f[1], f[2], f[3], f[4], f[5], f[6], f[7], P);
+            k_ns_update<T><<<blocks(vol), B, 0, st>>>(f[0], f[1], f[2], f[3], f[4], f[5], f[6], f[7], P);
             FDM_LAUNCH_CHECK();
         }
     }
@@ -343,24 +373,22 @@ struct NSPlan {
 using namespace fdmgpu;
 
 struct fdmgpu_nscube {
-    NSPlan plan;
+    int dtype = FDMGPU_F64;
+    std::unique_ptr<NSPlanT<double>> d;
+    std::unique_ptr<NSPlanT<float>> f;
 };
 
-extern "C" {
+namespace {
+// runs fn on the handle's plan, whichever element type it has
+template <typename Fn>
+void with_plan(fdmgpu_nscube* h, Fn&& fn) {
+    if (h->d) fn(*h->d);
+    else fn(*h->f);
+}
 
-int fdmgpu_nscube_create(fdmgpu_nscube** h, int dtype, int nx, int nz, double x1, double y1, double z1, double x2,
-                         double y2, double z2, double u0, double Re, double dt) {
-    FDM_API_BEGIN
-    if (!h) FDM_FAIL(FDMGPU_EINVAL, "null handle pointer");
-    *h = nullptr;
-    if (dtype != FDMGPU_F64) FDM_FAIL(FDMGPU_ENOTSUP, "NSCube is implemented for FP64");
-    if (nx < 2 || nz < 2 || nx > FDMGPU_MAX_N || nz > FDMGPU_MAX_N || ilog2_exact(nx + 1) < 0 ||
-        ilog2_exact(nz + 1) < 0)
-        FDM_FAIL(FDMGPU_ESIZE, "verify((1<<n) == N) failed: nx+1 and nz+1 must be powers of two (nx=%d nz=%d)", nx,
-                 nz);
-    if (!(x2 > x1 && y2 > y1 && z2 > z1 && Re > 0 && dt > 0)) FDM_FAIL(FDMGPU_EINVAL, "bad domain or parameters");
-    std::unique_ptr<fdmgpu_nscube> p(new fdmgpu_nscube());
-    NSPlan& s = p->plan;
+template <typename T>
+void setup_plan(NSPlanT<T>& s, int nx, int nz, double x1, double y1, double z1, double x2, double y2, double z2,
+                double u0, double Re, double dt) {
     s.x1 = x1; s.y1 = y1; s.z1 = z1; s.x2 = x2; s.y2 = y2; s.z2 = z2;
     s.P.nx = nx; s.P.ny = nx; s.P.nz = nz;  // ny from key "nx", src/ns_cube.h:57-59
     s.P.U0 = u0; s.P.Re = Re; s.P.dt = dt;
@@ -372,6 +400,31 @@ int fdmgpu_nscube_create(fdmgpu_nscube** h, int dtype, int nx, int nz, double x1
     s.P.ddt = cdiv_of(dt);
     s.P.dt_dx = dt / s.P.dx; s.P.dt_dy = dt / s.P.dy; s.P.dt_dz = dt / s.P.dz;
     s.init();
+}
+}  // namespace
+
+extern "C" {
+
+int fdmgpu_nscube_create(fdmgpu_nscube** h, int dtype, int nx, int nz, double x1, double y1, double z1, double x2,
+                         double y2, double z2, double u0, double Re, double dt) {
+    FDM_API_BEGIN
+    if (!h) FDM_FAIL(FDMGPU_EINVAL, "null handle pointer");
+    *h = nullptr;
+    if (dtype != FDMGPU_F64 && dtype != FDMGPU_F32) FDM_FAIL(FDMGPU_EINVAL, "bad dtype %d", dtype);
+    if (nx < 2 || nz < 2 || nx > FDMGPU_MAX_N || nz > FDMGPU_MAX_N || ilog2_exact(nx + 1) < 0 ||
+        ilog2_exact(nz + 1) < 0)
+        FDM_FAIL(FDMGPU_ESIZE, "verify((1<<n) == N) failed: nx+1 and nz+1 must be powers of two (nx=%d nz=%d)", nx,
+                 nz);
+    if (!(x2 > x1 && y2 > y1 && z2 > z1 && Re > 0 && dt > 0)) FDM_FAIL(FDMGPU_EINVAL, "bad domain or parameters");
+    std::unique_ptr<fdmgpu_nscube> p(new fdmgpu_nscube());
+    p->dtype = dtype;
+    if (dtype == FDMGPU_F64) {
+        p->d.reset(new NSPlanT<double>());
+        setup_plan(*p->d, nx, nz, x1, y1, z1, x2, y2, z2, u0, Re, dt);
+    } else {
+        p->f.reset(new NSPlanT<float>());
+        setup_plan(*p->f, nx, nz, x1, y1, z1, x2, y2, z2, u0, Re, dt);
+    }
     *h = p.release();
     FDM_API_END
 }
@@ -380,7 +433,7 @@ int fdmgpu_nscube_step(fdmgpu_nscube* h, int k) {
     FDM_API_BEGIN
     if (!h) FDM_FAIL(FDMGPU_EINVAL, "null handle");
     if (k < 0) FDM_FAIL(FDMGPU_EINVAL, "negative step count");
-    h->plan.step(k);
+    with_plan(h, [&](auto& s) { s.step(k); });
     FDM_API_END
 }
 
@@ -397,56 +450,108 @@ int fdmgpu_check_const_division(long long n, const double* d_a, const double* d_
 int fdmgpu_nscube_set_stream(fdmgpu_nscube* h, void* stream) {
     FDM_API_BEGIN
     if (!h) FDM_FAIL(FDMGPU_EINVAL, "null handle");
-    NSPlan& s = h->plan;
-    FDM_CUDA(cudaStreamSynchronize(s.st));
-    if (s.own_stream) FDM_CUDA(cudaStreamDestroy(s.st));
-    s.own_stream = false;
-    s.st = (cudaStream_t)stream;
+    with_plan(h, [&](auto& s) {
+        FDM_CUDA(cudaStreamSynchronize(s.st));
+        if (s.own_stream) FDM_CUDA(cudaStreamDestroy(s.st));
+        s.own_stream = false;
+        s.st = (cudaStream_t)stream;
+    });
     FDM_API_END
 }
 
 int fdmgpu_nscube_field_info(fdmgpu_nscube* h, int field, size_t* count, int* r) {
     FDM_API_BEGIN
     if (!h || field < 0 || field > 8) FDM_FAIL(FDMGPU_EINVAL, "bad handle or field %d", field);
-    const Field& f = h->plan.f[field];
-    if (count) *count = (size_t)f.size;
-    if (r) {
-        r[0] = f.z1; r[1] = f.z2; r[2] = f.y1; r[3] = f.y2; r[4] = f.x1; r[5] = f.x2;
-    }
+    with_plan(h, [&](auto& s) {
+        const auto& f = s.f[field];
+        if (count) *count = (size_t)f.size;
+        if (r) {
+            r[0] = f.z1; r[1] = f.z2; r[2] = f.y1; r[3] = f.y2; r[4] = f.x1; r[5] = f.x2;
+        }
+    });
     FDM_API_END
 }
 
+/* host buffers hold the handle's element type (double or float) */
 int fdmgpu_nscube_get_field(fdmgpu_nscube* h, int field, void* host, size_t count) {
     FDM_API_BEGIN
     if (!h || !host || field < 0 || field > 8) FDM_FAIL(FDMGPU_EINVAL, "bad argument");
-    const Field& f = h->plan.f[field];
-    if (count != (size_t)f.size) FDM_FAIL(FDMGPU_EINVAL, "field has %lld elements, got %zu", f.size, count);
-    FDM_CUDA(cudaStreamSynchronize(h->plan.st));
-    FDM_CUDA(cudaMemcpy(host, f.p, count * sizeof(double), cudaMemcpyDeviceToHost));
+    with_plan(h, [&](auto& s) {
+        const auto& f = s.f[field];
+        if (count != (size_t)f.size) FDM_FAIL(FDMGPU_EINVAL, "field has %lld elements, got %zu", f.size, count);
+        FDM_CUDA(cudaStreamSynchronize(s.st));
+        FDM_CUDA(cudaMemcpy(host, f.p, count * sizeof(*f.p), cudaMemcpyDeviceToHost));
+    });
     FDM_API_END
 }
 
 int fdmgpu_nscube_set_field(fdmgpu_nscube* h, int field, const void* host, size_t count) {
     FDM_API_BEGIN
     if (!h || !host || field < 0 || field > 8) FDM_FAIL(FDMGPU_EINVAL, "bad argument");
-    const Field& f = h->plan.f[field];
-    if (count != (size_t)f.size) FDM_FAIL(FDMGPU_EINVAL, "field has %lld elements, got %zu", f.size, count);
-    FDM_CUDA(cudaStreamSynchronize(h->plan.st));
-    FDM_CUDA(cudaMemcpy(f.p, host, count * sizeof(double), cudaMemcpyHostToDevice));
+    with_plan(h, [&](auto& s) {
+        const auto& f = s.f[field];
+        if (count != (size_t)f.size) FDM_FAIL(FDMGPU_EINVAL, "field has %lld elements, got %zu", f.size, count);
+        FDM_CUDA(cudaStreamSynchronize(s.st));
+        FDM_CUDA(cudaMemcpy(f.p, host, count * sizeof(*f.p), cudaMemcpyHostToDevice));
+    });
     FDM_API_END
 }
 
 int fdmgpu_nscube_field_device(fdmgpu_nscube* h, int field, void** dptr) {
     FDM_API_BEGIN
     if (!h || !dptr || field < 0 || field > 8) FDM_FAIL(FDMGPU_EINVAL, "bad argument");
-    *dptr = h->plan.f[field].p;
+    with_plan(h, [&](auto& s) { *dptr = (void*)s.f[field].p; });
+    FDM_API_END
+}
+
+int fdmgpu_nscube_dtype(fdmgpu_nscube* h, int* dtype) {
+    FDM_API_BEGIN
+    if (!h || !dtype) FDM_FAIL(FDMGPU_EINVAL, "bad argument");
+    *dtype = h->dtype;
+    FDM_API_END
+}
+
+int fdmgpu_nscube_vtk_out(fdmgpu_nscube* h, const char* path) {
+    FDM_API_BEGIN
+    if (!h || !path) FDM_FAIL(FDMGPU_EINVAL, "null argument");
+    with_plan(h, [&](auto& s) {
+        using T = std::remove_reference_t<decltype(*s.f[0].p)>;
+        const int nx = s.P.nx, ny = s.P.ny, nz = s.P.nz;
+        const long long cells = (long long)nx * ny * nz;
+        DevBuf d;
+        d.get((size_t)cells * 3 * sizeof(double));
+        k_ns_cell_velocity<T><<<(unsigned)((cells + 255) / 256), 256, 0, s.st>>>(s.f[0], s.f[1], s.f[2], s.P,
+                                                                                 (double*)d.p);
+        FDM_LAUNCH_CHECK();
+        std::vector<double> c((size_t)cells * 3);
+        FDM_CUDA(cudaStreamSynchronize(s.st));
+        FDM_CUDA(cudaMemcpy(c.data(), d.p, c.size() * sizeof(double), cudaMemcpyDeviceToHost));
+        FILE* f = fopen(path, "wb");
+        if (!f) FDM_FAIL(FDMGPU_EINVAL, "cannot open %s for writing", path);
+        // header and number format of velocity_plotter::vtk_out for a cube
+        // (src/velocity_plot.cpp:113-119, 200-217)
+        fprintf(f, "# vtk DataFile Version 3.0\n");
+        fprintf(f, "step %d\n", s.time_index);
+        fprintf(f, "ASCII\n");
+        fprintf(f, "DATASET STRUCTURED_POINTS\n");
+        fprintf(f, "DIMENSIONS %d %d %d\n", nx, ny, nz);
+        fprintf(f, "ASPECT_RATIO 1 1 1\n");
+        fprintf(f, "ORIGIN %f %f %f\n", s.x1, s.y1, s.z1);
+        fprintf(f, "SPACING %f %f %f\n", s.P.dx, s.P.dy, s.P.dz);
+        fprintf(f, "POINT_DATA %lld\n", cells);
+        fprintf(f, "VECTORS u double\n");
+        for (long long e = 0; e < cells; e++) fprintf(f, "%f %f %f\n", c[3 * e], c[3 * e + 1], c[3 * e + 2]);
+        const bool ok = ferror(f) == 0;
+        fclose(f);
+        if (!ok) FDM_FAIL(FDMGPU_EINVAL, "write to %s failed", path);
+    });
     FDM_API_END
 }
 
 int fdmgpu_nscube_time_index(fdmgpu_nscube* h, int* t) {
     FDM_API_BEGIN
     if (!h || !t) FDM_FAIL(FDMGPU_EINVAL, "bad argument");
-    *t = h->plan.time_index;
+    with_plan(h, [&](auto& s) { *t = s.time_index; });
     FDM_API_END
 }
 

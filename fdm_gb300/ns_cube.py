@@ -39,10 +39,14 @@ class Tensor3:
 
 
 class NSCube:
-    def __init__(self, cfg: Config | None = None, dtype=np.float64, **overrides):
+    def __init__(self, cfg: Config | None = None, dtype=None, **overrides):
         cfg = cfg or Config()
         for k, v in overrides.items():
             cfg.set("ns", k, v)
+        if dtype is None:
+            # solver:datatype selects NSCube<float> or NSCube<double>, as the
+            # reference's cavity driver does (test/test_ns_cube.cpp:89-97)
+            dtype = np.float32 if str(cfg.get("solver", "datatype", "double")) == "float" else np.float64
         self.x1 = cfg.get("ns", "x1", -math.pi)
         self.y1 = cfg.get("ns", "y1", -math.pi)
         self.z1 = cfg.get("ns", "z1", -math.pi)
@@ -56,11 +60,13 @@ class NSCube:
         self.ny = cfg.get("ns", "nx", 32)
         self.nz = cfg.get("ns", "nz", 32)
         self.verbose = cfg.get("ns", "verbose", 0)
-        if np.dtype(dtype) != np.float64:
-            raise N.FdmError(N.ENOTSUP, "NSCube is implemented for float64")
+        self.dtype = np.dtype(dtype)
+        if self.dtype not in (np.float64, np.float32):
+            raise N.FdmError(N.ENOTSUP, "NSCube is implemented for float64 and float32")
         self._lib = N.load()
         h = c_void_p()
-        N.check(self._lib.fdmgpu_nscube_create(byref(h), N.F64, int(self.nx), int(self.nz), float(self.x1),
+        code = N.F64 if self.dtype == np.float64 else N.F32
+        N.check(self._lib.fdmgpu_nscube_create(byref(h), code, int(self.nx), int(self.nz), float(self.x1),
                                                float(self.y1), float(self.z1), float(self.x2), float(self.y2),
                                                float(self.z2), float(self.U0), float(self.Re), float(self.dt)))
         self._h = h
@@ -88,14 +94,14 @@ class NSCube:
         fid = FIELDS.index(name)
         cnt, r = self.field_info(name)
         shape = (r[1] - r[0] + 1, r[3] - r[2] + 1, r[5] - r[4] + 1)
-        out = np.empty(shape, np.float64)
+        out = np.empty(shape, self.dtype)
         N.check(self._lib.fdmgpu_nscube_get_field(self._h, fid, out.ctypes.data, cnt))
         return Tensor3(out, r)
 
     def set(self, name: str, data: np.ndarray) -> None:
         fid = FIELDS.index(name)
         cnt, _ = self.field_info(name)
-        a = np.ascontiguousarray(data, np.float64)
+        a = np.ascontiguousarray(data, self.dtype)
         if a.size != cnt:
             raise N.FdmError(N.EINVAL, "field %s has %d elements" % (name, cnt))
         N.check(self._lib.fdmgpu_nscube_set_field(self._h, fid, a.ctypes.data, cnt))
@@ -109,6 +115,11 @@ class NSCube:
         if name in FIELDS:
             return self.get(name)
         raise AttributeError(name)
+
+    def vtk_out(self, path: str) -> None:
+        """ASCII VTK snapshot of the cell-centred velocity in the format of
+        the reference's velocity_plotter::vtk_out (src/velocity_plot.cpp:113)."""
+        N.check(self._lib.fdmgpu_nscube_vtk_out(self._h, str(path).encode()))
 
     def close(self) -> None:
         if getattr(self, "_h", None):

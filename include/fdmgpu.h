@@ -219,7 +219,12 @@ int fdmgpu_tridiag_device(int dtype, int n, int nsys, const void* d_lower, const
  * ns:{x1,y1,z1,x2,y2,z2,u0,Re,dt,nx,nz} (ny is read from key nx, as in the
  * reference, src/ns_cube.h:57-59), step() (src/ns_cube.cpp:27-62) and the
  * public tensors u,v,w,p,x,F,G,H,RHS in the reference layouts (inclusive
- * index ranges, x fastest).  State lives on the device. */
+ * index ranges, x fastest).  State lives on the device.  dtype FDMGPU_F64
+ * is NSCube<double>; FDMGPU_F32 is NSCube<float> (src/ns_cube.cpp:281-282):
+ * fields in float, each expression evaluated with the reference's C++
+ * promotions (float where only fields meet, double once a double parameter
+ * enters), the pressure solve by the FP32 LaplCube.  Host buffers of the
+ * field copies hold the handle's element type. */
 typedef struct fdmgpu_nscube fdmgpu_nscube;
 enum {
     FDMGPU_NS_U = 0, FDMGPU_NS_V, FDMGPU_NS_W, FDMGPU_NS_P, FDMGPU_NS_X,
@@ -241,6 +246,12 @@ int fdmgpu_nscube_set_field(fdmgpu_nscube* h, int field, const void* host, size_
 /* device pointer of a field's storage */
 int fdmgpu_nscube_field_device(fdmgpu_nscube* h, int field, void** dptr);
 int fdmgpu_nscube_time_index(fdmgpu_nscube* h, int* t);
+int fdmgpu_nscube_dtype(fdmgpu_nscube* h, int* dtype);
+/* ASCII VTK snapshot of the cell-centred velocity, as the reference's
+ * velocity_plotter::vtk_out writes it for a cube (src/velocity_plot.cpp:
+ * 113-119, 200-217): STRUCTURED_POINTS header, one "%f %f %f" line per
+ * interior cell, x fastest.  Synchronous. */
+int fdmgpu_nscube_vtk_out(fdmgpu_nscube* h, const char* path);
 int fdmgpu_nscube_destroy(fdmgpu_nscube* h);
 /* Diagnostic of the NSCube stencils' division by run constants (h, h^2, Re,
  * dt): writes the IEEE quotient a/b and the library's constant-divisor

@@ -114,12 +114,15 @@ class _NS:
         if not h:
             raise ValueError("bad size")
 
+    def _fn(self, what):
+        return getattr(self.L, {"orc": "orc_ns_", "ref": "ref_nscube_", "reff": "ref_nscubef_"}[self.kind] + what)
+
     def step(self, k: int = 1) -> None:
-        (self.L.orc_ns_step if self.kind == "orc" else self.L.ref_nscube_step)(self.h, int(k))
+        self._fn("step")(self.h, int(k))
 
     def get(self, name: str) -> np.ndarray:
         fid = self.FIELDS.index(name)
-        getter = self.L.orc_ns_get if self.kind == "orc" else self.L.ref_nscube_get
+        getter = self._fn("get")
         n = getter(self.h, fid, None)
         out = np.zeros(n)
         getter(self.h, fid, _p(out))
@@ -127,7 +130,7 @@ class _NS:
 
     def close(self):
         if self.h:
-            (self.L.orc_ns_destroy if self.kind == "orc" else self.L.ref_nscube_destroy)(self.h)
+            self._fn("destroy")(self.h)
             self.h = None
 
     def __del__(self):
@@ -153,6 +156,12 @@ class Reference:
         L.ref_nscube_get.restype = c_long
         L.ref_nscube_get.argtypes = [c_void_p, c_int, _dp]
         L.ref_nscube_destroy.argtypes = [c_void_p]
+        L.ref_nscubef_create.restype = c_void_p
+        L.ref_nscubef_create.argtypes = [c_int, c_int] + [c_double] * 9
+        L.ref_nscubef_step.argtypes = [c_void_p, c_int]
+        L.ref_nscubef_get.restype = c_long
+        L.ref_nscubef_get.argtypes = [c_void_p, c_int, _dp]
+        L.ref_nscubef_destroy.argtypes = [c_void_p]
         self.L = L
 
     def sfft(self, s: np.ndarray, dx: float = 1.0) -> np.ndarray:
@@ -190,9 +199,34 @@ class Reference:
     def nscube(self, nx, nz, Re, dt, u0=1.0, box=(-np.pi, -np.pi, -np.pi, np.pi, np.pi, np.pi)):
         return _NS(self.L, self.L.ref_nscube_create(nx, nz, Re, dt, u0, *box), "ref")
 
+    def nscube_float(self, nx, nz, Re, dt, u0=1.0, box=(-np.pi, -np.pi, -np.pi, np.pi, np.pi, np.pi)):
+        """NSCube<float,false>; fields come back widened to float64."""
+        return _NS(self.L, self.L.ref_nscubef_create(nx, nz, Re, dt, u0, *box), "reff")
+
 
 _port = None
 _ref = None
+
+
+def vtk_text(u, v, w, nx, ny, nz, origin, spacing, time_index) -> str:
+    """Restatement of velocity_plotter::vtk_out for a cube
+    (src/velocity_plot.cpp:113-119, 200-217): header, then the cell-centred
+    velocity 0.5(u[i][k][j]+u[i][k][j-1]), 0.5(v[i][k][j]+v[i][k-1][j]),
+    0.5(w[i][k][j]+w[i-1][k][j]) of every interior cell, "%f %f %f", x
+    fastest.  u, v, w are the NSCube field storages (flat or shaped) with
+    the index ranges of src/ns_cube.h:64-66."""
+    U = np.asarray(u, dtype=np.float64).reshape(nz + 2, ny + 2, nx + 3)   # z 0.., y 0.., x -1..
+    V = np.asarray(v, dtype=np.float64).reshape(nz + 2, ny + 3, nx + 2)   # z 0.., y -1.., x 0..
+    W = np.asarray(w, dtype=np.float64).reshape(nz + 3, ny + 2, nx + 2)   # z -1.., y 0.., x 0..
+    out = ["# vtk DataFile Version 3.0", "step %d" % time_index, "ASCII", "DATASET STRUCTURED_POINTS",
+           "DIMENSIONS %d %d %d" % (nx, ny, nz), "ASPECT_RATIO 1 1 1", "ORIGIN %f %f %f" % tuple(origin),
+           "SPACING %f %f %f" % tuple(spacing), "POINT_DATA %d" % (nx * ny * nz), "VECTORS u double"]
+    for i in range(1, nz + 1):
+        for k in range(1, ny + 1):
+            for j in range(1, nx + 1):
+                out.append("%f %f %f" % (0.5 * (U[i, k, j + 1] + U[i, k, j]), 0.5 * (V[i, k + 1, j] + V[i, k, j]),
+                                         0.5 * (W[i + 1, k, j] + W[i, k, j])))
+    return "\n".join(out) + "\n"
 
 
 def port() -> Port:

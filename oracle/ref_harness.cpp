@@ -177,4 +177,53 @@ void ref_nscube_destroy(void* hp) {
     delete h;
 }
 
+// The float instantiation, NSCube<float,false> (src/ns_cube.cpp:281-282),
+// same keys; fields are copied out widened to double.
+struct RefNSf {
+    Config cfg;
+    NSCube<float, false>* ns = nullptr;
+};
+
+void* ref_nscubef_create(int nx, int nz, double Re, double dt, double u0,
+                         double x1, double y1, double z1, double x2, double y2, double z2) {
+    auto* h = new RefNSf();
+    char buf[16][96];
+    const char* keys[] = {"nx", "nz", "Re", "dt", "u0", "x1", "y1", "z1", "x2", "y2", "z2"};
+    double vals[] = {(double)nx, (double)nz, Re, dt, u0, x1, y1, z1, x2, y2, z2};
+    char* argv[16];
+    argv[0] = (char*)"ref";
+    for (int i = 0; i < 11; i++) {
+        if (i < 2) snprintf(buf[i], sizeof(buf[i]), "--ns:%s=%d", keys[i], (int)vals[i]);
+        else snprintf(buf[i], sizeof(buf[i]), "--ns:%s=%.17g", keys[i], vals[i]);
+        argv[i + 1] = buf[i];
+    }
+    h->cfg.rewrite(12, argv);
+    h->ns = new NSCube<float, false>(h->cfg);
+    return h;
+}
+
+int ref_nscubef_step(void* hp, int k) {
+    auto* h = (RefNSf*)hp;
+    for (int i = 0; i < k; i++) h->ns->step();
+    return 0;
+}
+
+long ref_nscubef_get(void* hp, int field, double* out) {
+    auto* h = (RefNSf*)hp;
+    auto* ns = h->ns;
+    tensor<float, 3, false>* t[] = {&ns->u, &ns->v, &ns->w, &ns->p, &ns->x,
+                                    &ns->F, &ns->G, &ns->H, &ns->RHS};
+    if (field < 0 || field > 8) return -1;
+    long n = t[field]->size;
+    if (out)
+        for (long i = 0; i < n; i++) out[i] = (double)t[field]->vec[i];
+    return n;
+}
+
+void ref_nscubef_destroy(void* hp) {
+    auto* h = (RefNSf*)hp;
+    delete h->ns;
+    delete h;
+}
+
 }  // extern "C"

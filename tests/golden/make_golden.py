@@ -190,6 +190,16 @@ def main():
         for k, v in checksums(m.get(name)).items():
             ns["n31_s10_%s_%s" % (name, k)] = v
     m.close()
+    # NSCube<float> (src/ns_cube.cpp:281-282), same cavity
+    m = R.nscube_float(15, 15, 250.0, 0.01)
+    m.step(20)
+    for name in ("u", "v", "w", "p"):
+        ns["f32_n15_s20_" + name] = m.get(name).astype(np.float32)
+    m.step(80)
+    for name in ("u", "v", "w", "p"):
+        for k, v in checksums(m.get(name)).items():
+            ns["f32_n15_s100_%s_%s" % (name, k)] = v
+    m.close()
     np.savez_compressed(OUT / "ns_cube.npz", **ns)
     for p in sorted(OUT.glob("*.npz")):
         print(p.name, p.stat().st_size)

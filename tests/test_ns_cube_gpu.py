@@ -121,3 +121,53 @@ def test_constant_division_matches_ieee(cuda):
     assert np.array_equal(x.view(np.int64), (a / b).view(np.int64))  # the device's IEEE division
     bad = np.flatnonzero(x.view(np.int64) != y.view(np.int64))
     assert bad.size == 0, (bad.size, a[bad[:4]], b[bad[:4]])
+
+
+def test_vtk_snapshot_matches_reference_format(cuda, port, tmp_path):
+    """NSCube.vtk_out writes velocity_plotter::vtk_out's cube format: the
+    header line for line and the cell-centred velocities of the oracle's
+    fields to the printed precision."""
+    from oracle.oracle import vtk_text
+    m = make(15)
+    o = port.nscube(15, 15, 250.0, 0.01)
+    m.step(20)
+    o.step(20)
+    path = tmp_path / "step.vtk"
+    m.vtk_out(str(path))
+    got = path.read_text().splitlines()
+    h = 2 * math.pi / 15
+    ref = vtk_text(o.get("u"), o.get("v"), o.get("w"), 15, 15, 15, (-math.pi,) * 3, (h, h, h), 20).splitlines()
+    assert got[:10] == ref[:10]
+    assert len(got) == len(ref) == 10 + 15 ** 3
+    a = np.array([[float(t) for t in line.split()] for line in got[10:]])
+    b = np.array([[float(t) for t in line.split()] for line in ref[10:]])
+    assert np.abs(a - b).max() <= 1.5e-6
+    assert np.abs(b).max() > 1e-3  # the flow has reached the interior cells
+
+
+def test_float_cavity_vs_reference_float(cuda, golden):
+    """NSCube<float> (solver:datatype=float, src/ns_cube.cpp:281-282) against
+    the reference's own float cavity after 20 steps at 15^3: the GPU float
+    fields are as close to the reference's float fields as those are to
+    the double cavity (the float-vs-double gap is the scale of float
+    round-off in this flow: 1.5e-8 relative in u, 5.6e-6 in v)."""
+    g = golden("ns_cube")
+    c = Config()
+    c.rewrite(["prog", "--ns:nx=15", "--ns:nz=15", "--ns:Re=250", "--ns:dt=0.01", "--ns:u0=1",
+               "--solver:datatype=float"])
+    m = NSCube(c)
+    assert m.dtype == np.float32
+    m.step(20)
+    for name in ("u", "v", "w", "p"):
+        got = m.get(name).data.ravel().astype(np.float64)
+        ref32 = g["f32_n15_s20_" + name].astype(np.float64)
+        ref64 = g["n15_s20_" + name]
+        gap = np.linalg.norm(ref32 - ref64)
+        assert got.dtype == np.float64 and m.get(name).data.dtype == np.float32
+        assert np.linalg.norm(got - ref32) <= 10 * gap + 1e-6 * np.linalg.norm(ref64), name
+    m.step(80)
+    for name in ("u", "w", "p"):
+        got = m.get(name).data.ravel().astype(np.float64)
+        idx = g["f32_n15_s100_%s_idx" % name]
+        scale = max(1.0, float(g["f32_n15_s100_%s_maxabs" % name]))
+        assert np.abs(got[idx] - g["f32_n15_s100_%s_vals" % name]).max() <= 1e-4 * scale, name
