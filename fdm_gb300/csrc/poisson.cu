@@ -24,6 +24,7 @@
 #include "sine.cuh"
 #include "sine_rg.cuh"
 #include "sine_tc.cuh"
+#include "pfft.cuh"
 #include "solve_kernels.cuh"
 
 namespace fdmgpu {
@@ -78,6 +79,54 @@ static void upload_lambda(DevBuf& buf, int n, double h) {
         v[j - 1] = (T)(4. / (h * h) * (s * s));
     }
     FDM_CUDA(cudaMemcpy(buf.get(n * sizeof(T)), v.data(), n * sizeof(T), cudaMemcpyHostToDevice));
+}
+
+// ---------------------------------------------------------------------------
+// periodic LaplCube: twiddles, eigenvalues, the transform launcher and the
+// divide
+// ---------------------------------------------------------------------------
+template <typename T>
+static void upload_ptwiddles(DevBuf& buf, int n) {
+    std::vector<vec2_t<T>> v(n);
+    for (int t = 0; t < n; t++) {
+        const double a = -2.0 * M_PI * t / n;
+        v[t].x = (T)std::cos(a);
+        v[t].y = (T)std::sin(a);
+    }
+    FDM_CUDA(cudaMemcpy(buf.get(n * sizeof(vec2_t<T>)), v.data(), n * sizeof(vec2_t<T>), cudaMemcpyHostToDevice));
+}
+
+// lm[p] = 4/h^2 sin^2(p pi / n), p = 0..n-1 (src/lapl_cube.cpp:150, periodic)
+template <typename T>
+static void upload_plambda(DevBuf& buf, int n, double h) {
+    std::vector<T> v(n);
+    for (int p = 0; p < n; p++) {
+        const double s = std::sin(p * M_PI / n);
+        v[p] = (T)(4. / (h * h) * (s * s));
+    }
+    FDM_CUDA(cudaMemcpy(buf.get(n * sizeof(T)), v.data(), n * sizeof(T), cudaMemcpyHostToDevice));
+}
+
+template <typename T, bool INV>
+static void launch_pfft(const T* in, T* out, const PLineGeom& g, int n, const void* tw, double scale,
+                        cudaStream_t st) {
+    const int LPB = pfft_lines_per_block(n);
+    const unsigned grid = (unsigned)((g.lines + LPB - 1) / LPB);
+    FDM_TIMED(INV ? "pfft_inverse" : "pfft_forward", st);
+    k_pfft<T, INV><<<grid, 256, pfft_smem_bytes<T>(n), st>>>(in, out, g, n, (const vec2_t<T>*)tw, (T)scale);
+    FDM_LAUNCH_CHECK();
+}
+
+// W /= -(lz[i] + ly[k] + lx[j]) (in T, as the reference's k2), zero mode := 0
+template <typename T>
+__global__ void k_pdivide(T* W, int nx, int ny, int nz, long long total, const T* lx, const T* ly, const T* lz) {
+    const long long e = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (e >= total) return;
+    const long long vol = (long long)nx * ny * nz;
+    const long long r = e % vol;
+    const int j = (int)(r % nx), k = (int)((r / nx) % ny), i = (int)(r / ((long long)nx * ny));
+    const T k2 = lz[i] + ly[k] + lx[j];
+    W[e] = (i == 0 && k == 0 && j == 0) ? T(0) : W[e] / -k2;
 }
 
 // ---------------------------------------------------------------------------
@@ -368,6 +417,7 @@ static void check_grid_y(int nrhs) {
 }
 
 static bool pow2_interior(int n) { return n >= 1 && n <= FDMGPU_MAX_N && ilog2_exact(n + 1) > 0; }
+static bool pow2_periodic(int n) { return n >= 2 && n <= 512 && ilog2_exact(n) > 0; }
 
 // ---------------------------------------------------------------------------
 // LaplCube
@@ -388,6 +438,8 @@ struct CubePlan {
     DevBuf ztab64, ztab32;  // partitioned z-solve factors per mode
     int zmode = 1;          // 1: table-driven z-solve when the line splits, 0: factors computed per solve
     int dst_tc = 0;         // 1: plain FP32 DST passes of 32- or 64-point axes on the tensor cores
+    bool periodic = false;  // all three axes periodic (real FFTs, divide, inverse FFTs)
+    DevBuf ptw_x, ptw_y, ptw_z, plam_x, plam_y, plam_z;
     DevBuf tc_img_x, tc_img_y, tc_err;
     int zm64 = 0, zP64 = 0, zm32 = 0, zP32 = 0;
     DevBuf hin, hout;
@@ -450,7 +502,57 @@ struct CubePlan {
         last_nrhs = 1;
     }
 
+    // periodic plan (LaplCube<T,check,periodic^3>, src/lapl_cube.h:58-100):
+    // the reference shares lm_y with x (resp. z) when the point counts match
+    void init_periodic() {
+        slx = std::sqrt(2. / lx);
+        sly = std::sqrt(2. / ly);
+        if (dtype == FDMGPU_F64) {
+            upload_ptwiddles<double>(ptw_x, nx);
+            upload_ptwiddles<double>(ptw_y, ny);
+            upload_ptwiddles<double>(ptw_z, nz);
+            upload_plambda<double>(plam_y, ny, dy);
+            upload_plambda<double>(plam_x, nx, nx == ny ? dy : dx);
+            upload_plambda<double>(plam_z, nz, nz == ny ? dy : dz);
+        } else {
+            upload_ptwiddles<float>(ptw_x, nx);
+            upload_ptwiddles<float>(ptw_y, ny);
+            upload_ptwiddles<float>(ptw_z, nz);
+            upload_plambda<float>(plam_y, ny, dy);
+            upload_plambda<float>(plam_x, nx, nx == ny ? dy : dx);
+            upload_plambda<float>(plam_z, nz, nz == ny ? dy : dz);
+        }
+    }
+
+    // forward transforms z, y, x (scale h*sqrt(2/l)), divide, inverse x, y,
+    // z (scale sqrt(2/l)), as src/lapl_cube.cpp:9-142 orders them
+    template <typename T>
+    void run_periodic(T* ans, const T* rhs, int nrhs, cudaStream_t st) {
+        const double slz = std::sqrt(2. / lz);
+        const long long v = vol();
+        PLineGeom gx{(long long)nrhs * nz * ny, 1, nx, 0, 1};
+        PLineGeom gy{(long long)nrhs * nz * nx, nx, (long long)nx * ny, 1, nx};
+        PLineGeom gz{(long long)nrhs * nx * ny, (long long)nx * ny, v, 1, (long long)nx * ny};
+        launch_pfft<T, false>(rhs, ans, gz, nz, ptw_z.p, dz * slz, st);
+        launch_pfft<T, false>(ans, ans, gy, ny, ptw_y.p, dy * sly, st);
+        launch_pfft<T, false>(ans, ans, gx, nx, ptw_x.p, dx * slx, st);
+        {
+            const long long total = v * nrhs;
+            FDM_TIMED("pdivide", st);
+            k_pdivide<T><<<(unsigned)((total + 255) / 256), 256, 0, st>>>(ans, nx, ny, nz, total, (const T*)plam_x.p,
+                                                                           (const T*)plam_y.p, (const T*)plam_z.p);
+            FDM_LAUNCH_CHECK();
+        }
+        launch_pfft<T, true>(ans, ans, gx, nx, ptw_x.p, slx, st);
+        launch_pfft<T, true>(ans, ans, gy, ny, ptw_y.p, sly, st);
+        launch_pfft<T, true>(ans, ans, gz, nz, ptw_z.p, slz, st);
+    }
+
     void init() {
+        if (periodic) {
+            init_periodic();
+            return;
+        }
         slx = std::sqrt(2. / lx);
         sly = std::sqrt(2. / ly);
         const double slz = std::sqrt(2. / lz);
@@ -537,6 +639,12 @@ struct CubePlan {
         check_grid_y(nrhs);
         last_stream = st;
         last_nrhs = nrhs;
+        if (periodic) {
+            last_sweeps = 0;
+            if (dtype == FDMGPU_F64) run_periodic<double>((double*)ans, (const double*)rhs, nrhs, st);
+            else run_periodic<float>((float*)ans, (const float*)rhs, nrhs, st);
+            return;
+        }
         if (precision == FDMGPU_PLAIN) {
             last_sweeps = 0;
             if (dtype == FDMGPU_F64) run_plain<double>((double*)ans, (const double*)rhs, nrhs, tx64, ty64, lamx64,
@@ -1171,16 +1279,24 @@ int fdmgpu_lapl_cube_create(fdmgpu_lapl_cube** h, int dtype, int bc_flags, doubl
     if (!h) FDM_FAIL(FDMGPU_EINVAL, "null handle pointer");
     *h = nullptr;
     if (dtype != FDMGPU_F64 && dtype != FDMGPU_F32) FDM_FAIL(FDMGPU_EINVAL, "bad dtype %d", dtype);
-    if (bc_flags != FDMGPU_DIRICHLET) FDM_FAIL(FDMGPU_ENOTSUP, "only Dirichlet boundaries are implemented");
-    if (!pow2_interior(nx) || !pow2_interior(ny) || !pow2_interior(nz))
+    if (bc_flags != FDMGPU_DIRICHLET && bc_flags != FDMGPU_PERIODIC)
+        FDM_FAIL(FDMGPU_ENOTSUP, "boundary flags %d: all Dirichlet (0) or all periodic (7)", bc_flags);
+    const bool periodic = bc_flags == FDMGPU_PERIODIC;
+    if (periodic) {
+        if (!pow2_periodic(nx) || !pow2_periodic(ny) || !pow2_periodic(nz))
+            FDM_FAIL(FDMGPU_ESIZE, "verify((1<<n) == N) failed: periodic n must be a power of two in [2, 512] "
+                                   "(got %d,%d,%d)", nx, ny, nz);
+    } else if (!pow2_interior(nx) || !pow2_interior(ny) || !pow2_interior(nz)) {
         FDM_FAIL(FDMGPU_ESIZE, "verify((1<<n) == N) failed: n+1 must be a power of two and n <= %d (got %d,%d,%d)",
                  FDMGPU_MAX_N, nx, ny, nz);
+    }
     if (!(dx > 0 && dy > 0 && dz > 0 && lx > 0 && ly > 0 && lz > 0))
         FDM_FAIL(FDMGPU_EINVAL, "spacings and lengths must be positive");
     std::unique_ptr<fdmgpu_lapl_cube> p(new fdmgpu_lapl_cube());
     CubePlan& c = p->plan;
     c.dtype = dtype; c.nx = nx; c.ny = ny; c.nz = nz;
     c.dx = dx; c.dy = dy; c.dz = dz; c.lx = lx; c.ly = ly; c.lz = lz;
+    c.periodic = periodic;
     c.init();
     *h = p.release();
     FDM_API_END
@@ -1192,6 +1308,8 @@ int fdmgpu_lapl_cube_set_precision(fdmgpu_lapl_cube* h, int precision, double to
     if (precision != FDMGPU_PLAIN && precision != FDMGPU_MIXED) FDM_FAIL(FDMGPU_EINVAL, "bad precision %d", precision);
     if (precision == FDMGPU_MIXED && h->plan.dtype != FDMGPU_F64)
         FDM_FAIL(FDMGPU_ENOTSUP, "mixed precision needs FP64 arrays");
+    if (precision == FDMGPU_MIXED && h->plan.periodic)
+        FDM_FAIL(FDMGPU_ENOTSUP, "the periodic LaplCube is plain precision only");
     h->plan.precision = precision;
     h->plan.tol = tol > 0 ? tol : 1e-10;
     h->plan.max_sweeps = max_sweeps >= 0 ? max_sweeps : 3;

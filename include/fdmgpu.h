@@ -55,9 +55,14 @@ enum {
                          accurate residual, iterative refinement             */
 };
 
-/* boundary flags per axis (bit 0 = x, 1 = y, 2 = z); only Dirichlet (0) is
- * implemented; periodic flags return FDMGPU_ENOTSUP. */
-enum { FDMGPU_DIRICHLET = 0 };
+/* boundary flags per axis (bit 0 = x, 1 = y, 2 = z, set = periodic).  The
+ * reference instantiates all-Dirichlet and all-periodic LaplCube
+ * (src/lapl_cube.cpp:174-182); mixed flags return FDMGPU_ENOTSUP.  Periodic:
+ * n = nx, ny, nz points per axis, each a power of two <= 512, arrays of
+ * nz*ny*nx points as the reference's periodic callers pass them
+ * (ut/ut_lapl_cube.cpp:156-243); plain precision only; the zero mode of
+ * the answer is set to 0 (src/lapl_cube.cpp:82-84). */
+enum { FDMGPU_DIRICHLET = 0, FDMGPU_PERIODIC = 7 };
 
 #define FDMGPU_MAX_N 1023 /* largest interior size per axis */
 

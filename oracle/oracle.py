@@ -156,6 +156,9 @@ class Reference:
         L.ref_nscube_get.restype = c_long
         L.ref_nscube_get.argtypes = [c_void_p, c_int, _dp]
         L.ref_nscube_destroy.argtypes = [c_void_p]
+        L.ref_pfft1_d.argtypes = [_dp, _dp, c_double, c_int]
+        L.ref_pfft_d.argtypes = [_dp, _dp, c_double, c_int]
+        L.ref_lapl_cube_periodic_d.argtypes = [c_int] * 3 + [c_double] * 6 + [_dp, _dp]
         L.ref_nscubef_create.restype = c_void_p
         L.ref_nscubef_create.argtypes = [c_int, c_int] + [c_double] * 9
         L.ref_nscubef_step.argtypes = [c_void_p, c_int]
@@ -175,6 +178,27 @@ class Reference:
         r = np.ascontiguousarray(rhs, np.float64)
         ans = np.zeros_like(r)
         self.L.ref_lapl_cube_solve_d(nx, ny, nz, dx, dy, dz, lx, ly, lz, 0, _p(ans), _p(r), int(reps))
+        return ans
+
+    def pfft1(self, s: np.ndarray, dx: float = 1.0) -> np.ndarray:
+        """FFT<double>::pFFT_1: values -> coefficients (src/fft.cpp:108)."""
+        S = np.zeros(s.size)
+        a = np.array(s, np.float64)
+        self.L.ref_pfft1_d(_p(S), _p(a), dx, s.size)
+        return S
+
+    def pfft(self, s: np.ndarray, dx: float = 1.0) -> np.ndarray:
+        """FFT<double>::pFFT: coefficients -> values (src/fft.cpp:195)."""
+        S = np.zeros(s.size)
+        a = np.array(s, np.float64)
+        self.L.ref_pfft_d(_p(S), _p(a), dx, s.size)
+        return S
+
+    def lapl_cube_periodic(self, rhs, dx, dy, dz, lx, ly, lz) -> np.ndarray:
+        nz, ny, nx = rhs.shape
+        r = np.ascontiguousarray(rhs, np.float64)
+        ans = np.zeros_like(r)
+        self.L.ref_lapl_cube_periodic_d(nx, ny, nz, dx, dy, dz, lx, ly, lz, _p(ans), _p(r))
         return ans
 
     def lapl_rect(self, rhs, dx, dy, lx, ly, fft2: bool = False) -> np.ndarray:
@@ -206,6 +230,65 @@ class Reference:
 
 _port = None
 _ref = None
+
+
+def pfft1(f: np.ndarray, dx: float, axis: int = -1) -> np.ndarray:
+    """Restatement of FFT<T>::pFFT_1 (src/fft.cpp:108-194) along `axis`:
+    S[k] = dx sum_j f_j cos(2 pi jk/n) for k <= n/2 and S[n-k] =
+    dx sum_j f_j sin(2 pi jk/n) for 0 < k < n/2 (the layout its recursion
+    produces; checked against the compiled reference in tests)."""
+    f = np.moveaxis(np.asarray(f, np.float64), axis, -1)
+    n = f.shape[-1]
+    F = np.fft.rfft(f, axis=-1) * dx
+    S = np.empty_like(f)
+    S[..., : n // 2 + 1] = F.real
+    k = np.arange(1, n // 2)
+    S[..., n - k] = -F.imag[..., k]
+    return np.moveaxis(S, -1, axis)
+
+
+def pfft(S: np.ndarray, dx: float, axis: int = -1) -> np.ndarray:
+    """Restatement of FFT<T>::pFFT (src/fft.cpp:195-212), the inverse layout:
+    f_j = dx (S_0/2 + sum_{0<k<n/2} (S_k cos + S_{n-k} sin)(2 pi jk/n)
+    + S_{n/2}/2 cos(pi j))."""
+    S = np.moveaxis(np.asarray(S, np.float64), axis, -1)
+    n = S.shape[-1]
+    H = np.zeros(S.shape[:-1] + (n // 2 + 1,), complex)
+    H[..., 0] = S[..., 0]
+    H[..., n // 2] = S[..., n // 2]
+    k = np.arange(1, n // 2)
+    H[..., k] = S[..., k] - 1j * S[..., n - k]
+    f = np.fft.irfft(H, n=n, axis=-1) * (n * dx / 2)
+    return np.moveaxis(f, -1, axis)
+
+
+def lapl_cube_periodic(rhs, dx, dy, dz, lx, ly, lz) -> np.ndarray:
+    """Restatement of LaplCube<double,check,periodic^3>::solve
+    (src/lapl_cube.cpp:9-142; eigenvalues :145-172): pFFT_1 along z, y, x
+    with scale h sqrt(2/l), divide by -(lz_i + ly_k + lx_j) with
+    l_p = 4/h^2 sin^2(p pi/n) (lm_y shared with x / z when the point counts
+    match), zero mode := 0, pFFT along x, y, z with scale sqrt(2/l).  The
+    reference addresses its {1..n} tensors with periodic wrap from index 0,
+    a cyclic shift that the shift-invariant solve undoes."""
+    r = np.asarray(rhs, np.float64)
+    nz, ny, nx = r.shape
+    slx, sly, slz = np.sqrt(2 / lx), np.sqrt(2 / ly), np.sqrt(2 / lz)
+
+    def lam(n, h):
+        return 4.0 / (h * h) * np.sin(np.arange(n) * np.pi / n) ** 2
+    ly_ = lam(ny, dy)
+    lx_ = ly_ if nx == ny else lam(nx, dx)
+    lz_ = ly_ if nz == ny else lam(nz, dz)
+    a = pfft1(r, dz * slz, axis=0)
+    a = pfft1(a, dy * sly, axis=1)
+    a = pfft1(a, dx * slx, axis=2)
+    k2 = lz_[:, None, None] + ly_[None, :, None] + lx_[None, None, :]
+    with np.errstate(divide="ignore", invalid="ignore"):
+        a = a / -k2
+    a[0, 0, 0] = 0.0
+    a = pfft(a, slx, axis=2)
+    a = pfft(a, sly, axis=1)
+    return pfft(a, slz, axis=0)
 
 
 def vtk_text(u, v, w, nx, ny, nz, origin, spacing, time_index) -> str:

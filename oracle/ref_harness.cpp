@@ -106,6 +106,34 @@ int ref_sfft_f(float* S, float* s, float dx, int N) {
     return 0;
 }
 
+// Periodic real transforms of the reference: values -> coefficients
+// (FFT<T>::pFFT_1, src/fft.cpp:108-194) and back (FFT<T>::pFFT,
+// src/fft.cpp:195-212).  Both overwrite their input.
+int ref_pfft1_d(double* S, double* s, double dx, int N) {
+    FFTTable<double> t(N);
+    FFT<double> ft(t, N);
+    ft.pFFT_1(S, s, dx);
+    return 0;
+}
+int ref_pfft_d(double* S, double* s, double dx, int N) {
+    FFTTable<double> t(N);
+    FFT<double> ft(t, N);
+    ft.pFFT(S, s, dx);
+    return 0;
+}
+
+// Periodic LaplCube<double,false,periodic^3> (src/lapl_cube.h:9-106 with
+// F = tensor_flags<periodic,periodic,periodic>): rhs/ans hold n_z*n_y*n_x
+// points, x fastest, as the reference's periodic test passes them
+// (ut/ut_lapl_cube.cpp:156-243: &RHS[0][0][0] of a {0..n-1}^3 tensor).
+int ref_lapl_cube_periodic_d(int nx, int ny, int nz, double dx, double dy, double dz, double lx, double ly,
+                             double lz, double* ans, double* rhs) {
+    using F = tensor_flags<tensor_flag::periodic, tensor_flag::periodic, tensor_flag::periodic>;
+    LaplCube<double, false, F> lapl(dx, dy, dz, lx, ly, lz, nx, ny, nz);
+    lapl.solve(ans, rhs);
+    return 0;
+}
+
 int ref_cyclic_reduction_d(double* d, double* e, double* f, double* b, int q, int n, int general) {
     if (general) cyclic_reduction_general(d, e, f, b, q, n);
     else cyclic_reduction(d, e, f, b, q, n);

@@ -140,6 +140,26 @@ def main():
     c["ut31_err"] = np.abs(out - exact).max() / np.abs(exact).max()
     np.savez_compressed(OUT / "lapl_cube.npz", **c)
 
+    # periodic LaplCube<double,false,periodic^3> and its transforms
+    # (FFT<T>::pFFT_1 / pFFT); arrays of n_z*n_y*n_x as the periodic callers
+    # pass them (ut/ut_lapl_cube.cpp:156-243)
+    per = {}
+    rng = np.random.default_rng(21)
+    for N in (8, 64, 512):
+        s = rng.uniform(-1, 1, N)
+        per["pf_s_%d" % N] = s
+        per["pf1_%d" % N] = R.pfft1(s, 0.7)
+        per["pf_%d" % N] = R.pfft(s, 0.3)
+    for name, shape, h in (("c16", (16, 16, 16), (0.3, 0.3, 0.3)), ("a8x16x32", (8, 16, 32), (0.1, 0.2, 0.3)),
+                           ("b32x16x16", (32, 16, 16), (0.2, 0.1, 0.05))):
+        nz, ny, nx = shape
+        f = rng.standard_normal(shape)
+        args = (h[0], h[1], h[2], nx * h[0], ny * h[1], nz * h[2])
+        per["rhs_" + name] = f
+        per["args_" + name] = np.array(args)
+        per["ans_" + name] = R.lapl_cube_periodic(f, *args)
+    np.savez_compressed(OUT / "lapl_cube_periodic.npz", **per)
+
     # LaplRect / LaplRectFFT2
     r = {}
     rng = np.random.default_rng(5)

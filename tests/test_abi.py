@@ -42,7 +42,10 @@ def test_status_codes_without_gpu(native):
     assert b"verify" in lib.fdmgpu_last_error()
     assert lib.fdmgpu_lapl_cube_create(byref(h), N.F64, 0, .1, .1, .1, 3.2, 3.2, 3.2, 2047, 31, 31) == N.ESIZE
     assert lib.fdmgpu_lapl_cube_create(byref(h), 7, 0, .1, .1, .1, 3.2, 3.2, 3.2, 31, 31, 31) == N.EINVAL
-    assert lib.fdmgpu_lapl_cube_create(byref(h), N.F64, 7, .1, .1, .1, 3.2, 3.2, 3.2, 31, 31, 31) == N.ENOTSUP
+    # mixed boundary flags are not instantiated by the reference
+    assert lib.fdmgpu_lapl_cube_create(byref(h), N.F64, 3, .1, .1, .1, 3.2, 3.2, 3.2, 31, 31, 31) == N.ENOTSUP
+    # all periodic: n must be a power of two
+    assert lib.fdmgpu_lapl_cube_create(byref(h), N.F64, 7, .1, .1, .1, 3.2, 3.2, 3.2, 31, 32, 32) == N.ESIZE
     assert lib.fdmgpu_lapl_cube_create(None, N.F64, 0, .1, .1, .1, 3.2, 3.2, 3.2, 31, 31, 31) == N.EINVAL
     assert lib.fdmgpu_lapl_cube_create(byref(h), N.F64, 0, -.1, .1, .1, 3.2, 3.2, 3.2, 31, 31, 31) == N.EINVAL
     assert lib.fdmgpu_lapl_rect_create(byref(h), N.F64, 0, .1, .1, 3.2, 3.2, 20, 62) == N.ESIZE

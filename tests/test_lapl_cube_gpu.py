@@ -222,3 +222,71 @@ def test_mixed_tensor_core_dst_vs_plain(cuda, shape):
         assert not m.device_failed()
         err = (torch.linalg.norm(b - a) / torch.linalg.norm(a)).item()
         assert err <= tol, (shape, tol, err)
+
+
+def _periodic_manufactured(nx, ny, nz, h, seed):
+    """u = sum of 6 exact discrete Fourier modes; f = periodic 7-point
+    Laplacian of u.  The solve returns u minus its mean (zero here)."""
+    rng = np.random.default_rng(seed)
+    z, y, x = np.meshgrid(np.arange(nz), np.arange(ny), np.arange(nx), indexing="ij")
+    u = np.zeros((nz, ny, nx))
+    for _ in range(6):
+        kx, ky, kz = rng.integers(0, nx // 2), rng.integers(0, ny // 2), rng.integers(1, nz // 2)
+        ph = rng.uniform(0, 2 * np.pi)
+        u += rng.standard_normal() * np.cos(2 * np.pi * (kx * x / nx + ky * y / ny + kz * z / nz) + ph)
+
+    def d2(a, ax, hh):
+        return (np.roll(a, 1, ax) - 2 * a + np.roll(a, -1, ax)) / (hh * hh)
+    f = d2(u, 2, h[0]) + d2(u, 1, h[1]) + d2(u, 0, h[2])
+    return f, u
+
+
+def test_periodic_vs_reference(cuda, golden):
+    """All-periodic LaplCube (LaplCube<T,check,periodic^3>) against the
+    reference's outputs, FP64 and FP32."""
+    g = golden("lapl_cube_periodic")
+    for name, (nz, ny, nx) in (("c16", (16, 16, 16)), ("a8x16x32", (8, 16, 32)), ("b32x16x16", (32, 16, 16))):
+        args = tuple(g["args_" + name]) + (nx, ny, nz)
+        rhs, ref = g["rhs_" + name], g["ans_" + name]
+        lc = LaplCube(*args, periodic=True)
+        ans = np.zeros_like(rhs)
+        lc.solve(ans, rhs)
+        assert rel_l2(ans, ref) <= 1e-12, name
+        lc32 = LaplCube(*args, periodic=True, dtype=np.float32)
+        a32 = np.zeros(rhs.shape, np.float32)
+        lc32.solve(a32, rhs.astype(np.float32))
+        assert rel_l2(a32.astype(np.float64), ref) <= 1e-5, name
+
+
+@pytest.mark.parametrize("shape", [(64, 64, 64), (128, 32, 256), (512, 8, 16)])
+def test_periodic_manufactured_and_batched(cuda, shape):
+    """Exact discrete modes come back to round-off at larger sizes (x- and
+    z-extents up to 512), and batched volumes equal single solves."""
+    import torch
+    nx, ny, nz = shape
+    h = (2 * np.pi / nx, 0.7 * 2 * np.pi / ny, 1.3 * 2 * np.pi / nz)
+    # distinct spacings only take effect when the point counts differ from ny
+    args = (h[0], h[1], h[2], nx * h[0], ny * h[1], nz * h[2], nx, ny, nz)
+    hx_eff = h[1] if nx == ny else h[0]
+    hz_eff = h[1] if nz == ny else h[2]
+    f, u = _periodic_manufactured(nx, ny, nz, (hx_eff, h[1], hz_eff), seed=nx + nz)
+    lc = LaplCube(*args, periodic=True)
+    tf = torch.tensor(np.stack([f, 2 * f]), device=cuda)
+    out = torch.empty_like(tf)
+    lc.solve_device(out, tf, nrhs=2)
+    one = torch.empty_like(tf[0])
+    lc.solve_device(one, tf[0].contiguous())
+    torch.cuda.synchronize()
+    a = out.cpu().numpy()
+    assert rel_l2(a[0], u - u.mean()) <= 1e-12
+    assert rel_l2(a[1], 2 * (u - u.mean())) <= 1e-12
+    assert torch.equal(one, out[0])
+
+
+def test_periodic_errors(cuda):
+    with pytest.raises(FdmError) as e:
+        LaplCube(0.1, 0.1, 0.1, 1.6, 1.6, 1.5, 16, 16, 15, periodic=True)
+    assert e.value.status == 2
+    with pytest.raises(FdmError) as e:
+        LaplCube(0.1, 0.1, 0.1, 1.6, 1.6, 1.6, 16, 16, 16, periodic=True, precision="mixed")
+    assert e.value.status == 6

@@ -121,3 +121,25 @@ def test_nscube_matches_reference(port, golden):
 def test_nscube_rejects_bad_size(port):
     with pytest.raises(ValueError):
         port.nscube(32, 32, 250.0, 0.01)
+
+
+def test_periodic_transforms_match_reference(golden):
+    """The restated pFFT_1 / pFFT layouts against the reference's own
+    FFT<double> on the fixture vectors."""
+    from oracle.oracle import pfft, pfft1
+    g = golden("lapl_cube_periodic")
+    for N in (8, 64, 512):
+        s = g["pf_s_%d" % N]
+        assert np.abs(pfft1(s, 0.7) - g["pf1_%d" % N]).max() <= 1e-13 * N
+        assert np.abs(pfft(s, 0.3) - g["pf_%d" % N]).max() <= 1e-13 * N
+        # round trip of the reference's convention: pFFT_1(pFFT(s, 1), 2/N) = s
+        assert np.abs(pfft1(pfft(s, 1.0), 2.0 / N) - s).max() <= 1e-14 * N
+
+
+def test_periodic_lapl_cube_matches_reference(golden):
+    from oracle.oracle import lapl_cube_periodic
+    g = golden("lapl_cube_periodic")
+    for name in ("c16", "a8x16x32", "b32x16x16"):
+        ans = lapl_cube_periodic(g["rhs_" + name], *g["args_" + name])
+        ref = g["ans_" + name]
+        assert np.linalg.norm(ans - ref) / np.linalg.norm(ref) <= 1e-14, name
