@@ -254,6 +254,53 @@ def measure_uneven_batch(torch, fdm_gb300, workloads, stream, dev, count=512, to
     }
 
 
+# published Poisson-stage times of the reference's N-body driver, a periodic
+# LaplCube<double> solve per step (test/nbody_result.org:9, 24, 39)
+PERIODIC_PUBLISHED_MS = {32: {"ryzen_3700x_16t": 1.26, "apple_m1": 1.7},
+                         64: {"ryzen_3700x_16t": 6.90, "apple_m1": 8.87},
+                         128: {"ryzen_3700x_16t": 62.50, "apple_m1": 68.83}}
+
+
+def measure_periodic(torch, fdm_gb300, stream, reps=50):
+    """Periodic LaplCube<double> solve (FP64) at 32^3, 64^3, 128^3: device
+    time per solve (CUDA events, median of reps) and the host-array call the
+    reference's N-body driver makes (copies in and out included)."""
+    import numpy as np
+    out = {}
+    for n in (32, 64, 128):
+        h = 1.0 / n
+        lc = fdm_gb300.LaplCube(h, h, h, 1.0, 1.0, 1.0, n, n, n, periodic=True)
+        rng = np.random.default_rng(n)
+        f = rng.standard_normal((n, n, n))
+        f -= f.mean()
+        df = torch.tensor(f, device="cuda")
+        du = torch.empty_like(df)
+        for _ in range(3):
+            lc.solve_device(du, df, stream=stream)
+        stream.synchronize()
+        times = []
+        for _ in range(reps):
+            e0 = torch.cuda.Event(enable_timing=True)
+            e1 = torch.cuda.Event(enable_timing=True)
+            e0.record(stream)
+            lc.solve_device(du, df, stream=stream)
+            e1.record(stream)
+            e1.synchronize()
+            times.append(e0.elapsed_time(e1))
+        ans = np.zeros_like(f)
+        lc.solve(ans, f)
+        t0 = time.perf_counter()
+        for _ in range(10):
+            lc.solve(ans, f)
+        host_ms = (time.perf_counter() - t0) * 100.0
+        dev_ms = statistics.median(times)
+        pub = PERIODIC_PUBLISHED_MS[n]
+        out["%d^3" % n] = {"device_ms": dev_ms, "host_call_ms": host_ms, "published_cpu_ms": pub,
+                           "speedup_vs_published_m1_host_call": pub["apple_m1"] / host_ms}
+        lc.close()
+    return out
+
+
 SERVE_RATES = (100, 300, 1000, 3000, 5000)
 
 
@@ -293,8 +340,7 @@ def measure_serving(torch, fdm_gb300, workloads, dev, rates=SERVE_RATES, seconds
     ref_sq = {sh: float(np.sum(np.square(r))) for sh, r in ref.items()}
 
     def check(sh, buf):
-        # numpy's own reductions: BLAS-backed norms are not safe to call from
-        # several threads of this pool at once
+        # relative L2 error of one answer against the FP64 form
         d = buf.numpy() - ref[sh]
         return sh, buf, math.sqrt(float(np.sum(d * d)) / ref_sq[sh])
 
@@ -579,6 +625,7 @@ def main():
     del out, f
     torch.cuda.empty_cache()
     uneven = measure_uneven_batch(torch, fdm_gb300, workloads, stream, dev)
+    periodic = measure_periodic(torch, fdm_gb300, stream)
     rates = tuple(int(x) for x in args.serve_rates.split(",")) if args.serve_rates else SERVE_RATES
     serving = measure_serving(torch, fdm_gb300, workloads, dev, rates=rates) if not args.no_serving else None
 
@@ -611,6 +658,7 @@ def main():
         "plain_fp64_gpu": {"value": plain_rate, "unit": UNIT},
         "nscube_63cubed": {"ms_per_step": ns_ms, "steps_timed": 200, "Re": 250.0, "dt": 0.01},
         "uneven_batch": uneven,
+        "periodic_poisson": periodic,
         "serving": serving,
         "clocks": clocks,
     }
