@@ -3,6 +3,7 @@
 // through a small key/value reader (any object with the reference Config's
 // get(section, name, default) overloads works); step() runs on the GPU.
 // Fields are copied to host in the reference tensor layout with field().
+// T = double is NSCube<double>, T = float NSCube<float>.
 #pragma once
 
 #include <cmath>
@@ -21,8 +22,7 @@ public:
           x2(c.get("ns", "x2", M_PI)), y2(c.get("ns", "y2", M_PI)), z2(c.get("ns", "z2", M_PI)),
           U0(c.get("ns", "u0", 1.0)), Re(c.get("ns", "Re", 1.0)), dt(c.get("ns", "dt", 0.001)),
           nx(c.get("ns", "nx", 32)), ny(c.get("ns", "nx", 32)), nz(c.get("ns", "nz", 32)) {
-        static_assert(sizeof(T) == sizeof(double), "NSCube is implemented for double");
-        fdmgpu_verify(fdmgpu_nscube_create(&h_, FDMGPU_F64, nx, nz, x1, y1, z1, x2, y2, z2, U0, Re, dt),
+        fdmgpu_verify(fdmgpu_nscube_create(&h_, fdmgpu_dtype<T>::value, nx, nz, x1, y1, z1, x2, y2, z2, U0, Re, dt),
                       "fdmgpu_nscube_create");
     }
     ~NSCube() { fdmgpu_nscube_destroy(h_); }

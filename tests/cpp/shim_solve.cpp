@@ -1,0 +1,84 @@
+// A reference-style caller of the C++ shims (include/fdm_gb300/*.h): the
+// code a user of fdm::LaplCube / fdm::NSCube keeps, with the include and
+// link line changed.  Reads right-hand sides from binary files, writes the
+// answers next to them.
+//
+//   shim_solve dirichlet <nx> <ny> <nz> <dx> <dy> <dz> <lx> <ly> <lz> <rhs> <ans>
+//   shim_solve periodic  <nx> <ny> <nz> <dx> <dy> <dz> <lx> <ly> <lz> <rhs> <ans>
+//   shim_solve nscube    <n> <steps> <out_u>
+#include <cstdio>
+#include <cstdlib>
+#include <cstring>
+#include <string>
+#include <vector>
+
+#include "fdm_gb300/lapl_cube.h"
+#include "fdm_gb300/ns_cube.h"
+
+namespace {
+
+std::vector<double> read_all(const char* path, size_t n) {
+    std::vector<double> v(n);
+    FILE* f = fopen(path, "rb");
+    if (!f || fread(v.data(), sizeof(double), n, f) != n) {
+        fprintf(stderr, "cannot read %s\n", path);
+        exit(2);
+    }
+    fclose(f);
+    return v;
+}
+
+void write_all(const char* path, const std::vector<double>& v) {
+    FILE* f = fopen(path, "wb");
+    if (!f || fwrite(v.data(), sizeof(double), v.size(), f) != v.size()) {
+        fprintf(stderr, "cannot write %s\n", path);
+        exit(2);
+    }
+    fclose(f);
+}
+
+// the reference's Config::get(section, key, default) shape
+struct Cfg {
+    int n;
+    double get(const char*, const char* key, double def) const {
+        if (!strcmp(key, "Re")) return 250.0;
+        if (!strcmp(key, "dt")) return 0.01;
+        return def;
+    }
+    int get(const char*, const char* key, int def) const {
+        if (!strcmp(key, "nx") || !strcmp(key, "nz")) return n;
+        return def;
+    }
+};
+
+}  // namespace
+
+int main(int argc, char** argv) {
+    if (argc < 2) return 1;
+    const std::string mode = argv[1];
+    if (mode == "nscube" && argc == 5) {
+        Cfg c{atoi(argv[2])};
+        fdm::NSCube<double, false> ns(c);
+        for (int i = 0; i < atoi(argv[3]); i++) ns.step();
+        write_all(argv[4], ns.field(FDMGPU_NS_U));
+        return 0;
+    }
+    if (argc != 13) return 1;
+    const int nx = atoi(argv[2]), ny = atoi(argv[3]), nz = atoi(argv[4]);
+    const double dx = atof(argv[5]), dy = atof(argv[6]), dz = atof(argv[7]);
+    const double lx = atof(argv[8]), ly = atof(argv[9]), lz = atof(argv[10]);
+    std::vector<double> rhs = read_all(argv[11], (size_t)nx * ny * nz), ans(rhs.size());
+    if (mode == "dirichlet") {
+        fdm::LaplCube<double, true> lapl(dx, dy, dz, lx, ly, lz, nx, ny, nz);  // src/lapl_cube.h:58
+        lapl.solve(&ans[0], &rhs[0]);
+    } else if (mode == "periodic") {
+        using P = fdm::tensor_flags<fdm::tensor_flag::periodic, fdm::tensor_flag::periodic,
+                                    fdm::tensor_flag::periodic>;
+        fdm::LaplCube<double, false, P> lapl(dx, dy, dz, lx, ly, lz, nx, ny, nz);
+        lapl.solve(&ans[0], &rhs[0]);
+    } else {
+        return 1;
+    }
+    write_all(argv[12], ans);
+    return 0;
+}

@@ -1,0 +1,53 @@
+"""The header-only C++ shims (include/fdm_gb300/*.h) as a reference caller
+uses them: a program written against fdm::LaplCube / fdm::NSCube compiles
+and links against libfdmgpu.so with only the include and link line changed
+(CPU), and gives the reference's answers (GPU)."""
+import shutil
+import subprocess
+from pathlib import Path
+
+import numpy as np
+import pytest
+
+from tests.helpers import rel_l2
+
+ROOT = Path(__file__).resolve().parents[1]
+
+
+def _build(tmp_path, native) -> Path:
+    if not shutil.which("g++"):
+        pytest.skip("g++ not found")
+    exe = tmp_path / "shim_solve"
+    lib = ROOT / "fdm_gb300"
+    subprocess.run(["g++", "-std=c++17", "-O1", "-I", str(ROOT / "include"), str(ROOT / "tests/cpp/shim_solve.cpp"),
+                    "-o", str(exe), "-L", str(lib), "-lfdmgpu", "-Wl,-rpath," + str(lib)], check=True)
+    return exe
+
+
+def test_shim_program_compiles_and_links(tmp_path, native):
+    exe = _build(tmp_path, native)
+    assert exe.exists()
+
+
+@pytest.mark.gpu
+def test_shim_program_matches_reference(tmp_path, native, cuda, golden):
+    exe = _build(tmp_path, native)
+    g = golden("lapl_cube")
+    rhs = g["aniso_rhs"]
+    (tmp_path / "rhs").write_bytes(np.ascontiguousarray(rhs).tobytes())
+    subprocess.run([str(exe), "dirichlet", "15", "15", "7", *[repr(float(v)) for v in g["aniso_args"]],
+                    str(tmp_path / "rhs"), str(tmp_path / "ans")], check=True)
+    ans = np.frombuffer((tmp_path / "ans").read_bytes()).reshape(rhs.shape)
+    assert rel_l2(ans, g["aniso_ans"]) <= 1e-12
+    p = golden("lapl_cube_periodic")
+    rhs = p["rhs_a8x16x32"]
+    (tmp_path / "prhs").write_bytes(np.ascontiguousarray(rhs).tobytes())
+    subprocess.run([str(exe), "periodic", "32", "16", "8", *[repr(float(v)) for v in p["args_a8x16x32"]],
+                    str(tmp_path / "prhs"), str(tmp_path / "pans")], check=True)
+    ans = np.frombuffer((tmp_path / "pans").read_bytes()).reshape(rhs.shape)
+    assert rel_l2(ans, p["ans_a8x16x32"]) <= 1e-12
+    ns = golden("ns_cube")
+    subprocess.run([str(exe), "nscube", "15", "20", str(tmp_path / "u")], check=True)
+    u = np.frombuffer((tmp_path / "u").read_bytes())
+    ref = ns["n15_s20_u"]
+    assert np.abs(u - ref).max() <= 1e-12 * max(1.0, np.abs(ref).max())
