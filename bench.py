@@ -250,7 +250,7 @@ def measure_uneven_batch(torch, fdm_gb300, workloads, stream, dev, count=512, to
         "rel_l2_vs_fp64_max": max(errs), "tune_s": tune_s,
         "chunks": sorted(set(g["chunk"] for g in sched)),
         "ztable_groups": sum(g["ztable"] for g in sched),
-        "tensor_core_dst_groups": sum(g["dst_tc"] for g in sched),
+        "tensor_core_dst_groups": sum(1 for g in sched if g["dst_tc"]),
     }
 
 

@@ -173,7 +173,7 @@ static void launch_rg(const Tin* in, Tout* out, int nx, int ny, int nz, int nvol
 }
 
 // ---------------------------------------------------------------------------
-// Tensor-core DST (N = 32, 64): the pre-swizzled TF32 high / low image of
+// Tensor-core DST (N = 32, 64, 128): the pre-swizzled TF32 high / low image of
 // the zero-padded sine matrix, and the launcher
 // ---------------------------------------------------------------------------
 static std::vector<float> tc_sine_image(int N) {
@@ -194,16 +194,23 @@ static std::vector<float> tc_sine_image(int N) {
     return img;
 }
 
-static bool tc_supported(int N) { return N == 32 || N == 64; }
+static bool tc_supported(int N) { return N == 32 || N == 64 || N == 128; }
+
+template <int N, int AXIS>
+static auto tc_kernel() {
+    if constexpr (N == 128) return k_sine_tc128<AXIS>;
+    else return k_sine_tc<N, AXIS>;
+}
 
 template <int N, int AXIS>
 static void launch_tc_n(const float* in, float* out, const SineTcGeom& g, const float* img, float scale, int* err,
                         cudaStream_t st) {
     using C = TcCfg<N>;
+    const auto kern = tc_kernel<N, AXIS>();
     static int grid_cap = 0;
     if (!grid_cap) {
-        FDM_CUDA(cudaFuncSetAttribute(k_sine_tc<N, AXIS>, cudaFuncAttributeMaxDynamicSharedMemorySize, C::kSmem));
-        FDM_CUDA(cudaFuncSetAttribute(k_sine_tc<N, AXIS>, cudaFuncAttributePreferredSharedMemoryCarveout, 100));
+        FDM_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, C::kSmem));
+        FDM_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributePreferredSharedMemoryCarveout, 100));
         // resident CTAs per SM from the kernel's own registers and shared
         // memory, and tensor memory (512 columns per SM across CTAs)
         int dev = 0, sms = 0, smem_sm = 0, regs_sm = 0;
@@ -212,7 +219,7 @@ static void launch_tc_n(const float* in, float* out, const SineTcGeom& g, const 
         FDM_CUDA(cudaDeviceGetAttribute(&smem_sm, cudaDevAttrMaxSharedMemoryPerMultiprocessor, dev));
         FDM_CUDA(cudaDeviceGetAttribute(&regs_sm, cudaDevAttrMaxRegistersPerMultiprocessor, dev));
         cudaFuncAttributes fa;
-        FDM_CUDA(cudaFuncGetAttributes(&fa, k_sine_tc<N, AXIS>));
+        FDM_CUDA(cudaFuncGetAttributes(&fa, kern));
         const int smem_cta = C::kSmem + (int)fa.sharedSizeBytes + 1024;  // + the per-CTA reservation
         const int regs_cta = ((fa.numRegs + 7) / 8 * 8) * kTcThreads;
         int per_sm = std::min(smem_sm / smem_cta, regs_sm / std::max(regs_cta, 1));
@@ -225,7 +232,7 @@ static void launch_tc_n(const float* in, float* out, const SineTcGeom& g, const 
     const unsigned grid = (unsigned)((tiles + rounds - 1) / std::max<long long>(rounds, 1));
     if (grid == 0) return;
     FDM_TIMED(AXIS == 0 ? "sine_x_tc" : "sine_y_tc", st);
-    k_sine_tc<N, AXIS><<<grid, kTcThreads, C::kSmem, st>>>(in, out, g, img, scale, err);
+    kern<<<grid, kTcThreads, C::kSmem, st>>>(in, out, g, img, scale, err);
     FDM_LAUNCH_CHECK();
 }
 
@@ -241,7 +248,8 @@ static void launch_sine_tc(int N, const float* in, float* out, long long lines, 
     g.plane = (long long)nx * (N - 1);
     if (N == 32) return launch_tc_n<32, AXIS>(in, out, g, img, (float)scale, err, st);
     if (N == 64) return launch_tc_n<64, AXIS>(in, out, g, img, (float)scale, err, st);
-    FDM_FAIL(FDMGPU_ESIZE, "tensor-core DST supports N = 32, 64 (got %d)", N);
+    if (N == 128) return launch_tc_n<128, AXIS>(in, out, g, img, (float)scale, err, st);
+    FDM_FAIL(FDMGPU_ESIZE, "tensor-core DST supports N = 32, 64, 128 (got %d)", N);
 }
 
 template <typename Tin, typename T, typename Tout, int AXIS, int MODE = kPlain>
@@ -437,7 +445,8 @@ struct CubePlan {
     DevBuf work32, uhi, ulo, norms, work64;
     DevBuf ztab64, ztab32;  // partitioned z-solve factors per mode
     int zmode = 1;          // 1: table-driven z-solve when the line splits, 0: factors computed per solve
-    int dst_tc = 0;         // 1: plain FP32 DST passes of 32- or 64-point axes on the tensor cores
+    int dst_tc = 0;         // bit 0 / bit 1: plain FP32 DST passes along x / y on the tensor cores (32-, 64-,
+                            // 128-point axes)
     bool periodic = false;  // all three axes periodic (real FFTs, divide, inverse FFTs)
     DevBuf ptw_x, ptw_y, ptw_z, plam_x, plam_y, plam_z;
     DevBuf tc_img_x, tc_img_y, tc_err;
@@ -588,12 +597,12 @@ struct CubePlan {
 
     long long vol() const { return (long long)nx * ny * nz; }
 
-    // plain FP32 DST pass along AXIS, on the tensor cores when enabled and
-    // the axis has 32 or 64 points
+    // plain FP32 DST pass along AXIS, on the tensor cores when enabled for
+    // the axis and it has 32, 64 or 128 points
     template <int AXIS>
     void sine32(const float* in, float* out, int nrhs, double scale, cudaStream_t st) {
         const int N = (AXIS == 0 ? nx : ny) + 1;
-        if (dst_tc && tc_supported(N)) {
+        if (((dst_tc >> AXIS) & 1) && tc_supported(N)) {
             DevBuf& img = AXIS == 0 ? tc_img_x : tc_img_y;
             if (!img.p) {
                 std::vector<float> h = tc_sine_image(N);
@@ -983,7 +992,8 @@ struct BatchPlan {
     // time each schedule candidate of every group on its data; keep the best
     // that keeps the tolerance.  Candidates: right-hand sides per launch
     // sequence x z-solve variant (factor table / per-solve factors) x DST
-    // passes (FFT / tensor cores, for 32- and 64-point axes).  A variant is
+    // passes per axis (FFT / tensor cores, for 32-, 64-, 128-point axes).  A
+    // variant is
     // accurate enough when its first-sweep correction estimate e (the FP32
     // solve's relative error) predicts 10 e^(sweeps+1) <= tol; with no sweep
     // only the default variants qualify.
@@ -998,8 +1008,9 @@ struct BatchPlan {
             int bc = m, bz = 1, bt = 0;
             const bool mixed = precision == FDMGPU_MIXED;
             const int sweeps = mixed ? gr.plan->sweeps_for_tol() : -1;
-            const bool tc_ok = mixed && (tc_supported(gr.nx + 1) || tc_supported(gr.ny + 1));
-            for (int tc = 0; tc <= (tc_ok ? 1 : 0); tc++) {
+            const int tc_axes = mixed ? ((tc_supported(gr.nx + 1) ? 1 : 0) | (tc_supported(gr.ny + 1) ? 2 : 0)) : 0;
+            for (int tc = 0; tc <= 3; tc++) {
+                if (tc & ~tc_axes) continue;
                 for (int zm = 1; zm >= 0; zm--) {
                     const bool is_default = zm == 1 && tc == 0;
                     if (!is_default && mixed && sweeps == 0) continue;
@@ -1536,7 +1547,7 @@ int fdmgpu_sine_tc_device(int N, int axis, int nx, long long count, double scale
                           void* stream) {
     FDM_API_BEGIN
     if (!d_out || !d_in) FDM_FAIL(FDMGPU_EINVAL, "null argument");
-    if (!tc_supported(N)) FDM_FAIL(FDMGPU_ESIZE, "tensor-core DST supports N = 32, 64 (got %d)", N);
+    if (!tc_supported(N)) FDM_FAIL(FDMGPU_ESIZE, "tensor-core DST supports N = 32, 64, 128 (got %d)", N);
     if (count < 1 || (axis != 0 && axis != 1) || (axis == 1 && nx < 1))
         FDM_FAIL(FDMGPU_EINVAL, "bad axis, nx or count");
     cudaStream_t st = (cudaStream_t)stream;
@@ -1562,7 +1573,7 @@ int fdmgpu_sine_tc_device(int N, int axis, int nx, long long count, double scale
 int fdmgpu_lapl_cube_set_schedule(fdmgpu_lapl_cube* h, int ztable, int dst_tc) {
     FDM_API_BEGIN
     if (!h) FDM_FAIL(FDMGPU_EINVAL, "null handle");
-    if ((ztable != 0 && ztable != 1) || (dst_tc != 0 && dst_tc != 1)) FDM_FAIL(FDMGPU_EINVAL, "flags must be 0 or 1");
+    if ((ztable != 0 && ztable != 1) || dst_tc < 0 || dst_tc > 3) FDM_FAIL(FDMGPU_EINVAL, "ztable 0/1, dst_tc 0..3");
     h->plan.zmode = ztable;
     h->plan.dst_tc = dst_tc;
     FDM_API_END

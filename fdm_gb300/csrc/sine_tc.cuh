@@ -1,4 +1,4 @@
-// DST-I of short lines (N = 32, 64: n = N-1 = 31, 63 points) as a dense
+// DST-I of short lines (N = 32, 64, 128: n = N-1 = 31, 63, 127 points) as a dense
 // contraction on the 5th-generation tensor cores.
 //
 //   Y[l][k] = scale * sum_j X[l][j] sin(pi (j+1)(k+1) / N),  j, k < n
@@ -34,11 +34,14 @@ template <int N>
 struct TcCfg {
     static constexpr int n = N - 1;
     static constexpr int M = 128;                          // lines per tile
+    static constexpr int KB = N > 64 ? 64 : N;             // K values of the line tile held at a time
+    static constexpr int NKB = N / KB;                     // K blocks per tile
     static constexpr int kSBytes = N * N * 4;              // one TF32 part of S
-    static constexpr int kABytes = M * N * 4;              // one TF32 part of the line tile
-    static constexpr int kStage = M * (N + 1) * 4;         // AXIS 0 output staging (reuses the A parts)
+    static constexpr int kABytes = M * KB * 4;             // one TF32 part of a K block of the line tile
+    static constexpr int kStage = M * n * 4;               // AXIS 0 output staging (reuses the A parts)
     static constexpr int kSmem = 1024 /*align*/ + 2 * kSBytes + 2 * kABytes + 64;
     static_assert(2 * kABytes >= kStage, "staging must fit in the A parts");
+    static_assert(2 * kABytes >= M * (KB + 1) * 4, "K-block staging must fit in the A parts");
 };
 
 // byte offset of element (r, k) in a K-major, 128-byte-swizzled operand of
@@ -313,6 +316,203 @@ __global__ void __launch_bounds__(kTcThreads, (N == 32 ? 3 : 2))
                     ((float4*)dst)[q] = ((const float4*)raw_out)[q];
                 } else {
                     for (int i = 4 * q; i < cnt; i++) dst[i] = raw_out[i];
+                }
+            }
+            __syncthreads();
+        }
+        tc_fence_after();
+    }
+    if (s_fail && tid == 0) atomicExch(err, 1);
+    tc_fence_before();
+    __syncthreads();
+    if (warp == 0) asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(N));
+#endif
+}
+
+// N = 128: the split-TF32 sine matrix (128 KB) stays in shared memory and
+// the line tile goes through in two K blocks of 64 (64 KB for both parts);
+// the MMAs of a block accumulate onto the previous block's in TMEM.  One
+// CTA per SM (193 KB of shared memory).  Each K block is read coalesced
+// into a padded staging image, then redistributed as half-rows (AXIS 0), or
+// read straight into half-rows (AXIS 1); the next block's loads are in
+// registers while the current block's MMAs run.
+template <int AXIS>
+__global__ void __launch_bounds__(kTcThreads, 1)
+    k_sine_tc128(const float* in, float* out, SineTcGeom g, const float* __restrict__ simg, float scale, int* err) {
+#if defined(__CUDA_ARCH__)
+    constexpr int N = 128;
+    using C = TcCfg<N>;
+    constexpr int n = C::n, M = C::M, T = kTcThreads, KB = C::KB, NKB = C::NKB;
+    constexpr int KH = KB / 2;          // values of a half-row of one K block
+    constexpr int KS = KB + 1;          // padded row stride of the AXIS 0 staging
+    constexpr int kLd = M * KB / T;     // AXIS 0 loads per thread per K block
+    extern __shared__ unsigned char tc_raw[];
+    unsigned char* base = (unsigned char*)(((uintptr_t)tc_raw + 1023) & ~(uintptr_t)1023);
+    unsigned char* s_hi = base;
+    unsigned char* s_lo = base + C::kSBytes;
+    unsigned char* a_hi = base + 2 * C::kSBytes;
+    unsigned char* a_lo = a_hi + C::kABytes;
+    float* raw = (float*)a_hi;  // AXIS 0: one K block as read / the tile as written
+    uint64_t* mbar = (uint64_t*)(a_hi + 2 * C::kABytes);
+    uint32_t* tslot = (uint32_t*)(mbar + 1);
+    __shared__ int s_fail;
+
+    const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+    const int r = tid & (M - 1), kh = (tid >> 7) * KH;
+    if (tid == 0) {
+        s_fail = 0;
+        asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(tc_smem(mbar)), "r"(1));
+    }
+    {
+        const float4* src = (const float4*)simg;
+        float4* dst = (float4*)s_hi;
+        for (int i = tid; i < 2 * C::kSBytes / 16; i += T) dst[i] = __ldg(src + i);
+    }
+    if (warp == 0) {
+        asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(tc_smem(tslot)),
+                     "r"(N));
+        asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;");
+    }
+    tc_fence_async_smem();
+    tc_fence_before();
+    __syncthreads();
+    tc_fence_after();
+    const uint32_t tmem = *tslot;
+    const uint32_t idesc = (1u << 4) | (2u << 7) | (2u << 10) | ((uint32_t)(N >> 3) << 17) | ((uint32_t)(M >> 4) << 24);
+    const uint32_t sa_hi = tc_smem(a_hi), sa_lo = tc_smem(a_lo), ss_hi = tc_smem(s_hi), ss_lo = tc_smem(s_lo);
+    const uint32_t mb = tc_smem(mbar);
+    const long long ntiles = (g.lines + M - 1) / M;
+    uint32_t phase = 0;
+
+    constexpr int kRegs = AXIS == 0 ? kLd : KH;
+    float v[kRegs];
+    // loads of K block kb of a tile into registers
+    auto fetch = [&](long long tile, int kb) {
+        const long long L0 = tile * M;
+        const int rows = (int)(g.lines - L0 < M ? g.lines - L0 : M);
+        if (AXIS == 0) {
+#pragma unroll
+            for (int j = 0; j < kLd; j++) {
+                const int e = tid + j * T, line = e / KB, c = e - line * KB, k = kb * KB + c;
+                v[j] = (line < rows && k < n) ? in[(L0 + line) * n + k] : 0.f;
+            }
+        } else {
+            const bool ok = r < rows;
+            const long long L = L0 + r;
+            const long long p = ok ? L / g.nx : 0;
+            const float* src = in + p * g.plane + (ok ? L - p * g.nx : 0);
+#pragma unroll
+            for (int j = 0; j < KH; j++) {
+                const int k = kb * KB + kh + j;
+                v[j] = (ok && k < n) ? src[(long long)k * g.nx] : 0.f;
+            }
+        }
+    };
+    // this thread's half-row of the current K block -> TF32 parts
+    auto put_half = [&](const float* w) {
+        const uint32_t rowoff = ((uint32_t)r >> 3) * 1024u + ((uint32_t)r & 7) * 128u;
+#pragma unroll
+        for (int c = 0; c < KH / 4; c++) {
+            const int k = kh + 4 * c;  // within the block
+            const uint32_t o = (uint32_t)(k >> 5) * (uint32_t)M * 128u + rowoff +
+                               ((((uint32_t)k >> 2) & 7) ^ ((uint32_t)r & 7)) * 16u;
+            float4 h, l;
+            h.x = tc_tf32(w[4 * c]);     l.x = tc_tf32(w[4 * c] - h.x);
+            h.y = tc_tf32(w[4 * c + 1]); l.y = tc_tf32(w[4 * c + 1] - h.y);
+            h.z = tc_tf32(w[4 * c + 2]); l.z = tc_tf32(w[4 * c + 2] - h.z);
+            h.w = tc_tf32(w[4 * c + 3]); l.w = tc_tf32(w[4 * c + 3] - h.w);
+            *(float4*)(a_hi + o) = h;
+            *(float4*)(a_lo + o) = l;
+        }
+    };
+    if (blockIdx.x < ntiles) fetch(blockIdx.x, 0);
+
+    for (long long tile = blockIdx.x; tile < ntiles; tile += gridDim.x) {
+        const long long L0 = tile * M;
+        const int rows = (int)(g.lines - L0 < M ? g.lines - L0 : M);
+#pragma unroll 1
+        for (int kb = 0; kb < NKB; kb++) {
+            if (AXIS == 0) {
+#pragma unroll
+                for (int j = 0; j < kLd; j++) {
+                    const int e = tid + j * T, line = e / KB, c = e - line * KB;
+                    raw[line * KS + c] = v[j];
+                }
+                __syncthreads();
+                float w[KH];
+#pragma unroll
+                for (int j = 0; j < KH; j++) w[j] = raw[r * KS + kh + j];
+                __syncthreads();
+                put_half(w);
+            } else {
+                put_half(v);
+            }
+            tc_fence_async_smem();
+            tc_fence_before();
+            __syncthreads();
+            tc_fence_after();
+            if (tid == 0) {
+#pragma unroll 1
+                for (int part = 0; part < 3; part++) {
+                    const uint32_t a = part == 2 ? sa_lo : sa_hi;
+                    const uint32_t b = part == 1 ? ss_lo : ss_hi;
+#pragma unroll
+                    for (int s = 0; s < KB / 8; s++) {
+                        const int k0 = s * 8;               // within the block (A)
+                        const int kg = kb * KB + k0;        // within S (B)
+                        const uint32_t koff_a = (uint32_t)(k0 >> 5) * M * 128u + (uint32_t)((k0 & 31) >> 3) * 32u;
+                        const uint32_t koff_b = (uint32_t)(kg >> 5) * N * 128u + (uint32_t)((kg & 31) >> 3) * 32u;
+                        tc_mma_tf32(tmem, tc_desc(a + koff_a), tc_desc(b + koff_b), idesc, (kb | part | s) != 0);
+                    }
+                }
+                asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(mb)
+                             : "memory");
+            }
+            if (kb + 1 < NKB) fetch(tile, kb + 1);
+            else if (tile + gridDim.x < ntiles) fetch(tile + gridDim.x, 0);
+            {
+                unsigned spins = 0;
+                bool done = false;
+                while (!(done = tc_try_wait(mb, phase)) && ++spins < kTcSpinLimit) {
+                }
+                if (!done) s_fail = 1;
+            }
+            phase ^= 1;
+            tc_fence_after();
+            __syncthreads();
+            if (s_fail) break;
+        }
+        if (s_fail) break;
+        // ---- accumulators -> output: warp w reads lanes 32(w%4).. and half (w/4) of the columns
+        const int er = (warp & 3) * 32 + lane;
+        const long long L = L0 + er;
+        const int cbeg = (warp >> 2) * (N / 2);
+#pragma unroll 1
+        for (int c0 = cbeg; c0 < cbeg + N / 2; c0 += 16) {
+            float y[16];
+            tc_ld16(tmem + ((uint32_t)((warp & 3) * 32) << 16) + (uint32_t)c0, y);
+            if (AXIS == 0) {
+#pragma unroll
+                for (int j = 0; j < 16; j++)
+                    if (c0 + j < n) raw[er * n + c0 + j] = y[j] * scale;
+            } else if (er < rows) {
+                const long long p = L / g.nx;
+                float* dst = out + p * g.plane + (L - p * g.nx);
+#pragma unroll
+                for (int j = 0; j < 16; j++)
+                    if (c0 + j < n) dst[(long long)(c0 + j) * g.nx] = y[j] * scale;
+            }
+        }
+        tc_fence_before();
+        __syncthreads();
+        if (AXIS == 0) {
+            const int cnt = rows * n;
+            float* dst = out + L0 * n;
+            for (int q = tid; 4 * q < cnt; q += T) {
+                if (4 * q + 3 < cnt) {
+                    ((float4*)dst)[q] = ((const float4*)raw)[q];
+                } else {
+                    for (int i = 4 * q; i < cnt; i++) dst[i] = raw[i];
                 }
             }
             __syncthreads();

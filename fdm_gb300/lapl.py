@@ -113,11 +113,13 @@ class LaplCube:
                                                         _dev_ptr(rhs, eb, self.count * nrhs), int(nrhs),
                                                         _stream_ptr(stream)))
 
-    def set_schedule(self, ztable: bool = True, dst_tc: bool = False) -> None:
+    def set_schedule(self, ztable: bool = True, dst_tc=False) -> None:
         """Mixed-form schedule: per-mode z factor table (default) or factors
-        per solve; plain FP32 DST passes of 32/64-point axes on the tensor
-        cores (dst_tc) or as FFTs (default)."""
-        N.check(self._lib.fdmgpu_lapl_cube_set_schedule(self._h, int(bool(ztable)), int(bool(dst_tc))))
+        per solve; plain FP32 DST passes of 32/64/128-point axes on the
+        tensor cores or as FFTs (default).  dst_tc: True for both axes, or a
+        mask (1 = x, 2 = y)."""
+        mask = 3 if dst_tc is True else int(dst_tc)
+        N.check(self._lib.fdmgpu_lapl_cube_set_schedule(self._h, int(bool(ztable)), mask))
 
     def device_failed(self) -> bool:
         """True if a tensor-core pass of this solver gave up waiting for its
@@ -294,7 +296,7 @@ def sine_transform_device(out, inp, N_points: int, nlines: int, scale: float = 1
 
 def sine_transform_tc_device(out, inp, N_points: int, count: int, scale: float = 1.0, axis: int = 0, nx: int = 1,
                              stream=None) -> None:
-    """FP32 DST-I on the tensor cores (N_points = 32 or 64).  axis 0: `count`
+    """FP32 DST-I on the tensor cores (N_points = 32, 64 or 128).  axis 0: `count`
     contiguous lines of N-1 values; axis 1: `count` planes of (N-1) x nx
     values transformed along their rows (stride nx).  Synchronous."""
     lib = N.load()

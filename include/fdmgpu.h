@@ -145,8 +145,9 @@ int fdmgpu_lapl_cube_last_info(fdmgpu_lapl_cube* h, int* sweeps, double* est, in
 /* bytes of device scratch the handle holds */
 int fdmgpu_lapl_cube_scratch_bytes(fdmgpu_lapl_cube* h, size_t* bytes);
 /* schedule of the mixed form: ztable = 1 uses the per-mode z factor table
- * (default), 0 computes the factors per solve; dst_tc = 1 runs the plain
- * FP32 DST passes of 32- and 64-point axes on the tensor cores (default 0) */
+ * (default), 0 computes the factors per solve; dst_tc bit 0 / bit 1 runs the
+ * plain FP32 DST passes along x / y on the tensor cores when that axis has
+ * 32, 64 or 128 points (default 0: FFTs) */
 int fdmgpu_lapl_cube_set_schedule(fdmgpu_lapl_cube* h, int ztable, int dst_tc);
 /* 1 in *failed if a tensor-core pass of this handle gave up waiting for its
  * MMAs (synchronises the device) */
@@ -174,8 +175,8 @@ int fdmgpu_batch_solve(fdmgpu_batch* h, void* const* d_ans, const void* const* d
 /* groups formed and kernel launches one graph launch replays */
 int fdmgpu_batch_info(fdmgpu_batch* h, int* groups, int* launches_per_solve);
 /* schedule of one group: sizes, members, chunk, 1 = table-driven z-solve,
- * 1 = DST passes on the tensor cores, and its tuned time in ms (0 before
- * tuning) */
+ * the tensor-core axes (bit 0 x, bit 1 y), and its tuned time in ms (0
+ * before tuning) */
 int fdmgpu_batch_schedule(fdmgpu_batch* h, int group, int* n3, int* members, int* chunk, int* ztable,
                           int* dst_tc, double* tuned_ms);
 int fdmgpu_batch_destroy(fdmgpu_batch* h);
@@ -208,7 +209,7 @@ int fdmgpu_lapl_rect_destroy(fdmgpu_lapl_rect* h);
  * src/cyclic_reduction.h:20-107, src/asp_gauss.cpp:185-207). */
 int fdmgpu_sine_device(int dtype, int N, int nlines, double scale,
                        void* d_out, const void* d_in, void* stream);
-/* DST-I of FP32 lines of N-1 points (N = 32 or 64) as a dense contraction
+/* DST-I of FP32 lines of N-1 points (N = 32, 64 or 128) as a dense contraction
  * with the sine matrix on the tensor cores (split TF32, FP32 accumulation;
  * no counterpart in the reference).  axis 0: `count` contiguous lines;
  * axis 1: `count` planes of (N-1) rows x nx, transformed along the rows.

@@ -98,7 +98,7 @@ def _dst_matrix(N):
     return np.sin(np.pi * np.outer(j, j) / N)
 
 
-@pytest.mark.parametrize("N", [32, 64])
+@pytest.mark.parametrize("N", [32, 64, 128])
 def test_sine_tc_lines_vs_fp64(cuda, N):
     """Tensor-core DST (split TF32, FP32 accumulation) of contiguous lines,
     including a ragged last tile, against the FP64 matrix product."""
@@ -120,7 +120,7 @@ def test_sine_tc_lines_vs_fp64(cuda, N):
     assert torch.equal(tx, torch.tensor(y.astype(np.float32), device=cuda))
 
 
-@pytest.mark.parametrize("N,nx", [(32, 37), (64, 63)])
+@pytest.mark.parametrize("N,nx", [(32, 37), (64, 63), (128, 129)])
 def test_sine_tc_columns_vs_fp64(cuda, N, nx):
     """Along y: planes of (N-1) x nx, transformed along the stride-nx rows."""
     import torch
