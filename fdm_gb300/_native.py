@@ -79,6 +79,10 @@ _SIGS = [
      [c_void_p, c_int, POINTER(c_int), POINTER(c_int), POINTER(c_int), POINTER(c_int), POINTER(c_int),
       POINTER(c_double)]),
     ("fdmgpu_batch_destroy", c_int, [c_void_p]),
+    ("fdmgpu_lapl_cyl_create", c_int, [POINTER(c_void_p), c_int, c_int] + [c_double] * 5 + [c_int] * 3),
+    ("fdmgpu_lapl_cyl_solve", c_int, [c_void_p, c_void_p, c_void_p]),
+    ("fdmgpu_lapl_cyl_solve_device", c_int, [c_void_p, c_void_p, c_void_p, c_int, c_void_p]),
+    ("fdmgpu_lapl_cyl_destroy", c_int, [c_void_p]),
     ("fdmgpu_lapl_rect_create", c_int,
      [POINTER(c_void_p), c_int, c_int] + [c_double] * 4 + [c_int] * 2),
     ("fdmgpu_lapl_rect_solve", c_int, [c_void_p, c_void_p, c_void_p]),

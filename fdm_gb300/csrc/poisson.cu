@@ -1110,6 +1110,151 @@ struct fdmgpu_lapl_rect {
 namespace fdmgpu {
 
 // ---------------------------------------------------------------------------
+// LaplCyl3FFT2: Poisson in a cylindrical annulus (src/lapl_cyl.h:178-262,
+// src/lapl_cyl.cpp:10-166).  Arrays (nphi, nz, nr), r fastest.  Periodic
+// transform along phi, DST (Dirichlet z) or periodic transform (periodic z)
+// along z, then per (phi-mode, z-mode) a radial tridiagonal system with
+// variable coefficients, eliminated without row swaps (the reference's
+// LAPACK gttrf / gttrs; the matrices are diagonally dominant so partial
+// pivoting does not swap); the elimination factors are prepared once per
+// plan, laid out [j][system] so that the threads of a warp (consecutive
+// systems) read them coalesced.
+// ---------------------------------------------------------------------------
+template <typename T>
+__global__ void k_cyl_rsolve(T* W, long long nsys, int nr, const T* __restrict__ fact, const T* __restrict__ piv,
+                             const T* __restrict__ up) {
+    const long long s = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (s >= nsys) return;
+    T* b = W + s * nr;
+    const long long ns = nsys;
+    T prev = b[0];
+    for (int j = 0; j + 1 < nr; j++) {
+        const T f = fact[(long long)j * ns + s];
+        const T cur = b[j + 1] - f * prev;
+        b[j + 1] = cur;
+        prev = cur;
+    }
+    T x = b[nr - 1] / piv[(long long)(nr - 1) * ns + s];
+    b[nr - 1] = x;
+    for (int j = nr - 2; j >= 0; j--) {
+        x = (b[j] - up[j] * x) / piv[(long long)j * ns + s];
+        b[j] = x;
+    }
+}
+
+struct CylPlan {
+    int dtype = FDMGPU_F64;
+    bool periodic_z = false;
+    int nr, nz, nphi;
+    double dr, dz, r0, lr, lz;
+    AxisTables<double> tz64;
+    AxisTables<float> tz32;
+    DevBuf tw_phi, tw_z, fact, piv, up;
+
+    long long vol() const { return (long long)nphi * nz * nr; }
+    long long nsys() const { return (long long)nphi * nz; }
+
+    template <typename T>
+    void build() {
+        const double dphi = 2 * M_PI / nphi, dphi2 = dphi * dphi, dr2 = dr * dr, dz2 = dz * dz;
+        const int zpoints = periodic_z ? nz : nz + 1;
+        std::vector<T> lm_phi(nphi), lm_z(nz);
+        for (int i = 0; i < nphi; i++) {
+            const double sn = std::sin(i * dphi * 0.5);
+            lm_phi[i] = (T)(4.0 / dphi2 * (sn * sn));
+        }
+        for (int kk = 0; kk < nz; kk++) {
+            // z1..zn: 1..nz (Dirichlet), 0..nz-1 (periodic)
+            const int k = periodic_z ? kk : kk + 1;
+            const double sn = periodic_z ? std::sin(k * M_PI / zpoints) : std::sin(k * M_PI * 0.5 / zpoints);
+            lm_z[kk] = (T)(4. / dz2 * (sn * sn));
+        }
+        const long long ns = nsys();
+        std::vector<T> hf((size_t)nr * ns), hp((size_t)nr * ns), hu(nr), hl(nr);
+        for (int j = 1; j <= nr; j++) {
+            const double r = r0 + j * dr;
+            hl[j - 1] = (T)((r - 0.5 * dr) / dr2 / r);
+            hu[j - 1] = (T)((r + 0.5 * dr) / dr2 / r);
+        }
+        for (int i = 0; i < nphi; i++)
+            for (int kk = 0; kk < nz; kk++) {
+                const long long sidx = (long long)i * nz + kk;
+                // D_j = -2/dr^2 - lm_phi/r/r - lm_z (src/lapl_cyl.cpp:142), LU without swaps
+                T dd = 0;
+                for (int j = 1; j <= nr; j++) {
+                    const double r = r0 + j * dr;
+                    const T d = (T)(-2 / dr2 - lm_phi[i] / r / r - lm_z[kk]);
+                    if (j == 1) {
+                        dd = d;
+                    } else {
+                        const T f = hl[j - 1] / dd;
+                        hf[(size_t)(j - 2) * ns + sidx] = f;
+                        dd = d - f * hu[j - 2];
+                    }
+                    hp[(size_t)(j - 1) * ns + sidx] = dd;
+                }
+            }
+        FDM_CUDA(cudaMemcpy(fact.get(hf.size() * sizeof(T)), hf.data(), hf.size() * sizeof(T), cudaMemcpyHostToDevice));
+        FDM_CUDA(cudaMemcpy(piv.get(hp.size() * sizeof(T)), hp.data(), hp.size() * sizeof(T), cudaMemcpyHostToDevice));
+        FDM_CUDA(cudaMemcpy(up.get(hu.size() * sizeof(T)), hu.data(), hu.size() * sizeof(T), cudaMemcpyHostToDevice));
+        upload_ptwiddles<T>(tw_phi, nphi);
+        if (periodic_z) upload_ptwiddles<T>(tw_z, nz);
+        else if (sizeof(T) == 8) tz64.build(nz + 1);
+        else tz32.build(nz + 1);
+    }
+
+    void init() {
+        if (dtype == FDMGPU_F64) build<double>();
+        else build<float>();
+    }
+
+    template <typename T>
+    void run(T* ans, const T* rhs, int nrhs, cudaStream_t st) {
+        const double inv_sqrt_pi = 0.56418958354775629;  // the reference's SQRT_M_1_PI
+        const double dphi = 2 * M_PI / nphi, slz = std::sqrt(2. / lz);
+        const long long v = vol(), plane = (long long)nz * nr;
+        PLineGeom gphi{(long long)nrhs * plane, plane, v, 1, plane};
+        PLineGeom gz{(long long)nrhs * nphi * nr, nr, plane, 1, nr};
+        launch_pfft<T, false>(rhs, ans, gphi, nphi, tw_phi.p, (double)(T)(dphi * inv_sqrt_pi), st);
+        if (periodic_z) launch_pfft<T, false>(ans, ans, gz, nz, tw_z.p, dz * slz, st);
+        else launch_sine<T, T, T, 1>(ans, ans, nr, nz, nphi, nrhs, table<T>().view(), dz * slz, st);
+        {
+            const long long ns = nsys();
+            FDM_TIMED("cyl_rsolve", st);
+            for (int v0 = 0; v0 < nrhs; v0++) {
+                k_cyl_rsolve<T><<<(unsigned)((ns + 127) / 128), 128, 0, st>>>(ans + v0 * v, ns, nr, (const T*)fact.p,
+                                                                              (const T*)piv.p, (const T*)up.p);
+                FDM_LAUNCH_CHECK();
+            }
+        }
+        if (periodic_z) launch_pfft<T, true>(ans, ans, gz, nz, tw_z.p, slz, st);
+        else launch_sine<T, T, T, 1>(ans, ans, nr, nz, nphi, nrhs, table<T>().view(), slz, st);
+        launch_pfft<T, true>(ans, ans, gphi, nphi, tw_phi.p, (double)(T)inv_sqrt_pi, st);
+    }
+
+    template <typename T>
+    const AxisTables<T>& table() const;
+
+    void solve_device(void* ans, const void* rhs, int nrhs, cudaStream_t st) {
+        check_grid_y(nrhs);
+        if (dtype == FDMGPU_F64) run<double>((double*)ans, (const double*)rhs, nrhs, st);
+        else run<float>((float*)ans, (const float*)rhs, nrhs, st);
+    }
+};
+template <>
+const AxisTables<double>& CylPlan::table<double>() const { return tz64; }
+template <>
+const AxisTables<float>& CylPlan::table<float>() const { return tz32; }
+
+}  // namespace fdmgpu
+
+struct fdmgpu_lapl_cyl {
+    CylPlan plan;
+};
+
+namespace fdmgpu {
+
+// ---------------------------------------------------------------------------
 // Mixed-precision solve that allocates nothing
 //
 // Some callers cannot allocate device memory when they solve: an application
@@ -1450,6 +1595,52 @@ int fdmgpu_batch_schedule(fdmgpu_batch* h, int group, int* n3, int* members, int
 }
 
 int fdmgpu_batch_destroy(fdmgpu_batch* h) {
+    FDM_API_BEGIN
+    delete h;
+    FDM_API_END
+}
+
+int fdmgpu_lapl_cyl_create(fdmgpu_lapl_cyl** h, int dtype, int periodic_z, double dr, double dz, double r0,
+                           double lr, double lz, int nr, int nz, int nphi) {
+    FDM_API_BEGIN
+    if (!h) FDM_FAIL(FDMGPU_EINVAL, "null handle pointer");
+    *h = nullptr;
+    if (dtype != FDMGPU_F64 && dtype != FDMGPU_F32) FDM_FAIL(FDMGPU_EINVAL, "bad dtype %d", dtype);
+    if (!pow2_periodic(nphi)) FDM_FAIL(FDMGPU_ESIZE, "verify((1<<n) == N) failed: nphi=%d", nphi);
+    if (periodic_z ? !pow2_periodic(nz) : !pow2_interior(nz))
+        FDM_FAIL(FDMGPU_ESIZE, "verify((1<<n) == N) failed: nz=%d (periodic %d)", nz, periodic_z);
+    if (nr < 1 || nr > 4096) FDM_FAIL(FDMGPU_ESIZE, "nr must be in [1, 4096], got %d", nr);
+    if (!(dr > 0 && dz > 0 && r0 >= 0 && lr > 0 && lz > 0)) FDM_FAIL(FDMGPU_EINVAL, "bad geometry");
+    std::unique_ptr<fdmgpu_lapl_cyl> p(new fdmgpu_lapl_cyl());
+    CylPlan& c = p->plan;
+    c.dtype = dtype; c.periodic_z = periodic_z != 0;
+    c.nr = nr; c.nz = nz; c.nphi = nphi;
+    c.dr = dr; c.dz = dz; c.r0 = r0; c.lr = lr; c.lz = lz;
+    c.init();
+    *h = p.release();
+    FDM_API_END
+}
+
+int fdmgpu_lapl_cyl_solve(fdmgpu_lapl_cyl* h, void* ans, const void* rhs) {
+    FDM_API_BEGIN
+    if (!h || !ans || !rhs) FDM_FAIL(FDMGPU_EINVAL, "null argument");
+    CylPlan& c = h->plan;
+    const size_t bytes = (size_t)c.vol() * (c.dtype == FDMGPU_F64 ? 8 : 4);
+    DevBuf din, dout;
+    FDM_CUDA(cudaMemcpy(din.get(bytes), rhs, bytes, cudaMemcpyHostToDevice));
+    c.solve_device(dout.get(bytes), din.p, 1, 0);
+    FDM_CUDA(cudaMemcpy(ans, dout.p, bytes, cudaMemcpyDeviceToHost));
+    FDM_API_END
+}
+
+int fdmgpu_lapl_cyl_solve_device(fdmgpu_lapl_cyl* h, void* d_ans, const void* d_rhs, int nrhs, void* stream) {
+    FDM_API_BEGIN
+    if (!h || !d_ans || !d_rhs) FDM_FAIL(FDMGPU_EINVAL, "null argument");
+    h->plan.solve_device(d_ans, d_rhs, nrhs, (cudaStream_t)stream);
+    FDM_API_END
+}
+
+int fdmgpu_lapl_cyl_destroy(fdmgpu_lapl_cyl* h) {
     FDM_API_BEGIN
     delete h;
     FDM_API_END

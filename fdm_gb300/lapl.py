@@ -235,6 +235,45 @@ class BatchSolver:
             pass
 
 
+class LaplCyl3FFT2:
+    """Poisson in a cylindrical annulus, fdm::LaplCyl3FFT2<T,check,zflag>
+    (src/lapl_cyl.h:178-262, src/lapl_cyl.cpp:10-166): arrays shaped
+    (nphi, nz, nr), r fastest; phi periodic, z Dirichlet or periodic."""
+
+    def __init__(self, dr, dz, r0, lr, lz, nr, nz, nphi, dtype=np.float64, periodic_z=False):
+        self._lib = N.load()
+        self.dtype = np.dtype(dtype)
+        self.nr, self.nz, self.nphi = int(nr), int(nz), int(nphi)
+        self.count = self.nr * self.nz * self.nphi
+        h = c_void_p()
+        N.check(self._lib.fdmgpu_lapl_cyl_create(byref(h), _dtype_code(dtype), int(bool(periodic_z)), float(dr),
+                                                 float(dz), float(r0), float(lr), float(lz), self.nr, self.nz,
+                                                 self.nphi))
+        self._h = h
+
+    def solve(self, ans: np.ndarray, rhs: np.ndarray) -> None:
+        pa = _host_ptr(ans, self.dtype, self.count, True)
+        pr = _host_ptr(np.ascontiguousarray(rhs), self.dtype, self.count, False)
+        N.check(self._lib.fdmgpu_lapl_cyl_solve(self._h, pa, pr))
+
+    def solve_device(self, ans, rhs, nrhs: int = 1, stream=None) -> None:
+        eb = self.dtype.itemsize
+        N.check(self._lib.fdmgpu_lapl_cyl_solve_device(self._h, _dev_ptr(ans, eb, self.count * nrhs),
+                                                       _dev_ptr(rhs, eb, self.count * nrhs), int(nrhs),
+                                                       _stream_ptr(stream)))
+
+    def close(self) -> None:
+        if getattr(self, "_h", None):
+            self._lib.fdmgpu_lapl_cyl_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
 class LaplRect:
     """2-D Dirichlet Poisson solver, fdm::LaplRect<T,check,F>: DST along y,
     tridiagonal solve along x per y-mode (src/lapl_rect.cpp:63-110)."""

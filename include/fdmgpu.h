@@ -181,6 +181,19 @@ int fdmgpu_batch_schedule(fdmgpu_batch* h, int group, int* n3, int* members, int
                           int* dst_tc, double* tuned_ms);
 int fdmgpu_batch_destroy(fdmgpu_batch* h);
 
+/* ---- LaplCyl3FFT2: Poisson in a cylindrical annulus ----------------------
+ * Replaces fdm::LaplCyl3FFT2<T,check,zflag> (src/lapl_cyl.h:178-262,
+ * src/lapl_cyl.cpp:10-166): ctor (dr, dz, r0, lr, lz, nr, nz, nphi), arrays of
+ * nphi x nz x nr points, r fastest (the tensor {0..nphi-1, z1..zn, 1..nr}).
+ * phi periodic (nphi a power of two <= 512); z Dirichlet (nz+1 a power of
+ * two) or periodic (periodic_z, nz a power of two <= 512). */
+typedef struct fdmgpu_lapl_cyl fdmgpu_lapl_cyl;
+int fdmgpu_lapl_cyl_create(fdmgpu_lapl_cyl** h, int dtype, int periodic_z, double dr, double dz, double r0,
+                           double lr, double lz, int nr, int nz, int nphi);
+int fdmgpu_lapl_cyl_solve(fdmgpu_lapl_cyl* h, void* ans, const void* rhs);
+int fdmgpu_lapl_cyl_solve_device(fdmgpu_lapl_cyl* h, void* d_ans, const void* d_rhs, int nrhs, void* stream);
+int fdmgpu_lapl_cyl_destroy(fdmgpu_lapl_cyl* h);
+
 /* ---- LaplRect / LaplRectFFT2: 2-D Dirichlet Poisson ----------------------
  * Replaces fdm::LaplRect<T,check,F> (src/lapl_rect.h:11-73, solve
  * src/lapl_rect.cpp:63-110: DST-y, tridiagonal solve along x per y-mode,

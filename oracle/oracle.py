@@ -159,6 +159,7 @@ class Reference:
         L.ref_pfft1_d.argtypes = [_dp, _dp, c_double, c_int]
         L.ref_pfft_d.argtypes = [_dp, _dp, c_double, c_int]
         L.ref_lapl_cube_periodic_d.argtypes = [c_int] * 3 + [c_double] * 6 + [_dp, _dp]
+        L.ref_lapl_cyl_d.argtypes = [c_int] * 4 + [c_double] * 5 + [_dp, _dp]
         L.ref_nscubef_create.restype = c_void_p
         L.ref_nscubef_create.argtypes = [c_int, c_int] + [c_double] * 9
         L.ref_nscubef_step.argtypes = [c_void_p, c_int]
@@ -199,6 +200,14 @@ class Reference:
         r = np.ascontiguousarray(rhs, np.float64)
         ans = np.zeros_like(r)
         self.L.ref_lapl_cube_periodic_d(nx, ny, nz, dx, dy, dz, lx, ly, lz, _p(ans), _p(r))
+        return ans
+
+    def lapl_cyl(self, rhs, dr, dz, r0, lr, lz, periodic_z: bool = False) -> np.ndarray:
+        """LaplCyl3FFT2<double,false,zflag>::solve; rhs shaped (nphi, nz, nr)."""
+        nphi, nz, nr = rhs.shape
+        r = np.ascontiguousarray(rhs, np.float64)
+        ans = np.zeros_like(r)
+        self.L.ref_lapl_cyl_d(1 if periodic_z else 0, nr, nz, nphi, dr, dz, r0, lr, lz, _p(ans), _p(r))
         return ans
 
     def lapl_rect(self, rhs, dx, dy, lx, ly, fft2: bool = False) -> np.ndarray:
@@ -289,6 +298,60 @@ def lapl_cube_periodic(rhs, dx, dy, dz, lx, ly, lz) -> np.ndarray:
     a = pfft(a, slx, axis=2)
     a = pfft(a, sly, axis=1)
     return pfft(a, slz, axis=0)
+
+
+def dst1(x: np.ndarray, dx: float, axis: int = -1) -> np.ndarray:
+    """FFT<T>::sFFT on the interior entries (src/fft.cpp:294-365): for n
+    points along `axis`, N = n + 1, S_k = dx sum_{j=1}^{n} x_j sin(pi jk/N)."""
+    x = np.moveaxis(np.asarray(x, np.float64), axis, -1)
+    n = x.shape[-1]
+    j = np.arange(1, n + 1)
+    S = np.sin(np.pi * np.outer(j, j) / (n + 1))
+    return np.moveaxis(x @ S * dx, -1, axis)
+
+
+def lapl_cyl(rhs, dr, dz, r0, lr, lz, periodic_z: bool = False) -> np.ndarray:
+    """Restatement of LaplCyl3FFT2<double,check,zflag>::solve
+    (src/lapl_cyl.cpp:10-128, init_solver :130-166) on arrays shaped
+    (nphi, nz, nr), r fastest: pFFT_1 along phi (scale dphi/sqrt(pi)), sFFT
+    (Dirichlet z) or pFFT_1 (periodic z) along z (scale dz sqrt(2/lz)), per
+    (phi-mode i, z-mode k) the radial system D_j = -2/dr^2 - lm_phi_i/r^2 -
+    lm_z_k, L_j = (r - dr/2)/(dr^2 r), U_j = (r + dr/2)/(dr^2 r),
+    r = r0 + j dr, solved by elimination without row swaps (the matrices
+    are diagonally dominant, so partial pivoting does not swap), then the
+    inverse transforms (scales sqrt(2/lz), 1/sqrt(pi))."""
+    f = np.asarray(rhs, np.float64)
+    nphi, nz, nr = f.shape
+    dphi = 2 * np.pi / nphi
+    inv_sqrt_pi = 0.56418958354775629
+    slz = np.sqrt(2.0 / lz)
+    zpoints = nz if periodic_z else nz + 1
+    lm_phi = 4.0 / dphi ** 2 * np.sin(np.arange(nphi) * dphi * 0.5) ** 2
+    if periodic_z:
+        lm_z = 4.0 / dz ** 2 * np.sin(np.arange(nz) * np.pi / zpoints) ** 2
+    else:
+        lm_z = 4.0 / dz ** 2 * np.sin(np.arange(1, nz + 1) * np.pi * 0.5 / zpoints) ** 2
+    a = pfft1(f, dphi * inv_sqrt_pi, axis=0)
+    a = pfft1(a, dz * slz, axis=1) if periodic_z else dst1(a, dz * slz, axis=1)
+    r = r0 + np.arange(1, nr + 1) * dr
+    lo = (r - 0.5 * dr) / (dr * dr) / r
+    up = (r + 0.5 * dr) / (dr * dr) / r
+    out = np.empty_like(a)
+    for i in range(nphi):
+        for k in range(nz):
+            d = -2 / (dr * dr) - lm_phi[i] / r / r - lm_z[k]
+            b = a[i, k].copy()
+            dd = d.copy()
+            for j in range(nr - 1):
+                fact = lo[j + 1] / dd[j]
+                dd[j + 1] -= fact * up[j]
+                b[j + 1] -= fact * b[j]
+            b[nr - 1] /= dd[nr - 1]
+            for j in range(nr - 2, -1, -1):
+                b[j] = (b[j] - up[j] * b[j + 1]) / dd[j]
+            out[i, k] = b
+    out = pfft(out, slz, axis=1) if periodic_z else dst1(out, slz, axis=1)
+    return pfft(out, inv_sqrt_pi, axis=0)
 
 
 def vtk_text(u, v, w, nx, ny, nz, origin, spacing, time_index) -> str:

@@ -23,6 +23,7 @@
 #include "lapl_cube.h"
 #include "lapl_rect.h"
 #include "ns_cube.h"
+#include "lapl_cyl.h"
 #include "cyclic_reduction.h"
 #include "asp_gauss.h"
 #include "config.h"
@@ -47,6 +48,50 @@ extern "C" void sgtsv_(int* n, int* nrhs, float* dl, float* d, float* du,
     *info = 0;
     if (*nrhs != 1) { *info = -2; return; }
     solve_tdiag_linearf_my(b, dl, d, du, *n);
+}
+
+// LAPACK ?gttrf_ / ?gttrs_ (LU of a tridiagonal matrix, then solves) are
+// referenced by LaplCyl3FFT2 (src/lapl_cyl.cpp:75-82, 150-166;
+// src/blas.h:17-22).  Its radial matrices are diagonally dominant
+// (|D| = 2/dr^2 + lm_phi/r^2 + lm_z >= |L| + |U| = 2/dr^2 in the interior,
+// strictly in the first and last rows), so LAPACK's partial pivoting, which
+// swaps only when |dl(i)| > |d(i)|, never swaps; the adapters perform that
+// no-swap elimination: multipliers in dl, updated pivots in d, du2 = 0,
+// ipiv(i) = i.
+template <typename T>
+static void gttrf_noswap(int n, T* dl, T* d, T* du, T* du2, int* ipiv) {
+    for (int i = 0; i < n; i++) ipiv[i] = i + 1;
+    for (int i = 0; i + 2 < n; i++) du2[i] = 0;
+    for (int i = 0; i + 1 < n; i++) {
+        const T fact = dl[i] / d[i];
+        dl[i] = fact;
+        d[i + 1] -= fact * du[i];
+    }
+}
+template <typename T>
+static void gttrs_noswap(int n, const T* dl, const T* d, const T* du, T* b) {
+    for (int i = 0; i + 1 < n; i++) b[i + 1] -= dl[i] * b[i];
+    b[n - 1] /= d[n - 1];
+    if (n > 1) b[n - 2] = (b[n - 2] - du[n - 2] * b[n - 1]) / d[n - 2];
+    for (int i = n - 3; i >= 0; i--) b[i] = (b[i] - du[i] * b[i + 1]) / d[i];
+}
+extern "C" void dgttrf_(int* n, double* dl, double* d, double* du, double* du2, int* ipiv, int* info) {
+    *info = 0;
+    gttrf_noswap(*n, dl, d, du, du2, ipiv);
+}
+extern "C" void sgttrf_(int* n, float* dl, float* d, float* du, float* du2, int* ipiv, int* info) {
+    *info = 0;
+    gttrf_noswap(*n, dl, d, du, du2, ipiv);
+}
+extern "C" void dgttrs_(const char*, int* n, int* nrhs, double* dl, double* d, double* du, double*, int*,
+                        double* b, int*, int* info) {
+    *info = *nrhs == 1 ? 0 : -3;
+    if (!*info) gttrs_noswap(*n, dl, d, du, b);
+}
+extern "C" void sgttrs_(const char*, int* n, int* nrhs, float* dl, float* d, float* du, float*, int*,
+                        float* b, int*, int* info) {
+    *info = *nrhs == 1 ? 0 : -3;
+    if (!*info) gttrs_noswap(*n, dl, d, du, b);
 }
 
 namespace {
@@ -131,6 +176,21 @@ int ref_lapl_cube_periodic_d(int nx, int ny, int nz, double dx, double dy, doubl
     using F = tensor_flags<tensor_flag::periodic, tensor_flag::periodic, tensor_flag::periodic>;
     LaplCube<double, false, F> lapl(dx, dy, dz, lx, ly, lz, nx, ny, nz);
     lapl.solve(ans, rhs);
+    return 0;
+}
+
+// LaplCyl3FFT2<double,false,zflag> (src/lapl_cyl.h:178-262,
+// src/lapl_cyl.cpp:10-166): arrays of nphi x nz' x nr points (r fastest;
+// nz' = nz Dirichlet, nz periodic), as the tensor {0..nphi-1, z1..zn, 1..nr}.
+int ref_lapl_cyl_d(int periodic_z, int nr, int nz, int nphi, double dr, double dz, double r0, double lr,
+                   double lz, double* ans, double* rhs) {
+    if (periodic_z) {
+        LaplCyl3FFT2<double, false, tensor_flag::periodic> lapl(dr, dz, r0, lr, lz, nr, nz, nphi);
+        lapl.solve(ans, rhs);
+    } else {
+        LaplCyl3FFT2<double, false, tensor_flag::none> lapl(dr, dz, r0, lr, lz, nr, nz, nphi);
+        lapl.solve(ans, rhs);
+    }
     return 0;
 }
 

@@ -160,6 +160,22 @@ def main():
         per["ans_" + name] = R.lapl_cube_periodic(f, *args)
     np.savez_compressed(OUT / "lapl_cube_periodic.npz", **per)
 
+    # LaplCyl3FFT2<double,false,zflag> (src/lapl_cyl.cpp:10-166): arrays
+    # (nphi, nz, nr), r fastest
+    cyl = {}
+    rng = np.random.default_rng(33)
+    for name, pz, shape, geo in (("d16x15x20", False, (16, 15, 20), (0.1, 0.2, 0.5)),
+                                 ("p8x16x12", True, (8, 16, 12), (0.05, 0.3, 1.0)),
+                                 ("d32x31x7", False, (32, 31, 7), (0.2, 0.1, 0.0))):
+        nphi, nz, nr = shape
+        dr, dz, r0 = geo
+        args = (dr, dz, r0, (nr + 1) * dr, (nz if pz else nz + 1) * dz)
+        f = rng.standard_normal(shape)
+        cyl["rhs_" + name] = f
+        cyl["args_" + name] = np.array(args)
+        cyl["ans_" + name] = R.lapl_cyl(f, *args, periodic_z=pz)
+    np.savez_compressed(OUT / "lapl_cyl.npz", **cyl)
+
     # LaplRect / LaplRectFFT2
     r = {}
     rng = np.random.default_rng(5)
