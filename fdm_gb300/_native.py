@@ -104,6 +104,12 @@ _SIGS = [
     ("fdmgpu_nscube_dtype", c_int, [c_void_p, POINTER(c_int)]),
     ("fdmgpu_nscube_destroy", c_int, [c_void_p]),
     ("fdmgpu_check_const_division", c_int, [c_longlong, c_void_p, c_void_p, c_void_p, c_void_p, c_void_p]),
+    ("fdmgpu_nscyl_create", c_int, [POINTER(c_void_p), c_int, c_int] + [c_double] * 7 + [c_int] * 3),
+    ("fdmgpu_nscyl_step", c_int, [c_void_p, c_int]),
+    ("fdmgpu_nscyl_field_info", c_int, [c_void_p, c_int, POINTER(c_size_t), POINTER(c_int)]),
+    ("fdmgpu_nscyl_get_field", c_int, [c_void_p, c_int, c_void_p, c_size_t]),
+    ("fdmgpu_nscyl_time_index", c_int, [c_void_p, POINTER(c_int)]),
+    ("fdmgpu_nscyl_destroy", c_int, [c_void_p]),
     ("fdmgpu_server_create", c_int, [POINTER(c_void_p), c_double, c_int, c_int]),
     ("fdmgpu_server_submit_solve", c_int,
      [c_void_p, POINTER(c_ulonglong), POINTER(c_int), POINTER(c_double), POINTER(c_double), c_double, c_void_p,

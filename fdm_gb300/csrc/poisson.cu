@@ -1423,6 +1423,10 @@ static void noalloc_solve(double dx, double dy, double dz, double lx, double ly,
 void cube_solve_device(fdmgpu_lapl_cube* h, void* ans, const void* rhs, int nrhs, cudaStream_t st) {
     h->plan.solve_device(ans, rhs, nrhs, st);
 }
+
+void cyl_solve_device(fdmgpu_lapl_cyl* h, void* ans, const void* rhs, int nrhs, cudaStream_t st) {
+    h->plan.solve_device(ans, rhs, nrhs, st);
+}
 }  // namespace fdmgpu
 
 static size_t elem_size(int dtype) { return dtype == FDMGPU_F64 ? sizeof(double) : sizeof(float); }

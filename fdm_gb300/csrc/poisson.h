@@ -11,4 +11,7 @@ namespace fdmgpu {
 // (created through fdmgpu_lapl_cube_create).  Throws fdmgpu::Error.
 void cube_solve_device(fdmgpu_lapl_cube* h, void* ans, const void* rhs, int nrhs, cudaStream_t st);
 
+// The same for a LaplCyl3FFT2 plan (fdmgpu_lapl_cyl_create), used by NSCyl.
+void cyl_solve_device(fdmgpu_lapl_cyl* h, void* ans, const void* rhs, int nrhs, cudaStream_t st);
+
 }  // namespace fdmgpu

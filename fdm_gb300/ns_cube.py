@@ -131,3 +131,64 @@ class NSCube:
             self.close()
         except Exception:
             pass
+
+
+class NSCyl:
+    """Host-side mirror of fdm::NSCyl<T,check,zflag> (src/ns_cyl.h:18-134):
+    flow between coaxial cylinders, inner one rotating with u0.  Config keys
+    ns:{R, r, h1, h2, u0, Re, dt, nr, nz, nphi} with the reference defaults;
+    periodic_z selects zflag = periodic.  Fields are (phi, z, r) with r
+    fastest, returned as Tensor3 over their inclusive ranges."""
+
+    def __init__(self, cfg: Config | None = None, dtype=np.float64, periodic_z: bool = False, **overrides):
+        cfg = cfg or Config()
+        for k, v in overrides.items():
+            cfg.set("ns", k, v)
+        self.R = cfg.get("ns", "R", math.pi)
+        self.r0 = cfg.get("ns", "r", math.pi / 2)
+        self.h1 = cfg.get("ns", "h1", 0.0)
+        self.h2 = cfg.get("ns", "h2", 10.0)
+        self.U0 = cfg.get("ns", "u0", 1.0)
+        self.Re = cfg.get("ns", "Re", 1.0)
+        self.dt = cfg.get("ns", "dt", 0.001)
+        self.nr = cfg.get("ns", "nr", 32)
+        self.nz = cfg.get("ns", "nz", 31)
+        self.nphi = cfg.get("ns", "nphi", 32)
+        self.dtype = np.dtype(dtype)
+        self._lib = N.load()
+        h = c_void_p()
+        N.check(self._lib.fdmgpu_nscyl_create(byref(h), N.F64 if self.dtype == np.float64 else N.F32,
+                                              int(bool(periodic_z)), float(self.R), float(self.r0), float(self.h1),
+                                              float(self.h2), float(self.U0), float(self.Re), float(self.dt),
+                                              int(self.nr), int(self.nz), int(self.nphi)))
+        self._h = h
+
+    def step(self, k: int = 1) -> None:
+        N.check(self._lib.fdmgpu_nscyl_step(self._h, int(k)))
+
+    @property
+    def time_index(self) -> int:
+        t = c_int()
+        N.check(self._lib.fdmgpu_nscyl_time_index(self._h, byref(t)))
+        return t.value
+
+    def get(self, name: str) -> Tensor3:
+        fid = FIELDS.index(name)
+        cnt = c_size_t()
+        r = (c_int * 6)()
+        N.check(self._lib.fdmgpu_nscyl_field_info(self._h, fid, byref(cnt), r))
+        shape = (r[1] - r[0] + 1, r[3] - r[2] + 1, r[5] - r[4] + 1)
+        out = np.empty(shape, self.dtype)
+        N.check(self._lib.fdmgpu_nscyl_get_field(self._h, fid, out.ctypes.data, cnt.value))
+        return Tensor3(out, tuple(r))
+
+    def close(self) -> None:
+        if getattr(self, "_h", None):
+            self._lib.fdmgpu_nscyl_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass

@@ -342,6 +342,23 @@ int fdmgpu_server_stats_reset(fdmgpu_server* h);
 /* cancels queued requests, waits for running ones, frees everything */
 int fdmgpu_server_destroy(fdmgpu_server* h);
 
+/* ---- NSCyl: flow between coaxial cylinders -------------------------------
+ * Replaces fdm::NSCyl<T,check,zflag> (src/ns_cyl.h:18-134,
+ * src/ns_cyl.cpp:22-485): Config keys ns:{R, r, h1, h2, u0, Re, dt, nr, nz,
+ * nphi}, step(), public tensors u (r), v (z), w (phi), p, x, F, G, H, RHS
+ * (field ids FDMGPU_NS_*) in the reference layouts (phi, z, r), r fastest,
+ * ranges {0..nphi-1, z-range, r-range}.  The pressure solve is
+ * LaplCyl3FFT2.  Dirichlet z needs nz <= nr (the reference's axial ghost loop
+ * runs r over the z bounds, src/ns_cyl.cpp:106-111). */
+typedef struct fdmgpu_nscyl fdmgpu_nscyl;
+int fdmgpu_nscyl_create(fdmgpu_nscyl** h, int dtype, int periodic_z, double R, double r0, double h1, double h2,
+                        double u0, double Re, double dt, int nr, int nz, int nphi);
+int fdmgpu_nscyl_step(fdmgpu_nscyl* h, int k);
+int fdmgpu_nscyl_field_info(fdmgpu_nscyl* h, int field, size_t* count, int* ranges6);
+int fdmgpu_nscyl_get_field(fdmgpu_nscyl* h, int field, void* host, size_t count);
+int fdmgpu_nscyl_time_index(fdmgpu_nscyl* h, int* t);
+int fdmgpu_nscyl_destroy(fdmgpu_nscyl* h);
+
 #ifdef __cplusplus
 }
 #endif

@@ -115,7 +115,8 @@ class _NS:
             raise ValueError("bad size")
 
     def _fn(self, what):
-        return getattr(self.L, {"orc": "orc_ns_", "ref": "ref_nscube_", "reff": "ref_nscubef_"}[self.kind] + what)
+        return getattr(self.L, {"orc": "orc_ns_", "ref": "ref_nscube_", "reff": "ref_nscubef_",
+                                "cyl": "ref_nscyl_"}[self.kind] + what)
 
     def step(self, k: int = 1) -> None:
         self._fn("step")(self.h, int(k))
@@ -160,6 +161,12 @@ class Reference:
         L.ref_pfft_d.argtypes = [_dp, _dp, c_double, c_int]
         L.ref_lapl_cube_periodic_d.argtypes = [c_int] * 3 + [c_double] * 6 + [_dp, _dp]
         L.ref_lapl_cyl_d.argtypes = [c_int] * 4 + [c_double] * 5 + [_dp, _dp]
+        L.ref_nscyl_create.restype = c_void_p
+        L.ref_nscyl_create.argtypes = [c_int] + [c_double] * 7 + [c_int] * 3
+        L.ref_nscyl_step.argtypes = [c_void_p, c_int]
+        L.ref_nscyl_get.restype = c_long
+        L.ref_nscyl_get.argtypes = [c_void_p, c_int, _dp]
+        L.ref_nscyl_destroy.argtypes = [c_void_p]
         L.ref_nscubef_create.restype = c_void_p
         L.ref_nscubef_create.argtypes = [c_int, c_int] + [c_double] * 9
         L.ref_nscubef_step.argtypes = [c_void_p, c_int]
@@ -231,6 +238,11 @@ class Reference:
 
     def nscube(self, nx, nz, Re, dt, u0=1.0, box=(-np.pi, -np.pi, -np.pi, np.pi, np.pi, np.pi)):
         return _NS(self.L, self.L.ref_nscube_create(nx, nz, Re, dt, u0, *box), "ref")
+
+    def nscyl(self, nr, nz, nphi, Re, dt, u0=1.0, R=np.pi, r0=np.pi / 2, h1=0.0, h2=10.0, periodic_z=False):
+        """NSCyl<double,false,zflag> (src/ns_cyl.h:18-134)."""
+        return _NS(self.L, self.L.ref_nscyl_create(1 if periodic_z else 0, R, r0, h1, h2, u0, Re, dt, nr, nz,
+                                                   nphi), "cyl")
 
     def nscube_float(self, nx, nz, Re, dt, u0=1.0, box=(-np.pi, -np.pi, -np.pi, np.pi, np.pi, np.pi)):
         """NSCube<float,false>; fields come back widened to float64."""

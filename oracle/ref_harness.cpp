@@ -24,6 +24,7 @@
 #include "lapl_rect.h"
 #include "ns_cube.h"
 #include "lapl_cyl.h"
+#include "ns_cyl.h"
 #include "cyclic_reduction.h"
 #include "asp_gauss.h"
 #include "config.h"
@@ -192,6 +193,69 @@ int ref_lapl_cyl_d(int periodic_z, int nr, int nz, int nphi, double dr, double d
         lapl.solve(ans, rhs);
     }
     return 0;
+}
+
+// NSCyl<double,false,zflag> (src/ns_cyl.h:18-134) from ns:{R,r,h1,h2,u0,Re,dt,
+// nr,nz,nphi}; fields copied out whole (ghosts included), layout of the
+// reference tensor (phi, z, r), r fastest.
+struct RefNSCyl {
+    Config cfg;
+    NSCyl<double, false, tensor_flag::none>* d = nullptr;
+    NSCyl<double, false, tensor_flag::periodic>* p = nullptr;
+};
+
+void* ref_nscyl_create(int periodic_z, double R, double r0, double h1, double h2, double u0, double Re, double dt,
+                       int nr, int nz, int nphi) {
+    auto* h = new RefNSCyl();
+    char buf[16][96];
+    const char* keys[] = {"nr", "nz", "nphi", "R", "r", "h1", "h2", "u0", "Re", "dt"};
+    double vals[] = {(double)nr, (double)nz, (double)nphi, R, r0, h1, h2, u0, Re, dt};
+    char* argv[16];
+    argv[0] = (char*)"ref";
+    for (int i = 0; i < 10; i++) {
+        if (i < 3) snprintf(buf[i], sizeof(buf[i]), "--ns:%s=%d", keys[i], (int)vals[i]);
+        else snprintf(buf[i], sizeof(buf[i]), "--ns:%s=%.17g", keys[i], vals[i]);
+        argv[i + 1] = buf[i];
+    }
+    h->cfg.rewrite(11, argv);
+    if (periodic_z) h->p = new NSCyl<double, false, tensor_flag::periodic>(h->cfg);
+    else h->d = new NSCyl<double, false, tensor_flag::none>(h->cfg);
+    return h;
+}
+
+int ref_nscyl_step(void* hp, int k) {
+    auto* h = (RefNSCyl*)hp;
+    for (int i = 0; i < k; i++) {
+        if (h->d) h->d->step();
+        else h->p->step();
+    }
+    return 0;
+}
+
+}  // extern "C"
+
+template <typename NS>
+static long nscyl_get(NS* ns, int field, double* out) {
+    auto* t = field == 0 ? &ns->u : field == 1 ? &ns->v : field == 2 ? &ns->w : field == 3 ? &ns->p
+            : field == 4 ? &ns->x : field == 5 ? &ns->F : field == 6 ? &ns->G : field == 7 ? &ns->H : &ns->RHS;
+    long n = t->size;
+    if (out) memcpy(out, t->vec, sizeof(double) * n);
+    return n;
+}
+
+extern "C" {
+
+long ref_nscyl_get(void* hp, int field, double* out) {
+    auto* h = (RefNSCyl*)hp;
+    if (field < 0 || field > 8) return -1;
+    return h->d ? nscyl_get(h->d, field, out) : nscyl_get(h->p, field, out);
+}
+
+void ref_nscyl_destroy(void* hp) {
+    auto* h = (RefNSCyl*)hp;
+    delete h->d;
+    delete h->p;
+    delete h;
 }
 
 int ref_cyclic_reduction_d(double* d, double* e, double* f, double* b, int q, int n, int general) {

@@ -174,6 +174,15 @@ def main():
         cyl["rhs_" + name] = f
         cyl["args_" + name] = np.array(args)
         cyl["ans_" + name] = R.lapl_cyl(f, *args, periodic_z=pz)
+    # NSCyl<double,false,zflag> (src/ns_cyl.cpp:22-485): Dirichlet z
+    # (nr 16, nz 15, nphi 16) and periodic z (nr 16, nz 16, nphi 8), Re 100,
+    # dt 0.01, the reference's default radii and heights; 20 steps
+    for name, pz, (nr, nz, nphi) in (("d16x15x16", False, (16, 15, 16)), ("p16x16x8", True, (16, 16, 8))):
+        m = R.nscyl(nr, nz, nphi, 100.0, 0.01, periodic_z=pz)
+        m.step(20)
+        for f in ("u", "v", "w", "p", "x"):
+            cyl["ns_%s_s20_%s" % (name, f)] = m.get(f)
+        m.close()
     np.savez_compressed(OUT / "lapl_cyl.npz", **cyl)
 
     # LaplRect / LaplRectFFT2

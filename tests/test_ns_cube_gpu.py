@@ -171,3 +171,22 @@ def test_float_cavity_vs_reference_float(cuda, golden):
         idx = g["f32_n15_s100_%s_idx" % name]
         scale = max(1.0, float(g["f32_n15_s100_%s_maxabs" % name]))
         assert np.abs(got[idx] - g["f32_n15_s100_%s_vals" % name]).max() <= 1e-4 * scale, name
+
+
+@pytest.mark.parametrize("name,pz,shape", [("d16x15x16", False, (16, 15, 16)), ("p16x16x8", True, (16, 16, 8))])
+def test_nscyl_vs_reference(cuda, golden, name, pz, shape):
+    """NSCyl (flow between coaxial cylinders, the inner one rotating) against
+    the reference's NSCyl<double,false,zflag> after 20 steps, Dirichlet and
+    periodic z: every field over its whole storage, ghost layers included."""
+    from fdm_gb300 import NSCyl
+    g = golden("lapl_cyl")
+    nr, nz, nphi = shape
+    m = NSCyl(nr=nr, nz=nz, nphi=nphi, Re=100.0, dt=0.01, u0=1.0, periodic_z=pz)
+    m.step(20)
+    assert m.time_index == 20
+    for f in ("u", "v", "w", "p", "x"):
+        got = m.get(f).data.ravel()
+        ref = g["ns_%s_s20_%s" % (name, f)]
+        assert got.size == ref.size, f
+        assert np.abs(got - ref).max() <= 1e-11 * max(1.0, np.abs(ref).max()), f
+    m.close()
