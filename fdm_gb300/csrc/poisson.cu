@@ -157,10 +157,13 @@ static void launch_rg(const Tin* in, Tout* out, int nx, int ny, int nz, int nvol
                       double scale, cudaStream_t st, const SineFused& fu, SineGeom geo) {
     constexpr int L = RgGeom<N, AXIS>::L;
     constexpr size_t smem = rg_smem_bytes<T, N, AXIS>();
+    const auto kern = [] {
+        if constexpr (rg_use_occ<T, AXIS, N>()) return k_sine_rg_occ<Tin, T, Tout, AXIS, MODE, N>;
+        else return k_sine_rg<Tin, T, Tout, AXIS, MODE, N>;
+    }();
     static bool attr_set = false;
     if (!attr_set) {
-        FDM_CUDA(cudaFuncSetAttribute(k_sine_rg<Tin, T, Tout, AXIS, MODE, N>,
-                                      cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+        FDM_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
         attr_set = true;
     }
     unsigned gx;
@@ -168,7 +171,7 @@ static void launch_rg(const Tin* in, Tout* out, int nx, int ny, int nz, int nvol
     else gx = (unsigned)(nz * ((nx + L - 1) / L));
     dim3 grid(gx, nvol);
     FDM_TIMED((sine_name<Tin, T, Tout, AXIS, MODE>()), st);
-    k_sine_rg<Tin, T, Tout, AXIS, MODE, N><<<grid, 256, smem, st>>>(in, out, geo, tb, (T)scale, fu);
+    kern<<<grid, 256, smem, st>>>(in, out, geo, tb, (T)scale, fu);
     FDM_LAUNCH_CHECK();
 }
 

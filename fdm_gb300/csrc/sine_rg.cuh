@@ -116,8 +116,8 @@ __device__ __forceinline__ void dft_reg(vec2_t<T>* v) {
 __device__ __forceinline__ int sk(int k) { return k + (k >> 4); }
 
 template <typename Tin, typename T, typename Tout, int AXIS, int MODE, int N>
-__global__ void __launch_bounds__(256) k_sine_rg(const Tin* in, Tout* out, SineGeom geo, SineTables<T> tb, T scale,
-                                                 SineFused fu) {
+__device__ __forceinline__ void sine_rg_body(const Tin* in, Tout* out, const SineGeom& geo, const SineTables<T>& tb,
+                                             T scale, const SineFused& fu) {
     using T2 = vec2_t<T>;
     using Gm = RgGeom<N, AXIS>;
     constexpr int M = Gm::M, R1 = Gm::R1, R2 = Gm::R2, G = Gm::G, L = Gm::L, D2 = Gm::D2, E = Gm::E;
@@ -410,6 +410,27 @@ __global__ void __launch_bounds__(256) k_sine_rg(const Tin* in, Tout* out, SineG
                 out[base + (long long)y * nx + c] = Tout(scale * Sr[2 * ((size_t)c * LS2 + sk(i >> 1)) + (i & 1)]);
         }
     }
+}
+
+template <typename Tin, typename T, typename Tout, int AXIS, int MODE, int N>
+__global__ void __launch_bounds__(256) k_sine_rg(const Tin* in, Tout* out, SineGeom geo, SineTables<T> tb, T scale,
+                                                 SineFused fu) {
+    sine_rg_body<Tin, T, Tout, AXIS, MODE, N>(in, out, geo, tb, scale, fu);
+}
+
+// The same kernel held to 64 registers (4 CTAs of 256 threads per SM): for
+// the FP32 x-line passes of 256 and 512 points, whose unconstrained
+// allocation (70-78 registers) leaves 3 CTAs per SM and which run faster
+// at the higher occupancy without spilling.
+template <typename Tin, typename T, typename Tout, int AXIS, int MODE, int N>
+__global__ void __launch_bounds__(256, 4) k_sine_rg_occ(const Tin* in, Tout* out, SineGeom geo, SineTables<T> tb,
+                                                        T scale, SineFused fu) {
+    sine_rg_body<Tin, T, Tout, AXIS, MODE, N>(in, out, geo, tb, scale, fu);
+}
+
+template <typename T, int AXIS, int N>
+constexpr bool rg_use_occ() {
+    return sizeof(T) == 4 && AXIS == 0 && N >= 256;
 }
 
 template <typename T, int N, int AXIS>
