@@ -6,7 +6,7 @@ importing anything that solves raises immediately.  There is no CPU fallback.
 from __future__ import annotations
 
 import ctypes
-from ctypes import POINTER, c_char_p, c_double, c_int, c_longlong, c_size_t, c_ulonglong, c_void_p
+from ctypes import POINTER, c_char_p, c_double, c_int, c_longlong, c_size_t, c_uint, c_ulonglong, c_void_p
 from pathlib import Path
 
 LIB_PATH = Path(__file__).resolve().parent / "libfdmgpu.so"
@@ -89,6 +89,7 @@ _SIGS = [
     ("fdmgpu_lapl_rect_solve_device", c_int, [c_void_p, c_void_p, c_void_p, c_int, c_void_p]),
     ("fdmgpu_lapl_rect_destroy", c_int, [c_void_p]),
     ("fdmgpu_sine_device", c_int, [c_int, c_int, c_int, c_double, c_void_p, c_void_p, c_void_p]),
+    ("fdmgpu_check_bounded_wait", c_int, [c_uint]),
     ("fdmgpu_sine_tc_device", c_int, [c_int, c_int, c_int, c_longlong, c_double, c_void_p, c_void_p, c_void_p]),
     ("fdmgpu_tridiag_device", c_int, [c_int, c_int, c_int, c_void_p, c_void_p, c_void_p, c_void_p, c_void_p]),
     ("fdmgpu_nscube_create", c_int,

@@ -1768,6 +1768,21 @@ int fdmgpu_sine_tc_device(int N, int axis, int nx, long long count, double scale
     FDM_API_END
 }
 
+int fdmgpu_check_bounded_wait(unsigned spins) {
+    FDM_API_BEGIN
+    if (spins < 1 || spins > (1u << 20)) FDM_FAIL(FDMGPU_EINVAL, "spins must be in [1, 2^20]");
+    DevBuf flag;
+    flag.get(sizeof(int));
+    FDM_CUDA(cudaMemset(flag.p, 0xff, sizeof(int)));
+    k_bounded_wait_check<<<1, 32>>>(spins, (int*)flag.p);
+    FDM_LAUNCH_CHECK();
+    int gave_up = -1;
+    FDM_CUDA(cudaMemcpy(&gave_up, flag.p, sizeof(int), cudaMemcpyDeviceToHost));
+    if (gave_up == 1) FDM_FAIL(FDMGPU_ETIMEOUT, "bounded wait gave up after %u tries (nothing arrived)", spins);
+    if (gave_up != 0) FDM_FAIL(FDMGPU_ECUDA, "bounded-wait check did not run");
+    FDM_API_END
+}
+
 int fdmgpu_lapl_cube_set_schedule(fdmgpu_lapl_cube* h, int ztable, int dst_tc) {
     FDM_API_BEGIN
     if (!h) FDM_FAIL(FDMGPU_EINVAL, "null handle");

@@ -123,6 +123,24 @@ constexpr unsigned kTcSpinLimit = 1u << 24;
 
 constexpr int kTcThreads = 256;
 
+// Diagnostic of the bounded wait the tensor-core kernels use: one thread
+// waits on an mbarrier that nothing arrives at, with the same try_wait loop
+// and a caller-given spin limit, and reports whether it gave up (1) or saw
+// the phase complete (0).  It ends after `spins` tries either way.
+__global__ void k_bounded_wait_check(unsigned spins, int* gave_up) {
+#if defined(__CUDA_ARCH__)
+    __shared__ __align__(8) uint64_t mbar;
+    if (threadIdx.x == 0) {
+        asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(tc_smem(&mbar)), "r"(1));
+        unsigned n = 0;
+        bool done = false;
+        while (!(done = tc_try_wait(tc_smem(&mbar), 0)) && ++n < spins) {
+        }
+        *gave_up = done ? 0 : 1;
+    }
+#endif
+}
+
 template <int N, int AXIS>
 __global__ void __launch_bounds__(kTcThreads, (N == 32 ? 3 : 2))
     k_sine_tc(const float* in, float* out, SineTcGeom g, const float* __restrict__ simg, float scale, int* err) {

@@ -230,6 +230,11 @@ int fdmgpu_sine_device(int dtype, int N, int nlines, double scale,
  * gave up. */
 int fdmgpu_sine_tc_device(int N, int axis, int nx, long long count, double scale, void* d_out,
                           const void* d_in, void* stream);
+/* Diagnostic of the bounded mbarrier wait of the tensor-core kernels: waits
+ * `spins` tries on an mbarrier that nothing arrives at and returns
+ * FDMGPU_ETIMEOUT when the wait gives up, as it must (no fault, no hang; the
+ * context stays usable).  spins in [1, 2^20]. */
+int fdmgpu_check_bounded_wait(unsigned spins);
 int fdmgpu_tridiag_device(int dtype, int n, int nsys, const void* d_lower, const void* d_diag,
                           const void* d_upper, void* d_b, void* stream);
 

@@ -159,3 +159,22 @@ def test_cylindrical_vs_reference(cuda, golden):
         torch.cuda.synchronize()
         o = out.cpu().numpy()
         assert np.array_equal(o[0], ans) and np.array_equal(o[1], -ans), name
+
+
+def test_bounded_wait_gives_up_and_context_survives(cuda):
+    """The tensor-core kernels wait for their MMAs with a bounded try_wait
+    loop that records a failure instead of hanging.  Made to run out on an
+    mbarrier that nothing arrives at, it reports ETIMEOUT, and the context
+    keeps working afterwards."""
+    import torch
+    from fdm_gb300 import FdmError, sine_transform_tc_device
+    from fdm_gb300 import _native as N
+    lib = N.load()
+    assert lib.fdmgpu_check_bounded_wait(1000) == N.ETIMEOUT
+    assert b"gave up" in lib.fdmgpu_last_error()
+    x = torch.ones((128, 31), dtype=torch.float32, device=cuda)
+    y = torch.empty_like(x)
+    sine_transform_tc_device(y, x, 32, 128, 1.0)  # the context is intact
+    assert torch.isfinite(y).all()
+    with pytest.raises(FdmError):
+        N.check(lib.fdmgpu_check_bounded_wait(0))
