@@ -621,6 +621,15 @@ def main():
     torch.cuda.synchronize()
     ns_ms = (time.perf_counter() - t0) * 1e3 / 200
     ns.close()
+    # the cylindrical step at the reference's defaults (nr 32, nz 31, nphi 32)
+    cyl = fdm_gb300.NSCyl(Re=100.0, dt=0.001)
+    cyl.step(5)
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    cyl.step(200)
+    torch.cuda.synchronize()
+    cyl_ms = (time.perf_counter() - t0) * 1e3 / 200
+    cyl.close()
 
     del out, f
     torch.cuda.empty_cache()
@@ -657,6 +666,7 @@ def main():
         "kernels_ms_per_step": {k: v[1] / 2 for k, v in sorted(prof.items(), key=lambda kv: -kv[1][1])},
         "plain_fp64_gpu": {"value": plain_rate, "unit": UNIT},
         "nscube_63cubed": {"ms_per_step": ns_ms, "steps_timed": 200, "Re": 250.0, "dt": 0.01},
+        "nscyl_32x31x32": {"ms_per_step": cyl_ms, "steps_timed": 200, "Re": 100.0, "dt": 0.001},
         "uneven_batch": uneven,
         "periodic_poisson": periodic,
         "serving": serving,
