@@ -261,6 +261,48 @@ PERIODIC_PUBLISHED_MS = {32: {"ryzen_3700x_16t": 1.26, "apple_m1": 1.7},
                          128: {"ryzen_3700x_16t": 62.50, "apple_m1": 68.83}}
 
 
+def measure_nbody(torch, fdm_gb300, steps=200):
+    """The particle-mesh N-body driver at the reference's defaults
+    (test/nbody.cpp:593-611: N 100000 bodies, 32^3 periodic mass grid, npp
+    64, dt 0.001, G 1, FP64), without and with the pair forces (local 0 / 1).
+    Bodies stay on the device; every step after the first is one CUDA graph
+    launch.  e2e adds, per step, the copy of positions and velocities back to
+    host arrays (what the reference's plot task takes)."""
+    from fdm_gb300 import _native
+
+    out = {"workload": "nbody_pm_100000_bodies_32^3", "N": 100000, "n": 32, "npp": 64, "dtype": "f64"}
+    for local in (0, 1):
+        nb = fdm_gb300.NBody(local=local)
+        nb.step(3)
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        nb.step_async(steps)
+        nb.sync()
+        ms = (time.perf_counter() - t0) * 1e3 / steps
+        e2e_steps = 20
+        t0 = time.perf_counter()
+        for _ in range(e2e_steps):
+            nb.step(1)
+            nb.bodies()
+        e2e_ms = (time.perf_counter() - t0) * 1e3 / e2e_steps
+        # per-kernel device time of one eager calc_a_pm (the graph hides its
+        # launches from the per-launch timers)
+        _native.profile_reset()
+        _native.profile_enable(True)
+        l0 = _native.launch_count()
+        nb.calc_a_pm()
+        launches = _native.launch_count() - l0
+        _native.profile_enable(False)
+        prof = _native.profile_collect()
+        out["local%d" % local] = {
+            "ms_per_step": ms, "steps_per_s": 1e3 / ms, "e2e_ms_per_step": e2e_ms,
+            "kernels_per_step": launches,
+            "kernels_ms": {k: v[1] for k, v in sorted(prof.items(), key=lambda kv: -kv[1][1])},
+        }
+        nb.close()
+    return out
+
+
 def measure_periodic(torch, fdm_gb300, stream, reps=50):
     """Periodic LaplCube<double> solve (FP64) at 32^3, 64^3, 128^3: device
     time per solve (CUDA events, median of reps) and the host-array call the
@@ -635,6 +677,7 @@ def main():
     torch.cuda.empty_cache()
     uneven = measure_uneven_batch(torch, fdm_gb300, workloads, stream, dev)
     periodic = measure_periodic(torch, fdm_gb300, stream)
+    nbody = measure_nbody(torch, fdm_gb300)
     rates = tuple(int(x) for x in args.serve_rates.split(",")) if args.serve_rates else SERVE_RATES
     serving = measure_serving(torch, fdm_gb300, workloads, dev, rates=rates) if not args.no_serving else None
 
@@ -669,6 +712,7 @@ def main():
         "nscyl_32x31x32": {"ms_per_step": cyl_ms, "steps_timed": 200, "Re": 100.0, "dt": 0.001},
         "uneven_batch": uneven,
         "periodic_poisson": periodic,
+        "nbody": nbody,
         "serving": serving,
         "clocks": clocks,
     }
@@ -682,6 +726,13 @@ def main():
         o.step(10)
         line["cpu_baseline"]["nscube_63cubed_ms_per_step"] = (time.perf_counter() - t0) * 1e3 / 10
         o.close()
+        from oracle.nbody import NBodyPort
+        p = NBodyPort(-10.0, -10.0, -10.0, 20.0, 32, 64, 100000, 0.001, 1.0)
+        p.step(1)
+        t0 = time.perf_counter()
+        p.step(3)
+        line["cpu_baseline"]["nbody_100000_ms_per_step"] = (time.perf_counter() - t0) * 1e3 / 3
+        line["cpu_baseline"]["nbody_kind"] = "port (numpy, 1 thread)"
     if rank == 0:
         print(json.dumps(line), flush=True)
     if world > 1:

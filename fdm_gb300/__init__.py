@@ -8,5 +8,6 @@ from ._native import FdmError, load as load_library, LIB_PATH, MAX_N  # noqa: F4
 from .config import Config  # noqa: F401
 from .lapl import (BatchSolver, LaplCube, LaplCyl3FFT2, LaplRect, LaplRectFFT2, sine_transform_device,  # noqa: F401
                    sine_transform_tc_device, tridiag_device)  # noqa: F401
+from .nbody import NBody  # noqa: F401
 from .ns_cube import NSCube, NSCyl, Tensor3  # noqa: F401
 from .serve import Server  # noqa: F401

@@ -111,6 +111,19 @@ _SIGS = [
     ("fdmgpu_nscyl_get_field", c_int, [c_void_p, c_int, c_void_p, c_size_t]),
     ("fdmgpu_nscyl_time_index", c_int, [c_void_p, POINTER(c_int)]),
     ("fdmgpu_nscyl_destroy", c_int, [c_void_p]),
+    ("fdmgpu_nbody_create", c_int, [POINTER(c_void_p), c_int] + [c_double] * 4 + [c_int] * 3 + [c_double] * 3
+     + [c_int] * 3 + [c_double]),
+    ("fdmgpu_nbody_info", c_int, [c_void_p, POINTER(c_int), POINTER(c_double), POINTER(c_double),
+                                  POINTER(c_longlong)]),
+    ("fdmgpu_nbody_set_bodies", c_int, [c_void_p] * 6),
+    ("fdmgpu_nbody_get_bodies", c_int, [c_void_p] * 7),
+    ("fdmgpu_nbody_step", c_int, [c_void_p, c_int]),
+    ("fdmgpu_nbody_step_async", c_int, [c_void_p, c_int]),
+    ("fdmgpu_nbody_sync", c_int, [c_void_p]),
+    ("fdmgpu_nbody_calc_forces", c_int, [c_void_p]),
+    ("fdmgpu_nbody_direct_forces", c_int, [c_void_p, c_void_p]),
+    ("fdmgpu_nbody_get_field", c_int, [c_void_p, c_int, c_void_p, c_size_t]),
+    ("fdmgpu_nbody_destroy", c_int, [c_void_p]),
     ("fdmgpu_server_create", c_int, [POINTER(c_void_p), c_double, c_int, c_int]),
     ("fdmgpu_server_submit_solve", c_int,
      [c_void_p, POINTER(c_ulonglong), POINTER(c_int), POINTER(c_double), POINTER(c_double), c_double, c_void_p,

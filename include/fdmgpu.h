@@ -364,6 +364,44 @@ int fdmgpu_nscyl_get_field(fdmgpu_nscyl* h, int field, void* host, size_t count)
 int fdmgpu_nscyl_time_index(fdmgpu_nscyl* h, int* t);
 int fdmgpu_nscyl_destroy(fdmgpu_nscyl* h);
 
+/* ---- NBody: particle-mesh gravity around the periodic LaplCube ------------
+ * Replaces NBody<T,check,CIC3<T>> of test/nbody.cpp:25-511: the constructor
+ * NBody(x0, y0, z0, l, n, npp, N, dt, G, vel, sgn, local, solar, crit, debug)
+ * (:97-127, Config keys nbody:{x0, y0, z0, l, n, npp, N, dt, G, vel, sign,
+ * local, solar, rcrit}), which draws the bodies (init_points, :515-590);
+ * step() = calc_a_pm + move (:134-143); calc_error's pair sum (:145-183).
+ * dtype selects T (solver:datatype).  n is the periodic mass grid (a power
+ * of two), npp the particle-particle grid, rcrit = (l / npp) * crit.
+ * Body arrays are host arrays in T, N x 3 for x, v, a, aprev, F (the
+ * reference's Body::x[3] layout) and N for mass. */
+typedef struct fdmgpu_nbody fdmgpu_nbody;
+enum { FDMGPU_NBODY_DENSITY = 0, FDMGPU_NBODY_RHS = 1, FDMGPU_NBODY_PSI = 2, FDMGPU_NBODY_E = 3 };
+int fdmgpu_nbody_create(fdmgpu_nbody** h, int dtype, double x0, double y0, double z0, double l, int n, int npp,
+                        int nbodies, double dt, double G, double vel, int sgn, int local, int solar, double crit);
+/* body count (10 for the solar set), G (2.96e-6 for the solar set), total
+ * mass (double sum in index order) and steps taken; NULL skips */
+int fdmgpu_nbody_info(fdmgpu_nbody* h, int* nbodies, double* G, double* total_mass, long long* steps_done);
+/* replaces every body; a / aprev may be NULL (zero).  The total mass is
+ * re-summed and the cell lists hold the new bodies. */
+int fdmgpu_nbody_set_bodies(fdmgpu_nbody* h, const void* x, const void* v, const void* a, const void* aprev,
+                            const void* mass);
+int fdmgpu_nbody_get_bodies(fdmgpu_nbody* h, void* x, void* v, void* a, void* aprev, void* mass, void* F);
+/* steps x (calc_a_pm + move); synchronous.  The _async form only enqueues
+ * (one CUDA graph launch per step after the first); fdmgpu_nbody_sync waits. */
+int fdmgpu_nbody_step(fdmgpu_nbody* h, int steps);
+int fdmgpu_nbody_step_async(fdmgpu_nbody* h, int steps);
+int fdmgpu_nbody_sync(fdmgpu_nbody* h);
+/* calc_a_pm alone: a = F + PM field.  As in the reference it empties the
+ * cell lists, so the next step deposits no mass. */
+int fdmgpu_nbody_calc_forces(fdmgpu_nbody* h);
+/* calc_error's exact sum F_i = sum_{j != i} sgn m_j G (x_i - x_j) / R^3,
+ * R = |x_i - x_j| + 1e-5, into F (N x 3, T) */
+int fdmgpu_nbody_direct_forces(fdmgpu_nbody* h, void* F);
+/* the grids of the last calc_a_pm: density f, rhs, psi (n^3, x fastest) or
+ * E (n^3 x 3) */
+int fdmgpu_nbody_get_field(fdmgpu_nbody* h, int field, void* out, size_t count);
+int fdmgpu_nbody_destroy(fdmgpu_nbody* h);
+
 #ifdef __cplusplus
 }
 #endif

@@ -76,6 +76,16 @@ def f32_line(N: int, t: int) -> np.ndarray:
     return np.random.default_rng(1000 + t).uniform(-1, 1, N - 1).astype(np.float32)
 
 
+# tag, T, N, n, npp, local, solar (solar: the ten-body table, N ignored)
+NBODY_CASES = (
+    ("d", np.float64, 400, 16, 8, 0, 0),
+    ("d_pp", np.float64, 400, 8, 8, 1, 0),
+    ("f", np.float32, 400, 16, 8, 0, 0),
+    ("f_pp", np.float32, 400, 8, 8, 1, 0),
+    ("solar", np.float64, 0, 16, 8, 1, 1),
+)
+
+
 def main():
     R = reference()
     if R is None:
@@ -246,6 +256,29 @@ def main():
             ns["f32_n15_s100_%s_%s" % (name, k)] = v
     m.close()
     np.savez_compressed(OUT / "ns_cube.npz", **ns)
+
+    # particle-mesh N-body driver, NBody<T,false,CIC3<T>> (test/nbody.cpp):
+    # the constructor's bodies, then the state after 1 and 5 steps
+    from oracle.nbody import RefNBody  # noqa: E402
+    nb = {}
+    for tag, T, N, n, npp, local, solar in NBODY_CASES:
+        m = RefNBody(R.L, -10.0, -10.0, -10.0, 20.0, n, npp, N, 0.001, 1.0, 4.0, -1, local, solar, 1.0, dtype=T)
+        b = m.bodies()
+        for k in ("x", "v", "mass"):
+            nb["%s_init_%s" % (tag, k)] = b[k].astype(T)
+        nb[tag + "_total_mass"] = np.float64(m.total_mass)
+        m.step(1)
+        b, fl = m.bodies(), m.fields()
+        for k in ("x", "v", "a", "F"):
+            nb["%s_s1_%s" % (tag, k)] = b[k].astype(T)
+        for k in ("f", "rhs", "psi", "E"):
+            nb["%s_s1_%s" % (tag, k)] = fl[k].astype(T)
+        m.step(4)
+        b = m.bodies()
+        for k in ("x", "v", "a", "aprev"):
+            nb["%s_s5_%s" % (tag, k)] = b[k].astype(T)
+        m.close()
+    np.savez_compressed(OUT / "nbody.npz", **nb)
     for p in sorted(OUT.glob("*.npz")):
         print(p.name, p.stat().st_size)
 
