@@ -283,7 +283,7 @@ def measure_nbody(torch, fdm_gb300, steps=200):
         t0 = time.perf_counter()
         for _ in range(e2e_steps):
             nb.step(1)
-            nb.bodies()
+            nb.bodies(("x", "v"))
         e2e_ms = (time.perf_counter() - t0) * 1e3 / e2e_steps
         # per-kernel device time of one eager calc_a_pm (the graph hides its
         # launches from the per-launch timers)
@@ -487,8 +487,9 @@ def run_ncu_case(which: str = "solve"):
     """solve: two mixed solves of 2 RHS at 255^3 (266 MB of FP64 input,
     larger than L2) with nothing else on the GPU.  nscube: a 63^3 cavity,
     Re 250, dt 0.01, stepped 4 times (the first eager, then one captured
-    graph replayed).  tc: two mixed solves of 16 RHS at 63^3 (32 MB of FP64
-    input per RHS, 512 MB in all) with the tensor-core DST passes.  The
+    graph replayed).  tc: two mixed solves of 16 RHS at 63^3 (2 MB of FP64
+    input per RHS, 32 MB in all) with the tensor-core DST passes.  nbody /
+    nbody_pp: four N-body steps, 100000 bodies on the 32^3 mass grid.  The
     cases the committed ncu summaries capture."""
     import torch
     import fdm_gb300
@@ -502,6 +503,12 @@ def run_ncu_case(which: str = "solve"):
         for _ in range(2):
             m.solve_device(out, f, nrhs=16)
         torch.cuda.synchronize()
+        print("ncu case done")
+        return
+    if which in ("nbody", "nbody_pp"):
+        nb = fdm_gb300.NBody(local=1 if which == "nbody_pp" else 0)
+        nb.step(4)
+        nb.close()
         print("ncu case done")
         return
     if which == "nscube":
@@ -531,10 +538,12 @@ def main():
     ap.add_argument("--no-serving", action="store_true", help="skip the serving-loop sweep")
     ap.add_argument("--serve-rates", default=None,
                     help="comma-separated arrival rates (req/s) of the serving sweep (default 100,300,1000,3000,5000)")
-    ap.add_argument("--ncu-case", nargs="?", const="solve", default=None, choices=["solve", "nscube", "tc"],
+    ap.add_argument("--ncu-case", nargs="?", const="solve", default=None,
+                    choices=["solve", "nscube", "tc", "nbody", "nbody_pp"],
                     help="run only a small case for profiler captures: 'solve' (two mixed solves of 2 RHS at "
-                         "255^3), 'nscube' (four 63^3 cavity steps) or 'tc' (two mixed solves of 16 RHS at 63^3 "
-                         "with the tensor-core DST passes)")
+                         "255^3), 'nscube' (four 63^3 cavity steps), 'tc' (two mixed solves of 16 RHS at 63^3 "
+                         "with the tensor-core DST passes), 'nbody' / 'nbody_pp' (four N-body steps at the "
+                         "driver's defaults, without / with the pair forces)")
     ap.add_argument("--chunk", type=int, default=NRHS,
                     help="right-hand sides per solve call within a step (divides 16)")
     args = ap.parse_args()

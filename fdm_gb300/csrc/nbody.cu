@@ -68,6 +68,24 @@ __device__ __forceinline__ double sub_rn(double a, double b) { return __dsub_rn(
 template <>
 __device__ __forceinline__ float sub_rn(float a, float b) { return __fsub_rn(a, b); }
 
+// a / b for finite operands through the correctly rounded reciprocal y of b
+// and two remainder corrections (Markstein's theorem: the result equals the
+// IEEE quotient bit for bit); five FP64 operations instead of a division
+struct CDiv {
+    double b, y;
+};
+static inline CDiv cdiv_of(double b) { return CDiv{b, 1.0 / b}; }
+__device__ __forceinline__ double cdiv(double a, CDiv d) {
+    const double q0 = a * d.y;
+    double q = fma(fma(-q0, d.b, a), d.y, q0);
+    q = fma(fma(-q, d.b, a), d.y, q);
+    return (__double_as_longlong(a) << 1) == 0 ? q0 : q;
+}
+__device__ __forceinline__ CDiv cdiv_dev(double b) { return CDiv{b, 1.0 / b}; }
+// a / b in T: FP64 through cdiv, FP32 by the (fast) IEEE float division
+__device__ __forceinline__ double tdiv(double a, CDiv d) { return cdiv(a, d); }
+__device__ __forceinline__ float tdiv(float a, CDiv d) { return a / (float)d.b; }
+
 __host__ __device__ __forceinline__ int wrap(int v, int n) {
     v %= n;
     return v < 0 ? v + n : v;
@@ -89,6 +107,7 @@ struct Params {
     double l, h, hpp;
     double dt, hdt, hdt2;  // dt, 0.5 dt, 0.5 dt dt
     double G, rcrit, rhs_scale, sqrtpi;
+    CDiv dhT, dh, dhpp, drc, dsqrtpi;  // h in T (the CIC3 argument), h, l / npp, rcrit, sqrt(pi)
     int n, npp, N, local, sgn;
     int lists_empty;  // the cell lists hold no bodies: nothing deposits, no pair forces
     long long n3;
@@ -113,11 +132,11 @@ __global__ void __launch_bounds__(256) k_nb_cic(Bodies<T> B, Params<T> P, T* __r
 #pragma unroll
     for (int m = 0; m < 3; m++) {
         const T xx = sub_rn<T>(B.x[m * N + b], P.org[m]);
-        const int ci = (int)floor(xx / P.hT);  // CIC3: int j = floor(x / h)
-        w[m] = sub_rn<T>(xx, mul_rn<T>((T)ci, P.hT)) / P.hT;
+        const int ci = (int)floor(tdiv(xx, P.dhT));  // CIC3: int j = floor(x / h), h in T
+        w[m] = tdiv(sub_rn<T>(xx, mul_rn<T>((T)ci, P.hT)), P.dhT);
         c[m] = wrap(ci, n);
-        lc[m] = wrap((int)floor((double)xx / P.h), n);  // NBody::move: floor((x - origin) / h)
-        if (P.local) pc[m] = wrap((int)floor((double)xx / P.hpp), P.npp);
+        lc[m] = wrap((int)floor(cdiv((double)xx, P.dh)), n);  // NBody::move: floor((x - origin) / h)
+        if (P.local) pc[m] = wrap((int)floor(cdiv((double)xx, P.dhpp)), P.npp);
     }
     // M[i][k][j] = w_z * w_y * w_x with w = (1 - r, r), left to right
 #pragma unroll
@@ -293,35 +312,39 @@ __global__ void __launch_bounds__(256) k_nb_sort_big(const int* __restrict__ sta
 
 // 3. density and right-hand side, gathered per grid point
 template <typename T>
-__global__ void __launch_bounds__(256) k_nb_deposit(Params<T> P, const T* __restrict__ mass, const T* __restrict__ M,
+__global__ void __launch_bounds__(64) k_nb_deposit(Params<T> P, const T* __restrict__ mass, const T* __restrict__ M,
                                                     const int* __restrict__ start, const int* __restrict__ sorted,
                                                     T* __restrict__ f, T* __restrict__ rhs) {
     const long long e = (long long)blockIdx.x * blockDim.x + threadIdx.x;
     if (e >= P.n3) return;
     const int n = P.n, N = P.N;
     const int j = (int)(e % n), k = (int)((e / n) % n), i = (int)(e / ((long long)n * n));
+    // the sixteen bin bounds first (independent loads), then the bodies
+    int lo[16], hi[16];
+#pragma unroll
+    for (int q = 0; q < 16; q++) {
+        const int pass = q >> 3, a = (q >> 2) & 1, bb = (q >> 1) & 1, cc = q & 1;
+        const long long bin = pass * P.n3 + ((long long)wrap(i - a, n) * n + wrap(k - bb, n)) * n + wrap(j - cc, n);
+        lo[q] = start[bin];
+        hi[q] = start[bin + 1];
+    }
     T acc = P.f0;
-    for (int pass = 0; pass < 2; pass++)
-        for (int a = 0; a < 2; a++)
-            for (int bb = 0; bb < 2; bb++)
-                for (int cc = 0; cc < 2; cc++) {
-                    const long long bin = pass * P.n3 +
-                                          ((long long)wrap(i - a, n) * n + wrap(k - bb, n)) * n + wrap(j - cc, n);
-                    const int s1 = start[bin + 1];
-                    const T* Mw = M + (long long)(4 * a + 2 * bb + cc) * N;
-                    for (int s = start[bin]; s < s1; s++) {
-                        const int b = sorted[s];
-                        acc = add_rn<T>(acc, mul_rn<T>(mass[b], Mw[b]));
-                    }
-                }
+#pragma unroll
+    for (int q = 0; q < 16; q++) {
+        const T* Mw = M + (long long)(q & 7) * N;
+        for (int s = lo[q]; s < hi[q]; s++) {
+            const int b = sorted[s];
+            acc = add_rn<T>(acc, mul_rn<T>(mass[b], Mw[b]));
+        }
+    }
     f[e] = acc;
     // 4 * G * M_PI * f / h / h / h in double
-    rhs[e] = (T)(__dmul_rn(P.rhs_scale, (double)acc) / P.h / P.h / P.h);
+    rhs[e] = (T)cdiv(cdiv(cdiv(__dmul_rn(P.rhs_scale, (double)acc), P.dh), P.dh), P.dh);
 }
 
 // 5. E = -grad psi, periodic
 template <typename T>
-__global__ void __launch_bounds__(256) k_nb_efield(Params<T> P, const T* __restrict__ psi, T* __restrict__ E) {
+__global__ void __launch_bounds__(64) k_nb_efield(Params<T> P, const T* __restrict__ psi, T* __restrict__ E) {
     const long long e = (long long)blockIdx.x * blockDim.x + threadIdx.x;
     if (e >= P.n3) return;
     const int n = P.n;
@@ -339,9 +362,10 @@ __global__ void __launch_bounds__(256) k_nb_efield(Params<T> P, const T* __restr
     d2[2] = sub_rn<T>(at(i + 2, k, j), at(i - 2, k, j));
 #pragma unroll
     for (int m = 0; m < 3; m++) {
-        // -beta*(d1)/2/h - (1-beta)*(d2)/4/h
-        const double t1 = (double)(mul_rn<T>(mbeta, d1[m]) / T(2)) / P.h;
-        const double t2 = (double)(mul_rn<T>(obeta, d2[m]) / T(4)) / P.h;
+        // -beta*(d1)/2/h - (1-beta)*(d2)/4/h; halving and quartering are
+        // exact scalings, the same in either form
+        const double t1 = cdiv((double)mul_rn<T>(mul_rn<T>(mbeta, d1[m]), T(0.5)), P.dh);
+        const double t2 = cdiv((double)mul_rn<T>(mul_rn<T>(obeta, d2[m]), T(0.25)), P.dh);
         E[m * P.n3 + e] = (T)__dsub_rn(t1, t2);
     }
 }
@@ -386,12 +410,16 @@ __global__ void __launch_bounds__(128) k_nb_pp(Bodies<T> B, Params<T> P, const i
                     }
                     R = __dadd_rn(sqrt(R), 0.001);
                     if (R < rc) {
-                        const double ex = exp(__dmul_rn(-R, R) / 4 / rc / rc);
-                        const double sh = __dadd_rn(erfc(R / 2 / rc), __dmul_rn(R / rc / P.sqrtpi, ex));
+                        // erfc(R/2/rcrit) + R/rcrit/sqrt(pi) * exp(-R*R/4/rcrit/rcrit)
+                        const double ex = exp(cdiv(cdiv(__dmul_rn(__dmul_rn(-R, R), 0.25), P.drc), P.drc));
+                        const double sh = __dadd_rn(erfc(cdiv(__dmul_rn(R, 0.5), P.drc)),
+                                                    __dmul_rn(cdiv(cdiv(R, P.drc), P.dsqrtpi), ex));
                         const double mG = __dmul_rn((double)(-B.mass[bj]), P.G);
+                        const CDiv dR = cdiv_dev(R);
 #pragma unroll
                         for (int m = 0; m < 3; m++)
-                            F[m] = (T)__dadd_rn((double)F[m], __dmul_rn(__dmul_rn(mG, (double)d[m]) / R / R / R, sh));
+                            F[m] = (T)__dadd_rn((double)F[m],
+                                                __dmul_rn(cdiv(cdiv(cdiv(__dmul_rn(mG, (double)d[m]), dR), dR), dR), sh));
                     }
                 }
             }
@@ -478,8 +506,10 @@ __global__ void __launch_bounds__(kDirectTile) k_nb_direct(Bodies<T> B, Params<T
                 }
                 R = __dadd_rn(sqrt(R), 0.00001);
                 const double mG = __dmul_rn((double)mul_rn<T>(sg, sm[u]), P.G);
+                const CDiv dR = cdiv_dev(R);
 #pragma unroll
-                for (int m = 0; m < 3; m++) F[m] = (T)__dadd_rn((double)F[m], __dmul_rn(mG, (double)d[m]) / R / R / R);
+                for (int m = 0; m < 3; m++)
+                    F[m] = (T)__dadd_rn((double)F[m], cdiv(cdiv(cdiv(__dmul_rn(mG, (double)d[m]), dR), dR), dR));
             }
         __syncthreads();
     }
@@ -536,6 +566,11 @@ struct Plan {
         P.rcrit = P.hpp * (double)(T)crit;  // rcrit(hpp * crit), crit of type T
         P.rhs_scale = 4 * G * M_PI;
         P.sqrtpi = std::sqrt(M_PI);
+        P.dhT = cdiv_of((double)P.hT);
+        P.dh = cdiv_of(P.h);
+        P.dhpp = cdiv_of(P.hpp);
+        P.drc = cdiv_of(P.rcrit);
+        P.dsqrtpi = cdiv_of(P.sqrtpi);
         P.n = n; P.npp = npp; P.N = N; P.local = local; P.sgn = sgn;
         P.n3 = (long long)n * n * n;
         P.dep_bins = 2 * P.n3;
@@ -606,32 +641,46 @@ struct Plan {
             FDM_LAUNCH_CHECK();
         }
         {
-            FDM_TIMED("nb_scan", st);
+            FDM_TIMED("nb_scan_local", st);
             k_nb_scan_local<<<nchunks, kScanThreads, 0, st>>>(count, start, partial, nbins);
             FDM_LAUNCH_CHECK();
+        }
+        {
+            FDM_TIMED("nb_scan_partials", st);
             k_nb_scan_partials<<<1, kScanThreads, 0, st>>>(partial, nchunks, start + nbins, bigcount);
             FDM_LAUNCH_CHECK();
+        }
+        {
+            FDM_TIMED("nb_scan_add", st);
             k_nb_scan_add<<<blocks(nbins, T256), T256, 0, st>>>(start, partial, nbins);
             FDM_LAUNCH_CHECK();
         }
         {
-            FDM_TIMED("nb_bin", st);
+            FDM_TIMED("nb_fill", st);
             k_nb_fill<<<blocks(N, T256), T256, 0, st>>>(key, N, nkeys, start, count, sorted);
             FDM_LAUNCH_CHECK();
+        }
+        {
+            FDM_TIMED("nb_sort_small", st);
             k_nb_sort_small<<<blocks(nbins, T256), T256, 0, st>>>(start, nbins, sorted, bigcount, biglist);
             FDM_LAUNCH_CHECK();
+        }
+        {
+            FDM_TIMED("nb_sort_big", st);
             k_nb_sort_big<<<152, T256, 0, st>>>(start, sorted, tmp, bigcount, biglist);
             FDM_LAUNCH_CHECK();
         }
         {
+            // 64-thread blocks: the mass grid is small (32^3 points at the
+            // driver's defaults), so spread it over every SM
             FDM_TIMED("nb_deposit", st);
-            k_nb_deposit<T><<<blocks(P.n3, T256), T256, 0, st>>>(P, B.mass, M, start, sorted, f, rhs);
+            k_nb_deposit<T><<<blocks(P.n3, 64), 64, 0, st>>>(P, B.mass, M, start, sorted, f, rhs);
             FDM_LAUNCH_CHECK();
         }
         cube_solve_device(lapl, psi, rhs, 1, st);
         {
             FDM_TIMED("nb_efield", st);
-            k_nb_efield<T><<<blocks(P.n3, T256), T256, 0, st>>>(P, psi, E);
+            k_nb_efield<T><<<blocks(P.n3, 64), 64, 0, st>>>(P, psi, E);
             FDM_LAUNCH_CHECK();
         }
         if (P.local) {

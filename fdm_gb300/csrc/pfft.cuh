@@ -32,24 +32,30 @@ __device__ __forceinline__ long long pline_base(const PLineGeom& g, long long L)
     return (L / g.A) * g.B + (L % g.A) * g.C;
 }
 
-// lines per block: 1024 / n (at least 1), 256 threads
+// lines per block: at most 1024 / n (at least 1), 256 threads; fewer when
+// that leaves most SMs without a block (small transforms)
 __host__ __device__ constexpr int pfft_lines_per_block(int n) { return n >= 1024 ? 1 : 1024 / n; }
 
-template <typename T>
-size_t pfft_smem_bytes(int n) {
-    // two complex buffers of n/2 points per line (Stockham ping-pong); the
-    // real staging of n values aliases the second one
-    return (size_t)pfft_lines_per_block(n) * 2 * (size_t)(n / 2 > 0 ? n / 2 : 1) * 2 * sizeof(T);
+inline int pfft_lines_per_block(int n, long long lines, int sms) {
+    int lpb = pfft_lines_per_block(n);
+    while (lpb > 1 && (lines + lpb - 1) / lpb < 2LL * sms) lpb /= 2;
+    return lpb;
 }
 
-// tw[t] = e^{-2 pi i t / n}, t < n
+template <typename T>
+size_t pfft_smem_bytes(int n, int lpb) {
+    // two complex buffers of n/2 points per line (Stockham ping-pong); the
+    // real staging of n values aliases the second one
+    return (size_t)lpb * 2 * (size_t)(n / 2 > 0 ? n / 2 : 1) * 2 * sizeof(T);
+}
+
+// tw[t] = e^{-2 pi i t / n}, t < n; LPB lines per block
 template <typename T, bool INV>
 __global__ void __launch_bounds__(256)
-    k_pfft(const T* in, T* out, PLineGeom g, int n, const vec2_t<T>* __restrict__ tw, T scale) {
+    k_pfft(const T* in, T* out, PLineGeom g, int n, int LPB, const vec2_t<T>* __restrict__ tw, T scale) {
     using T2 = vec2_t<T>;
     extern __shared__ __align__(16) unsigned char pf_raw[];
     const int M = n / 2;
-    const int LPB = pfft_lines_per_block(n);
     T2* bufA = reinterpret_cast<T2*>(pf_raw);
     T2* bufB = bufA + (size_t)LPB * M;
     T* stage = reinterpret_cast<T*>(bufB);  // n reals per line

@@ -107,13 +107,26 @@ static void upload_plambda(DevBuf& buf, int n, double h) {
     FDM_CUDA(cudaMemcpy(buf.get(n * sizeof(T)), v.data(), n * sizeof(T), cudaMemcpyHostToDevice));
 }
 
+// streaming multiprocessors of the current device (cached per process)
+static int sm_count() {
+    static int sms = 0;
+    if (!sms) {
+        int dev = 0, v = 0;
+        FDM_CUDA(cudaGetDevice(&dev));
+        FDM_CUDA(cudaDeviceGetAttribute(&v, cudaDevAttrMultiProcessorCount, dev));
+        sms = v > 0 ? v : 1;
+    }
+    return sms;
+}
+
 template <typename T, bool INV>
 static void launch_pfft(const T* in, T* out, const PLineGeom& g, int n, const void* tw, double scale,
                         cudaStream_t st) {
-    const int LPB = pfft_lines_per_block(n);
+    const int LPB = pfft_lines_per_block(n, g.lines, sm_count());
     const unsigned grid = (unsigned)((g.lines + LPB - 1) / LPB);
     FDM_TIMED(INV ? "pfft_inverse" : "pfft_forward", st);
-    k_pfft<T, INV><<<grid, 256, pfft_smem_bytes<T>(n), st>>>(in, out, g, n, (const vec2_t<T>*)tw, (T)scale);
+    k_pfft<T, INV><<<grid, 256, pfft_smem_bytes<T>(n, LPB), st>>>(in, out, g, n, LPB, (const vec2_t<T>*)tw,
+                                                                  (T)scale);
     FDM_LAUNCH_CHECK();
 }
 

@@ -71,11 +71,12 @@ class NBody:
     def steps(self) -> int:
         return self._info()[3]
 
-    def bodies(self) -> dict:
+    def bodies(self, fields=("x", "v", "a", "aprev", "mass", "F")) -> dict:
+        """Host copies of the requested body arrays (x, v, a, aprev, F: N x 3;
+        mass: N)."""
         n = self.N
-        out = {k: np.empty((n, 3), self.dtype) for k in ("x", "v", "a", "aprev", "F")}
-        out["mass"] = np.empty(n, self.dtype)
-        N.check(self._lib.fdmgpu_nbody_get_bodies(self._h, *(out[k].ctypes.data for k in
+        out = {k: np.empty((n,) if k == "mass" else (n, 3), self.dtype) for k in fields}
+        N.check(self._lib.fdmgpu_nbody_get_bodies(self._h, *(out[k].ctypes.data if k in out else None for k in
                                                               ("x", "v", "a", "aprev", "mass", "F"))))
         return out
 

@@ -176,3 +176,23 @@ def test_nbody_errors():
         N.check(nb._lib.fdmgpu_nbody_get_field(nb._h, 7, buf.ctypes.data, ctypes.c_size_t(3)))
     assert e.value.status == N.EINVAL
     nb.close()
+
+
+@pytest.mark.parametrize("T", [np.float64, np.float32])
+def test_nbody_cic3_known_answers(T):
+    """ut/ut_interpolate.cpp test_CIC3 (:67-114) through the device deposit:
+    a body of mass 10 at (0.5, 0.5, 0.5) with h = 1 puts m/8 on each corner
+    of cell 0; at (0.5, 0.6, 0.7) the eight shares sum to m."""
+    nb = make(("cic", T, 1, 8, 8, 0, 0), x0=0.0, y0=0.0, z0=0.0, l=8.0)
+    f0 = float(T(-10.0 / 8.0 / 8.0 / 8.0))
+    for pos, exact in (((0.5, 0.5, 0.5), True), ((0.5, 0.6, 0.7), False)):
+        nb.set_bodies(np.array([pos]), np.zeros((1, 3)), np.array([10.0]))
+        nb.step(1)
+        f = nb.field("f").astype(np.float64)
+        corner = f[:2, :2, :2] - f0
+        assert np.all(np.delete(f.ravel(), [i * 64 + k * 8 + j for i in (0, 1) for k in (0, 1) for j in (0, 1)])
+                      == f0)
+        if exact:
+            assert np.all(np.abs(corner - 10.0 / 8.0) <= (1e-12 if T == np.float64 else 1e-5))
+        assert abs(corner.sum() - 10.0) <= (1e-12 if T == np.float64 else 1e-5)
+    nb.close()

@@ -86,3 +86,17 @@ def test_parity_classes_and_list_lifecycle():
     p.calc_a_pm()
     assert np.all(p.f == p.f[0])
     assert np.all(p.F == 0)
+
+
+@pytest.mark.parametrize("T", [np.float64, np.float32])
+def test_cic3_known_answers(T):
+    """ut/ut_interpolate.cpp test_CIC3 (:67-114) on the restatement's CIC."""
+    p = NBodyPort(0.0, 0.0, 0.0, 8.0, 8, 8, 1, 0.001, 1.0, dtype=T,
+                  bodies=(np.array([[0.5, 0.5, 0.5]]), np.zeros((1, 3)), np.array([10.0])))
+    c0, M = p._cic()
+    assert list(c0[0]) == [0, 0, 0]
+    assert np.all(np.abs(10.0 * M[:, 0].astype(np.float64) - 10.0 / 8.0) <= 1e-12)
+    p.set_bodies(np.array([[0.5, 0.6, 0.7]]), np.zeros((1, 3)), np.array([10.0]))
+    c0, M = p._cic()
+    assert list(c0[0]) == [0, 0, 0]
+    assert abs(float(np.sum(T(10.0) * M[:, 0])) - 10.0) <= (1e-12 if T == np.float64 else 1e-5)
