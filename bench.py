@@ -303,6 +303,71 @@ def measure_nbody(torch, fdm_gb300, steps=200):
     return out
 
 
+# test/nbody_result.org: ms per step, 1000000 particles, per stage; the
+# "Nvidia RTX 3060" column is the reference's Vulkan/GLSL port, the others
+# its OpenMP CPU code
+NBODY_PUBLISHED = {
+    "n32_npp64_pp": {"apple_m1_cpu": 239.66, "apple_m1_gpu": 117.48, "ryzen_3700x_16t": 285.75, "rtx_3060": 31.49,
+                     "stages_rtx_3060": {"density": 1.36, "poisson": 0.25, "field": 0.04, "local_forces": 28.84,
+                                         "new_positions": 1.00}},
+    "n64_npp64_pp": {"apple_m1_cpu": 420.98, "apple_m1_gpu": 128.78, "ryzen_3700x_16t": 440.89, "rtx_3060": 33.54,
+                     "stages_rtx_3060": {"density": 2.26, "poisson": 0.86, "field": 0.14, "local_forces": 28.87,
+                                         "new_positions": 1.41}},
+    "n128_pm": {"apple_m1_cpu": 264.22, "apple_m1_gpu": 97.81, "ryzen_3700x_16t": 359.14, "rtx_3060": 17.57,
+                "stages_rtx_3060": {"density": 6.58, "poisson": 5.50, "field": 3.71, "new_positions": 1.78}},
+}
+# the same file's PM totals on the Nvidia GPU (no local forces), ms per step
+NBODY_PM_PUBLISHED = {(2, 32): 4.80, (2, 128): 19.33, (8, 32): 17.33, (8, 128): 43.00, (100, 32): 190.63,
+                      (100, 128): 392.87}
+NBODY_STAGES = {"density": ("nb_cic", "nb_scan_local", "nb_scan_partials", "nb_scan_add", "nb_fill",
+                            "nb_sort_small", "nb_sort_big", "nb_deposit"),
+                "poisson": ("pfft_forward", "pdivide", "pfft_inverse"), "field": ("nb_efield",),
+                "local_forces": ("nb_pp",), "new_positions": ("nb_accel",)}
+
+
+def measure_nbody_published(torch, fdm_gb300, steps=5):
+    """The configurations of the reference's published N-body table
+    (test/nbody_result.org): 10^6 particles on 32^3 and 64^3 mass grids with
+    the 64^3 local-force grid, 128^3 without local forces; and PM-only totals
+    for 2, 8 and 100 million particles on 32^3 and 128^3 grids.  FP64, the
+    driver's other defaults (l 20, dt 0.001, G 1).  Totals are graph-launched
+    steps timed with a host clock around a synchronised run; per-stage times
+    come from CUDA events of one eager calc_a_pm (the stage grouping of the
+    published table)."""
+    from fdm_gb300 import _native
+
+    def run(N, n, npp, local, stages):
+        nb = fdm_gb300.NBody(n=n, npp=npp, N_bodies=N, local=local)
+        nb.step(2)
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        nb.step_async(steps)
+        nb.sync()
+        ms = (time.perf_counter() - t0) * 1e3 / steps
+        out = {"ms_per_step": ms}
+        if stages:
+            _native.profile_reset()
+            _native.profile_enable(True)
+            nb.calc_a_pm()
+            _native.profile_enable(False)
+            prof = _native.profile_collect()
+            out["stages_ms"] = {st: sum(prof.get(k, (0, 0.0))[1] for k in ks) for st, ks in NBODY_STAGES.items()
+                                if local or st != "local_forces"}
+        nb.close()
+        return out
+
+    res = {"N": 1000000, "dtype": "f64", "published_ms": NBODY_PUBLISHED}
+    res["n32_npp64_pp"] = run(1000000, 32, 64, 1, True)
+    res["n64_npp64_pp"] = run(1000000, 64, 64, 1, True)
+    res["n128_pm"] = run(1000000, 128, 64, 0, True)
+    pm = {}
+    for (mil, n), pub in NBODY_PM_PUBLISHED.items():
+        r = run(mil * 1000000, n, 64, 0, False)
+        pm["%dM_n%d" % (mil, n)] = {"ms_per_step": r["ms_per_step"], "published_rtx_3060_ms": pub}
+    res["pm_large"] = pm
+    return res
+
+
 def measure_periodic(torch, fdm_gb300, stream, reps=50):
     """Periodic LaplCube<double> solve (FP64) at 32^3, 64^3, 128^3: device
     time per solve (CUDA events, median of reps) and the host-array call the
@@ -687,6 +752,7 @@ def main():
     uneven = measure_uneven_batch(torch, fdm_gb300, workloads, stream, dev)
     periodic = measure_periodic(torch, fdm_gb300, stream)
     nbody = measure_nbody(torch, fdm_gb300)
+    nbody["published_configs"] = measure_nbody_published(torch, fdm_gb300)
     rates = tuple(int(x) for x in args.serve_rates.split(",")) if args.serve_rates else SERVE_RATES
     serving = measure_serving(torch, fdm_gb300, workloads, dev, rates=rates) if not args.no_serving else None
 

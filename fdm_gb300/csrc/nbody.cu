@@ -108,6 +108,7 @@ struct Params {
     double dt, hdt, hdt2;  // dt, 0.5 dt, 0.5 dt dt
     double G, rcrit, rhs_scale, sqrtpi;
     CDiv dhT, dh, dhpp, drc, dsqrtpi;  // h in T (the CIC3 argument), h, l / npp, rcrit, sqrt(pi)
+    double rc2_out;  // a double at or above rcrit^2: pairs with R^2 >= it are out of range
     int n, npp, N, local, sgn;
     int lists_empty;  // the cell lists hold no bodies: nothing deposits, no pair forces
     long long n3;
@@ -132,10 +133,13 @@ __global__ void __launch_bounds__(256) k_nb_cic(Bodies<T> B, Params<T> P, T* __r
 #pragma unroll
     for (int m = 0; m < 3; m++) {
         const T xx = sub_rn<T>(B.x[m * N + b], P.org[m]);
-        const int ci = (int)floor(tdiv(xx, P.dhT));  // CIC3: int j = floor(x / h), h in T
+        const T q = tdiv(xx, P.dhT);
+        const int ci = (int)floor(q);  // CIC3: int j = floor(x / h), h in T
         w[m] = tdiv(sub_rn<T>(xx, mul_rn<T>((T)ci, P.hT)), P.dhT);
         c[m] = wrap(ci, n);
-        lc[m] = wrap((int)floor(cdiv((double)xx, P.dh)), n);  // NBody::move: floor((x - origin) / h)
+        // NBody::move: floor((x - origin) / h) in double, the CIC quotient itself in FP64
+        const double qd = sizeof(T) == 8 ? (double)q : cdiv((double)xx, P.dh);
+        lc[m] = wrap((int)floor(qd), n);
         if (P.local) pc[m] = wrap((int)floor(cdiv((double)xx, P.dhpp)), P.npp);
     }
     // M[i][k][j] = w_z * w_y * w_x with w = (1 - r, r), left to right
@@ -148,7 +152,7 @@ __global__ void __launch_bounds__(256) k_nb_cic(Bodies<T> B, Params<T> P, T* __r
                 const T wz = a ? w[2] : sub_rn<T>(T(1), w[2]);
                 const T wy = bb ? w[1] : sub_rn<T>(T(1), w[1]);
                 const T wx = cc ? w[0] : sub_rn<T>(T(1), w[0]);
-                M[(4 * a + 2 * bb + cc) * N + b] = mul_rn<T>(mul_rn<T>(wz, wy), wx);
+                M[(long long)(4 * a + 2 * bb + cc) * N + b] = mul_rn<T>(mul_rn<T>(wz, wy), wx);
             }
     corner[b] = pack3(c[2], c[1], c[0]);
     const int p0 = lc[0] & 1;
@@ -370,61 +374,138 @@ __global__ void __launch_bounds__(64) k_nb_efield(Params<T> P, const T* __restri
     }
 }
 
-// 6. short-range pair forces (local), per body in the reference's order
+// 6. short-range pair forces (local), per body in the reference's order.
+// A thread owns a body and walks its candidates (the 27 neighbour cells,
+// each cell's bodies in index order); only about one candidate in six lies
+// within rcrit, so the pairs that do are queued per warp (ballot + prefix,
+// which keeps each lane's pairs in its own candidate order) and their
+// erfc / exp terms are evaluated 32 at a time, one pair per lane; each owner
+// then adds its pairs' terms in queue order.  The result is the serial
+// loop's, term for term, without paying the transcendental branch on every
+// candidate of every lane.
+constexpr int kPpWarps = 4;
+constexpr int kPpQueue = 64;
+
 template <typename T>
-__global__ void __launch_bounds__(128) k_nb_pp(Bodies<T> B, Params<T> P, const int* __restrict__ pcell,
-                                               const int* __restrict__ start, const int* __restrict__ sorted) {
-    const int bi = blockIdx.x * blockDim.x + threadIdx.x;
-    if (bi >= P.N) return;
-    const int N = P.N, n = P.n, npp = P.npp;
-    int pi, pk, pj;
-    unpack3(pcell[bi], pi, pk, pj);
-    T xi[3];
-    T F[3] = {T(0), T(0), T(0)};
+struct PpQueue {
+    double R[kPpQueue];
+    double t[3][kPpQueue];
+    T d[3][kPpQueue];
+    int bj[kPpQueue];
+    unsigned char lane[kPpQueue];
+};
+
+template <typename T>
+__device__ __forceinline__ void pp_flush(PpQueue<T>& q, int cnt, int lane, const Params<T>& P,
+                                         const T* __restrict__ mass, T F[3]) {
+    __syncwarp();
+    if (lane < cnt) {
+        const double R = q.R[lane];
+        // erfc(R/2/rcrit) + R/rcrit/sqrt(pi) * exp(-R*R/4/rcrit/rcrit)
+        const double ex = exp(cdiv(cdiv(__dmul_rn(__dmul_rn(-R, R), 0.25), P.drc), P.drc));
+        const double sh = __dadd_rn(erfc(cdiv(__dmul_rn(R, 0.5), P.drc)), __dmul_rn(cdiv(cdiv(R, P.drc), P.dsqrtpi), ex));
+        const double mG = __dmul_rn((double)(-mass[q.bj[lane]]), P.G);
+        const CDiv dR = cdiv_dev(R);
 #pragma unroll
-    for (int m = 0; m < 3; m++) xi[m] = B.x[m * N + bi];
+        for (int m = 0; m < 3; m++)
+            q.t[m][lane] = __dmul_rn(cdiv(cdiv(cdiv(__dmul_rn(mG, (double)q.d[m][lane]), dR), dR), dR), sh);
+    }
+    __syncwarp();
+    for (int e = 0; e < cnt; e++)
+        if (q.lane[e] == lane)
+#pragma unroll
+            for (int m = 0; m < 3; m++) F[m] = (T)__dadd_rn((double)F[m], q.t[m][e]);
+    __syncwarp();
+}
+
+template <typename T>
+__global__ void __launch_bounds__(kPpWarps * 32) k_nb_pp(Bodies<T> B, Params<T> P, const int* __restrict__ pcell,
+                                                        const int* __restrict__ start, const int* __restrict__ sorted) {
+    __shared__ PpQueue<T> queues[kPpWarps];
+    PpQueue<T>& q = queues[threadIdx.x >> 5];
+    const int lane = threadIdx.x & 31;
+    const int bi = blockIdx.x * blockDim.x + threadIdx.x;
+    const bool active = bi < P.N;
+    const int N = P.N, n = P.n, npp = P.npp;
+    int pi = 0, pk = 0, pj = 0;
+    T xi[3] = {T(0), T(0), T(0)};
+    T F[3] = {T(0), T(0), T(0)};
+    if (active) {
+        unpack3(pcell[bi], pi, pk, pj);
+#pragma unroll
+        for (int m = 0; m < 3; m++) xi[m] = B.x[m * N + bi];
+    }
     const double rc = P.rcrit;
-    for (int i0 = -1; i0 <= 1; i0++)
-        for (int k0 = -1; k0 <= 1; k0++)
-            for (int j0 = -1; j0 <= 1; j0++) {
+    int cell = -1, s = 0, s1 = 0;  // candidate iterator: neighbour cell 0..26, position in its bin
+    T off[3] = {T(0), T(0), T(0)};
+    int qn = 0;  // queued pairs (the same in every lane)
+    const unsigned lt = (1u << lane) - 1u;
+    while (true) {
+        bool has = false;
+        int bj = -1;
+        if (active) {
+            while (s >= s1 && cell < 26) {
+                cell++;
+                const int i0 = cell / 9 - 1, k0 = (cell / 3) % 3 - 1, j0 = cell % 3 - 1;
                 // image offsets as test/nbody.cpp:364-369 set them
-                T off[3] = {T(0), T(0), T(0)};
-                if (pk + k0 < 0) off[0] = -P.lT;
-                if (pk + k0 >= n) off[0] = P.lT;
-                if (pj + j0 < 0) off[1] = -P.lT;
-                if (pj + j0 >= n) off[1] = P.lT;
-                if (pi + i0 < 0) off[2] = -P.lT;
-                if (pi + i0 >= n) off[2] = P.lT;
+                off[0] = (pk + k0 < 0) ? -P.lT : ((pk + k0 >= n) ? P.lT : T(0));
+                off[1] = (pj + j0 < 0) ? -P.lT : ((pj + j0 >= n) ? P.lT : T(0));
+                off[2] = (pi + i0 < 0) ? -P.lT : ((pi + i0 >= n) ? P.lT : T(0));
                 const long long bin =
                     P.dep_bins + ((long long)wrap(pi + i0, npp) * npp + wrap(pk + k0, npp)) * npp + wrap(pj + j0, npp);
-                const int s1 = start[bin + 1];
-                for (int s = start[bin]; s < s1; s++) {
-                    const int bj = sorted[s];
-                    if (bj == bi) continue;
-                    T d[3];
-                    double R = 0;
-#pragma unroll
-                    for (int m = 0; m < 3; m++) {
-                        d[m] = sub_rn<T>(xi[m], add_rn<T>(B.x[m * N + bj], off[m]));
-                        R = __dadd_rn(R, __dmul_rn((double)d[m], (double)d[m]));
-                    }
-                    R = __dadd_rn(sqrt(R), 0.001);
-                    if (R < rc) {
-                        // erfc(R/2/rcrit) + R/rcrit/sqrt(pi) * exp(-R*R/4/rcrit/rcrit)
-                        const double ex = exp(cdiv(cdiv(__dmul_rn(__dmul_rn(-R, R), 0.25), P.drc), P.drc));
-                        const double sh = __dadd_rn(erfc(cdiv(__dmul_rn(R, 0.5), P.drc)),
-                                                    __dmul_rn(cdiv(cdiv(R, P.drc), P.dsqrtpi), ex));
-                        const double mG = __dmul_rn((double)(-B.mass[bj]), P.G);
-                        const CDiv dR = cdiv_dev(R);
-#pragma unroll
-                        for (int m = 0; m < 3; m++)
-                            F[m] = (T)__dadd_rn((double)F[m],
-                                                __dmul_rn(cdiv(cdiv(cdiv(__dmul_rn(mG, (double)d[m]), dR), dR), dR), sh));
-                    }
-                }
+                s = start[bin];
+                s1 = start[bin + 1];
             }
+            if (s < s1) {
+                bj = sorted[s++];
+                has = true;
+            }
+        }
+        if (!__any_sync(0xffffffffu, has)) break;
+        bool inr = false;
+        double R = 0;
+        T d[3];
+        if (has && bj != bi) {
 #pragma unroll
-    for (int m = 0; m < 3; m++) B.F[m * N + bi] = F[m];
+            for (int m = 0; m < 3; m++) {
+                d[m] = sub_rn<T>(xi[m], add_rn<T>(B.x[m * N + bj], off[m]));
+                R = __dadd_rn(R, __dmul_rn((double)d[m], (double)d[m]));
+            }
+            // R^2 >= rcrit^2 already fails sqrt(R^2) + 0.001 < rcrit
+            if (R < P.rc2_out) {
+                R = __dadd_rn(sqrt(R), 0.001);
+                inr = R < rc;
+            }
+        }
+        const unsigned mask = __ballot_sync(0xffffffffu, inr);
+        if (inr) {
+            const int pos = qn + __popc(mask & lt);
+            q.R[pos] = R;
+#pragma unroll
+            for (int m = 0; m < 3; m++) q.d[m][pos] = d[m];
+            q.bj[pos] = bj;
+            q.lane[pos] = (unsigned char)lane;
+        }
+        qn += __popc(mask);
+        if (qn >= 32) {
+            pp_flush<T>(q, 32, lane, P, B.mass, F);
+            // keep the overflow, in order, at the front
+            if (lane < qn - 32) {
+                const int src = 32 + lane;
+                q.R[lane] = q.R[src];
+#pragma unroll
+                for (int m = 0; m < 3; m++) q.d[m][lane] = q.d[m][src];
+                q.bj[lane] = q.bj[src];
+                q.lane[lane] = q.lane[src];
+            }
+            __syncwarp();
+            qn -= 32;
+        }
+    }
+    if (qn > 0) pp_flush<T>(q, qn, lane, P, B.mass, F);
+    if (active)
+#pragma unroll
+        for (int m = 0; m < 3; m++) B.F[m * N + bi] = F[m];
 }
 
 // 7. accelerations, then (MOVE) the velocity-Verlet update
@@ -446,7 +527,7 @@ __global__ void __launch_bounds__(256) k_nb_accel(Bodies<T> B, Params<T> P, cons
 #pragma unroll
             for (int cc = 0; cc < 2; cc++) {
                 const long long e = ((long long)wrap(ci + a, n) * n + wrap(ck + bb, n)) * n + wrap(cj + cc, n);
-                const T w = M[(4 * a + 2 * bb + cc) * N + b];
+                const T w = M[(long long)(4 * a + 2 * bb + cc) * N + b];
 #pragma unroll
                 for (int m = 0; m < 3; m++) acc[m] = add_rn<T>(acc[m], mul_rn<T>(E[m * P.n3 + e], w));
             }
@@ -570,6 +651,7 @@ struct Plan {
         P.dh = cdiv_of(P.h);
         P.dhpp = cdiv_of(P.hpp);
         P.drc = cdiv_of(P.rcrit);
+        P.rc2_out = std::nextafter(std::nextafter(P.rcrit * P.rcrit, INFINITY), INFINITY);
         P.dsqrtpi = cdiv_of(P.sqrtpi);
         P.n = n; P.npp = npp; P.N = N; P.local = local; P.sgn = sgn;
         P.n3 = (long long)n * n * n;
@@ -685,7 +767,7 @@ struct Plan {
         }
         if (P.local) {
             FDM_TIMED("nb_pp", st);
-            k_nb_pp<T><<<blocks(N, 128), 128, 0, st>>>(B, P, pcell, start, sorted);
+            k_nb_pp<T><<<blocks(N, kPpWarps * 32), kPpWarps * 32, 0, st>>>(B, P, pcell, start, sorted);
             FDM_LAUNCH_CHECK();
         }
         {
@@ -855,6 +937,7 @@ int fdmgpu_nbody_create(fdmgpu_nbody** h, int dtype, double x0, double y0, doubl
     if (npp < 1 || npp > 1023) FDM_FAIL(FDMGPU_ESIZE, "npp must be in [1, 1023], got %d", npp);
     const int N = solar ? 10 : nbodies;
     if (N < 1) FDM_FAIL(FDMGPU_EINVAL, "need at least one body, got %d", nbodies);
+    if (N > (1 << 28)) FDM_FAIL(FDMGPU_ESIZE, "at most 2^28 bodies, got %d", N);
     if (!(l > 0) || !(dt > 0)) FDM_FAIL(FDMGPU_EINVAL, "l and dt must be positive");
     std::unique_ptr<fdmgpu_nbody> p(new fdmgpu_nbody());
     p->dtype = dtype;
