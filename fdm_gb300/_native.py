@@ -110,6 +110,9 @@ _SIGS = [
     ("fdmgpu_nscyl_field_info", c_int, [c_void_p, c_int, POINTER(c_size_t), POINTER(c_int)]),
     ("fdmgpu_nscyl_get_field", c_int, [c_void_p, c_int, c_void_p, c_size_t]),
     ("fdmgpu_nscyl_time_index", c_int, [c_void_p, POINTER(c_int)]),
+    ("fdmgpu_nscyl_set_field", c_int, [c_void_p, c_int, c_void_p, c_size_t]),
+    ("fdmgpu_nscyl_l_step", c_int, [c_void_p, c_int]),
+    ("fdmgpu_nscyl_vrandom", c_int, [c_void_p]),
     ("fdmgpu_nscyl_destroy", c_int, [c_void_p]),
     ("fdmgpu_nbody_create", c_int, [POINTER(c_void_p), c_int] + [c_double] * 4 + [c_int] * 3 + [c_double] * 3
      + [c_int] * 3 + [c_double]),

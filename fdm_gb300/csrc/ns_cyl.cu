@@ -15,6 +15,7 @@
 #include <cmath>
 #include <cstdio>
 #include <memory>
+#include <random>
 #include <type_traits>
 #include <vector>
 
@@ -232,6 +233,109 @@ __global__ void __launch_bounds__(256) k_fgh(Field<T> u, Field<T> v, Field<T> w,
     }
 }
 
+// ---- L_FGH (src/ns_cyl.cpp:279-404): FGH linearised about (u0, v0, w0) ----
+// The reference's expressions term for term (including its
+// (0.5*u[j] + u[j+1]) factor in the radial advection of F), with the same
+// correctly rounded constant and radius divisions as k_fgh.
+template <typename T>
+__global__ void __launch_bounds__(256) k_lfgh(Field<T> u, Field<T> v, Field<T> w, Field<T> u0, Field<T> v0,
+                                              Field<T> w0, Field<T> F, Field<T> G, Field<T> H, Params P,
+                                              const Radii* __restrict__ R) {
+    const long long e = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    const int nj = P.nr + 1, nk = P.zn - P.z0 + 1;
+    if (e >= (long long)P.nphi * nk * nj) return;
+    const int j = (int)(e % nj);
+    const int k = (int)((e / nj) % nk) + P.z0;
+    const int i = (int)(e / ((long long)nj * nk));
+    const double dt = P.dt;
+    auto dif = [&](double x, CDiv d2) { return cdiv(cdiv(x, P.dRe), d2); };
+    if (k >= P.z1) {
+        const Radii& q = R[j];
+        const double r2 = q.rf2, r1 = q.rf1;
+        F(i, k, j) = u(i, k, j) + dt * (
+            dif(r2 * u(i, k, j + 1) - 2 * u(i, k, j) + r1 * u(i, k, j - 1), P.ddr2) +
+            dif(u(i, k + 1, j) - 2 * u(i, k, j) + u(i, k - 1, j), P.ddz2) +
+            cdiv(dif(u(i + 1, k, j) - 2 * u(i, k, j) + u(i - 1, k, j), P.ddphi2), q.drfr) -
+            cdiv(r2 * (0.5 * u(i, k, j) + u(i, k, j + 1)) * (u0(i, k, j) + u0(i, k, j + 1)) -
+                     r1 * (0.5 * u(i, k, j - 1) + u(i, k, j)) * (u0(i, k, j - 1) + u0(i, k, j)),
+                 P.ddr) -
+            cdiv(0.25 * ((u(i, k, j) + u(i, k + 1, j)) * (v0(i, k, j + 1) + v0(i, k, j)) -
+                         (u(i, k - 1, j) + u(i, k, j)) * (v0(i, k - 1, j + 1) + v0(i, k - 1, j))),
+                 P.ddz) -
+            cdiv(0.25 * ((u0(i, k, j) + u0(i, k + 1, j)) * (v(i, k, j + 1) + v(i, k, j)) -
+                         (u0(i, k - 1, j) + u0(i, k, j)) * (v(i, k - 1, j + 1) + v(i, k - 1, j))),
+                 P.ddz) -
+            cdiv(cdiv(0.25 * ((u(i, k, j) + u(i + 1, k, j)) * (w0(i, k, j + 1) + w0(i, k, j)) -
+                              (u(i - 1, k, j) + u(i, k, j)) * (w0(i - 1, k, j + 1) + w0(i - 1, k, j))),
+                      P.ddphi),
+                 q.drf) -
+            cdiv(cdiv(0.25 * ((u0(i, k, j) + u0(i + 1, k, j)) * (w(i, k, j + 1) + w(i, k, j)) -
+                              (u0(i - 1, k, j) + u0(i, k, j)) * (w(i - 1, k, j + 1) + w(i - 1, k, j))),
+                      P.ddphi),
+                 q.drf)
+            + cdiv(0.5 * (w(i, k, j + 1) + w(i, k, j)) * (w0(i, k, j + 1) + w0(i, k, j)), q.drf)
+            - cdiv(cdiv(u(i, k, j), q.drfr), P.dRe)
+            - cdiv(cdiv(cdiv(2 * (0.5 * (w(i, k, j + 1) + w(i, k, j)) - 0.5 * (w(i - 1, k, j + 1) + w(i - 1, k, j))),
+                             q.drfr),
+                        P.ddphi),
+                   P.dRe));
+    }
+    if (j >= 1) {
+        const Radii& q = R[j];
+        const double r2 = q.rc2, r1 = q.rc1;
+        G(i, k, j) = v(i, k, j) + dt * (
+            dif(r2 * v(i, k, j + 1) - 2 * v(i, k, j) + r1 * v(i, k, j - 1), P.ddr2) +
+            dif(v(i, k + 1, j) - 2 * v(i, k, j) + v(i, k - 1, j), P.ddz2) +
+            cdiv(dif(v(i + 1, k, j) - 2 * v(i, k, j) + v(i - 1, k, j), P.ddphi2), q.drcr) -
+            cdiv(0.5 * (v(i, k, j) + v(i, k + 1, j)) * (v0(i, k, j) + v0(i, k + 1, j)) -
+                     0.5 * (v(i, k - 1, j) + v(i, k, j)) * (v0(i, k - 1, j) + v0(i, k, j)),
+                 P.ddz) -
+            cdiv(0.25 * (r2 * (u(i, k, j) + u(i, k + 1, j)) * (v0(i, k, j + 1) + v0(i, k, j)) -
+                         r1 * (u(i, k, j - 1) + u(i, k + 1, j - 1)) * (v0(i, k, j) + v0(i, k, j - 1))),
+                 P.ddr) -
+            cdiv(0.25 * (r2 * (u0(i, k, j) + u0(i, k + 1, j)) * (v(i, k, j + 1) + v(i, k, j)) -
+                         r1 * (u0(i, k, j - 1) + u0(i, k + 1, j - 1)) * (v(i, k, j) + v(i, k, j - 1))),
+                 P.ddr) -
+            cdiv(cdiv(0.25 * ((w(i, k, j) + w(i, k + 1, j)) * (v0(i, k, j) + v0(i + 1, k, j)) -
+                              (w(i - 1, k, j) + w(i - 1, k + 1, j)) * (v0(i - 1, k, j) + v0(i, k, j))),
+                      P.ddphi),
+                 q.drc) -
+            cdiv(cdiv(0.25 * ((w0(i, k, j) + w0(i, k + 1, j)) * (v(i, k, j) + v(i + 1, k, j)) -
+                              (w0(i - 1, k, j) + w0(i - 1, k + 1, j)) * (v(i - 1, k, j) + v(i, k, j))),
+                      P.ddphi),
+                 q.drc));
+        if (k >= P.z1) {
+            H(i, k, j) = w(i, k, j) + dt * (
+                dif(r2 * w(i, k, j + 1) - 2 * w(i, k, j) + r1 * w(i, k, j - 1), P.ddr2) +
+                dif(w(i, k + 1, j) - 2 * w(i, k, j) + w(i, k - 1, j), P.ddz2) +
+                cdiv(dif(w(i + 1, k, j) - 2 * w(i, k, j) + w(i - 1, k, j), P.ddphi2), q.drcr) -
+                cdiv(cdiv(0.5 * (w(i + 1, k, j) + w(i, k, j)) * (w0(i + 1, k, j) + w0(i, k, j)) -
+                              0.5 * (w(i - 1, k, j) + w(i, k, j)) * (w0(i - 1, k, j) + w0(i, k, j)),
+                          P.ddphi),
+                     q.drc) -
+                cdiv(0.25 * (r2 * (u(i + 1, k, j) + u(i, k, j)) * (w0(i, k, j + 1) + w0(i, k, j)) -
+                             r1 * (u(i + 1, k, j - 1) + u(i, k, j - 1)) * (w0(i, k, j) + w0(i, k, j - 1))),
+                     P.ddr) -
+                cdiv(0.25 * (r2 * (u0(i + 1, k, j) + u0(i, k, j)) * (w(i, k, j + 1) + w(i, k, j)) -
+                             r1 * (u0(i + 1, k, j - 1) + u0(i, k, j - 1)) * (w(i, k, j) + w(i, k, j - 1))),
+                     P.ddr) -
+                cdiv(0.25 * ((w(i, k, j) + w(i, k + 1, j)) * (v0(i, k, j) + v0(i + 1, k, j)) -
+                             (w(i, k - 1, j) + w(i, k, j)) * (v0(i, k - 1, j) + v0(i + 1, k - 1, j))),
+                     P.ddz) -
+                cdiv(0.25 * ((w0(i, k, j) + w0(i, k + 1, j)) * (v(i, k, j) + v(i + 1, k, j)) -
+                             (w0(i, k - 1, j) + w0(i, k, j)) * (v(i, k - 1, j) + v(i + 1, k - 1, j))),
+                     P.ddz)
+                - cdiv(w0(i, k, j) * 0.5 * (u(i + 1, k, j) + u(i, k, j)), q.drc)
+                - cdiv(w(i, k, j) * 0.5 * (u0(i + 1, k, j) + u0(i, k, j)), q.drc)
+                - cdiv(cdiv(w(i, k, j), q.drcr), P.dRe)
+                + cdiv(cdiv(cdiv(2 * (0.5 * (u(i + 1, k, j) + u(i, k, j)) - 0.5 * (u(i, k, j) + u(i - 1, k, j))),
+                                 q.drcr),
+                            P.ddphi),
+                       P.dRe));
+        }
+    }
+}
+
 // ---- poisson right-hand side (src/ns_cyl.cpp:407-441) ----------------------
 template <typename T>
 __global__ void k_rhs(Field<T> F, Field<T> G, Field<T> H, Field<T> p, Field<T> RHS, Params P,
@@ -277,19 +381,23 @@ __global__ void k_update(Field<T> u, Field<T> v, Field<T> w, Field<T> p, Field<T
 template <typename T>
 struct NSCylPlan {
     cyl::Params P;
-    cyl::Field<T> f[9];  // u v w p x F G H RHS
+    // u v w p x F G H RHS, then the linearisation point u0 v0 w0 of L_step
+    // (src/ns_cyl.h:40-41, the layouts of u, v, w)
+    cyl::Field<T> f[12];
     void* mem = nullptr;
     DevBuf radii;
     fdmgpu_lapl_cyl* lapl = nullptr;
     cudaStream_t st = nullptr;
-    cudaGraph_t graph = nullptr;
-    cudaGraphExec_t gexec = nullptr;
+    cudaGraph_t graph = nullptr, lgraph = nullptr;
+    cudaGraphExec_t gexec = nullptr, lgexec = nullptr;
     int time_index = 0;
-    int steps_run = 0;
+    int steps_run = 0, lsteps_run = 0;
 
     ~NSCylPlan() {
         if (gexec) cudaGraphExecDestroy(gexec);
         if (graph) cudaGraphDestroy(graph);
+        if (lgexec) cudaGraphExecDestroy(lgexec);
+        if (lgraph) cudaGraphDestroy(lgraph);
         if (lapl) fdmgpu_lapl_cyl_destroy(lapl);
         if (mem) cudaFree(mem);
         if (st) cudaStreamDestroy(st);
@@ -307,6 +415,9 @@ struct NSCylPlan {
         f[6] = cyl::make<T>(nphi, zp, P.z0, P.zn, 1, nr);
         f[7] = cyl::make<T>(nphi, zp, P.z1, P.zn, 1, nr);
         f[8] = cyl::make<T>(nphi, zp, P.z1, P.zn, 1, nr);
+        f[9] = f[0];
+        f[10] = f[1];
+        f[11] = f[2];
         size_t total = 0;
         for (auto& fi : f) total += (size_t)((fi.size + 31) / 32 * 32);
         FDM_CUDA(cudaMalloc(&mem, total * sizeof(T)));
@@ -343,7 +454,7 @@ struct NSCylPlan {
         if (rc) throw Error{rc};
     }
 
-    void enqueue_step() {
+    void enqueue_step(bool linear = false) {
         const int B = 256;
         auto blocks = [&](long long n) { return (unsigned)((n + B - 1) / B); };
         const int nr = P.nr, nphi = P.nphi;
@@ -360,10 +471,15 @@ struct NSCylPlan {
             cyl::k_bound_c<T><<<blocks(nc), B, 0, st>>>(f[0], f[1], f[3], P);
             FDM_LAUNCH_CHECK();
         }
-        {
+        if (!linear) {
             FDM_TIMED("cyl_fgh", st);
             cyl::k_fgh<T><<<blocks((long long)nphi * (P.zn - P.z0 + 1) * (nr + 1)), B, 0, st>>>(
                 f[0], f[1], f[2], f[5], f[6], f[7], P, R);
+            FDM_LAUNCH_CHECK();
+        } else {
+            FDM_TIMED("cyl_lfgh", st);
+            cyl::k_lfgh<T><<<blocks((long long)nphi * (P.zn - P.z0 + 1) * (nr + 1)), B, 0, st>>>(
+                f[0], f[1], f[2], f[9], f[10], f[11], f[5], f[6], f[7], P, R);
             FDM_LAUNCH_CHECK();
         }
         const long long cells = (long long)nphi * (P.zn - P.z1 + 1) * nr;
@@ -380,29 +496,51 @@ struct NSCylPlan {
         }
     }
 
-    void step(int k) {
+    // step() (linear = false) or L_step() (linear = true): the first of each
+    // kind runs eagerly, later ones replay its captured graph
+    void step(int k, bool linear = false) {
+        int& run = linear ? lsteps_run : steps_run;
+        cudaGraph_t& g_ = linear ? lgraph : graph;
+        cudaGraphExec_t& ge = linear ? lgexec : gexec;
         for (int s = 0; s < k; s++) {
-            if (steps_run == 0) {
-                enqueue_step();
+            if (run == 0) {
+                enqueue_step(linear);
             } else {
-                if (!gexec) {
+                if (!ge) {
                     FDM_CUDA(cudaStreamBeginCapture(st, cudaStreamCaptureModeThreadLocal));
                     try {
-                        enqueue_step();
+                        enqueue_step(linear);
                     } catch (...) {
                         cudaGraph_t g = nullptr;
                         cudaStreamEndCapture(st, &g);
                         if (g) cudaGraphDestroy(g);
                         throw;
                     }
-                    FDM_CUDA(cudaStreamEndCapture(st, &graph));
-                    FDM_CUDA(cudaGraphInstantiate(&gexec, graph, 0));
+                    FDM_CUDA(cudaStreamEndCapture(st, &g_));
+                    FDM_CUDA(cudaGraphInstantiate(&ge, g_, 0));
                 }
-                FDM_CUDA(cudaGraphLaunch(gexec, st));
+                FDM_CUDA(cudaGraphLaunch(ge, st));
             }
-            steps_run++;
+            run++;
             time_index++;
         }
+    }
+
+    // the constructor's ns:vrandom=1 perturbation (src/ns_cyl.h:99-109): v
+    // over phi, z1..zn, r 1..nr drawn in that order from the standard
+    // library's default engine, uniform in [-1e-3, 1e-3) in T
+    void vrandom() {
+        const auto& v = f[1];
+        std::vector<T> host((size_t)v.size);
+        FDM_CUDA(cudaStreamSynchronize(st));
+        FDM_CUDA(cudaMemcpy(host.data(), v.p, host.size() * sizeof(T), cudaMemcpyDeviceToHost));
+        std::default_random_engine gen;
+        std::uniform_real_distribution<T> dist(-1e-3, 1e-3);
+        for (int i = 0; i < P.nphi; i++)
+            for (int k = P.z1; k <= P.zn; k++)
+                for (int j = 1; j <= P.nr; j++)
+                    host[(size_t)i * v.sz + (size_t)(k - v.z1) * v.sy + (size_t)(j - v.x1)] = dist(gen);
+        FDM_CUDA(cudaMemcpy(v.p, host.data(), host.size() * sizeof(T), cudaMemcpyHostToDevice));
     }
 };
 
@@ -486,7 +624,7 @@ int fdmgpu_nscyl_step(fdmgpu_nscyl* h, int k) {
 
 int fdmgpu_nscyl_field_info(fdmgpu_nscyl* h, int field, size_t* count, int* r) {
     FDM_API_BEGIN
-    if (!h || field < 0 || field > 8) FDM_FAIL(FDMGPU_EINVAL, "bad handle or field %d", field);
+    if (!h || field < 0 || field > 11) FDM_FAIL(FDMGPU_EINVAL, "bad handle or field %d", field);
     with_cyl(h, [&](auto& s) {
         const auto& f = s.f[field];
         if (count) *count = (size_t)f.size;
@@ -497,9 +635,41 @@ int fdmgpu_nscyl_field_info(fdmgpu_nscyl* h, int field, size_t* count, int* r) {
     FDM_API_END
 }
 
+int fdmgpu_nscyl_set_field(fdmgpu_nscyl* h, int field, const void* host, size_t count) {
+    FDM_API_BEGIN
+    if (!h || !host || field < 0 || field > 11) FDM_FAIL(FDMGPU_EINVAL, "bad argument");
+    with_cyl(h, [&](auto& s) {
+        const auto& f = s.f[field];
+        if (count != (size_t)f.size) FDM_FAIL(FDMGPU_EINVAL, "field has %lld elements, got %zu", f.size, count);
+        FDM_CUDA(cudaStreamSynchronize(s.st));
+        FDM_CUDA(cudaMemcpy(f.p, host, count * sizeof(*f.p), cudaMemcpyHostToDevice));
+    });
+    FDM_API_END
+}
+
+int fdmgpu_nscyl_l_step(fdmgpu_nscyl* h, int k) {
+    FDM_API_BEGIN
+    if (!h) FDM_FAIL(FDMGPU_EINVAL, "null handle");
+    if (k < 0) FDM_FAIL(FDMGPU_EINVAL, "negative step count");
+    with_cyl(h, [&](auto& s) { s.step(k, true); });
+    FDM_API_END
+}
+
+int fdmgpu_nscyl_vrandom(fdmgpu_nscyl* h) {
+    FDM_API_BEGIN
+    if (!h) FDM_FAIL(FDMGPU_EINVAL, "null handle");
+    with_cyl(h, [&](auto& s) {
+        if (!s.P.zper)
+            FDM_FAIL(FDMGPU_ENOTSUP, "vrandom perturbs v on the z walls, which the reference's Dirichlet-z "
+                                     "step rejects: verify(std::abs(v[i][nz][j]) < 1e-15), src/ns_cyl.cpp:160");
+        s.vrandom();
+    });
+    FDM_API_END
+}
+
 int fdmgpu_nscyl_get_field(fdmgpu_nscyl* h, int field, void* host, size_t count) {
     FDM_API_BEGIN
-    if (!h || !host || field < 0 || field > 8) FDM_FAIL(FDMGPU_EINVAL, "bad argument");
+    if (!h || !host || field < 0 || field > 11) FDM_FAIL(FDMGPU_EINVAL, "bad argument");
     with_cyl(h, [&](auto& s) {
         const auto& f = s.f[field];
         if (count != (size_t)f.size) FDM_FAIL(FDMGPU_EINVAL, "field has %lld elements, got %zu", f.size, count);

@@ -140,6 +140,8 @@ class NSCyl:
     periodic_z selects zflag = periodic.  Fields are (phi, z, r) with r
     fastest, returned as Tensor3 over their inclusive ranges."""
 
+    FIELDS = FIELDS + ("u0", "v0", "w0")
+
     def __init__(self, cfg: Config | None = None, dtype=np.float64, periodic_z: bool = False, **overrides):
         cfg = cfg or Config()
         for k, v in overrides.items():
@@ -162,9 +164,26 @@ class NSCyl:
                                               float(self.h2), float(self.U0), float(self.Re), float(self.dt),
                                               int(self.nr), int(self.nz), int(self.nphi)))
         self._h = h
+        if int(cfg.get("ns", "vrandom", 0)) == 1:
+            N.check(self._lib.fdmgpu_nscyl_vrandom(self._h))
 
     def step(self, k: int = 1) -> None:
         N.check(self._lib.fdmgpu_nscyl_step(self._h, int(k)))
+
+    def L_step(self, k: int = 1) -> None:
+        """NSCyl::L_step: the step linearised about u0, v0, w0."""
+        N.check(self._lib.fdmgpu_nscyl_l_step(self._h, int(k)))
+
+    def set(self, name: str, values) -> None:
+        """Overwrites a whole field (ghosts included), e.g. the
+        linearisation point w0 or a perturbation of u, v, w, p."""
+        fid = self.FIELDS.index(name)
+        cnt = c_size_t()
+        N.check(self._lib.fdmgpu_nscyl_field_info(self._h, fid, byref(cnt), None))
+        a = np.ascontiguousarray(values.data if isinstance(values, Tensor3) else values, self.dtype).ravel()
+        if a.size != cnt.value:
+            raise ValueError("%s has %d elements, got %d" % (name, cnt.value, a.size))
+        N.check(self._lib.fdmgpu_nscyl_set_field(self._h, fid, a.ctypes.data, cnt.value))
 
     @property
     def time_index(self) -> int:
@@ -173,7 +192,7 @@ class NSCyl:
         return t.value
 
     def get(self, name: str) -> Tensor3:
-        fid = FIELDS.index(name)
+        fid = self.FIELDS.index(name)
         cnt = c_size_t()
         r = (c_int * 6)()
         N.check(self._lib.fdmgpu_nscyl_field_info(self._h, fid, byref(cnt), r))

@@ -361,6 +361,16 @@ int fdmgpu_nscyl_create(fdmgpu_nscyl** h, int dtype, int periodic_z, double R, d
 int fdmgpu_nscyl_step(fdmgpu_nscyl* h, int k);
 int fdmgpu_nscyl_field_info(fdmgpu_nscyl* h, int field, size_t* count, int* ranges6);
 int fdmgpu_nscyl_get_field(fdmgpu_nscyl* h, int field, void* host, size_t count);
+/* Fields 9, 10, 11 are u0, v0, w0, the state L_step linearises about
+ * (src/ns_cyl.h:40-41, zero until set; layouts of u, v, w).  set_field
+ * overwrites a whole field, ghosts included. */
+int fdmgpu_nscyl_set_field(fdmgpu_nscyl* h, int field, const void* host, size_t count);
+/* NSCyl::L_step (src/ns_cyl.cpp:65-77): init_bound, L_FGH (:279-404),
+ * poisson, update; k steps, captured into its own CUDA graph */
+int fdmgpu_nscyl_l_step(fdmgpu_nscyl* h, int k);
+/* the constructor's ns:vrandom=1 option (src/ns_cyl.h:99-109): call right
+ * after fdmgpu_nscyl_create */
+int fdmgpu_nscyl_vrandom(fdmgpu_nscyl* h);
 int fdmgpu_nscyl_time_index(fdmgpu_nscyl* h, int* t);
 int fdmgpu_nscyl_destroy(fdmgpu_nscyl* h);
 

@@ -107,7 +107,7 @@ class Port:
 
 
 class _NS:
-    FIELDS = ("u", "v", "w", "p", "x", "F", "G", "H", "RHS")
+    FIELDS = ("u", "v", "w", "p", "x", "F", "G", "H", "RHS", "u0", "v0", "w0")
 
     def __init__(self, L, h, kind):
         self.L, self.h, self.kind = L, h, kind
@@ -128,6 +128,16 @@ class _NS:
         out = np.zeros(n)
         getter(self.h, fid, _p(out))
         return out
+
+    def l_step(self, k: int = 1) -> None:
+        """NSCyl::L_step (cylindrical reference only)."""
+        self._fn("l_step")(self.h, int(k))
+
+    def set(self, name: str, values) -> None:
+        """Overwrites a whole field, ghosts included (cylindrical reference only)."""
+        a = np.ascontiguousarray(values, np.float64).ravel()
+        assert a.size == self._fn("get")(self.h, self.FIELDS.index(name), None)
+        self._fn("set")(self.h, self.FIELDS.index(name), _p(a))
 
     def close(self):
         if self.h:
@@ -167,6 +177,11 @@ class Reference:
         L.ref_nscyl_get.restype = c_long
         L.ref_nscyl_get.argtypes = [c_void_p, c_int, _dp]
         L.ref_nscyl_destroy.argtypes = [c_void_p]
+        L.ref_nscyl_create_v.restype = c_void_p
+        L.ref_nscyl_create_v.argtypes = [c_int] + [c_double] * 7 + [c_int] * 4
+        L.ref_nscyl_l_step.argtypes = [c_void_p, c_int]
+        L.ref_nscyl_set.restype = c_long
+        L.ref_nscyl_set.argtypes = [c_void_p, c_int, _dp]
         L.ref_nscubef_create.restype = c_void_p
         L.ref_nscubef_create.argtypes = [c_int, c_int] + [c_double] * 9
         L.ref_nscubef_step.argtypes = [c_void_p, c_int]
@@ -239,10 +254,12 @@ class Reference:
     def nscube(self, nx, nz, Re, dt, u0=1.0, box=(-np.pi, -np.pi, -np.pi, np.pi, np.pi, np.pi)):
         return _NS(self.L, self.L.ref_nscube_create(nx, nz, Re, dt, u0, *box), "ref")
 
-    def nscyl(self, nr, nz, nphi, Re, dt, u0=1.0, R=np.pi, r0=np.pi / 2, h1=0.0, h2=10.0, periodic_z=False):
-        """NSCyl<double,false,zflag> (src/ns_cyl.h:18-134)."""
-        return _NS(self.L, self.L.ref_nscyl_create(1 if periodic_z else 0, R, r0, h1, h2, u0, Re, dt, nr, nz,
-                                                   nphi), "cyl")
+    def nscyl(self, nr, nz, nphi, Re, dt, u0=1.0, R=np.pi, r0=np.pi / 2, h1=0.0, h2=10.0, periodic_z=False,
+              vrandom=False):
+        """NSCyl<double,false,zflag> (src/ns_cyl.h:18-134); vrandom sets
+        ns:vrandom=1."""
+        return _NS(self.L, self.L.ref_nscyl_create_v(1 if periodic_z else 0, R, r0, h1, h2, u0, Re, dt, nr, nz,
+                                                     nphi, 1 if vrandom else 0), "cyl")
 
     def nscube_float(self, nx, nz, Re, dt, u0=1.0, box=(-np.pi, -np.pi, -np.pi, np.pi, np.pi, np.pi)):
         """NSCube<float,false>; fields come back widened to float64."""

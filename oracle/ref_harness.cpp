@@ -204,8 +204,10 @@ struct RefNSCyl {
     NSCyl<double, false, tensor_flag::periodic>* p = nullptr;
 };
 
-void* ref_nscyl_create(int periodic_z, double R, double r0, double h1, double h2, double u0, double Re, double dt,
-                       int nr, int nz, int nphi) {
+// ns:vrandom=1 when vrandom != 0 (the constructor's random v perturbation,
+// src/ns_cyl.h:99-109)
+void* ref_nscyl_create_v(int periodic_z, double R, double r0, double h1, double h2, double u0, double Re, double dt,
+                         int nr, int nz, int nphi, int vrandom) {
     auto* h = new RefNSCyl();
     char buf[16][96];
     const char* keys[] = {"nr", "nz", "nphi", "R", "r", "h1", "h2", "u0", "Re", "dt"};
@@ -217,10 +219,17 @@ void* ref_nscyl_create(int periodic_z, double R, double r0, double h1, double h2
         else snprintf(buf[i], sizeof(buf[i]), "--ns:%s=%.17g", keys[i], vals[i]);
         argv[i + 1] = buf[i];
     }
-    h->cfg.rewrite(11, argv);
+    int argc = 11;
+    if (vrandom) argv[argc++] = (char*)"--ns:vrandom=1";
+    h->cfg.rewrite(argc, argv);
     if (periodic_z) h->p = new NSCyl<double, false, tensor_flag::periodic>(h->cfg);
     else h->d = new NSCyl<double, false, tensor_flag::none>(h->cfg);
     return h;
+}
+
+void* ref_nscyl_create(int periodic_z, double R, double r0, double h1, double h2, double u0, double Re, double dt,
+                       int nr, int nz, int nphi) {
+    return ref_nscyl_create_v(periodic_z, R, r0, h1, h2, u0, Re, dt, nr, nz, nphi, 0);
 }
 
 int ref_nscyl_step(void* hp, int k) {
@@ -232,23 +241,64 @@ int ref_nscyl_step(void* hp, int k) {
     return 0;
 }
 
+// NSCyl::L_step (src/ns_cyl.cpp:65-77): the step linearised about u0, v0, w0
+int ref_nscyl_l_step(void* hp, int k) {
+    auto* h = (RefNSCyl*)hp;
+    for (int i = 0; i < k; i++) {
+        if (h->d) h->d->L_step();
+        else h->p->L_step();
+    }
+    return 0;
+}
+
 }  // extern "C"
+
+// fields 0..8: u v w p x F G H RHS; 9..11: the linearisation point u0 v0 w0
+template <typename NS>
+static typename NS::tensor* nscyl_field(NS* ns, int field) {
+    switch (field) {
+        case 0: return &ns->u;
+        case 1: return &ns->v;
+        case 2: return &ns->w;
+        case 3: return &ns->p;
+        case 4: return &ns->x;
+        case 5: return &ns->F;
+        case 6: return &ns->G;
+        case 7: return &ns->H;
+        case 8: return &ns->RHS;
+        case 9: return &ns->u0;
+        case 10: return &ns->v0;
+        default: return &ns->w0;
+    }
+}
 
 template <typename NS>
 static long nscyl_get(NS* ns, int field, double* out) {
-    auto* t = field == 0 ? &ns->u : field == 1 ? &ns->v : field == 2 ? &ns->w : field == 3 ? &ns->p
-            : field == 4 ? &ns->x : field == 5 ? &ns->F : field == 6 ? &ns->G : field == 7 ? &ns->H : &ns->RHS;
+    auto* t = nscyl_field(ns, field);
     long n = t->size;
     if (out) memcpy(out, t->vec, sizeof(double) * n);
     return n;
+}
+
+template <typename NS>
+static long nscyl_set(NS* ns, int field, const double* in) {
+    auto* t = nscyl_field(ns, field);
+    memcpy(t->vec, in, sizeof(double) * t->size);
+    return t->size;
 }
 
 extern "C" {
 
 long ref_nscyl_get(void* hp, int field, double* out) {
     auto* h = (RefNSCyl*)hp;
-    if (field < 0 || field > 8) return -1;
+    if (field < 0 || field > 11) return -1;
     return h->d ? nscyl_get(h->d, field, out) : nscyl_get(h->p, field, out);
+}
+
+long ref_nscyl_set(void* hp, int field, const double* in) {
+    auto* h = (RefNSCyl*)hp;
+    if (field < 0 || field > 11) return -1;
+    return h->d ? nscyl_set(h->d, field, in) : nscyl_set(h->p, field, in);
 }
 
 void ref_nscyl_destroy(void* hp) {

@@ -76,6 +76,19 @@ def f32_line(N: int, t: int) -> np.ndarray:
     return np.random.default_rng(1000 + t).uniform(-1, 1, N - 1).astype(np.float32)
 
 
+def couette_w0(nr, nz, nphi, pz, R=math.pi, r0=math.pi / 2, U0=1.0, h1=0.0, h2=10.0):
+    """The base flow test/test_ns_cyl_spectral.cpp:64-73 puts into w0:
+    -U0 r0^2/(R^2-r0^2) + U0 r0^2 R^2/(R^2-r0^2)/r/r at r = r0 + dr j + dr/2,
+    j = 0..nr, over w0's storage (phi, z0..znn, 0..nr+1); other entries 0."""
+    dr = (R - r0) / nr
+    zs = nz if pz else nz + 2
+    w0 = np.zeros((nphi, zs, nr + 2))
+    for j in range(nr + 1):
+        r = r0 + dr * j + dr / 2
+        w0[:, :nz, j] = (-U0 * r0 * r0 / (R * R - r0 * r0) + U0 * r0 * r0 * R * R / (R * R - r0 * r0) / r / r)
+    return w0.ravel()
+
+
 # tag, T, N, n, npp, local, solar (solar: the ten-body table, N ignored)
 NBODY_CASES = (
     ("d", np.float64, 400, 16, 8, 0, 0),
@@ -192,6 +205,33 @@ def main():
         m.step(20)
         for f in ("u", "v", "w", "p", "x"):
             cyl["ns_%s_s20_%s" % (name, f)] = m.get(f)
+        m.close()
+    # NSCyl::L_step (src/ns_cyl.cpp:65-77) as the spectral driver uses it
+    # (test/test_ns_cyl_spectral.cpp:60-96): the Couette profile as w0 and the
+    # wall speed set to 0.  Periodic z: the constructor's vrandom perturbation
+    # of v (stored, to pin it).  Dirichlet z (where vrandom trips the
+    # reference's own wall check, src/ns_cyl.cpp:160): a seeded perturbation
+    # of u (r < R) and w.  The fields after 10 linearised steps.
+    rng = np.random.default_rng(77)
+    for name, pz, (nr, nz, nphi) in (("d16x15x16", False, (16, 15, 16)), ("p16x16x8", True, (16, 16, 8))):
+        m = R.nscyl(nr, nz, nphi, 100.0, 0.01, u0=0.0, periodic_z=pz, vrandom=pz)
+        if pz:
+            cyl["lin_%s_v_init" % name] = m.get("v")
+        else:
+            u = m.get("u").reshape(nphi, nz + 2, nr + 3)  # z 0..nz+1, r -1..nr+1
+            w = m.get("w").reshape(nphi, nz + 2, nr + 2)  # r 0..nr+1
+            u[:, 1:nz + 1, 2:nr + 1] = 1e-3 * rng.standard_normal((nphi, nz, nr - 1))  # r 1..nr-1
+            w[:, 1:nz + 1, 1:nr + 1] = 1e-3 * rng.standard_normal((nphi, nz, nr))
+            cyl["lin_%s_u_init" % name] = u.ravel()
+            cyl["lin_%s_w_init" % name] = w.ravel()
+            m.set("u", u)
+            m.set("w", w)
+        w0 = couette_w0(nr, nz, nphi, pz)
+        cyl["lin_%s_w0" % name] = w0
+        m.set("w0", w0)
+        m.l_step(10)
+        for f in ("u", "v", "w", "p"):
+            cyl["lin_%s_s10_%s" % (name, f)] = m.get(f)
         m.close()
     np.savez_compressed(OUT / "lapl_cyl.npz", **cyl)
 

@@ -190,3 +190,37 @@ def test_nscyl_vs_reference(cuda, golden, name, pz, shape):
         assert got.size == ref.size, f
         assert np.abs(got - ref).max() <= 1e-11 * max(1.0, np.abs(ref).max()), f
     m.close()
+
+
+@pytest.mark.parametrize("name,pz,shape", [("d16x15x16", False, (16, 15, 16)), ("p16x16x8", True, (16, 16, 8))])
+def test_nscyl_l_step_vs_reference(cuda, golden, name, pz, shape):
+    """NSCyl::L_step, the step linearised about (u0, v0, w0), as the
+    reference's spectral driver runs it: w0 the Couette profile, wall speed
+    0; periodic z starts from the constructor's vrandom perturbation (bit for
+    bit the reference's draws), Dirichlet z from a seeded u, w perturbation.
+    Ten steps against the reference's own L_step."""
+    from fdm_gb300 import NSCyl
+    g = golden("lapl_cyl")
+    nr, nz, nphi = shape
+    m = NSCyl(nr=nr, nz=nz, nphi=nphi, Re=100.0, dt=0.01, u0=0.0, periodic_z=pz, vrandom=1 if pz else 0)
+    if pz:
+        assert np.array_equal(m.get("v").data.ravel(), g["lin_%s_v_init" % name])
+    else:
+        m.set("u", g["lin_%s_u_init" % name])
+        m.set("w", g["lin_%s_w_init" % name])
+    m.set("w0", g["lin_%s_w0" % name])
+    assert np.array_equal(m.get("w0").data.ravel(), g["lin_%s_w0" % name])
+    m.L_step(10)
+    assert m.time_index == 10
+    for f in ("u", "v", "w", "p"):
+        got = m.get(f).data.ravel()
+        ref = g["lin_%s_s10_%s" % (name, f)]
+        assert np.abs(got - ref).max() <= 1e-11 * max(1e-3, np.abs(ref).max()), f
+    m.close()
+
+
+def test_nscyl_vrandom_dirichlet_rejected(cuda):
+    from fdm_gb300 import FdmError, NSCyl
+    with pytest.raises(FdmError) as e:
+        NSCyl(nr=16, nz=15, nphi=16, vrandom=1)
+    assert e.value.status == 6
