@@ -436,6 +436,27 @@ static std::vector<double> lambda_host(int n, double h) {
     return v;
 }
 
+// Conditioning limit of the mixed-precision solve.  kappa = (sum over the
+// axes of the largest eigenvalue) / (sum of the smallest) of the discrete
+// operator.  Measured on GB300 with one refinement sweep at tol 1e-10:
+// 255^3 (kappa 2.7e4) reaches 2e-12 on smooth and 1.6e-11 on white-noise
+// data; axes of 1023 points (kappa 1.5e5 to 4.2e5) stall between 1e-10 and
+// 1e-7 however many sweeps run, because the second differences cancel more
+// digits (1/h^2 ~ 1e6) than the float-float residual carries and the FP32
+// tridiagonal z-solve of 1023 rows loses more than the refinement recovers.
+// Plans above the limit run the FP64 solver instead.
+constexpr double kMixedKappaMax = 3.0e4;
+
+static double lapl_kappa(int nx, int ny, int nz, double hx, double hy, double hz) {
+    auto lam = [](int n, double h, int j) {
+        const double s = std::sin(j * M_PI * 0.5 / (n + 1));
+        return 4. / (h * h) * (s * s);
+    };
+    const double hi = lam(nx, hx, nx) + lam(ny, hy, ny) + lam(nz, hz, nz);
+    const double lo = lam(nx, hx, 1) + lam(ny, hy, 1) + lam(nz, hz, 1);
+    return hi / lo;
+}
+
 static void check_grid_y(int nrhs) {
     if (nrhs < 1 || nrhs > 65535) FDM_FAIL(FDMGPU_EINVAL, "nrhs must be in [1, 65535], got %d", nrhs);
 }
@@ -464,6 +485,7 @@ struct CubePlan {
     int dst_tc = 0;         // bit 0 / bit 1: plain FP32 DST passes along x / y on the tensor cores (32-, 64-,
                             // 128-point axes)
     bool periodic = false;  // all three axes periodic (real FFTs, divide, inverse FFTs)
+    bool mixed_ok = true;   // within the mixed solve's conditioning limit (kMixedKappaMax)
     DevBuf ptw_x, ptw_y, ptw_z, plam_x, plam_y, plam_z;
     DevBuf tc_img_x, tc_img_y, tc_err;
     int zm64 = 0, zP64 = 0, zm32 = 0, zP32 = 0;
@@ -589,6 +611,7 @@ struct CubePlan {
         hz_eff = (nz == ny) ? dy : dz;
         zfac = dz * slz * slz * (nz + 1) / 2.0;
         S = (dx * slx * slx * (nx + 1) / 2.0) * (dy * sly * sly * (ny + 1) / 2.0) * zfac;
+        mixed_ok = lapl_kappa(nx, ny, nz, hx_eff, dy, hz_eff) <= kMixedKappaMax;
         if (dtype == FDMGPU_F64) {
             tx64.build(nx + 1);
             ty64.build(ny + 1);
@@ -670,8 +693,9 @@ struct CubePlan {
             else run_periodic<float>((float*)ans, (const float*)rhs, nrhs, st);
             return;
         }
-        if (precision == FDMGPU_PLAIN) {
-            last_sweeps = 0;
+        if (precision == FDMGPU_PLAIN || !mixed_ok) {
+            // a mixed plan beyond the conditioning limit solves in FP64
+            last_sweeps = precision == FDMGPU_PLAIN ? 0 : -1;
             if (dtype == FDMGPU_F64) run_plain<double>((double*)ans, (const double*)rhs, nrhs, tx64, ty64, lamx64,
                                                        lamy64, st);
             else run_plain<float>((float*)ans, (const float*)rhs, nrhs, tx32, ty32, lamx32, lamy32, st);
@@ -782,7 +806,7 @@ struct CubePlan {
     // volumes of the last mixed solve on st (synchronises st): the relative
     // error of the FP32 inner solve.  0 when the last solve ran no sweep.
     double first_sweep_est(int nrhs, cudaStream_t st) {
-        if (last_sweeps == 0 || !norms.p) return 0.0;
+        if (last_sweeps <= 0 || !norms.p) return 0.0;
         FDM_CUDA(cudaStreamSynchronize(st));
         std::vector<double> v((size_t)2 * nrhs);
         FDM_CUDA(cudaMemcpy(v.data(), norms.p, v.size() * sizeof(double), cudaMemcpyDeviceToHost));
@@ -1000,7 +1024,7 @@ struct BatchPlan {
         void* const* vout = (void* const*)gr.ptr_out.p;
         for (int s0 = 0; s0 < m; s0 += ch) {
             const int k = std::min(ch, m - s0);
-            if (precision == FDMGPU_MIXED) c.run_mixed(nullptr, nullptr, k, st, vin + s0, vout + s0);
+            if (precision == FDMGPU_MIXED && c.mixed_ok) c.run_mixed(nullptr, nullptr, k, st, vin + s0, vout + s0);
             else c.run_plain_ptrs(vin + s0, vout + s0, k, st);
         }
     }
@@ -1358,6 +1382,11 @@ static void noalloc_solve(double dx, double dy, double dz, double lx, double ly,
     const double zfac = dz * slz * slz * (nz + 1) / 2.0;
     const double S = (dx * slx * slx * (nx + 1) / 2.0) * (dy * sly * sly * (ny + 1) / 2.0) * zfac;
     int sweeps = tol >= 1e-5 ? 0 : (tol >= 1e-11 ? 1 : 2);
+    if (lapl_kappa(nx, ny, nz, hx_eff, dy, hz_eff) > kMixedKappaMax)
+        FDM_FAIL(FDMGPU_ENOTSUP,
+                 "%dx%dx%d is beyond the mixed-precision conditioning limit (kappa %.3g > %.3g): the handle API "
+                 "solves such sizes in FP64",
+                 nx, ny, nz, lapl_kappa(nx, ny, nz, hx_eff, dy, hz_eff), kMixedKappaMax);
 
     const long long V = (long long)nx * ny * nz * nrhs;
     const size_t need = noalloc_axis_bytes(nx + 1) + noalloc_axis_bytes(ny + 1) +
@@ -1528,7 +1557,7 @@ int fdmgpu_lapl_cube_last_info(fdmgpu_lapl_cube* h, int* sweeps, double* est, in
     if (sweeps) *sweeps = c.last_sweeps;
     if (est) {
         if (nrhs > c.last_nrhs) FDM_FAIL(FDMGPU_EINVAL, "asked for %d estimates, last solve had %d", nrhs, c.last_nrhs);
-        if (c.last_sweeps == 0) {
+        if (c.last_sweeps <= 0) {
             for (int i = 0; i < nrhs; i++) est[i] = -1.0;
         } else {
             std::vector<double> v((size_t)2 * c.last_nrhs);

@@ -98,7 +98,12 @@ int fdmgpu_lapl_cube_create(fdmgpu_lapl_cube** h, int dtype, int bc_flags,
                             double lx, double ly, double lz,
                             int nx, int ny, int nz);
 /* FDMGPU_MIXED needs dtype F64.  tol: target relative error (<= 0 selects
- * 1e-10); max_sweeps: refinement sweeps cap (< 0 selects 3). */
+ * 1e-10); max_sweeps: refinement sweeps cap (< 0 selects 3).  Sweeps run by
+ * the tolerance: none for tol >= 1e-5, one down to 1e-11, two below.  Plans
+ * whose operator is too ill-conditioned for FP32 inner solves (the ratio of
+ * the largest to the smallest eigenvalue, summed over the axes, above 3e4:
+ * 255^3 is 2.7e4, an axis of 511 or more points exceeds it) solve in FP64
+ * instead; last_info then reports sweeps = -1. */
 int fdmgpu_lapl_cube_set_precision(fdmgpu_lapl_cube* h, int precision, double tol, int max_sweeps);
 /* host pointers, synchronous (LaplCube::solve, src/lapl_cube.cpp:9) */
 int fdmgpu_lapl_cube_solve(fdmgpu_lapl_cube* h, void* ans, const void* rhs);
@@ -126,7 +131,9 @@ int fdmgpu_lapl_cube_solve_device(fdmgpu_lapl_cube* h, void* d_ans, const void* 
  * loaded on, until the process exits.  A solve needs about
  * 4*nx*ny*nz*nrhs bytes per FP32 volume (2 volumes for one refinement sweep,
  * 3 for two) plus a few KB; larger requests return FDMGPU_EBUDGET with the
- * byte counts in the message.  The first call on a device looks up the
+ * byte counts in the message, and sizes beyond the mixed solve's conditioning
+ * limit (see fdmgpu_lapl_cube_set_precision) return FDMGPU_ENOTSUP.  The
+ * first call on a device looks up the
  * array's device address (and loads the module there); make that first call
  * before any stream capture.  All calls on a device share the array: calls
  * that overlap on the GPU (other streams, other host threads) race on it, so
@@ -137,9 +144,10 @@ int fdmgpu_lapl_cube_solve_device(fdmgpu_lapl_cube* h, void* d_ans, const void* 
 int fdmgpu_lapl_cube_solve_mixed_noalloc(double dx, double dy, double dz, double lx, double ly, double lz,
                                          int nx, int ny, int nz, double tol, void* d_ans, const void* d_rhs,
                                          int nrhs, void* stream);
-/* refinement report of the last solve: sweeps done and, per RHS, the
- * relative size of the last correction ||c||_2/||u||_2 (an upper estimate of
- * the remaining relative error).  est may be NULL; it receives nrhs values.
+/* refinement report of the last solve: sweeps done (-1: a mixed plan that
+ * solved in FP64) and, per RHS, the relative size of the last correction
+ * ||c||_2/||u||_2 (an upper estimate of the remaining relative error; -1 when
+ * no sweep ran).  est may be NULL; it receives nrhs values.
  * Synchronises the handle's last stream. */
 int fdmgpu_lapl_cube_last_info(fdmgpu_lapl_cube* h, int* sweeps, double* est, int nrhs);
 /* bytes of device scratch the handle holds */

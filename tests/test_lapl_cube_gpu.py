@@ -290,3 +290,81 @@ def test_periodic_errors(cuda):
     with pytest.raises(FdmError) as e:
         LaplCube(0.1, 0.1, 0.1, 1.6, 1.6, 1.6, 16, 16, 16, periodic=True, precision="mixed")
     assert e.value.status == 6
+
+
+def _lap7_torch(u, hx, hy, hz):
+    """7-point Dirichlet Laplacian on the device (zero outside the box)."""
+    import torch
+    p = torch.nn.functional.pad(u, (1, 1, 1, 1, 1, 1))
+    return ((p[1:-1, 1:-1, 2:] + p[1:-1, 1:-1, :-2] - 2 * u) / hx ** 2
+            + (p[1:-1, 2:, 1:-1] + p[1:-1, :-2, 1:-1] - 2 * u) / hy ** 2
+            + (p[2:, 1:-1, 1:-1] + p[:-2, 1:-1, 1:-1] - 2 * u) / hz ** 2)
+
+
+def test_maximum_size_1023_cubed(cuda):
+    """The largest supported size, 1023^3 (8.6 GB per FP64 volume): the
+    plain FP64 answer satisfies the 7-point equation to round-off and the
+    mixed solve agrees with it at the requested tolerance (size-independent
+    properties; the CPU oracle would take minutes here)."""
+    import torch
+    n = 1023
+    f, _ = workloads.manufactured_torch(n, n, n, seed=9, kmax=100, noise=1e-3)
+    args = workloads.solver_args(n, n, n)
+    plain = LaplCube(*args)
+    u = torch.empty_like(f)
+    plain.solve_device(u, f)
+    torch.cuda.synchronize()
+    h = args[0]
+    r = _lap7_torch(u, h, h, h)
+    r -= f
+    assert (torch.linalg.norm(r) / torch.linalg.norm(f)).item() <= 1e-12
+    del r
+    # beyond the mixed solve's conditioning limit: the mixed handle solves in
+    # FP64 and says so
+    mixed = LaplCube(*args, precision="mixed", tol=1e-10)
+    um = torch.empty_like(f)
+    mixed.solve_device(um, f)
+    torch.cuda.synchronize()
+    assert mixed.last_info(1)[0] == -1
+    assert (torch.linalg.norm(um - u) / torch.linalg.norm(u)).item() <= 1e-10
+
+
+@pytest.mark.parametrize("shape", [(1, 1, 1), (1, 3, 7), (3, 1, 1), (1023, 1, 3), (7, 1023, 1)])
+def test_smallest_and_ragged_sizes_vs_oracle(cuda, port, shape):
+    """Degenerate and ragged sizes (one interior point per axis, n = 1023 on
+    one axis) against the oracle, plain FP64 and mixed.  The 1023-point axes
+    are beyond the mixed solve's conditioning limit (FP32 inner solves stall
+    near 1e-9 there), so the mixed handle solves them in FP64."""
+    nz, ny, nx = shape
+    rng = np.random.default_rng(sum(shape))
+    f = rng.standard_normal(shape)
+    args = workloads.solver_args(nx, ny, nz)
+    ref = port.lapl_cube(f, *args[:6])
+    ans = np.zeros_like(f)
+    LaplCube(*args).solve(ans, f)
+    # z is solved as tridiagonal systems where the reference transforms it: a
+    # 1023-row z line (eigenvalue ratio ~4e5) carries round-off of a few 1e-12
+    assert rel_l2(ans, ref) <= (5e-11 if nz == 1023 else 1e-12)
+    ans2 = np.zeros_like(f)
+    m = LaplCube(*args, precision="mixed", tol=1e-10)
+    m.solve(ans2, f)
+    assert rel_l2(ans2, ref) <= 1e-10
+    assert m.last_info(1)[0] == (-1 if max(shape) == 1023 else 1)
+
+
+def test_mixed_white_noise_at_the_conditioning_limit(cuda):
+    """255^3 (kappa 2.7e4, just inside the limit) with white-noise data, the
+    roughest right-hand side: one sweep still meets 1e-10."""
+    import torch
+    n = 255
+    g = torch.Generator(device="cuda").manual_seed(11)
+    f = torch.randn((n, n, n), dtype=torch.float64, device="cuda", generator=g)
+    args = workloads.solver_args(n, n, n)
+    u = torch.empty_like(f)
+    LaplCube(*args).solve_device(u, f)
+    m = LaplCube(*args, precision="mixed", tol=1e-10)
+    um = torch.empty_like(f)
+    m.solve_device(um, f)
+    torch.cuda.synchronize()
+    assert m.last_info(1)[0] == 1
+    assert (torch.linalg.norm(um - u) / torch.linalg.norm(u)).item() <= 1e-10

@@ -100,3 +100,9 @@ def test_noalloc_allocates_nothing_and_rejects_oversize(cuda):
     rc = _noalloc(lib, big, dummy, dummy, 1)
     assert rc == N.EBUDGET
     assert b"scratch" in lib.fdmgpu_last_error()
+    # an axis of 1023 points is beyond the mixed solve's conditioning limit:
+    # refused (the handle API solves it in FP64), nothing run
+    ragged = workloads.solver_args(3, 1, 1023)
+    rc = _noalloc(lib, ragged, dummy, dummy, 1)
+    assert rc == N.ENOTSUP
+    assert b"conditioning" in lib.fdmgpu_last_error()
