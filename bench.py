@@ -801,6 +801,15 @@ def main():
         o.step(10)
         line["cpu_baseline"]["nscube_63cubed_ms_per_step"] = (time.perf_counter() - t0) * 1e3 / 10
         o.close()
+        # the same solve on one host thread (one 255^3 solve)
+        pt = port()
+        threads = pt.threads()
+        pt.set_threads(1)
+        f1, _ = workloads.manufactured(N_INT, N_INT, N_INT, seed=0, kmax=KMAX, noise=NOISE)
+        t0 = time.perf_counter()
+        pt.lapl_cube(f1, *workloads.solver_args(N_INT, N_INT, N_INT)[:6])
+        line["cpu_baseline"]["one_thread_solves_per_s"] = 1.0 / (time.perf_counter() - t0)
+        pt.set_threads(threads)
         from oracle.nbody import NBodyPort
         p = NBodyPort(-10.0, -10.0, -10.0, 20.0, 32, 64, 100000, 0.001, 1.0)
         p.step(1)
