@@ -607,6 +607,7 @@ struct Plan {
     int nkeys = 1;
     int nchunks = 0;
     long long steps_done = 0;
+    int sms = 1;  // streaming multiprocessors (grid of the big-bin sort)
     // NBody's cell lists are filled by the constructor's random branch and by
     // every move, emptied at the end of calc_a_pm; the solar branch leaves
     // them empty, and so does calc_a_pm without a move (calc_error)
@@ -697,6 +698,9 @@ struct Plan {
         FDM_CUDA(cudaMemset(grid_mem.p, 0, grid_mem.bytes));
 
         FDM_CUDA(cudaStreamCreateWithFlags(&st, cudaStreamNonBlocking));
+        int dev = 0;
+        FDM_CUDA(cudaGetDevice(&dev));
+        FDM_CUDA(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
         // solver3(h, h, h, l, l, l, n, n, n), periodic in all three directions
         const int rc = fdmgpu_lapl_cube_create(&lapl, sizeof(T) == 8 ? FDMGPU_F64 : FDMGPU_F32, FDMGPU_PERIODIC, P.h,
                                                P.h, P.h, l, l, l, n, n, n);
@@ -749,7 +753,7 @@ struct Plan {
         }
         {
             FDM_TIMED("nb_sort_big", st);
-            k_nb_sort_big<<<152, T256, 0, st>>>(start, sorted, tmp, bigcount, biglist);
+            k_nb_sort_big<<<sms, T256, 0, st>>>(start, sorted, tmp, bigcount, biglist);
             FDM_LAUNCH_CHECK();
         }
         {
