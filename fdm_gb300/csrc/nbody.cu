@@ -108,7 +108,10 @@ struct Params {
     double dt, hdt, hdt2;  // dt, 0.5 dt, 0.5 dt dt
     double G, rcrit, rhs_scale, sqrtpi;
     CDiv dhT, dh, dhpp, drc, dsqrtpi;  // h in T (the CIC3 argument), h, l / npp, rcrit, sqrt(pi)
-    double rc2_out;  // a double at or above rcrit^2: pairs with R^2 >= it are out of range
+    // R^2 < r2_in exactly when sqrt(R^2) + 0.001 < rcrit in double (both
+    // operations correctly rounded and monotone, so the range test of
+    // apply_bi_bj is a threshold on R^2, found by bisection over doubles)
+    double r2_in;
     int n, npp, N, local, sgn;
     int lists_empty;  // the cell lists hold no bodies: nothing deposits, no pair forces
     long long n3;
@@ -400,7 +403,7 @@ __device__ __forceinline__ void pp_flush(PpQueue<T>& q, int cnt, int lane, const
                                          const T* __restrict__ mass, T F[3]) {
     __syncwarp();
     if (lane < cnt) {
-        const double R = q.R[lane];
+        const double R = __dadd_rn(sqrt(q.R[lane]), 0.001);  // the queue holds R^2
         // erfc(R/2/rcrit) + R/rcrit/sqrt(pi) * exp(-R*R/4/rcrit/rcrit)
         const double ex = exp(cdiv(cdiv(__dmul_rn(__dmul_rn(-R, R), 0.25), P.drc), P.drc));
         const double sh = __dadd_rn(erfc(cdiv(__dmul_rn(R, 0.5), P.drc)), __dmul_rn(cdiv(cdiv(R, P.drc), P.dsqrtpi), ex));
@@ -435,7 +438,6 @@ __global__ void __launch_bounds__(kPpWarps * 32) k_nb_pp(Bodies<T> B, Params<T> 
 #pragma unroll
         for (int m = 0; m < 3; m++) xi[m] = B.x[m * N + bi];
     }
-    const double rc = P.rcrit;
     int cell = -1, s = 0, s1 = 0;  // candidate iterator: neighbour cell 0..26, position in its bin
     T off[3] = {T(0), T(0), T(0)};
     int qn = 0;  // queued pairs (the same in every lane)
@@ -471,11 +473,7 @@ __global__ void __launch_bounds__(kPpWarps * 32) k_nb_pp(Bodies<T> B, Params<T> 
                 d[m] = sub_rn<T>(xi[m], add_rn<T>(B.x[m * N + bj], off[m]));
                 R = __dadd_rn(R, __dmul_rn((double)d[m], (double)d[m]));
             }
-            // R^2 >= rcrit^2 already fails sqrt(R^2) + 0.001 < rcrit
-            if (R < P.rc2_out) {
-                R = __dadd_rn(sqrt(R), 0.001);
-                inr = R < rc;
-            }
+            inr = R < P.r2_in;  // sqrt(R^2) + 0.001 < rcrit, without the square root
         }
         const unsigned mask = __ballot_sync(0xffffffffu, inr);
         if (inr) {
@@ -533,7 +531,7 @@ __global__ void __launch_bounds__(256) k_nb_accel(Bodies<T> B, Params<T> P, cons
             }
 #pragma unroll
     for (int m = 0; m < 3; m++) B.a[m * N + b] = acc[m];
-    if constexpr (!MOVE) return;
+    if constexpr (MOVE) {
 #pragma unroll
     for (int m = 0; m < 3; m++) {
         const T ap = B.ap[m * N + b];
@@ -549,6 +547,7 @@ __global__ void __launch_bounds__(256) k_nb_accel(Bodies<T> B, Params<T> P, cons
         const T s = add_rn<T>(acc[m], ap);
         B.v[m * N + b] = (T)__dadd_rn((double)B.v[m * N + b], __dmul_rn(P.hdt, (double)s));
         B.ap[m * N + b] = acc[m];
+    }
     }
 }
 
@@ -596,6 +595,24 @@ __global__ void __launch_bounds__(kDirectTile) k_nb_direct(Bodies<T> B, Params<T
     }
     if (bi < N)
         for (int m = 0; m < 3; m++) Fout[m * N + bi] = F[m];
+}
+
+// The smallest double R2 >= 0 with !(sqrt(R2) + 0.001 < rc): the pair test
+// of apply_bi_bj (test/nbody.cpp:403-411) is then R2 < threshold.
+static double pair_range_threshold(double rc) {
+    auto inr = [rc](double r2) { return std::sqrt(r2) + 0.001 < rc; };
+    if (!inr(0.0)) return 0.0;
+    unsigned long long lo = 0, hi = 0x7ff0000000000000ull;  // bit patterns of 0 and +inf
+    while (hi - lo > 1) {
+        const unsigned long long mid = lo + (hi - lo) / 2;
+        double v;
+        std::memcpy(&v, &mid, sizeof v);
+        if (inr(v)) lo = mid;
+        else hi = mid;
+    }
+    double t;
+    std::memcpy(&t, &hi, sizeof t);
+    return t;
 }
 
 template <typename T>
@@ -652,7 +669,7 @@ struct Plan {
         P.dh = cdiv_of(P.h);
         P.dhpp = cdiv_of(P.hpp);
         P.drc = cdiv_of(P.rcrit);
-        P.rc2_out = std::nextafter(std::nextafter(P.rcrit * P.rcrit, INFINITY), INFINITY);
+        P.r2_in = pair_range_threshold(P.rcrit);
         P.dsqrtpi = cdiv_of(P.sqrtpi);
         P.n = n; P.npp = npp; P.N = N; P.local = local; P.sgn = sgn;
         P.n3 = (long long)n * n * n;
