@@ -196,3 +196,24 @@ def test_nbody_cic3_known_answers(T):
             assert np.all(np.abs(corner - 10.0 / 8.0) <= (1e-12 if T == np.float64 else 1e-5))
         assert abs(corner.sum() - 10.0) <= (1e-12 if T == np.float64 else 1e-5)
     nb.close()
+
+
+def test_nbody_float_full_size_against_restatement():
+    """NBody<float> at the driver's defaults (100000 bodies, 32^3): the
+    density bit for bit and the accelerations to float round-off against the
+    restatement in float."""
+    from oracle.nbody import NBodyPort
+
+    nb = make(("full32", np.float32, 100000, 32, 64, 0, 0))
+    b = nb.bodies()
+    p = NBodyPort(-10.0, -10.0, -10.0, 20.0, 32, 64, 100000, 0.001, 1.0, dtype=np.float32,
+                  bodies=(b["x"], b["v"], b["mass"]))
+    p.calc_a_pm()
+    nb.step(1)
+    assert np.array_equal(nb.field("f").ravel(), p.f)
+    assert np.array_equal(nb.field("rhs").ravel(), p.rhs)
+    # the device solves the periodic problem in FP32 (as NBody<float> does),
+    # the restatement in FP64: FP32 solve round-off, sharpened by the field's
+    # differences
+    assert rel(nb.bodies()["a"], p.a) <= 1e-5
+    nb.close()

@@ -224,3 +224,20 @@ def test_nscyl_vrandom_dirichlet_rejected(cuda):
     with pytest.raises(FdmError) as e:
         NSCyl(nr=16, nz=15, nphi=16, vrandom=1)
     assert e.value.status == 6
+
+
+@pytest.mark.parametrize("name,pz,shape", [("d16x15x16", False, (16, 15, 16)), ("p16x16x8", True, (16, 16, 8))])
+def test_nscyl_float_tracks_the_fp64_reference(cuda, golden, name, pz, shape):
+    """NSCyl<float> (solver:datatype=float): 20 steps stay within float
+    round-off of the reference's NSCyl<double> fields."""
+    from fdm_gb300 import NSCyl
+    g = golden("lapl_cyl")
+    nr, nz, nphi = shape
+    m = NSCyl(nr=nr, nz=nz, nphi=nphi, Re=100.0, dt=0.01, u0=1.0, periodic_z=pz, dtype=np.float32)
+    m.step(20)
+    for f in ("u", "v", "w", "p"):
+        got = m.get(f).data.ravel().astype(np.float64)
+        assert m.get(f).data.dtype == np.float32
+        ref = g["ns_%s_s20_%s" % (name, f)]
+        assert np.abs(got - ref).max() <= 2e-5 * max(1.0, np.abs(ref).max()), f
+    m.close()
