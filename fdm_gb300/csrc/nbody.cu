@@ -8,7 +8,8 @@
 //   2. counting sort of the bodies into bins, each bin in ascending body
 //                   index (the order of the reference's cell lists):
 //                   k_nb_scan_* (exclusive scan of the bin counts), k_nb_fill,
-//                   k_nb_sort_small / k_nb_sort_big;
+//                   k_nb_sort_small / k_nb_sort_big; k_nb_shares lays out the
+//                   deposited bodies' CIC shares m M in that order;
 //   3. k_nb_deposit per grid point: f = -M/l^3 plus the CIC shares of the
 //                   bodies that distribute_masses visits, gathered in its
 //                   order, and rhs = 4 G pi f / h^3 (test/nbody.cpp:275-305);
@@ -36,6 +37,7 @@
 // driver parameter enters) with explicit round-to-nearest operations, so no
 // multiply-add is contracted where the reference's source has none.
 #include <algorithm>
+#include <climits>
 #include <cmath>
 #include <cstring>
 #include <memory>
@@ -124,7 +126,8 @@ struct Bodies {
     T *x, *v, *a, *ap, *F, *mass;
 };
 
-// 1. CIC weights, corner cell, list cells and the bin keys
+// 1. CIC weights (body-major: M[b * 8 + 4 i + 2 k + j]), corner cell, list
+// cells and the bin keys
 template <typename T>
 __global__ void __launch_bounds__(256) k_nb_cic(Bodies<T> B, Params<T> P, T* __restrict__ M, int* __restrict__ corner,
                                                 int* __restrict__ pcell, int* __restrict__ key, int* __restrict__ count) {
@@ -155,7 +158,7 @@ __global__ void __launch_bounds__(256) k_nb_cic(Bodies<T> B, Params<T> P, T* __r
                 const T wz = a ? w[2] : sub_rn<T>(T(1), w[2]);
                 const T wy = bb ? w[1] : sub_rn<T>(T(1), w[1]);
                 const T wx = cc ? w[0] : sub_rn<T>(T(1), w[0]);
-                M[(long long)(4 * a + 2 * bb + cc) * N + b] = mul_rn<T>(mul_rn<T>(wz, wy), wx);
+                M[(long long)b * 8 + 4 * a + 2 * bb + cc] = mul_rn<T>(mul_rn<T>(wz, wy), wx);
             }
     corner[b] = pack3(c[2], c[1], c[0]);
     const int p0 = lc[0] & 1;
@@ -295,33 +298,102 @@ __global__ void __launch_bounds__(256) k_nb_sort_small(const int* __restrict__ s
     }
 }
 
-// one warp per big bin: copy, then place each body at its rank
-__global__ void __launch_bounds__(256) k_nb_sort_big(const int* __restrict__ start, int* __restrict__ sorted,
-                                                     int* __restrict__ tmp, const int* __restrict__ bigcount,
-                                                     const int* __restrict__ biglist) {
-    const int lane = threadIdx.x & 31;
-    const int nwarps = gridDim.x * (blockDim.x >> 5);
-    const int nbig = *bigcount;
-    for (int w = blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5); w < nbig; w += nwarps) {
-        const int bin = biglist[w];
-        const int beg = start[bin], s = start[bin + 1] - beg;
-        for (int e = lane; e < s; e += 32) tmp[beg + e] = sorted[beg + e];
-        __syncwarp();
-        for (int e = lane; e < s; e += 32) {
-            const int v = tmp[beg + e];
-            int rank = 0;
-            for (int t = 0; t < s; t++) rank += tmp[beg + t] < v;
-            sorted[beg + rank] = v;
-        }
-        __syncwarp();
+// Big bins (more than 32 bodies).  Each CTA takes a chunk of eight entries
+// of the big-bin list: bins of up to kWarpSortMax bodies go one per warp
+// (each body placed at its rank, counted by the lanes), larger ones to the
+// whole CTA in turn: a bitonic network in shared memory up to kBitonicMax
+// bodies (padded with INT_MAX to a power of two), a CTA-wide rank count
+// beyond.
+constexpr int kWarpSortMax = 256;
+constexpr int kBitonicMax = 8192;
+constexpr int kSortBigThreads = 256;
+
+__device__ __forceinline__ void rank_place(const int* __restrict__ src, int* __restrict__ dst, int s, int e0,
+                                           int stride) {
+    for (int e = e0; e < s; e += stride) {
+        const int v = src[e];
+        int rank = 0;
+        for (int t = 0; t < s; t++) rank += src[t] < v;
+        dst[rank] = v;
     }
+}
+
+__global__ void __launch_bounds__(kSortBigThreads) k_nb_sort_big(const int* __restrict__ start, int* __restrict__ sorted,
+                                                                 int* __restrict__ tmp, const int* __restrict__ bigcount,
+                                                                 const int* __restrict__ biglist) {
+    __shared__ int sk[kBitonicMax];
+    constexpr int kWarps = kSortBigThreads / 32;
+    const int nbig = *bigcount;
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    for (int c0 = blockIdx.x * kWarps; c0 < nbig; c0 += gridDim.x * kWarps) {
+        // small big bins: one per warp
+        {
+            const int w = c0 + warp;
+            if (w < nbig) {
+                const int bin = biglist[w];
+                const int beg = start[bin], s = start[bin + 1] - beg;
+                if (s <= kWarpSortMax) {
+                    for (int e = lane; e < s; e += 32) tmp[beg + e] = sorted[beg + e];
+                    __syncwarp();
+                    rank_place(tmp + beg, sorted + beg, s, lane, 32);
+                }
+            }
+        }
+        // the chunk's larger bins, one after another with the whole CTA
+        for (int q = 0; q < kWarps && c0 + q < nbig; q++) {
+            const int bin = biglist[c0 + q];
+            const int beg = start[bin], s = start[bin + 1] - beg;
+            if (s <= kWarpSortMax) continue;
+            if (s <= kBitonicMax) {
+                int P = 512;
+                while (P < s) P <<= 1;
+                for (int e = threadIdx.x; e < P; e += blockDim.x) sk[e] = e < s ? sorted[beg + e] : INT_MAX;
+                __syncthreads();
+                for (int k = 2; k <= P; k <<= 1)
+                    for (int jj = k >> 1; jj > 0; jj >>= 1) {
+                        for (int e = threadIdx.x; e < P; e += blockDim.x) {
+                            const int p = e ^ jj;
+                            if (p > e) {
+                                const int a = sk[e], b = sk[p];
+                                const bool up = (e & k) == 0;
+                                if ((a > b) == up) {
+                                    sk[e] = b;
+                                    sk[p] = a;
+                                }
+                            }
+                        }
+                        __syncthreads();
+                    }
+                for (int e = threadIdx.x; e < s; e += blockDim.x) sorted[beg + e] = sk[e];
+            } else {
+                for (int e = threadIdx.x; e < s; e += blockDim.x) tmp[beg + e] = sorted[beg + e];
+                __syncthreads();
+                rank_place(tmp + beg, sorted + beg, s, threadIdx.x, blockDim.x);
+            }
+            __syncthreads();
+        }
+    }
+}
+
+// 2d. the eight CIC shares m * M of every deposited body, laid out corner
+// by corner in bin order, so the gather below walks contiguous memory
+template <typename T>
+__global__ void __launch_bounds__(256) k_nb_shares(const int* __restrict__ sorted, const int* __restrict__ ndep,
+                                                   const T* __restrict__ mass, const T* __restrict__ M, int N,
+                                                   T* __restrict__ share) {
+    const int s = blockIdx.x * blockDim.x + threadIdx.x;
+    if (s >= *ndep) return;
+    const int b = sorted[s];
+    const T m = mass[b];
+#pragma unroll
+    for (int w = 0; w < 8; w++) share[(long long)w * N + s] = mul_rn<T>(m, M[(long long)b * 8 + w]);
 }
 
 // 3. density and right-hand side, gathered per grid point
 template <typename T>
-__global__ void __launch_bounds__(64) k_nb_deposit(Params<T> P, const T* __restrict__ mass, const T* __restrict__ M,
-                                                    const int* __restrict__ start, const int* __restrict__ sorted,
-                                                    T* __restrict__ f, T* __restrict__ rhs) {
+__global__ void __launch_bounds__(64) k_nb_deposit(Params<T> P, const T* __restrict__ share,
+                                                    const int* __restrict__ start, T* __restrict__ f,
+                                                    T* __restrict__ rhs) {
     const long long e = (long long)blockIdx.x * blockDim.x + threadIdx.x;
     if (e >= P.n3) return;
     const int n = P.n, N = P.N;
@@ -338,11 +410,8 @@ __global__ void __launch_bounds__(64) k_nb_deposit(Params<T> P, const T* __restr
     T acc = P.f0;
 #pragma unroll
     for (int q = 0; q < 16; q++) {
-        const T* Mw = M + (long long)(q & 7) * N;
-        for (int s = lo[q]; s < hi[q]; s++) {
-            const int b = sorted[s];
-            acc = add_rn<T>(acc, mul_rn<T>(mass[b], Mw[b]));
-        }
+        const T* sw = share + (long long)(q & 7) * N;
+        for (int s = lo[q]; s < hi[q]; s++) acc = add_rn<T>(acc, sw[s]);
     }
     f[e] = acc;
     // 4 * G * M_PI * f / h / h / h in double
@@ -525,7 +594,7 @@ __global__ void __launch_bounds__(256) k_nb_accel(Bodies<T> B, Params<T> P, cons
 #pragma unroll
             for (int cc = 0; cc < 2; cc++) {
                 const long long e = ((long long)wrap(ci + a, n) * n + wrap(ck + bb, n)) * n + wrap(cj + cc, n);
-                const T w = M[(long long)(4 * a + 2 * bb + cc) * N + b];
+                const T w = M[(long long)b * 8 + 4 * a + 2 * bb + cc];
 #pragma unroll
                 for (int m = 0; m < 3; m++) acc[m] = add_rn<T>(acc[m], mul_rn<T>(E[m * P.n3 + e], w));
             }
@@ -632,7 +701,7 @@ struct Plan {
     cudaStream_t st = nullptr;
     DevBuf body_mem, work_mem, grid_mem;
     Bodies<T> B{};
-    T *M = nullptr, *f = nullptr, *rhs = nullptr, *psi = nullptr, *E = nullptr;
+    T *M = nullptr, *share = nullptr, *f = nullptr, *rhs = nullptr, *psi = nullptr, *E = nullptr;
     int *corner = nullptr, *pcell = nullptr, *key = nullptr, *count = nullptr, *start = nullptr, *partial = nullptr;
     int *bigcount = nullptr, *biglist = nullptr, *sorted = nullptr, *tmp = nullptr;
     fdmgpu_lapl_cube* lapl = nullptr;
@@ -689,12 +758,13 @@ struct Plan {
         B.mass = (T*)take(sizeof(T) * N);
         FDM_CUDA(cudaMemset(body_mem.p, 0, body_mem.bytes));
 
-        const size_t wbytes = al(sizeof(T) * 8 * N) + al(sizeof(int) * N) * 2 + al(sizeof(int) * 2 * N) +
+        const size_t wbytes = al(sizeof(T) * 8 * N) * 2 + al(sizeof(int) * N) * 2 + al(sizeof(int) * 2 * N) +
                               al(sizeof(int) * nbins) + al(sizeof(int) * (nbins + 1)) + al(sizeof(int) * nchunks) +
                               al(sizeof(int)) + al(sizeof(int) * (2 * (size_t)N / (kSmallBin + 1) + 1)) +
                               al(sizeof(int) * 2 * N) * 2;
         p = (char*)work_mem.get(wbytes);
         M = (T*)take(sizeof(T) * 8 * N);
+        share = (T*)take(sizeof(T) * 8 * N);
         corner = (int*)take(sizeof(int) * N);
         pcell = (int*)take(sizeof(int) * N);
         key = (int*)take(sizeof(int) * 2 * N);
@@ -770,14 +840,20 @@ struct Plan {
         }
         {
             FDM_TIMED("nb_sort_big", st);
-            k_nb_sort_big<<<sms, T256, 0, st>>>(start, sorted, tmp, bigcount, biglist);
+            k_nb_sort_big<<<sms * 2, kSortBigThreads, 0, st>>>(start, sorted, tmp, bigcount, biglist);
+            FDM_LAUNCH_CHECK();
+        }
+        {
+            // deposited bodies occupy the first start[dep_bins] positions
+            FDM_TIMED("nb_shares", st);
+            k_nb_shares<T><<<blocks(N, T256), T256, 0, st>>>(sorted, start + P.dep_bins, B.mass, M, N, share);
             FDM_LAUNCH_CHECK();
         }
         {
             // 64-thread blocks: the mass grid is small (32^3 points at the
             // driver's defaults), so spread it over every SM
             FDM_TIMED("nb_deposit", st);
-            k_nb_deposit<T><<<blocks(P.n3, 64), 64, 0, st>>>(P, B.mass, M, start, sorted, f, rhs);
+            k_nb_deposit<T><<<blocks(P.n3, 64), 64, 0, st>>>(P, share, start, f, rhs);
             FDM_LAUNCH_CHECK();
         }
         cube_solve_device(lapl, psi, rhs, 1, st);
