@@ -6,6 +6,8 @@
 //   shim_solve dirichlet <nx> <ny> <nz> <dx> <dy> <dz> <lx> <ly> <lz> <rhs> <ans>
 //   shim_solve periodic  <nx> <ny> <nz> <dx> <dy> <dz> <lx> <ly> <lz> <rhs> <ans>
 //   shim_solve nscube    <n> <steps> <out_u>
+//   shim_solve cyl       <periodic_z> <nr> <nz> <nphi> <dr> <dz> <r0> <lr> <lz> <rhs> <ans>
+//   shim_solve nscyl     <periodic_z> <nr> <nz> <nphi> <steps> <out_u>
 #include <cstdio>
 #include <cstdlib>
 #include <cstring>
@@ -13,7 +15,9 @@
 #include <vector>
 
 #include "fdm_gb300/lapl_cube.h"
+#include "fdm_gb300/lapl_cyl.h"
 #include "fdm_gb300/ns_cube.h"
+#include "fdm_gb300/ns_cyl.h"
 
 namespace {
 
@@ -40,12 +44,20 @@ void write_all(const char* path, const std::vector<double>& v) {
 // the reference's Config::get(section, key, default) shape
 struct Cfg {
     int n;
+    double Re = 250.0;
+    int nr = 0, nz = 0, nphi = 0;
     double get(const char*, const char* key, double def) const {
-        if (!strcmp(key, "Re")) return 250.0;
+        if (!strcmp(key, "Re")) return Re;
         if (!strcmp(key, "dt")) return 0.01;
         return def;
     }
     int get(const char*, const char* key, int def) const {
+        if (nr) {
+            if (!strcmp(key, "nr")) return nr;
+            if (!strcmp(key, "nz")) return nz;
+            if (!strcmp(key, "nphi")) return nphi;
+            return def;
+        }
         if (!strcmp(key, "nx") || !strcmp(key, "nz")) return n;
         return def;
     }
@@ -61,6 +73,40 @@ int main(int argc, char** argv) {
         fdm::NSCube<double, false> ns(c);
         for (int i = 0; i < atoi(argv[3]); i++) ns.step();
         write_all(argv[4], ns.field(FDMGPU_NS_U));
+        return 0;
+    }
+    if (mode == "nscyl" && argc == 8) {
+        Cfg c{0};
+        c.Re = 100.0;
+        c.nr = atoi(argv[3]);
+        c.nz = atoi(argv[4]);
+        c.nphi = atoi(argv[5]);
+        std::vector<double> u;
+        if (atoi(argv[2])) {
+            fdm::NSCyl<double, false, fdm::tensor_flag::periodic> ns(c);  // src/ns_cyl.h:56
+            for (int i = 0; i < atoi(argv[6]); i++) ns.step();
+            u = ns.field(FDMGPU_NS_U);
+        } else {
+            fdm::NSCyl<double, false> ns(c);
+            for (int i = 0; i < atoi(argv[6]); i++) ns.step();
+            u = ns.field(FDMGPU_NS_U);
+        }
+        write_all(argv[7], u);
+        return 0;
+    }
+    if (mode == "cyl" && argc == 13) {
+        const int pz = atoi(argv[2]), nr = atoi(argv[3]), nz = atoi(argv[4]), nphi = atoi(argv[5]);
+        const double dr = atof(argv[6]), dz = atof(argv[7]), r0 = atof(argv[8]), lr = atof(argv[9]),
+                     lz = atof(argv[10]);
+        std::vector<double> rhs = read_all(argv[11], (size_t)nr * nz * nphi), ans(rhs.size());
+        if (pz) {
+            fdm::LaplCyl3FFT2<double, false, fdm::tensor_flag::periodic> lapl(dr, dz, r0, lr, lz, nr, nz, nphi);
+            lapl.solve(&ans[0], &rhs[0]);
+        } else {
+            fdm::LaplCyl3FFT2<double, false> lapl(dr, dz, r0, lr, lz, nr, nz, nphi);  // src/lapl_cyl.h:212
+            lapl.solve(&ans[0], &rhs[0]);
+        }
+        write_all(argv[12], ans);
         return 0;
     }
     if (argc != 13) return 1;

@@ -51,3 +51,26 @@ def test_shim_program_matches_reference(tmp_path, native, cuda, golden):
     u = np.frombuffer((tmp_path / "u").read_bytes())
     ref = ns["n15_s20_u"]
     assert np.abs(u - ref).max() <= 1e-12 * max(1.0, np.abs(ref).max())
+
+
+@pytest.mark.gpu
+def test_shim_cylindrical_matches_reference(tmp_path, native, cuda, golden):
+    """fdm::LaplCyl3FFT2 and fdm::NSCyl through the C++ shims against the
+    reference's own answers (Dirichlet and periodic z)."""
+    exe = _build(tmp_path, native)
+    g = golden("lapl_cyl")
+    for name, pz, shape in (("d16x15x20", 0, (16, 15, 20)), ("p8x16x12", 1, (8, 16, 12))):
+        nphi, nz, nr = shape
+        rhs = g["rhs_" + name]
+        (tmp_path / "crhs").write_bytes(np.ascontiguousarray(rhs).tobytes())
+        subprocess.run([str(exe), "cyl", str(pz), str(nr), str(nz), str(nphi),
+                        *[repr(float(v)) for v in g["args_" + name]], str(tmp_path / "crhs"),
+                        str(tmp_path / "cans")], check=True)
+        ans = np.frombuffer((tmp_path / "cans").read_bytes()).reshape(rhs.shape)
+        assert rel_l2(ans, g["ans_" + name]) <= 1e-12, name
+    for name, pz, (nr, nz, nphi) in (("d16x15x16", 0, (16, 15, 16)), ("p16x16x8", 1, (16, 16, 8))):
+        subprocess.run([str(exe), "nscyl", str(pz), str(nr), str(nz), str(nphi), "20", str(tmp_path / "cu")],
+                       check=True)
+        u = np.frombuffer((tmp_path / "cu").read_bytes())
+        ref = g["ns_%s_s20_u" % name]
+        assert np.abs(u - ref).max() <= 1e-11 * max(1.0, np.abs(ref).max()), name
