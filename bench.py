@@ -368,6 +368,34 @@ def measure_nbody_published(torch, fdm_gb300, steps=5):
     return res
 
 
+def measure_fft3d(torch, fdm_gb300, stream, reps=20):
+    """The reference's own 3-D transform benchmark (test/test_fft_3d_bench.cpp:
+    FFT<T>::pFFT_1_3d and pFFT_3d of an N^3 cube, N = 32 .. 256, double and
+    float) on device-resident cubes: ms per transform, CUDA events over
+    `reps` calls."""
+    import numpy as np
+    out = {"workload": "pFFT_1_3d / pFFT_3d of an N^3 cube (test_fft_3d_bench.cpp)", "reps": reps}
+    for dt, tdt in (("double", torch.float64), ("float", torch.float32)):
+        for N in (32, 64, 128, 256):
+            g = torch.Generator(device="cuda").manual_seed(N)
+            s = torch.randn((N, N, N), dtype=tdt, device="cuda", generator=g)
+            S = torch.empty_like(s)
+            npdt = np.float64 if tdt == torch.float64 else np.float32
+            res = {}
+            for name, inv in (("pFFT_1_3d", False), ("pFFT_3d", True)):
+                fdm_gb300.pfft3d_device(S, s, N, 1.0, inverse=inv, dtype=npdt, stream=stream)
+                e0 = torch.cuda.Event(enable_timing=True)
+                e1 = torch.cuda.Event(enable_timing=True)
+                e0.record(stream)
+                for _ in range(reps):
+                    fdm_gb300.pfft3d_device(S, s, N, 1.0, inverse=inv, dtype=npdt, stream=stream)
+                e1.record(stream)
+                stream.synchronize()
+                res[name + "_ms"] = e0.elapsed_time(e1) / reps
+            out["%s_%d" % (dt, N)] = res
+    return out
+
+
 def measure_periodic(torch, fdm_gb300, stream, reps=50):
     """Periodic LaplCube<double> solve (FP64) at 32^3, 64^3, 128^3: device
     time per solve (CUDA events, median of reps) and the host-array call the
@@ -751,6 +779,7 @@ def main():
     torch.cuda.empty_cache()
     uneven = measure_uneven_batch(torch, fdm_gb300, workloads, stream, dev)
     periodic = measure_periodic(torch, fdm_gb300, stream)
+    periodic["fft3d"] = measure_fft3d(torch, fdm_gb300, stream)
     nbody = measure_nbody(torch, fdm_gb300)
     nbody["published_configs"] = measure_nbody_published(torch, fdm_gb300)
     rates = tuple(int(x) for x in args.serve_rates.split(",")) if args.serve_rates else SERVE_RATES

@@ -17,6 +17,7 @@
 #include <memory>
 #include <mutex>
 #include <deque>
+#include <map>
 #include <vector>
 
 #include "internal.h"
@@ -1474,6 +1475,39 @@ void cyl_solve_device(fdmgpu_lapl_cyl* h, void* ans, const void* rhs, int nrhs, 
 }
 }  // namespace fdmgpu
 
+// twiddles e^{-2 pi i t / n} of the periodic 3-D transforms, one table per
+// (device, element type, n), kept for the life of the process
+static const void* pfft3d_twiddles(int dtype, int n) {
+    static std::mutex mu;
+    static std::map<long long, std::unique_ptr<DevBuf>> cache;
+    int dev = 0;
+    FDM_CUDA(cudaGetDevice(&dev));
+    const long long key = ((long long)dev << 32) | ((long long)dtype << 16) | n;
+    std::lock_guard<std::mutex> lk(mu);
+    auto it = cache.find(key);
+    if (it != cache.end()) return it->second->p;
+    std::unique_ptr<DevBuf> b(new DevBuf());
+    if (dtype == FDMGPU_F64) upload_ptwiddles<double>(*b, n);
+    else upload_ptwiddles<float>(*b, n);
+    const void* p = b->p;
+    cache.emplace(key, std::move(b));
+    return p;
+}
+
+// FFT<T>::pFFT_1_3d / pFFT_3d (src/fft.cpp:214-292): the periodic transform
+// along x (fastest), then y, then z of `count` cubes of n^3, scale dx on
+// every pass
+template <typename T, bool INV>
+static void pfft3d_run(const T* in, T* out, int n, int count, double dx, const void* tw, cudaStream_t st) {
+    const long long n2 = (long long)n * n, lines = (long long)count * n2;
+    PLineGeom gx{lines, 1, n, 0, 1};
+    PLineGeom gy{lines, n, n2, 1, n};
+    PLineGeom gz{lines, n2, n2 * n, 1, n2};
+    launch_pfft<T, INV>(in, out, gx, n, tw, dx, st);
+    launch_pfft<T, INV>(out, out, gy, n, tw, dx, st);
+    launch_pfft<T, INV>(out, out, gz, n, tw, dx, st);
+}
+
 static size_t elem_size(int dtype) { return dtype == FDMGPU_F64 ? sizeof(double) : sizeof(float); }
 
 extern "C" {
@@ -1780,6 +1814,38 @@ int fdmgpu_sine_device(int dtype, int N, int nlines, double scale, void* d_out, 
     } else {
         FDM_FAIL(FDMGPU_EINVAL, "bad dtype %d", dtype);
     }
+    FDM_API_END
+}
+
+int fdmgpu_pfft3d_device(int dtype, int n, int inverse, double dx, void* d_out, const void* d_in, int count,
+                         void* stream) {
+    FDM_API_BEGIN
+    if (!d_out || !d_in) FDM_FAIL(FDMGPU_EINVAL, "null argument");
+    if (!pow2_periodic(n)) FDM_FAIL(FDMGPU_ESIZE, "verify((1<<n) == N) failed: N must be a power of two in [2, 512], got %d", n);
+    if (count < 1) FDM_FAIL(FDMGPU_EINVAL, "count must be positive");
+    if (dtype != FDMGPU_F64 && dtype != FDMGPU_F32) FDM_FAIL(FDMGPU_EINVAL, "bad dtype %d", dtype);
+    cudaStream_t st = (cudaStream_t)stream;
+    const void* tw = pfft3d_twiddles(dtype, n);
+    if (dtype == FDMGPU_F64) {
+        if (inverse) pfft3d_run<double, true>((const double*)d_in, (double*)d_out, n, count, dx, tw, st);
+        else pfft3d_run<double, false>((const double*)d_in, (double*)d_out, n, count, dx, tw, st);
+    } else {
+        if (inverse) pfft3d_run<float, true>((const float*)d_in, (float*)d_out, n, count, dx, tw, st);
+        else pfft3d_run<float, false>((const float*)d_in, (float*)d_out, n, count, dx, tw, st);
+    }
+    FDM_API_END
+}
+
+int fdmgpu_pfft3d(int dtype, int n, int inverse, double dx, void* out, const void* in) {
+    FDM_API_BEGIN
+    if (!out || !in) FDM_FAIL(FDMGPU_EINVAL, "null argument");
+    if (!pow2_periodic(n)) FDM_FAIL(FDMGPU_ESIZE, "verify((1<<n) == N) failed: N must be a power of two in [2, 512], got %d", n);
+    const size_t bytes = (size_t)n * n * n * (dtype == FDMGPU_F64 ? sizeof(double) : sizeof(float));
+    DevBuf din, dout;
+    FDM_CUDA(cudaMemcpy(din.get(bytes), in, bytes, cudaMemcpyHostToDevice));
+    const int rc = fdmgpu_pfft3d_device(dtype, n, inverse, dx, dout.get(bytes), din.p, 1, nullptr);
+    if (rc) return rc;
+    FDM_CUDA(cudaMemcpy(out, dout.p, bytes, cudaMemcpyDeviceToHost));
     FDM_API_END
 }
 

@@ -333,6 +333,38 @@ def sine_transform_device(out, inp, N_points: int, nlines: int, scale: float = 1
                                    _dev_ptr(out, eb, cnt), _dev_ptr(inp, eb, cnt), _stream_ptr(stream)))
 
 
+def pfft_1_3d(S: np.ndarray, s: np.ndarray, dx: float) -> None:
+    """FFT<T>::pFFT_1_3d (src/fft.cpp:254-292): the periodic forward transform
+    of an N^3 host cube (N a power of two) along x, y, z, scale dx, into S."""
+    _pfft3d_host(S, s, dx, 0)
+
+
+def pfft_3d(S: np.ndarray, s: np.ndarray, dx: float) -> None:
+    """FFT<T>::pFFT_3d (src/fft.cpp:214-251): the inverse layout, into S."""
+    _pfft3d_host(S, s, dx, 1)
+
+
+def _pfft3d_host(S, s, dx, inverse):
+    lib = N.load()
+    n = round(s.size ** (1.0 / 3.0))
+    if n ** 3 != s.size or S.size != s.size or S.dtype != s.dtype:
+        raise ValueError("pFFT_3d works on matching N^3 arrays")
+    if not (s.flags.c_contiguous and S.flags.c_contiguous):
+        raise ValueError("arrays must be C-contiguous")
+    N.check(lib.fdmgpu_pfft3d(_dtype_code(s.dtype), int(n), int(inverse), float(dx), S.ctypes.data, s.ctypes.data))
+
+
+def pfft3d_device(out, inp, n: int, dx: float, inverse: bool = False, count: int = 1, dtype=np.float64,
+                  stream=None) -> None:
+    """pFFT_1_3d / pFFT_3d of `count` device cubes of n^3 back to back,
+    asynchronous on stream."""
+    lib = N.load()
+    eb = np.dtype(dtype).itemsize
+    cnt = n * n * n * count
+    N.check(lib.fdmgpu_pfft3d_device(_dtype_code(dtype), int(n), int(bool(inverse)), float(dx),
+                                     _dev_ptr(out, eb, cnt), _dev_ptr(inp, eb, cnt), int(count), _stream_ptr(stream)))
+
+
 def sine_transform_tc_device(out, inp, N_points: int, count: int, scale: float = 1.0, axis: int = 0, nx: int = 1,
                              stream=None) -> None:
     """FP32 DST-I on the tensor cores (N_points = 32, 64 or 128).  axis 0: `count`

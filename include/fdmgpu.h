@@ -230,6 +230,15 @@ int fdmgpu_lapl_rect_destroy(fdmgpu_lapl_rect* h);
  * src/cyclic_reduction.h:20-107, src/asp_gauss.cpp:185-207). */
 int fdmgpu_sine_device(int dtype, int N, int nlines, double scale,
                        void* d_out, const void* d_in, void* stream);
+/* FFT<T>::pFFT_1_3d (inverse = 0) / pFFT_3d (inverse = 1) of
+ * src/fft.cpp:214-292: the periodic real transform in the reference's
+ * coefficient layout along x (fastest), then y, then z of an n^3 cube
+ * (n a power of two, 2..512), scale dx on every pass.  The _device form
+ * takes `count` cubes back to back and is asynchronous on stream; the host
+ * form is synchronous. */
+int fdmgpu_pfft3d_device(int dtype, int n, int inverse, double dx, void* d_out, const void* d_in, int count,
+                         void* stream);
+int fdmgpu_pfft3d(int dtype, int n, int inverse, double dx, void* out, const void* in);
 /* DST-I of FP32 lines of N-1 points (N = 32, 64 or 128) as a dense contraction
  * with the sine matrix on the tensor cores (split TF32, FP32 accumulation;
  * no counterpart in the reference).  axis 0: `count` contiguous lines;

@@ -169,6 +169,7 @@ class Reference:
         L.ref_nscube_destroy.argtypes = [c_void_p]
         L.ref_pfft1_d.argtypes = [_dp, _dp, c_double, c_int]
         L.ref_pfft_d.argtypes = [_dp, _dp, c_double, c_int]
+        L.ref_pfft3d_d.argtypes = [_dp, _dp, c_double, c_int, c_int]
         L.ref_lapl_cube_periodic_d.argtypes = [c_int] * 3 + [c_double] * 6 + [_dp, _dp]
         L.ref_lapl_cyl_d.argtypes = [c_int] * 4 + [c_double] * 5 + [_dp, _dp]
         L.ref_nscyl_create.restype = c_void_p
@@ -215,6 +216,13 @@ class Reference:
         S = np.zeros(s.size)
         a = np.array(s, np.float64)
         self.L.ref_pfft_d(_p(S), _p(a), dx, s.size)
+        return S
+
+    def pfft3d(self, s: np.ndarray, dx: float, inverse: bool = False) -> np.ndarray:
+        """FFT<double>::pFFT_1_3d (inverse False) / pFFT_3d of an N^3 cube."""
+        a = np.ascontiguousarray(s, np.float64)
+        S = np.zeros_like(a)
+        self.L.ref_pfft3d_d(_p(S), _p(a), dx, a.shape[0], 1 if inverse else 0)
         return S
 
     def lapl_cube_periodic(self, rhs, dx, dy, dz, lx, ly, lz) -> np.ndarray:
@@ -298,6 +306,16 @@ def pfft(S: np.ndarray, dx: float, axis: int = -1) -> np.ndarray:
     H[..., k] = S[..., k] - 1j * S[..., n - k]
     f = np.fft.irfft(H, n=n, axis=-1) * (n * dx / 2)
     return np.moveaxis(f, -1, axis)
+
+
+def pfft3d(s: np.ndarray, dx: float, inverse: bool = False) -> np.ndarray:
+    """Restatement of FFT<T>::pFFT_1_3d / pFFT_3d (src/fft.cpp:214-292):
+    the 1-D transform along the fastest axis (x), then y, then z of an N^3
+    cube (z, y, x), scale dx on every pass."""
+    f = pfft if inverse else pfft1
+    a = f(np.asarray(s, np.float64), dx, axis=2)
+    a = f(a, dx, axis=1)
+    return f(a, dx, axis=0)
 
 
 def lapl_cube_periodic(rhs, dx, dy, dz, lx, ly, lz) -> np.ndarray:

@@ -167,6 +167,14 @@ int ref_pfft_d(double* S, double* s, double dx, int N) {
     ft.pFFT(S, s, dx);
     return 0;
 }
+// FFT<double>::pFFT_1_3d / pFFT_3d (src/fft.cpp:214-292) of an N^3 cube
+int ref_pfft3d_d(double* S, double* s, double dx, int N, int inverse) {
+    FFTTable<double> t(N);
+    FFT<double> ft(t, N);
+    if (inverse) ft.pFFT_3d(S, s, dx);
+    else ft.pFFT_1_3d(S, s, dx);
+    return 0;
+}
 
 // Periodic LaplCube<double,false,periodic^3> (src/lapl_cube.h:9-106 with
 // F = tensor_flags<periodic,periodic,periodic>): rhs/ans hold n_z*n_y*n_x

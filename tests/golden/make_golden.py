@@ -181,6 +181,15 @@ def main():
         per["rhs_" + name] = f
         per["args_" + name] = np.array(args)
         per["ans_" + name] = R.lapl_cube_periodic(f, *args)
+    # FFT<double>::pFFT_1_3d / pFFT_3d on the cube test/test_fft_3d_bench.cpp
+    # fills (its formula, including the repeated j term)
+    for N in (8, 32):
+        i, j, k = np.meshgrid(np.arange(N), np.arange(N), np.arange(N), indexing="ij")
+        cube = (np.sin(2.0 * math.pi * i / N + 2.0 * math.pi * j / N + 2.0 * math.pi * j / N)
+                + 0.5 * np.cos(4.0 * math.pi * i / N + 4.0 * math.pi * j / N + 4.0 * math.pi * k / N))
+        per["fft3d_in_%d" % N] = cube
+        per["fft3d_fwd_%d" % N] = R.pfft3d(cube, 1.0)
+        per["fft3d_inv_%d" % N] = R.pfft3d(cube, 1.0, inverse=True)
     np.savez_compressed(OUT / "lapl_cube_periodic.npz", **per)
 
     # LaplCyl3FFT2<double,false,zflag> (src/lapl_cyl.cpp:10-166): arrays

@@ -368,3 +368,33 @@ def test_mixed_white_noise_at_the_conditioning_limit(cuda):
     torch.cuda.synchronize()
     assert m.last_info(1)[0] == 1
     assert (torch.linalg.norm(um - u) / torch.linalg.norm(u)).item() <= 1e-10
+
+
+@pytest.mark.parametrize("N", [8, 32])
+def test_pfft3d_vs_reference(cuda, golden, N):
+    """FFT<T>::pFFT_1_3d / pFFT_3d on the GPU against the reference's own
+    answers (test_fft_3d_bench.cpp's cube), FP64 and FP32, host and device
+    entry points; forward then inverse with scale 2/N returns the input."""
+    import torch
+    from fdm_gb300 import pfft3d_device, pfft_1_3d, pfft_3d
+    g = golden("lapl_cube_periodic")
+    s = np.ascontiguousarray(g["fft3d_in_%d" % N])
+    for inv, key, fn in ((False, "fft3d_fwd_%d", pfft_1_3d), (True, "fft3d_inv_%d", pfft_3d)):
+        ref = g[key % N]
+        S = np.zeros_like(s)
+        fn(S, s, 1.0)
+        assert np.abs(S - ref).max() <= 1e-13 * N * np.abs(ref).max()
+        S32 = np.zeros(s.shape, np.float32)
+        fn(S32, s.astype(np.float32), 1.0)
+        assert np.abs(S32.astype(np.float64) - ref).max() <= 2e-6 * N * np.abs(ref).max()
+    # device entry point, two cubes back to back, and the round trip
+    two = torch.tensor(np.stack([s, 2 * s]), device=cuda)
+    fwd = torch.empty_like(two)
+    pfft3d_device(fwd, two, N, 1.0, inverse=False, count=2)
+    back = torch.empty_like(two)
+    pfft3d_device(back, fwd, N, (2.0 / N), inverse=True, count=2)
+    torch.cuda.synchronize()
+    f = fwd.cpu().numpy()
+    assert np.abs(f[0] - g["fft3d_fwd_%d" % N]).max() <= 1e-13 * N * np.abs(f[0]).max()
+    assert np.abs(f[1] - 2 * f[0]).max() <= 1e-13 * np.abs(f[1]).max()
+    assert np.abs(back.cpu().numpy() - np.stack([s, 2 * s])).max() <= 1e-12

@@ -136,6 +136,18 @@ def test_periodic_transforms_match_reference(golden):
         assert np.abs(pfft1(pfft(s, 1.0), 2.0 / N) - s).max() <= 1e-14 * N
 
 
+def test_periodic_3d_transforms_match_reference(golden):
+    """pFFT_1_3d / pFFT_3d restated (x, y, z passes of pFFT_1 / pFFT) against
+    the reference's own FFT<double> on test_fft_3d_bench.cpp's cube."""
+    from oracle.oracle import pfft3d
+    g = golden("lapl_cube_periodic")
+    for N in (8, 32):
+        s = g["fft3d_in_%d" % N]
+        for inv, key in ((False, "fft3d_fwd_%d"), (True, "fft3d_inv_%d")):
+            ref = g[key % N]
+            assert np.abs(pfft3d(s, 1.0, inverse=inv) - ref).max() <= 1e-13 * N * np.abs(ref).max()
+
+
 def test_periodic_lapl_cube_matches_reference(golden):
     from oracle.oracle import lapl_cube_periodic
     g = golden("lapl_cube_periodic")
