@@ -114,6 +114,8 @@ _SIGS = [
     ("fdmgpu_nscyl_l_step", c_int, [c_void_p, c_int]),
     ("fdmgpu_nscyl_vrandom", c_int, [c_void_p]),
     ("fdmgpu_nscyl_destroy", c_int, [c_void_p]),
+    ("fdmgpu_lapl_rect_create_flags", c_int, [POINTER(c_void_p), c_int, c_int, c_int] + [c_double] * 4
+     + [c_int] * 2),
     ("fdmgpu_pfft3d_device", c_int, [c_int, c_int, c_int, c_double, c_void_p, c_void_p, c_int, c_void_p]),
     ("fdmgpu_pfft3d", c_int, [c_int, c_int, c_int, c_double, c_void_p, c_void_p]),
     ("fdmgpu_nbody_create", c_int, [POINTER(c_void_p), c_int] + [c_double] * 4 + [c_int] * 3 + [c_double] * 3

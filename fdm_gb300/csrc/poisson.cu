@@ -827,38 +827,54 @@ struct CubePlan {
 // LaplRect / LaplRectFFT2
 // ---------------------------------------------------------------------------
 template <typename T>
-__global__ void k_divide2d(T* W, int nx, int ny, long long vstride, const T* lamx, const T* lamy) {
+__global__ void k_divide2d(T* W, int nx, int ny, long long vstride, const T* lamx, const T* lamy, int hack) {
     const long long idx = (long long)blockIdx.x * blockDim.x + threadIdx.x;
     if (idx >= (long long)nx * ny) return;
     const int j = idx % nx, k = idx / nx;
     T* p = W + (long long)blockIdx.y * vstride + idx;
-    *p = *p / (-lamy[k] * T(1) - lamx[j]);
+    // doubly periodic: the reference sets the (0, 0) mode to 1
+    // ("hack for double-period", src/lapl_rect.cpp:169-172)
+    *p = (hack && idx == 0) ? T(1) : *p / (-lamy[k] * T(1) - lamx[j]);
 }
 
 struct RectPlan {
     int dtype, method, nx, ny;
+    // bit 1: y periodic (the reference's F::head), bit 0: x periodic
+    // (F::tail::head; LaplRectFFT2 only: LaplRect's tridiagonal x ignores it)
+    int flags = 0;
     double dx, dy, lx, ly;
     AxisTables<double> tx64, ty64;
     AxisTables<float> tx32, ty32;
     DevBuf lamx64, lamy64, lamx32, lamy32;
+    DevBuf ptw_x, ptw_y;  // periodic transforms' twiddles
     DevBuf hin, hout;
 
-    void init() {
-        if (dtype == FDMGPU_F64) {
-            ty64.build(ny + 1);
-            upload_lambda<double>(lamy64, ny, dy);
-            if (method == FDMGPU_RECT_FFT2) {
-                tx64.build(nx + 1);
-                upload_lambda<double>(lamx64, nx, nx == ny ? dy : dx);  // src/lapl_rect.cpp:40
-            }
+    bool py() const { return (flags & 2) != 0; }
+    bool px() const { return (flags & 1) != 0 && method == FDMGPU_RECT_FFT2; }
+
+    template <typename T>
+    void init_t(AxisTables<T>& tx, AxisTables<T>& ty, DevBuf& lamx, DevBuf& lamy) {
+        if (py()) {
+            upload_ptwiddles<T>(ptw_y, ny);
+            upload_plambda<T>(lamy, ny, dy);  // lm_y = 4/dy^2 sin^2(k pi/ny), src/lapl_rect.cpp:16
         } else {
-            ty32.build(ny + 1);
-            upload_lambda<float>(lamy32, ny, dy);
-            if (method == FDMGPU_RECT_FFT2) {
-                tx32.build(nx + 1);
-                upload_lambda<float>(lamx32, nx, nx == ny ? dy : dx);
-            }
+            ty.build(ny + 1);
+            upload_lambda<T>(lamy, ny, dy);
         }
+        if (method != FDMGPU_RECT_FFT2) return;
+        if (px()) {
+            upload_ptwiddles<T>(ptw_x, nx);
+            upload_plambda<T>(lamx, nx, dx);  // src/lapl_rect.cpp:30
+        } else {
+            tx.build(nx + 1);
+            // lm_y stands in for lm_x only without periodic flags (src/lapl_rect.cpp:35-40)
+            upload_lambda<T>(lamx, nx, (flags == 0 && nx == ny) ? dy : dx);
+        }
+    }
+
+    void init() {
+        if (dtype == FDMGPU_F64) init_t<double>(tx64, ty64, lamx64, lamy64);
+        else init_t<float>(tx32, ty32, lamx32, lamy32);
     }
 
     template <typename T>
@@ -866,19 +882,30 @@ struct RectPlan {
              const DevBuf& lamy, cudaStream_t st) {
         const double sly = std::sqrt(2. / ly), slx = std::sqrt(2. / lx);
         const long long vs = (long long)nx * ny;
-        launch_sine<T, T, T, 1>(rhs, ans, nx, ny, 1, nrhs, ty.view(), dy * sly, st);
+        // periodic lines: along y, line L = (volume, column) starts at
+        // (L / nx) * vs + L % nx with stride nx; along x, rows of nx
+        const PLineGeom gy{(long long)nrhs * nx, nx, vs, 1, nx};
+        const PLineGeom gx{(long long)nrhs * ny, 1, nx, 0, 1};
+        if (py()) launch_pfft<T, false>(rhs, ans, gy, ny, ptw_y.p, dy * sly, st);
+        else launch_sine<T, T, T, 1>(rhs, ans, nx, ny, 1, nrhs, ty.view(), dy * sly, st);
         if (method == FDMGPU_RECT_TRIDIAG) {
             // per y-mode k: (u[j-1] - 2u[j] + u[j+1])/dx^2 - lm_y[k] u[j] = g[j]
             launch_tridiag<T>(ans, ny, nx, 1, 0, nx, 1, vs, nrhs, nullptr, (const T*)lamy.p, dx * dx, dx * dx, st);
         } else {
-            launch_sine<T, T, T, 0>(ans, ans, nx, ny, 1, nrhs, tx.view(), dx * slx, st);
-            dim3 grid((unsigned)((vs + 255) / 256), nrhs);
-            FDM_TIMED("divide2d", st);
-            k_divide2d<T><<<grid, 256, 0, st>>>(ans, nx, ny, vs, (const T*)lamx.p, (const T*)lamy.p);
-            FDM_LAUNCH_CHECK();
-            launch_sine<T, T, T, 0>(ans, ans, nx, ny, 1, nrhs, tx.view(), slx, st);
+            if (px()) launch_pfft<T, false>(ans, ans, gx, nx, ptw_x.p, dx * slx, st);
+            else launch_sine<T, T, T, 0>(ans, ans, nx, ny, 1, nrhs, tx.view(), dx * slx, st);
+            {
+                dim3 grid((unsigned)((vs + 255) / 256), nrhs);
+                FDM_TIMED("divide2d", st);
+                k_divide2d<T><<<grid, 256, 0, st>>>(ans, nx, ny, vs, (const T*)lamx.p, (const T*)lamy.p,
+                                                    (px() && py()) ? 1 : 0);
+                FDM_LAUNCH_CHECK();
+            }
+            if (px()) launch_pfft<T, true>(ans, ans, gx, nx, ptw_x.p, slx, st);
+            else launch_sine<T, T, T, 0>(ans, ans, nx, ny, 1, nrhs, tx.view(), slx, st);
         }
-        launch_sine<T, T, T, 1>(ans, ans, nx, ny, 1, nrhs, ty.view(), sly, st);
+        if (py()) launch_pfft<T, true>(ans, ans, gy, ny, ptw_y.p, sly, st);
+        else launch_sine<T, T, T, 1>(ans, ans, nx, ny, 1, nrhs, ty.view(), sly, st);
     }
 
     void solve_device(void* ans, const void* rhs, int nrhs, cudaStream_t st) {
@@ -1729,25 +1756,37 @@ int fdmgpu_lapl_cyl_destroy(fdmgpu_lapl_cyl* h) {
     FDM_API_END
 }
 
-int fdmgpu_lapl_rect_create(fdmgpu_lapl_rect** h, int dtype, int method, double dx, double dy, double lx, double ly,
-                            int nx, int ny) {
+int fdmgpu_lapl_rect_create_flags(fdmgpu_lapl_rect** h, int dtype, int method, int flags, double dx, double dy,
+                                  double lx, double ly, int nx, int ny) {
     FDM_API_BEGIN
     if (!h) FDM_FAIL(FDMGPU_EINVAL, "null handle pointer");
     *h = nullptr;
     if (dtype != FDMGPU_F64 && dtype != FDMGPU_F32) FDM_FAIL(FDMGPU_EINVAL, "bad dtype %d", dtype);
     if (method != FDMGPU_RECT_TRIDIAG && method != FDMGPU_RECT_FFT2) FDM_FAIL(FDMGPU_EINVAL, "bad method %d", method);
-    if (!pow2_interior(ny)) FDM_FAIL(FDMGPU_ESIZE, "verify((1<<n) == N) failed: ny+1 must be a power of two (ny=%d)", ny);
-    if (method == FDMGPU_RECT_FFT2 && !pow2_interior(nx))
-        FDM_FAIL(FDMGPU_ESIZE, "verify((1<<n) == N) failed: nx+1 must be a power of two (nx=%d)", nx);
+    if (flags != 0 && flags != 2 && flags != 3)
+        FDM_FAIL(FDMGPU_ENOTSUP, "flags %d: the reference instantiates none (0), y periodic (2) and both (3), "
+                                 "src/lapl_rect.cpp:209-238", flags);
+    const bool py = (flags & 2) != 0, px = (flags & 1) != 0 && method == FDMGPU_RECT_FFT2;
+    if (py ? !pow2_periodic(ny) : !pow2_interior(ny))
+        FDM_FAIL(FDMGPU_ESIZE, "verify((1<<n) == N) failed: %s (ny=%d)",
+                 py ? "periodic ny must be a power of two in [2, 512]" : "ny+1 must be a power of two", ny);
+    if (method == FDMGPU_RECT_FFT2 && (px ? !pow2_periodic(nx) : !pow2_interior(nx)))
+        FDM_FAIL(FDMGPU_ESIZE, "verify((1<<n) == N) failed: %s (nx=%d)",
+                 px ? "periodic nx must be a power of two in [2, 512]" : "nx+1 must be a power of two", nx);
     if (nx < 1 || nx > kTriCk * kTriMaxCk) FDM_FAIL(FDMGPU_ESIZE, "nx must be in [1, %d]", kTriCk * kTriMaxCk);
     if (!(dx > 0 && dy > 0 && lx > 0 && ly > 0)) FDM_FAIL(FDMGPU_EINVAL, "spacings and lengths must be positive");
     std::unique_ptr<fdmgpu_lapl_rect> p(new fdmgpu_lapl_rect());
     RectPlan& r = p->plan;
-    r.dtype = dtype; r.method = method; r.nx = nx; r.ny = ny;
+    r.dtype = dtype; r.method = method; r.nx = nx; r.ny = ny; r.flags = flags;
     r.dx = dx; r.dy = dy; r.lx = lx; r.ly = ly;
     r.init();
     *h = p.release();
     FDM_API_END
+}
+
+int fdmgpu_lapl_rect_create(fdmgpu_lapl_rect** h, int dtype, int method, double dx, double dy, double lx, double ly,
+                            int nx, int ny) {
+    return fdmgpu_lapl_rect_create_flags(h, dtype, method, 0, dx, dy, lx, ly, nx, ny);
 }
 
 int fdmgpu_lapl_rect_solve_device(fdmgpu_lapl_rect* h, void* d_ans, const void* d_rhs, int nrhs, void* stream) {

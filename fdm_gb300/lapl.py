@@ -275,21 +275,25 @@ class LaplCyl3FFT2:
 
 
 class LaplRect:
-    """2-D Dirichlet Poisson solver, fdm::LaplRect<T,check,F>: DST along y,
-    tridiagonal solve along x per y-mode (src/lapl_rect.cpp:63-110)."""
+    """2-D Poisson solver, fdm::LaplRect<T,check,F>: DST (or, y periodic, the
+    periodic transform) along y, tridiagonal solve along x per y-mode
+    (src/lapl_rect.cpp:63-110).  periodic_y / periodic_x are the template's
+    flags (F::head, F::tail::head); periodic=True sets both."""
 
     _method = N.RECT_TRIDIAG
 
-    def __init__(self, dx, dy, lx, ly, nx, ny, dtype=np.float64, periodic=False):
+    def __init__(self, dx, dy, lx, ly, nx, ny, dtype=np.float64, periodic=False, periodic_y=False,
+                 periodic_x=False):
         if periodic:
-            raise N.FdmError(N.ENOTSUP, "periodic LaplRect is not implemented")
+            periodic_y = periodic_x = True
+        flags = (2 if periodic_y else 0) | (1 if periodic_x else 0)
         self._lib = N.load()
         self.dtype = np.dtype(dtype)
         self.nx, self.ny = int(nx), int(ny)
         self.count = self.nx * self.ny
         h = c_void_p()
-        N.check(self._lib.fdmgpu_lapl_rect_create(byref(h), _dtype_code(dtype), self._method, float(dx), float(dy),
-                                                  float(lx), float(ly), self.nx, self.ny))
+        N.check(self._lib.fdmgpu_lapl_rect_create_flags(byref(h), _dtype_code(dtype), self._method, flags, float(dx),
+                                                        float(dy), float(lx), float(ly), self.nx, self.ny))
         self._h = h
 
     def solve(self, ans: np.ndarray, rhs: np.ndarray) -> None:
@@ -316,8 +320,8 @@ class LaplRect:
 
 
 class LaplRectFFT2(LaplRect):
-    """2-D Dirichlet Poisson solver with DSTs on both axes,
-    fdm::LaplRectFFT2 (src/lapl_rect.cpp:113-207)."""
+    """2-D Poisson solver with transforms on both axes (DST, or the periodic
+    transform on a periodic axis), fdm::LaplRectFFT2 (src/lapl_rect.cpp:113-207)."""
 
     _method = N.RECT_FFT2
 

@@ -19,11 +19,9 @@ public:
 protected:
     LaplRect() = default;
     void create(int method, double dx, double dy, double lx, double ly, int nx, int ny) {
-        if (tensor_flags_mask<F>::value) {
-            fprintf(stderr, "verify(periodic LaplRect) failed: not implemented on the GPU\n");
-            abort();
-        }
-        fdmgpu_verify(fdmgpu_lapl_rect_create(&h_, fdmgpu_dtype<T>::value, method, dx, dy, lx, ly, nx, ny),
+        // the reference lists the flags y, x (src/lapl_rect.h:47-49, 81-83)
+        const int flags = (F::head == tensor_flag::periodic ? 2 : 0) | (F::tail::head == tensor_flag::periodic ? 1 : 0);
+        fdmgpu_verify(fdmgpu_lapl_rect_create_flags(&h_, fdmgpu_dtype<T>::value, method, flags, dx, dy, lx, ly, nx, ny),
                       "fdmgpu_lapl_rect_create");
     }
     fdmgpu_lapl_rect* h_ = nullptr;

@@ -214,6 +214,17 @@ typedef struct fdmgpu_lapl_rect fdmgpu_lapl_rect;
 
 int fdmgpu_lapl_rect_create(fdmgpu_lapl_rect** h, int dtype, int method,
                             double dx, double dy, double lx, double ly, int nx, int ny);
+/* The same with the reference's periodic flags (LaplRect(FFT2)<T,check,F>,
+ * src/lapl_rect.cpp:209-238): flags bit 1 = y periodic (F::head), bit 0 = x
+ * periodic (F::tail::head).  0, 2 (y) and 3 (y and x) are instantiated; other
+ * values return FDMGPU_ENOTSUP.  A periodic axis has n points, a power of two
+ * (pFFT_1 / pFFT along it, lm = 4/h^2 sin^2(k pi/n)); arrays are the
+ * reference's {y1..yn, x1..xn} ranges, ny x nx.  LaplRect solves x as
+ * tridiagonal systems whatever bit 0 says (as the reference does); with both
+ * axes periodic LaplRectFFT2 sets the (0, 0) mode to 1 as the reference's
+ * "hack for double-period" does (src/lapl_rect.cpp:169-172). */
+int fdmgpu_lapl_rect_create_flags(fdmgpu_lapl_rect** h, int dtype, int method, int flags,
+                                  double dx, double dy, double lx, double ly, int nx, int ny);
 int fdmgpu_lapl_rect_solve(fdmgpu_lapl_rect* h, void* ans, const void* rhs);
 int fdmgpu_lapl_rect_solve_device(fdmgpu_lapl_rect* h, void* d_ans, const void* d_rhs,
                                   int nrhs, void* stream);

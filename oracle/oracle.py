@@ -80,6 +80,16 @@ class Port:
             raise ValueError("bad size")
         return ans
 
+    def lapl_rect_flags(self, rhs, dx, dy, lx, ly, fft2: bool, flags: int) -> np.ndarray:
+        """LaplRect(FFT2)<double,false,F> with F periodic in y (flags 2) or in
+        y and x (flags 3)."""
+        ny, nx = rhs.shape
+        r = np.ascontiguousarray(rhs, np.float64)
+        ans = np.zeros_like(r)
+        if self.L.ref_lapl_rect_flags_d(nx, ny, dx, dy, lx, ly, 1 if fft2 else 0, flags, _p(ans), _p(r)):
+            raise ValueError("flags %d not instantiated" % flags)
+        return ans
+
     def lapl_rect(self, rhs, dx, dy, lx, ly, fft2: bool = False) -> np.ndarray:
         ny, nx = rhs.shape
         r = np.ascontiguousarray(rhs, np.float64)
@@ -170,6 +180,7 @@ class Reference:
         L.ref_pfft1_d.argtypes = [_dp, _dp, c_double, c_int]
         L.ref_pfft_d.argtypes = [_dp, _dp, c_double, c_int]
         L.ref_pfft3d_d.argtypes = [_dp, _dp, c_double, c_int, c_int]
+        L.ref_lapl_rect_flags_d.argtypes = [c_int] * 2 + [c_double] * 4 + [c_int] * 2 + [_dp, _dp]
         L.ref_lapl_cube_periodic_d.argtypes = [c_int] * 3 + [c_double] * 6 + [_dp, _dp]
         L.ref_lapl_cyl_d.argtypes = [c_int] * 4 + [c_double] * 5 + [_dp, _dp]
         L.ref_nscyl_create.restype = c_void_p
@@ -238,6 +249,16 @@ class Reference:
         r = np.ascontiguousarray(rhs, np.float64)
         ans = np.zeros_like(r)
         self.L.ref_lapl_cyl_d(1 if periodic_z else 0, nr, nz, nphi, dr, dz, r0, lr, lz, _p(ans), _p(r))
+        return ans
+
+    def lapl_rect_flags(self, rhs, dx, dy, lx, ly, fft2: bool, flags: int) -> np.ndarray:
+        """LaplRect(FFT2)<double,false,F> with F periodic in y (flags 2) or in
+        y and x (flags 3)."""
+        ny, nx = rhs.shape
+        r = np.ascontiguousarray(rhs, np.float64)
+        ans = np.zeros_like(r)
+        if self.L.ref_lapl_rect_flags_d(nx, ny, dx, dy, lx, ly, 1 if fft2 else 0, flags, _p(ans), _p(r)):
+            raise ValueError("flags %d not instantiated" % flags)
         return ans
 
     def lapl_rect(self, rhs, dx, dy, lx, ly, fft2: bool = False) -> np.ndarray:
@@ -355,6 +376,41 @@ def dst1(x: np.ndarray, dx: float, axis: int = -1) -> np.ndarray:
     j = np.arange(1, n + 1)
     S = np.sin(np.pi * np.outer(j, j) / (n + 1))
     return np.moveaxis(x @ S * dx, -1, axis)
+
+
+def lapl_rect_flags(rhs, dx, dy, lx, ly, fft2: bool, flags: int) -> np.ndarray:
+    """Restatement of LaplRect / LaplRectFFT2 with periodic flags
+    (src/lapl_rect.cpp:11-41, 63-207): flags 2 = y periodic (pFFT_1 / pFFT
+    along y, lm_y = 4/dy^2 sin^2(k pi/ny)), 3 = y and x periodic (FFT2: pFFT
+    along x too, lm_x = 4/dx^2 sin^2(j pi/nx), and the reference's
+    double-period hack: the (0, 0) mode := 1).  LaplRect solves x as
+    tridiagonal systems whatever the x flag.  rhs is (ny, nx)."""
+    r = np.asarray(rhs, np.float64)
+    ny, nx = r.shape
+    sly, slx = np.sqrt(2.0 / ly), np.sqrt(2.0 / lx)
+    lmy = 4.0 / (dy * dy) * np.sin(np.arange(ny) * np.pi / ny) ** 2
+    a = pfft1(r, dy * sly, axis=0)
+    px = bool(flags & 1) and fft2
+    if not fft2:
+        out = np.empty_like(a)
+        for k in range(ny):
+            A = (np.diag(np.full(nx, -2.0 / (dx * dx) - lmy[k])) + np.diag(np.full(nx - 1, 1.0 / (dx * dx)), 1)
+                 + np.diag(np.full(nx - 1, 1.0 / (dx * dx)), -1))
+            out[k] = np.linalg.solve(A, a[k])
+        a = out
+    elif px:
+        lmx = 4.0 / (dx * dx) * np.sin(np.arange(nx) * np.pi / nx) ** 2
+        b = pfft1(a, dx * slx, axis=1)
+        with np.errstate(divide="ignore", invalid="ignore"):
+            b = b / (-lmy[:, None] - lmx[None, :])
+        b[0, 0] = 1.0
+        a = pfft(b, slx, axis=1)
+    else:
+        lmx = 4.0 / (dx * dx) * np.sin(np.arange(1, nx + 1) * np.pi * 0.5 / (nx + 1)) ** 2
+        b = dst1(a, dx * slx, axis=1)
+        b = b / (-lmy[:, None] - lmx[None, :])
+        a = dst1(b, slx, axis=1)
+    return pfft(a, sly, axis=0)
 
 
 def lapl_cyl(rhs, dr, dz, r0, lr, lz, periodic_z: bool = False) -> np.ndarray:

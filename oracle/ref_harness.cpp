@@ -138,6 +138,37 @@ int ref_lapl_rect_solve_d(int nx, int ny, double dx, double dy, double lx, doubl
     return 0;
 }
 
+// LaplRect / LaplRectFFT2 with periodic flags (src/lapl_rect.cpp:209-238):
+// flags bit 1 = y periodic (F::head), bit 0 = x periodic (F::tail::head);
+// the instantiated sets are 2 (y) and 3 (y and x).  Arrays are the
+// {y1..yn, x1..xn} ranges: ny rows for periodic y, nx columns for periodic x.
+}  // extern "C"
+
+template <typename F>
+static void rect_flags(int nx, int ny, double dx, double dy, double lx, double ly, int fft2, double* ans,
+                       const double* rhs) {
+    std::vector<double> r(rhs, rhs + (size_t)nx * ny);
+    if (fft2) {
+        LaplRectFFT2<double, false, F> l(dx, dy, lx, ly, nx, ny);
+        l.solve(ans, r.data());
+    } else {
+        LaplRect<double, false, F> l(dx, dy, lx, ly, nx, ny);
+        l.solve(ans, r.data());
+    }
+}
+
+extern "C" {
+
+int ref_lapl_rect_flags_d(int nx, int ny, double dx, double dy, double lx, double ly, int fft2, int flags,
+                          double* ans, const double* rhs) {
+    using P1 = tensor_flags<tensor_flag::periodic>;
+    using P2 = tensor_flags<tensor_flag::periodic, tensor_flag::periodic>;
+    if (flags == 2) rect_flags<P1>(nx, ny, dx, dy, lx, ly, fft2, ans, rhs);
+    else if (flags == 3) rect_flags<P2>(nx, ny, dx, dy, lx, ly, fft2, ans, rhs);
+    else return -1;
+    return 0;
+}
+
 // S[1..N-1] = dx * sum_{j=1}^{N-1} s[j] sin(pi j k / N); s is overwritten.
 int ref_sfft_d(double* S, double* s, double dx, int N) {
     FFTTable<double> t(N);

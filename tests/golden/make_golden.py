@@ -256,6 +256,18 @@ def main():
         r["tri_%dx%d" % (nx, ny)] = R.lapl_rect(rhs, *args, fft2=False)
         if (nx + 1) & nx == 0:
             r["fft2_%dx%d" % (nx, ny)] = R.lapl_rect(rhs, *args, fft2=True)
+    # periodic flags (src/lapl_rect.cpp:209-238): y periodic (2) for both
+    # methods, y and x periodic (3) for LaplRectFFT2 (with the double-period
+    # zero mode) and for LaplRect (whose x stays tridiagonal)
+    for tag, fft2, flags, nx, ny in (("tri_py", False, 2, 20, 32), ("fft2_py", True, 2, 31, 64),
+                                     ("fft2_pxy", True, 3, 32, 16), ("tri_pxy", False, 3, 15, 8)):
+        px = fft2 and flags == 3
+        rhs = rng.standard_normal((ny, nx))
+        dx, dy = 0.09, 0.13
+        args = (dx, dy, (nx if px else nx + 1) * dx, ny * dy)
+        r["rhs_" + tag] = rhs
+        r["args_" + tag] = np.array(args)
+        r["ans_" + tag] = R.lapl_rect_flags(rhs, *args, fft2, flags)
     np.savez_compressed(OUT / "lapl_rect.npz", **r)
 
     # tridiagonal: Thomas and cyclic reduction on U(-1,1) systems with a

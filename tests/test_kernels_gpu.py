@@ -81,6 +81,45 @@ def test_rect_vs_reference(cuda, golden):
             assert rel_l2(ans2, g["fft2_" + key]) <= 1e-12
 
 
+@pytest.mark.parametrize("tag,fft2,flags", [("tri_py", False, 2), ("fft2_py", True, 2), ("fft2_pxy", True, 3),
+                                             ("tri_pxy", False, 3)])
+def test_rect_periodic_flags_vs_reference(cuda, golden, tag, fft2, flags):
+    """LaplRect / LaplRectFFT2 with the reference's periodic flags (y, or y
+    and x; the doubly periodic FFT2 sets its zero mode to 1 as the reference
+    does), FP64 and FP32, host and device entry points."""
+    import torch
+    g = golden("lapl_rect")
+    rhs, args, ref = g["rhs_" + tag], tuple(g["args_" + tag]), g["ans_" + tag]
+    ny, nx = rhs.shape
+    cls = LaplRectFFT2 if fft2 else LaplRect
+    kw = dict(periodic_y=True, periodic_x=flags == 3)
+    r = cls(*args, nx, ny, **kw)
+    ans = np.zeros_like(rhs)
+    r.solve(ans, rhs)
+    assert rel_l2(ans, ref) <= 1e-12
+    r32 = cls(*args, nx, ny, dtype=np.float32, **kw)
+    a32 = np.zeros(rhs.shape, np.float32)
+    r32.solve(a32, rhs.astype(np.float32))
+    assert rel_l2(a32.astype(np.float64), ref) <= 1e-5
+    two = torch.tensor(np.stack([rhs, rhs]), device=cuda)
+    out = torch.empty_like(two)
+    r.solve_device(out, two, nrhs=2)
+    torch.cuda.synchronize()
+    o = out.cpu().numpy()
+    assert np.array_equal(o[0], ans) and np.array_equal(o[1], ans)
+
+
+def test_rect_flags_errors(cuda):
+    from fdm_gb300 import FdmError
+    from fdm_gb300 import _native as N
+    with pytest.raises(FdmError) as e:
+        LaplRectFFT2(0.1, 0.1, 1.0, 1.0, 16, 16, periodic_x=True)  # x alone: not instantiated
+    assert e.value.status == N.ENOTSUP
+    with pytest.raises(FdmError) as e:
+        LaplRect(0.1, 0.1, 1.0, 1.0, 15, 24, periodic_y=True)  # periodic ny not a power of two
+    assert e.value.status == N.ESIZE
+
+
 def test_rect_formulations_agree_511(cuda):
     # ut/ut_lapl_rect.cpp:384-456
     n = 511
