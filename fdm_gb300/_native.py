@@ -118,6 +118,7 @@ _SIGS = [
      + [c_int] * 2),
     ("fdmgpu_pfft3d_device", c_int, [c_int, c_int, c_int, c_double, c_void_p, c_void_p, c_int, c_void_p]),
     ("fdmgpu_pfft3d", c_int, [c_int, c_int, c_int, c_double, c_void_p, c_void_p]),
+    ("fdmgpu_pfft_device", c_int, [c_int, c_int, c_int, c_int, c_double, c_void_p, c_void_p, c_void_p]),
     ("fdmgpu_nbody_create", c_int, [POINTER(c_void_p), c_int] + [c_double] * 4 + [c_int] * 3 + [c_double] * 3
      + [c_int] * 3 + [c_double]),
     ("fdmgpu_nbody_info", c_int, [c_void_p, POINTER(c_int), POINTER(c_double), POINTER(c_double),

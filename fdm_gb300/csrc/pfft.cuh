@@ -32,9 +32,10 @@ __device__ __forceinline__ long long pline_base(const PLineGeom& g, long long L)
     return (L / g.A) * g.B + (L % g.A) * g.C;
 }
 
-// lines per block: at most 1024 / n (at least 1), 256 threads; fewer when
-// that leaves most SMs without a block (small transforms)
-__host__ __device__ constexpr int pfft_lines_per_block(int n) { return n >= 1024 ? 1 : 1024 / n; }
+// lines per block: at most 2048 / n (at least 1; 32 KB of shared memory in
+// FP64), 256 threads; fewer when that leaves most SMs without a block (small
+// transforms)
+__host__ __device__ constexpr int pfft_lines_per_block(int n) { return n >= 2048 ? 1 : 2048 / n; }
 
 inline int pfft_lines_per_block(int n, long long lines, int sms) {
     int lpb = pfft_lines_per_block(n);

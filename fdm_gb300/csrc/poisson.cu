@@ -1875,6 +1875,26 @@ int fdmgpu_pfft3d_device(int dtype, int n, int inverse, double dx, void* d_out, 
     FDM_API_END
 }
 
+int fdmgpu_pfft_device(int dtype, int N, int inverse, int nlines, double dx, void* d_out, const void* d_in,
+                       void* stream) {
+    FDM_API_BEGIN
+    if (!d_out || !d_in) FDM_FAIL(FDMGPU_EINVAL, "null argument");
+    if (!pow2_periodic(N)) FDM_FAIL(FDMGPU_ESIZE, "verify((1<<n) == N) failed: N must be a power of two in [2, 512], got %d", N);
+    if (nlines < 1) FDM_FAIL(FDMGPU_EINVAL, "nlines must be positive");
+    if (dtype != FDMGPU_F64 && dtype != FDMGPU_F32) FDM_FAIL(FDMGPU_EINVAL, "bad dtype %d", dtype);
+    cudaStream_t st = (cudaStream_t)stream;
+    const void* tw = pfft3d_twiddles(dtype, N);
+    const PLineGeom g{nlines, 1, N, 0, 1};
+    if (dtype == FDMGPU_F64) {
+        if (inverse) launch_pfft<double, true>((const double*)d_in, (double*)d_out, g, N, tw, dx, st);
+        else launch_pfft<double, false>((const double*)d_in, (double*)d_out, g, N, tw, dx, st);
+    } else {
+        if (inverse) launch_pfft<float, true>((const float*)d_in, (float*)d_out, g, N, tw, dx, st);
+        else launch_pfft<float, false>((const float*)d_in, (float*)d_out, g, N, tw, dx, st);
+    }
+    FDM_API_END
+}
+
 int fdmgpu_pfft3d(int dtype, int n, int inverse, double dx, void* out, const void* in) {
     FDM_API_BEGIN
     if (!out || !in) FDM_FAIL(FDMGPU_EINVAL, "null argument");

@@ -358,6 +358,17 @@ def _pfft3d_host(S, s, dx, inverse):
     N.check(lib.fdmgpu_pfft3d(_dtype_code(s.dtype), int(n), int(inverse), float(dx), S.ctypes.data, s.ctypes.data))
 
 
+def pfft_device(out, inp, N_points: int, nlines: int, dx: float = 1.0, inverse: bool = False, dtype=np.float64,
+                stream=None) -> None:
+    """FFT<T>::pFFT_1 (inverse False) / pFFT of nlines contiguous lines of
+    N_points values on the device (src/fft.cpp:108-212)."""
+    lib = N.load()
+    eb = np.dtype(dtype).itemsize
+    cnt = N_points * nlines
+    N.check(lib.fdmgpu_pfft_device(_dtype_code(dtype), int(N_points), int(bool(inverse)), int(nlines), float(dx),
+                                   _dev_ptr(out, eb, cnt), _dev_ptr(inp, eb, cnt), _stream_ptr(stream)))
+
+
 def pfft3d_device(out, inp, n: int, dx: float, inverse: bool = False, count: int = 1, dtype=np.float64,
                   stream=None) -> None:
     """pFFT_1_3d / pFFT_3d of `count` device cubes of n^3 back to back,

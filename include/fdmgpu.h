@@ -250,6 +250,11 @@ int fdmgpu_sine_device(int dtype, int N, int nlines, double scale,
 int fdmgpu_pfft3d_device(int dtype, int n, int inverse, double dx, void* d_out, const void* d_in, int count,
                          void* stream);
 int fdmgpu_pfft3d(int dtype, int n, int inverse, double dx, void* out, const void* in);
+/* FFT<T>::pFFT_1 (inverse = 0) / pFFT (inverse = 1), src/fft.cpp:108-212, of
+ * nlines contiguous lines of N values (N a power of two, 2..512), scale dx;
+ * asynchronous on stream */
+int fdmgpu_pfft_device(int dtype, int N, int inverse, int nlines, double dx, void* d_out, const void* d_in,
+                       void* stream);
 /* DST-I of FP32 lines of N-1 points (N = 32, 64 or 128) as a dense contraction
  * with the sine matrix on the tensor cores (split TF32, FP32 accumulation;
  * no counterpart in the reference).  axis 0: `count` contiguous lines;

@@ -217,3 +217,23 @@ def test_bounded_wait_gives_up_and_context_survives(cuda):
     assert torch.isfinite(y).all()
     with pytest.raises(FdmError):
         N.check(lib.fdmgpu_check_bounded_wait(0))
+
+
+@pytest.mark.parametrize("N", [8, 64, 512])
+def test_pfft_lines_vs_reference(cuda, golden, N):
+    """FFT<T>::pFFT_1 / pFFT of contiguous lines on the device against the
+    reference's own outputs (lapl_cube_periodic.npz pf_* vectors)."""
+    import torch
+    from fdm_gb300 import pfft_device
+    g = golden("lapl_cube_periodic")
+    s = g["pf_s_%d" % N]
+    x = torch.tensor(np.stack([s, 3 * s]), device=cuda)
+    y = torch.empty_like(x)
+    pfft_device(y, x, N, 2, dx=0.7)
+    z = torch.empty_like(x)
+    pfft_device(z, x, N, 2, dx=0.3, inverse=True)
+    torch.cuda.synchronize()
+    yy, zz = y.cpu().numpy(), z.cpu().numpy()
+    assert np.abs(yy[0] - g["pf1_%d" % N]).max() <= 1e-13 * N
+    assert np.abs(yy[1] - 3 * yy[0]).max() <= 1e-13 * N
+    assert np.abs(zz[0] - g["pf_%d" % N]).max() <= 1e-13 * N
