@@ -105,6 +105,7 @@ _SIGS = [
     ("fdmgpu_nscube_dtype", c_int, [c_void_p, POINTER(c_int)]),
     ("fdmgpu_nscube_destroy", c_int, [c_void_p]),
     ("fdmgpu_check_const_division", c_int, [c_longlong, c_void_p, c_void_p, c_void_p, c_void_p, c_void_p]),
+    ("fdmgpu_check_dd_conversions", c_int, [c_longlong] + [c_void_p] * 10),
     ("fdmgpu_nscyl_create", c_int, [POINTER(c_void_p), c_int, c_int] + [c_double] * 7 + [c_int] * 3),
     ("fdmgpu_nscyl_step", c_int, [c_void_p, c_int]),
     ("fdmgpu_nscyl_field_info", c_int, [c_void_p, c_int, POINTER(c_size_t), POINTER(c_int)]),

@@ -70,9 +70,53 @@ __device__ __forceinline__ ff ff_mul(ff a, ff b) {
     return fast_two_sum(p.h, e);
 }
 
-// Nearest float to an FP64 value, by integer rounding of the bit pattern
-// (round half away from zero; exact hardware conversion outside the normal
-// float range).
+// The split and the FP64 assembly below cover zero, subnormal, huge, inf and
+// NaN operands with integer operations as well.  A short FP64 fallback for
+// those cases is compiled as predicated code that every element issues: it
+// kept the FP64 pipe of the residual and final passes busy (36 % and 66 %
+// active) although no element took it.  The plain rounding f64_to_f32 keeps
+// its one-instruction hardware fallback, which costs less there than the
+// integer form issued the same way.
+
+// Exact FP64 bit pattern of the float with bit pattern fb (zero, subnormal,
+// inf and NaN included).
+__device__ __forceinline__ long long f32_to_f64_bits(unsigned fb) {
+    const long long sign = (long long)(fb & 0x80000000u) << 32;
+    const unsigned e = (fb >> 23) & 0xffu, m = fb & 0x7fffffu;
+    if (e == 255u) return sign | (0x7ffLL << 52) | ((long long)m << 29);
+    if (e != 0u) return sign | ((long long)(e + 896u) << 52) | ((long long)m << 29);
+    if (m == 0u) return sign;
+    const int p = 31 - __clz((int)m);  // leading bit of the subnormal mantissa, 0..22
+    return sign | ((long long)(p + 874) << 52) | (((long long)m << (52 - p)) & 0xfffffffffffffLL);
+}
+
+// Round to nearest, ties to even, of the FP64 value with bit pattern b and
+// biased exponent e when the float result is zero, subnormal, the top binade,
+// inf or NaN (e < 897 or e > 1149): the hardware conversion's result.
+__device__ __forceinline__ float f64_to_f32_edge(long long b, int e) {
+    const unsigned sign = (unsigned)((unsigned long long)b >> 32) & 0x80000000u;
+    const long long mag = b & 0x7fffffffffffffffLL;
+    if (e == 2047) return __uint_as_float(mag > 0x7ff0000000000000LL ? 0x7fffffffu : (sign | 0x7f800000u));
+    if (e > 1150) return __uint_as_float(sign | 0x7f800000u);
+    if (e == 1150) {  // 2^127 <= |d| < 2^128: exponent 254, or inf when the rounding carries
+        long long r = mag >> 29;
+        const long long rem = mag & 0x1fffffffLL;
+        if (rem > 0x10000000LL || (rem == 0x10000000LL && (r & 1))) r++;
+        return __uint_as_float(sign | (unsigned)(r - (896LL << 23)));
+    }
+    // |d| < 2^-126: the result is a multiple of 2^-149
+    const int shift = 926 - e;  // >= 30
+    if (e == 0 || shift > 54) return __uint_as_float(sign);
+    const long long m = (mag & 0xfffffffffffffLL) | (1LL << 52);
+    long long q = m >> shift;
+    const long long rem = m & ((1LL << shift) - 1), half = 1LL << (shift - 1);
+    if (rem > half || (rem == half && (q & 1))) q++;
+    return __uint_as_float(sign | (unsigned)q);  // q = 2^23 is the smallest normal
+}
+
+// Nearest float to an FP64 value, by integer rounding of the bit pattern:
+// round half away from zero in the normal float range, the hardware
+// conversion (ties to even) outside it.
 __device__ __forceinline__ float f64_to_f32(double d) {
     const long long b = __double_as_longlong(d);
     const int e = (int)((b >> 52) & 0x7ff);
@@ -84,15 +128,10 @@ __device__ __forceinline__ float f64_to_f32(double d) {
     return __uint_as_float(bits);
 }
 
-// (hi, lo) with hi + lo == d to ~2^-48 relative: hi is d rounded to a float,
-// lo the rounded remainder.  Integer path for 2^-74 <= |d| < 2^127.
-__device__ __forceinline__ ff f64_split(double d) {
-    const long long b = __double_as_longlong(d);
-    const int e = (int)((b >> 52) & 0x7ff);
-    if (e < 949 || e > 1149) {
-        const float h = __double2float_rn(d);
-        return ff{h, __double2float_rn(d - (double)h)};
-    }
+// (hi, lo) of an FP64 pattern with biased exponent 949 <= e <= 1149
+// (2^-74 <= |d| < 2^127): hi is d rounded to a float, lo the rounded
+// remainder, hi + lo == d to ~2^-48 relative.
+__device__ __forceinline__ ff f64_split_normal(long long b, int e) {
     const long long mag = b & 0x7fffffffffffffffLL;
     const long long r = (mag + (1LL << 28)) & ~((1LL << 29) - 1);  // hi as an FP64 pattern
     const int er = (int)(r >> 52);
@@ -104,18 +143,47 @@ __device__ __forceinline__ ff f64_split(double d) {
     return ff{h, l};
 }
 
-// FP64 value of h + l for a normalised pair (|l| <= ulp_f32(h)/2), built by
-// integer addition on the FP64 bit pattern of h; exact to half an FP64 ulp.
-__device__ __forceinline__ double ff_to_f64(ff v) {
-    const unsigned hb = __float_as_uint(v.h);
+// f64_split outside 2^-74 <= |d| < 2^127.  Between 2^-126 and 2^-74 and
+// between 2^127 and 2^191 the pair of d scaled by 2^(+-64) is scaled back
+// (hi exact, lo rounded where it falls below the normal floats); below
+// 2^-126 hi is d rounded to the float grid and lo is 0; above 2^191, for inf
+// and for NaN hi is the hardware conversion and lo is -hi or NaN, the values
+// of rn(d - hi).
+__device__ __forceinline__ ff f64_split_edge(long long b, int e) {
+    if (e >= 897 && e < 949) {
+        const ff s = f64_split_normal(b + (64LL << 52), e + 64);
+        return ff{__fmul_rn(s.h, 0x1p-64f), __fmul_rn(s.l, 0x1p-64f)};
+    }
+    if (e > 1149 && e < 1214) {
+        const ff s = f64_split_normal(b - (64LL << 52), e - 64);
+        const float h = __fmul_rn(s.h, 0x1p64f);
+        return ff{h, (__float_as_uint(h) & 0x7fffffffu) == 0x7f800000u ? -h : __fmul_rn(s.l, 0x1p64f)};
+    }
+    const float h = f64_to_f32_edge(b, e);
+    if (e < 897) return ff{h, 0.f};
+    return ff{h, e == 2047 ? __uint_as_float(0x7fffffffu) : -h};
+}
+
+// (hi, lo) with hi + lo == d to ~2^-48 relative: hi is d rounded to a float,
+// lo the rounded remainder.
+__device__ __forceinline__ ff f64_split(double d) {
+    const long long b = __double_as_longlong(d);
+    const int e = (int)((b >> 52) & 0x7ff);
+    if (e < 949 || e > 1149) return f64_split_edge(b, e);
+    return f64_split_normal(b, e);
+}
+
+// FP64 value of h + l for a float h in the normal range and |l| <= ulp(h)/2
+// (l finite: zero, subnormal or normal), built by integer addition on the
+// FP64 bit pattern of h; exact to half an FP64 ulp.
+__device__ __forceinline__ double ff_to_f64_normal(unsigned hb, unsigned lb) {
     const int eh = (int)((hb >> 23) & 0xff);
-    const unsigned lb = __float_as_uint(v.l);
     const int el = (int)((lb >> 23) & 0xff);
-    if (eh == 0 || eh == 255) return (double)v.h + (double)v.l;
     long long D = ((long long)(eh + 896) << 52) | ((long long)(hb & 0x7fffffu) << 29);
-    if (el != 0) {
-        const long long ml = (long long)((lb & 0x7fffffu) | 0x800000u);
-        const int sh = el - eh + 29;  // <= 5 for a normalised pair
+    // l = ml * 2^(el' - 150): a subnormal l has no implicit bit and el' = 1
+    const long long ml = (long long)((lb & 0x7fffffu) | (el ? 0x800000u : 0u));
+    if (ml != 0) {
+        const int sh = (el ? el : 1) - eh + 29;  // <= 5 for a normalised pair
         long long q;
         if (sh >= 0) q = ml << sh;
         else if (sh > -26) q = (ml + (1LL << (-sh - 1))) >> (-sh);
@@ -129,6 +197,37 @@ __device__ __forceinline__ double ff_to_f64(ff v) {
     }
     D |= (long long)(hb & 0x80000000u) << 32;
     return __longlong_as_double(D);
+}
+
+// (double)h + (double)l when h is zero, subnormal, inf or NaN or l is inf or
+// NaN, by integer operations: NaN for a NaN operand or inf - inf, the inf
+// otherwise; with h zero or subnormal and l as well, the exact sum (a
+// multiple of 2^-149 below 2^-125); with l in the normal range (not a
+// normalised pair) l + h as ff_to_f64_normal forms it.
+__device__ __forceinline__ double ff_to_f64_edge(unsigned hb, unsigned lb) {
+    const unsigned ha = hb & 0x7fffffffu, la = lb & 0x7fffffffu;
+    if (ha > 0x7f800000u || la > 0x7f800000u ||
+        (ha == 0x7f800000u && la == 0x7f800000u && ((hb ^ lb) & 0x80000000u)))
+        return __longlong_as_double(0x7fffffffffffffffLL);
+    if (ha == 0x7f800000u) return __longlong_as_double(f32_to_f64_bits(hb));
+    if (la == 0x7f800000u) return __longlong_as_double(f32_to_f64_bits(lb));
+    if (la >= 0x00800000u) return ff_to_f64_normal(lb, hb);
+    // both zero or subnormal: integers in units of 2^-149
+    const int s = ((hb & 0x80000000u) ? -(int)ha : (int)ha) + ((lb & 0x80000000u) ? -(int)la : (int)la);
+    if (s == 0) return __longlong_as_double((long long)(hb & lb & 0x80000000u) << 32);
+    // |s| < 2^24 is the bit pattern of the float |s| * 2^-149 (subnormal, or
+    // the smallest normal binade)
+    return __longlong_as_double(f32_to_f64_bits((s < 0 ? 0x80000000u : 0u) | (unsigned)(s < 0 ? -s : s)));
+}
+
+// FP64 value of h + l for a normalised pair (|l| <= ulp_f32(h)/2), exact to
+// half an FP64 ulp, with integer operations only.
+__device__ __forceinline__ double ff_to_f64(ff v) {
+    const unsigned hb = __float_as_uint(v.h);
+    const unsigned lb = __float_as_uint(v.l);
+    const unsigned eh = (hb >> 23) & 0xffu;
+    if (eh == 0u || eh == 255u || (lb & 0x7f800000u) == 0x7f800000u) return ff_to_f64_edge(hb, lb);
+    return ff_to_f64_normal(hb, lb);
 }
 
 }  // namespace fdmgpu

@@ -1537,6 +1537,22 @@ static void pfft3d_run(const T* in, T* out, int n, int count, double dx, const v
 
 static size_t elem_size(int dtype) { return dtype == FDMGPU_F64 ? sizeof(double) : sizeof(float); }
 
+// Diagnostic: the integer FP64 <-> float conversions of the mixed path
+// beside the hardware conversions and the FP64 sum of a float pair.
+__global__ void k_dd_check(const double* x, const float* ph, const float* pl, long long n, float* f32, float* f32_hw,
+                           float* split_hi, float* split_lo, double* w, double* w_hw) {
+    const long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    const double d = x[i];
+    f32[i] = f64_to_f32(d);
+    f32_hw[i] = __double2float_rn(d);
+    const ff s = f64_split(d);
+    split_hi[i] = s.h;
+    split_lo[i] = s.l;
+    w[i] = ff_to_f64(ff{ph[i], pl[i]});
+    w_hw[i] = __dadd_rn((double)ph[i], (double)pl[i]);
+}
+
 extern "C" {
 
 int fdmgpu_lapl_cube_create(fdmgpu_lapl_cube** h, int dtype, int bc_flags, double dx, double dy, double dz,
@@ -1992,6 +2008,20 @@ int fdmgpu_tridiag_device(int dtype, int n, int nsys, const void* d_lower, const
     }
     FDM_LAUNCH_CHECK();
     FDM_CUDA(cudaStreamSynchronize(st));
+    FDM_API_END
+}
+
+int fdmgpu_check_dd_conversions(long long n, const double* d_x, const float* d_hi, const float* d_lo, float* d_f32,
+                                float* d_f32_hw, float* d_split_hi, float* d_split_lo, double* d_f64, double* d_f64_hw,
+                                void* stream) {
+    FDM_API_BEGIN
+    if (n < 0 || (n > 0 && (!d_x || !d_hi || !d_lo || !d_f32 || !d_f32_hw || !d_split_hi || !d_split_lo || !d_f64 ||
+                            !d_f64_hw)))
+        FDM_FAIL(FDMGPU_EINVAL, "bad argument");
+    if (n == 0) return FDMGPU_OK;
+    k_dd_check<<<(unsigned)((n + 255) / 256), 256, 0, (cudaStream_t)stream>>>(d_x, d_hi, d_lo, n, d_f32, d_f32_hw,
+                                                                              d_split_hi, d_split_lo, d_f64, d_f64_hw);
+    FDM_LAUNCH_CHECK();
     FDM_API_END
 }
 

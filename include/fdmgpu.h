@@ -316,6 +316,15 @@ int fdmgpu_nscube_destroy(fdmgpu_nscube* h);
  * pairs, so a test can check they agree bit for bit. */
 int fdmgpu_check_const_division(long long n, const double* d_a, const double* d_b, double* d_q_ieee,
                                 double* d_q_const, void* stream);
+/* Diagnostic: for n FP64 values x, the mixed path's integer conversions
+ * beside the hardware's -- f32 = its nearest float (ties away from zero in
+ * the normal float range, the hardware's ties-to-even outside it), f32_hw the
+ * hardware conversion, (split_hi, split_lo) its float pair -- and for n float
+ * pairs (hi, lo) the pair's FP64 value by integer assembly (f64) beside the
+ * hardware sum (f64_hw).  Device arrays; asynchronous on stream. */
+int fdmgpu_check_dd_conversions(long long n, const double* d_x, const float* d_hi, const float* d_lo, float* d_f32,
+                                float* d_f32_hw, float* d_split_hi, float* d_split_lo, double* d_f64, double* d_f64_hw,
+                                void* stream);
 
 /* ---- Serving loop (no counterpart in the reference, which runs one
  * solve or one NSCube on the caller's thread) ------------------------------

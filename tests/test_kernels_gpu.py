@@ -237,3 +237,84 @@ def test_pfft_lines_vs_reference(cuda, golden, N):
     assert np.abs(yy[0] - g["pf1_%d" % N]).max() <= 1e-13 * N
     assert np.abs(yy[1] - 3 * yy[0]).max() <= 1e-13 * N
     assert np.abs(zz[0] - g["pf_%d" % N]).max() <= 1e-13 * N
+
+
+def _dd_inputs():
+    """FP64 values over the whole exponent range (zero, subnormal doubles,
+    float-subnormal results and their ties, the top float binade, overflow,
+    inf, NaN) and float pairs (hi, lo) built from them."""
+    rng = np.random.default_rng(11)
+    sp = [0.0, 5e-324, 1e-310, 2.0 ** -150, 2.0 ** -149, 3 * 2.0 ** -150, 5 * 2.0 ** -151, 2.0 ** -126,
+          np.nextafter(2.0 ** -126, 0), 2.0 ** -127, 2.0 ** -74, np.nextafter(2.0 ** -74, 0), 2.0 ** 127,
+          np.nextafter(2.0 ** 127, 0), 2.0 ** 128, 2.0 ** 128 - 2.0 ** 103, 2.0 ** 128 - 2.0 ** 104,
+          np.nextafter(2.0 ** 128 - 2.0 ** 103, 0), 2.0 ** 191, 1.7 * 2.0 ** 190, 1.7976931348623157e308,
+          np.inf, np.nan, 1.0, 3e-40, 1e-45, 7e-46]
+    e = np.repeat(np.arange(-1080, 1031), 12)
+    m = 1.0 + rng.random(e.size)
+    m[::12] = 1.0
+    m[1::12] = 1.0 + 2.0 ** -24  # ties of the float rounding
+    m[2::12] = 1.0 + 3 * 2.0 ** -25
+    with np.errstate(over="ignore"):
+        x = np.r_[sp, np.ldexp(m, e)]
+    x = np.r_[x, -x]
+    with np.errstate(over="ignore", invalid="ignore"):
+        hi = x.astype(np.float32)
+        lo = np.where(np.isfinite(hi), (x - hi.astype(np.float64)), 0.0).astype(np.float32)
+    s = np.array([0.0, -0.0, 1e-45, -1e-45, 3e-40, -3e-40, 1.1754942e-38, np.inf, -np.inf, np.nan, 1.0], np.float32)
+    hi = np.r_[hi, np.repeat(s, s.size)]
+    lo = np.r_[lo, np.tile(s, s.size)]
+    x = np.r_[x, np.ones(hi.size - x.size)]
+    return x, hi, lo
+
+
+def test_dd_conversions_match_hardware(cuda):
+    """The mixed path's FP64 <-> float conversions use integer operations
+    only; outside the normal float range (zero, subnormal results, the top
+    binade, overflow, inf, NaN) they equal the hardware's conversions bit for
+    bit, inside it they differ only at exact ties; split pairs hold x to
+    2^-48 relative; the FP64 value of a float pair equals the hardware sum for
+    zero, subnormal, inf and NaN parts and is within one FP64 ulp of it for
+    normalised pairs."""
+    import torch
+    from fdm_gb300 import _native as N
+    x, hi, lo = _dd_inputs()
+    n = x.size
+    t = lambda a: torch.from_numpy(np.ascontiguousarray(a)).to(cuda)
+    tx, th, tl = t(x), t(hi), t(lo)
+    f32, f32hw, sh, sl = (torch.empty(n, dtype=torch.float32, device=cuda) for _ in range(4))
+    w, whw = (torch.empty(n, dtype=torch.float64, device=cuda) for _ in range(2))
+    N.check(N.load().fdmgpu_check_dd_conversions(n, tx.data_ptr(), th.data_ptr(), tl.data_ptr(), f32.data_ptr(),
+                                                 f32hw.data_ptr(), sh.data_ptr(), sl.data_ptr(), w.data_ptr(),
+                                                 whw.data_ptr(), None))
+    torch.cuda.synchronize()
+    f32, f32hw, sh, sl, w, whw = (a.cpu().numpy() for a in (f32, f32hw, sh, sl, w, whw))
+
+    def same(a, b):
+        return (np.isnan(a) & np.isnan(b)) | (a.view(np.int64 if a.dtype == np.float64 else np.int32)
+                                              == b.view(np.int64 if b.dtype == np.float64 else np.int32))
+
+    ax = np.abs(x)
+    edge = ~((ax >= 2.0 ** -126) & (ax < 2.0 ** 127))
+    assert same(f32, f32hw)[edge].all()
+    diff = ~same(f32, f32hw) & ~edge
+    # inside the normal range only exact ties differ (rounded away from zero)
+    assert np.array_equal(np.abs(f32[diff].astype(np.float64) - x[diff]), np.abs(f32hw[diff].astype(np.float64) - x[diff]))
+    assert diff.sum() < 0.02 * n
+
+    fin = np.isfinite(x) & (ax < 2.0 ** 191)
+    tiny = fin & (ax < 2.0 ** -126)
+    assert same(sh, f32hw)[tiny].all() and (sl[tiny] == 0).all()
+    mid = fin & ~tiny & np.isfinite(sh)
+    err = np.abs(x[mid] - (sh[mid].astype(np.float64) + sl[mid].astype(np.float64)))
+    assert (err <= np.ldexp(ax[mid], -48) + 2.0 ** -149).all()
+    big = ~np.isnan(x) & ~mid & ~tiny
+    assert np.isinf(sh[big]).all() and same(sh, f32hw)[big].all()
+    assert np.isnan(sh[np.isnan(x)]).all() and np.isnan(sl[np.isnan(x)]).all()
+
+    eh = (hi.view(np.uint32) >> 23) & 0xFF
+    el = (lo.view(np.uint32) >> 23) & 0xFF
+    pedge = (eh == 0) | (eh == 255) | (el == 255)
+    assert same(w, whw)[pedge].all()
+    ok = ~pedge & (np.abs(lo.astype(np.float64)) <= np.ldexp(np.abs(hi.astype(np.float64)), -24))
+    ulp = np.abs(np.nextafter(whw[ok], np.inf) - whw[ok])
+    assert (np.abs(w[ok] - whw[ok]) <= ulp).all()
