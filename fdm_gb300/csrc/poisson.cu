@@ -172,7 +172,8 @@ static void launch_rg(const Tin* in, Tout* out, int nx, int ny, int nz, int nvol
     constexpr int L = RgGeom<N, AXIS>::L;
     constexpr size_t smem = rg_smem_bytes<T, N, AXIS>();
     const auto kern = [] {
-        if constexpr (rg_use_occ<T, AXIS, N>()) return k_sine_rg_occ<Tin, T, Tout, AXIS, MODE, N>;
+        if constexpr (rg_use_occ5<T, AXIS, N>()) return k_sine_rg_occ5<Tin, T, Tout, AXIS, MODE, N>;
+        else if constexpr (rg_use_occ<T, AXIS, N>()) return k_sine_rg_occ<Tin, T, Tout, AXIS, MODE, N>;
         else return k_sine_rg<Tin, T, Tout, AXIS, MODE, N>;
     }();
     static bool attr_set = false;

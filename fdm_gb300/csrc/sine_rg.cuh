@@ -428,9 +428,23 @@ __global__ void __launch_bounds__(256, 4) k_sine_rg_occ(const Tin* in, Tout* out
     sine_rg_body<Tin, T, Tout, AXIS, MODE, N>(in, out, geo, tb, scale, fu);
 }
 
+// The FP32 column pass of 256 points held to 48 registers (5 CTAs of 256
+// threads per SM, no spills): 2.86 -> 2.84 ms per 16 x 255^3 step of its
+// four launches; 6 CTAs (40 registers) spill and take 3.22 ms.
+template <typename Tin, typename T, typename Tout, int AXIS, int MODE, int N>
+__global__ void __launch_bounds__(256, 5) k_sine_rg_occ5(const Tin* in, Tout* out, SineGeom geo, SineTables<T> tb,
+                                                         T scale, SineFused fu) {
+    sine_rg_body<Tin, T, Tout, AXIS, MODE, N>(in, out, geo, tb, scale, fu);
+}
+
 template <typename T, int AXIS, int N>
 constexpr bool rg_use_occ() {
     return sizeof(T) == 4 && AXIS == 0 && N >= 256;
+}
+
+template <typename T, int AXIS, int N>
+constexpr bool rg_use_occ5() {
+    return sizeof(T) == 4 && AXIS == 1 && N == 256;
 }
 
 template <typename T, int N, int AXIS>
