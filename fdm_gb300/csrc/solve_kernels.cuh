@@ -216,8 +216,9 @@ __global__ void __launch_bounds__(zpart_max_threads<T, m>()) k_zsolve_part(T* W,
 // pc[0..P-2], stored value-major (tab[v * modes + mode]) so lanes read
 // consecutive modes.  With no divisions left the kernel is FMA chains plus
 // coalesced loads; at 255^2 modes the FP32 table is 15.6 MB and stays in L2.
-template <typename T, int m>
-__global__ void __launch_bounds__(512, 2) k_zsolve_tab(T* W, int nx, int ny, int P, long long vstride,
+// MINB: resident CTAs per SM the register allocation is held to.
+template <typename T, int m, int MINB = 2>
+__global__ void __launch_bounds__(512, MINB) k_zsolve_tab(T* W, int nx, int ny, int P, long long vstride,
                                                     const T* __restrict__ tab, T gscale) {
     extern __shared__ __align__(16) unsigned char zsm[];
     T* s_vf = reinterpret_cast<T*>(zsm);
