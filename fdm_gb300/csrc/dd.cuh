@@ -180,19 +180,20 @@ __device__ __forceinline__ double ff_to_f64_normal(unsigned hb, unsigned lb) {
     const int eh = (int)((hb >> 23) & 0xff);
     const int el = (int)((lb >> 23) & 0xff);
     long long D = ((long long)(eh + 896) << 52) | ((long long)(hb & 0x7fffffu) << 29);
-    // l = ml * 2^(el' - 150): a subnormal l has no implicit bit and el' = 1
-    const long long ml = (long long)((lb & 0x7fffffu) | (el ? 0x800000u : 0u));
+    // l = ml * 2^(el' - 150): a subnormal l has no implicit bit and el' = 1;
+    // q, l in units of the FP64 ulp of h, stays below 2^30, so 32-bit shifts
+    const unsigned ml = (lb & 0x7fffffu) | (el ? 0x800000u : 0u);
     if (ml != 0) {
         const int sh = (el ? el : 1) - eh + 29;  // <= 5 for a normalised pair
-        long long q;
+        unsigned q;
         if (sh >= 0) q = ml << sh;
-        else if (sh > -26) q = (ml + (1LL << (-sh - 1))) >> (-sh);
+        else if (sh > -26) q = (ml + (1u << (-sh - 1))) >> (-sh);
         else q = 0;
         if ((hb ^ lb) & 0x80000000u) {
             if ((hb & 0x7fffffu) == 0) q <<= 1;  // h a power of two: step into the lower binade
-            D -= q;
+            D -= (long long)q;
         } else {
-            D += q;
+            D += (long long)q;
         }
     }
     D |= (long long)(hb & 0x80000000u) << 32;
@@ -200,10 +201,10 @@ __device__ __forceinline__ double ff_to_f64_normal(unsigned hb, unsigned lb) {
 }
 
 // (double)h + (double)l when h is zero, subnormal, inf or NaN or l is inf or
-// NaN, by integer operations: NaN for a NaN operand or inf - inf, the inf
-// otherwise; with h zero or subnormal and l as well, the exact sum (a
-// multiple of 2^-149 below 2^-125); with l in the normal range (not a
-// normalised pair) l + h as ff_to_f64_normal forms it.
+// NaN, by integer (and exact FP32) operations: NaN for a NaN operand or
+// inf - inf, the inf otherwise; with h zero or subnormal and l as well, the
+// exact sum (a multiple of 2^-149 below 2^-125); with l in the normal range
+// (not a normalised pair) l + h to half an FP64 ulp.
 __device__ __forceinline__ double ff_to_f64_edge(unsigned hb, unsigned lb) {
     const unsigned ha = hb & 0x7fffffffu, la = lb & 0x7fffffffu;
     if (ha > 0x7f800000u || la > 0x7f800000u ||
@@ -211,7 +212,14 @@ __device__ __forceinline__ double ff_to_f64_edge(unsigned hb, unsigned lb) {
         return __longlong_as_double(0x7fffffffffffffffLL);
     if (ha == 0x7f800000u) return __longlong_as_double(f32_to_f64_bits(hb));
     if (la == 0x7f800000u) return __longlong_as_double(f32_to_f64_bits(lb));
-    if (la >= 0x00800000u) return ff_to_f64_normal(lb, hb);
+    if (la >= 0x00800000u) {
+        // l normal, h zero or subnormal (not a normalised pair): l + h as the
+        // normalised pair fast_two_sum gives, exactly equal to it
+        const ff t = fast_two_sum(__uint_as_float(lb), __uint_as_float(hb));
+        const unsigned tb = __float_as_uint(t.h);
+        if ((tb & 0x7f800000u) != 0u) return ff_to_f64_normal(tb, __float_as_uint(t.l));
+        return __longlong_as_double(f32_to_f64_bits(tb));  // l + h subnormal: exact, t.l == 0
+    }
     // both zero or subnormal: integers in units of 2^-149
     const int s = ((hb & 0x80000000u) ? -(int)ha : (int)ha) + ((lb & 0x80000000u) ? -(int)la : (int)la);
     if (s == 0) return __longlong_as_double((long long)(hb & lb & 0x80000000u) << 32);
