@@ -74,3 +74,18 @@ def test_shim_cylindrical_matches_reference(tmp_path, native, cuda, golden):
         u = np.frombuffer((tmp_path / "cu").read_bytes())
         ref = g["ns_%s_s20_u" % name]
         assert np.abs(u - ref).max() <= 1e-11 * max(1.0, np.abs(ref).max()), name
+
+
+def test_dd_conversions_host_build(tmp_path):
+    """fdm_gb300/csrc/dd.cuh built for the host with the CUDA intrinsics
+    given their IEEE meaning: the integer FP64 <-> float conversions of the
+    mixed solver agree with the host's IEEE conversions and FP64 addition over
+    the whole exponent range (tests/cpp/dd_host_check.cpp).  The GPU build is
+    checked against the device's conversions in test_kernels_gpu.py."""
+    if not shutil.which("g++"):
+        pytest.skip("g++ not found")
+    exe = tmp_path / "dd_host_check"
+    subprocess.run(["g++", "-std=c++17", "-O1", "-ffp-contract=off", str(ROOT / "tests/cpp/dd_host_check.cpp"),
+                    "-o", str(exe)], check=True)
+    out = subprocess.run([str(exe)], capture_output=True, text=True)
+    assert out.returncode == 0, out.stdout + out.stderr
