@@ -78,6 +78,36 @@ def test_lapl_rect_matches_reference(port, golden):
             assert rel_l2(port.lapl_rect(rhs, *args, fft2=True), g["fft2_" + key]) <= 1e-14
 
 
+def _ut_lapl_rect_case(n=31):
+    """ut/ut_lapl_rect.cpp:21-33, 48-88: u = sin^2 x + cos^2 y at the cell
+    centres of [0,1]^2 (x = x1 + j dx - dx/2), f its Laplacian, the boundary
+    values folded into the right-hand side; LaplRect(dx, dy, 1+dx, 1+dy, n, n)."""
+    dx = dy = 1.0 / n
+    k, j = np.meshgrid(np.arange(1, n + 1), np.arange(1, n + 1), indexing="ij")
+
+    def ans(k, j):
+        x, y = j * dx - dx / 2, k * dy - dy / 2
+        return np.sin(x) ** 2 + np.cos(y) ** 2
+
+    x, y = j * dx - dx / 2, k * dy - dy / 2
+    rhs = 2 * np.sin(y) ** 2 - 2 * np.cos(y) ** 2 - 2 * np.sin(x) ** 2 + 2 * np.cos(x) ** 2
+    rhs[0, :] -= ans(k[0, :] - 1, j[0, :]) / dy / dy
+    rhs[:, 0] -= ans(k[:, 0], j[:, 0] - 1) / dx / dx
+    rhs[:, -1] -= ans(k[:, -1], j[:, -1] + 1) / dx / dx
+    rhs[-1, :] -= ans(k[-1, :] + 1, j[-1, :]) / dy / dy
+    return rhs, ans(k, j), (dx, dy, 1.0 + dx, 1.0 + dy)
+
+
+@pytest.mark.parametrize("fft2", [False, True])
+def test_lapl_rect_reference_unit_case(port, fft2):
+    """ut/ut_lapl_rect.cpp test_lapl_rect: relative max-norm error < 3e-3
+    (:116) for the DST + tridiagonal and the all-DST formulations."""
+    rhs, exact, args = _ut_lapl_rect_case(31)
+    got = port.lapl_rect(rhs, *args, fft2=fft2)
+    err = np.abs(got - exact).max() / np.abs(exact).max()
+    assert err < 3e-3
+
+
 def test_lapl_rect_two_formulations_agree(port):
     # ut/ut_lapl_rect.cpp:384-456 (511^2, |delta| <= 1e-15 absolute)
     n = 511
@@ -146,6 +176,25 @@ def test_periodic_3d_transforms_match_reference(golden):
         for inv, key in ((False, "fft3d_fwd_%d"), (True, "fft3d_inv_%d")):
             ref = g[key % N]
             assert np.abs(pfft3d(s, 1.0, inverse=inv) - ref).max() <= 1e-13 * N * np.abs(ref).max()
+
+
+def test_periodic_lapl_cube_reference_unit_case():
+    """ut/ut_lapl_cube.cpp test_lapl_cube_periodic (:134-243): n = 32 on
+    [0, 2 pi]^3, u = sin^3 x + cos^5 y - sin z and its Laplacian at the cell
+    centres (x = j h - h/2), the answer's mean removed as the test does
+    (dividing by nz*ny*nz), relative max-norm error < 1e-2."""
+    from oracle.oracle import lapl_cube_periodic
+    n = 32
+    h = 2 * np.pi / n
+    i, k, j = np.meshgrid(np.arange(n), np.arange(n), np.arange(n), indexing="ij")
+    x, y, z = j * h - h / 2, k * h - h / 2, i * h - h / 2
+    rhs = (1.0 / 16.0) * (-12.0 * np.sin(x) + 36.0 * np.sin(3 * x) - 10.0 * np.cos(y) - 45.0 * np.cos(3 * y)
+                          - 25.0 * np.cos(5 * y) + 16.0 * np.sin(z))
+    exact = np.sin(x) ** 3 + np.cos(y) ** 5 - np.sin(z)
+    ans = lapl_cube_periodic(rhs, h, h, h, 2 * np.pi, 2 * np.pi, 2 * np.pi)
+    ans = ans - ans.sum() / (n * n * n)
+    err = np.abs(ans - exact).max() / np.abs(exact).max()
+    assert err < 1e-2
 
 
 def test_periodic_lapl_cube_matches_reference(golden):
