@@ -197,6 +197,9 @@ class Reference:
         L.ref_nscubef_create.restype = c_void_p
         L.ref_nscubef_create.argtypes = [c_int, c_int] + [c_double] * 9
         L.ref_nscubef_step.argtypes = [c_void_p, c_int]
+        L.ref_config_get.argtypes = [ctypes.c_char_p, c_int, ctypes.POINTER(ctypes.c_char_p), ctypes.c_char_p,
+                                     ctypes.c_char_p, c_int, ctypes.c_char_p, _dp, ctypes.POINTER(c_int),
+                                     ctypes.c_char_p, c_int]
         L.ref_nscubef_get.restype = c_long
         L.ref_nscubef_get.argtypes = [c_void_p, c_int, _dp]
         L.ref_nscubef_destroy.argtypes = [c_void_p]
@@ -235,6 +238,18 @@ class Reference:
         S = np.zeros_like(a)
         self.L.ref_pfft3d_d(_p(S), _p(a), dx, a.shape[0], 1 if inverse else 0)
         return S
+
+    def config_get(self, path, argv, section: str, key: str, default):
+        """Config::open(path), rewrite(argv), get(section, key, default)
+        (src/config.cpp:78-150, 255-297) with the default's type."""
+        kind = 2 if isinstance(default, str) else 1 if isinstance(default, int) else 0
+        av = (ctypes.c_char_p * max(1, len(argv)))(*[a.encode() for a in argv])
+        d = np.zeros(1)
+        i = c_int(0)
+        buf = ctypes.create_string_buffer(4096)
+        self.L.ref_config_get(str(path).encode(), len(argv), av, section.encode(), key.encode(), kind,
+                              (default if kind == 2 else repr(default)).encode(), _p(d), ctypes.byref(i), buf, 4096)
+        return buf.value.decode() if kind == 2 else int(i.value) if kind == 1 else float(d[0])
 
     def lapl_cube_periodic(self, rhs, dx, dy, dz, lx, ly, lz) -> np.ndarray:
         nz, ny, nx = rhs.shape

@@ -16,6 +16,7 @@
 //   fdm::NSCube<T,false>                 src/ns_cube.h:14-92,    src/ns_cube.cpp:27-277
 #include <cmath>
 #include <cstdio>
+#include <cstdlib>
 #include <cstring>
 #include <string>
 #include <vector>
@@ -355,6 +356,28 @@ int ref_cyclic_reduction_d(double* d, double* e, double* f, double* b, int q, in
 
 int ref_thomas_d(double* b, double* lower, double* diag, double* upper, int n) {
     solve_tdiag_linear_my(b, lower, diag, upper, n);
+    return 0;
+}
+
+// Config (src/config.cpp:78-150, 255-297): load `path`, apply the argv
+// overrides, then read section:key with a default of the given kind
+// (0 double, 1 int, 2 string).  Checker for the Python Config mirror.
+extern "C" int ref_config_get(const char* path, int argc, const char** argv, const char* section, const char* key,
+                              int kind, const char* def, double* out_d, int* out_i, char* out_s, int out_len) {
+    Config c;
+    c.open(path);
+    std::vector<char*> av;
+    av.push_back((char*)"ref");
+    for (int i = 0; i < argc; i++) av.push_back((char*)argv[i]);
+    c.rewrite((int)av.size(), av.data());
+    if (kind == 0) {
+        *out_d = c.get(section, key, atof(def));
+    } else if (kind == 1) {
+        *out_i = c.get(section, key, atoi(def));
+    } else {
+        const std::string v = c.get(section, key, std::string(def));
+        snprintf(out_s, (size_t)out_len, "%s", v.c_str());
+    }
     return 0;
 }
 
