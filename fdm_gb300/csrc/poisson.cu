@@ -108,15 +108,15 @@ static void upload_plambda(DevBuf& buf, int n, double h) {
     FDM_CUDA(cudaMemcpy(buf.get(n * sizeof(T)), v.data(), n * sizeof(T), cudaMemcpyHostToDevice));
 }
 
-// streaming multiprocessors of the current device (cached per process)
+// streaming multiprocessors of the current device (cached per process;
+// the function-local static is initialised once, thread-safely)
 static int sm_count() {
-    static int sms = 0;
-    if (!sms) {
+    static const int sms = [] {
         int dev = 0, v = 0;
         FDM_CUDA(cudaGetDevice(&dev));
         FDM_CUDA(cudaDeviceGetAttribute(&v, cudaDevAttrMultiProcessorCount, dev));
-        sms = v > 0 ? v : 1;
-    }
+        return v > 0 ? v : 1;
+    }();
     return sms;
 }
 
@@ -176,11 +176,11 @@ static void launch_rg(const Tin* in, Tout* out, int nx, int ny, int nz, int nvol
         else if constexpr (rg_use_occ<T, AXIS, N>()) return k_sine_rg_occ<Tin, T, Tout, AXIS, MODE, N>;
         else return k_sine_rg<Tin, T, Tout, AXIS, MODE, N>;
     }();
-    static bool attr_set = false;
-    if (!attr_set) {
+    static const bool attr_set = [kern] {
         FDM_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
-        attr_set = true;
-    }
+        return true;
+    }();
+    (void)attr_set;
     unsigned gx;
     if (AXIS == 0) gx = (unsigned)((ny * (long long)nz + L - 1) / L);
     else gx = (unsigned)(nz * ((nx + L - 1) / L));
@@ -225,8 +225,7 @@ static void launch_tc_n(const float* in, float* out, const SineTcGeom& g, const 
                         cudaStream_t st) {
     using C = TcCfg<N>;
     const auto kern = tc_kernel<N, AXIS>();
-    static int grid_cap = 0;
-    if (!grid_cap) {
+    static const int grid_cap = [kern] {
         FDM_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, C::kSmem));
         FDM_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributePreferredSharedMemoryCarveout, 100));
         // resident CTAs per SM from the kernel's own registers and shared
@@ -242,8 +241,8 @@ static void launch_tc_n(const float* in, float* out, const SineTcGeom& g, const 
         const int regs_cta = ((fa.numRegs + 7) / 8 * 8) * kTcThreads;
         int per_sm = std::min(smem_sm / smem_cta, regs_sm / std::max(regs_cta, 1));
         per_sm = std::max(1, std::min(per_sm, 512 / N));
-        grid_cap = per_sm * sms;
-    }
+        return per_sm * sms;
+    }();
     // as many CTAs as the tiles need in the fewest rounds, spread evenly
     const long long tiles = (g.lines + C::M - 1) / C::M;
     const long long rounds = (tiles + grid_cap - 1) / grid_cap;
@@ -295,12 +294,12 @@ static void launch_sine(const Tin* in, Tout* out, int nx, int ny, int nz, int nv
     int Lshift = 0;
     while ((1 << Lshift) < L) Lshift++;
     const size_t smem = sine_smem_bytes<T>(tb.N, L);
-    static bool attr_set = false;
-    if (!attr_set) {
+    static const bool attr_set = [] {
         FDM_CUDA(cudaFuncSetAttribute(k_sine_pass<Tin, T, Tout, AXIS, MODE>,
                                       cudaFuncAttributeMaxDynamicSharedMemorySize, (int)(kSineSmemBudget + 1024)));
-        attr_set = true;
-    }
+        return true;
+    }();
+    (void)attr_set;
     unsigned gx;
     if (AXIS == 0) gx = (unsigned)((ny * (long long)nz + L - 1) / L);
     else gx = (unsigned)(nz * ((nx + L - 1) / L));
