@@ -68,6 +68,8 @@ _SIGS = [
     ("fdmgpu_lapl_cube_last_info", c_int, [c_void_p, POINTER(c_int), POINTER(c_double), c_int]),
     ("fdmgpu_lapl_cube_scratch_bytes", c_int, [c_void_p, POINTER(c_size_t)]),
     ("fdmgpu_lapl_cube_set_schedule", c_int, [c_void_p, c_int, c_int]),
+    ("fdmgpu_lapl_cube_set_pipeline", c_int, [c_void_p, c_int]),
+    ("fdmgpu_lapl_cube_pipeline_in_use", c_int, [c_void_p, POINTER(c_int)]),
     ("fdmgpu_lapl_cube_device_status", c_int, [c_void_p, POINTER(c_int)]),
     ("fdmgpu_lapl_cube_destroy", c_int, [c_void_p]),
     ("fdmgpu_batch_create", c_int,

@@ -19,6 +19,13 @@ void set_error(const char* fmt, ...) {
     va_end(ap);
 }
 
+int current_device() {
+    int dev = 0;
+    FDM_CUDA(cudaGetDevice(&dev));
+    if (dev < 0 || dev >= kMaxDevices) FDM_FAIL(FDMGPU_EINVAL, "device ordinal %d out of range", dev);
+    return dev;
+}
+
 // ---- launch accounting ---------------------------------------------------
 static std::atomic<unsigned long long> g_launches{0};
 static std::atomic<int> g_profile{0};

@@ -5,6 +5,7 @@
 
 #include <cstdarg>
 #include <cstdio>
+#include <mutex>
 #include <string>
 
 #include "../../include/fdmgpu.h"
@@ -50,6 +51,28 @@ struct LaunchTimer {
     ~LaunchTimer();
 };
 #define FDM_TIMED(name, st) ::fdmgpu::LaunchTimer fdm_timer_(name, st)
+
+// Largest device ordinal + 1 that per-device state is kept for.
+constexpr int kMaxDevices = 64;
+
+// The calling thread's current device, checked against kMaxDevices.
+int current_device();
+
+// A value computed once per device by the first caller on that device (with
+// the device current), e.g. a kernel's launch attributes, which are
+// per-device state, or a device property.  A failing initialiser throws and
+// leaves the slot to be tried again by the next caller.
+template <typename T>
+struct PerDevice {
+    std::once_flag once[kMaxDevices];
+    T val[kMaxDevices] = {};
+    template <typename F>
+    const T& get(F&& init) {
+        const int d = current_device();
+        std::call_once(once[d], [&] { val[d] = init(); });
+        return val[d];
+    }
+};
 
 // Device buffer that grows on demand and frees itself.
 struct DevBuf {

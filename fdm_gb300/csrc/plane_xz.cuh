@@ -1,0 +1,282 @@
+// One pass per y-mode plane of the mixed-precision Poisson pipeline: the
+// DST along x, the tridiagonal solve along z and the inverse DST along x.
+//
+// For y-mode ky of a batch of FP32 volumes (x fastest: rows of nx, planes of
+// nx*ny), the rows (z, ky), z = 0..nz-1, go through
+//   1. the DST along x of every row (the x-line transform of sine_rg.cuh),
+//   2. per x-mode i the Dirichlet tridiagonal system along z
+//          u[z-1] + b u[z] + u[z+1] = gs * g[z],  b = -2 - (lx_i + ly_ky) hz^2,
+//      which inverts what the reference does with DST_z, the division by
+//      -(lm_z + lm_y + lm_x) and the inverse DST_z (src/lapl_cube.cpp:13-30,
+//      :70-84, :124-141).  It is partitioned as k_zsolve_tab does it: P =
+//      (nz+1)/16 blocks of 15 rows and P-1 separator rows, every factor read
+//      from the per-mode table that the plan builds in FP64,
+//   3. the inverse DST along x, stored back in place;
+// one read and one write of the plane instead of three passes over the
+// volume (x, z, inverse x) with a write and a read between each.
+//
+// A 255 x 255 FP32 plane (254 KB) is larger than one CTA's shared memory, so
+// a cluster of C CTAs owns a plane: CTA r holds the L rows z = rL..rL+L-1
+// (L = the lines per CTA of the x-line transform; the last CTA has L-1
+// rows), which are the z blocks rB..rB+B-1 (B = L/16) with their separators.
+// Only the separator system crosses CTAs.  Each CTA publishes its blocks'
+// end values and its separators' right-hand sides in its own shared memory;
+// after a cluster barrier, CTA r solves the P-1 separator unknowns of its
+// share of the x-modes from those values (read from the peers' shared
+// memory) and writes each solution into the shared memory of the CTAs whose
+// blocks end on it; after a second barrier every CTA finishes its blocks
+// locally.  The cluster barriers are hardware barriers of co-scheduled CTAs;
+// no CTA leaves before the second one, so no peer memory is read after its
+// owner exits.
+#pragma once
+
+#include <cooperative_groups.h>
+
+#include "sine_rg.cuh"
+
+namespace fdmgpu {
+
+struct PlaneGeom {
+    int nx, ny, nz;
+    long long vstride;  // elements per volume
+    int modes;          // nx * ny: the z table's stride between values
+};
+
+template <int N>
+struct PlaneCfg {
+    using Gm = RgGeom<N, 0>;
+    static constexpr int L = Gm::L;      // rows per CTA
+    static constexpr int B = L / 16;     // z blocks per CTA
+    static constexpr int XS = 256;       // floats per x-mode array row (>= n)
+    static constexpr size_t smem() {
+        return (size_t)2 * L * Gm::LS2 * sizeof(float) + (size_t)(4 * B + 1) * XS * sizeof(float);
+    }
+};
+
+// W: the batch of volumes (in place), grid (C * ny, volumes), 256 threads, a
+// cluster of C CTAs along x.  gs: the forward x scale times the z-solve's
+// right-hand-side scale; sc_inv: the inverse x scale; tab: the per-mode z
+// factor table of k_zsolve_tab (block pivots, right-end responses,
+// separator pivots and multipliers, value-major over nx*ny modes).
+template <int N, int C, int MINB>
+__global__ void __launch_bounds__(256, MINB) k_plane_xz(float* __restrict__ W, PlaneGeom geo, SineTables<float> tb,
+                                                        float gs, float sc_inv, const float* __restrict__ tab) {
+    namespace cg = cooperative_groups;
+    using T2 = float2;
+    using Gm = RgGeom<N, 0>;
+    using Pc = PlaneCfg<N>;
+    constexpr int M = Gm::M, G = Gm::G, L = Gm::L, LS2 = Gm::LS2;
+    constexpr int n = N - 1, ITEMS = M + 1, nthr = L * G;
+    constexpr int m = 15, B = Pc::B, XS = Pc::XS;
+    constexpr int P = C * B;             // z blocks of the plane
+    constexpr int MPC = (n + C - 1) / C;  // x-modes whose separator system a CTA solves
+    static_assert(nthr == 256 && n < XS && MPC <= 256 && P <= 16, "plane layout");
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    T2* S = reinterpret_cast<T2*>(smem_raw);
+    float* Sr = reinterpret_cast<float*>(smem_raw);
+    float* xf = Sr + 2 * L * LS2;  // [B][XS] first value of each block's zero-end solution
+    float* xl = xf + B * XS;       // [B][XS] its last value
+    float* xg = xl + B * XS;       // [B][XS] separator right-hand sides (times gs)
+    float* xs = xg + B * XS;       // [B+1][XS] separator solutions s[rB-1 .. rB+B-1]
+
+    cg::cluster_group cl = cg::this_cluster();
+    const int r = (int)cl.block_rank();
+    const int ky = blockIdx.x / C;
+    const int nx = geo.nx, ny = geo.ny, nz = geo.nz;
+    const int tid = threadIdx.x, l = tid / G, g = tid % G;
+    const int z0 = r * L;
+    const int nact = min(L, nz - z0);
+    const long long rstride = (long long)ny * nx;  // between consecutive z rows
+    float* row0 = W + (long long)blockIdx.y * geo.vstride + ((long long)z0 * ny + ky) * nx;
+
+    // ---- 1. load + fold (item (line, j) reads x_j and x_{N-j}), DST along x
+    {
+        constexpr int total = L * ITEMS;
+        for (int e0 = tid; e0 < total; e0 += 4 * nthr) {
+            float av[4], bv[4];
+            int lv[4], jv[4];
+#pragma unroll
+            for (int q = 0; q < 4; q++) {
+                const int e = e0 + q * nthr;
+                const int line = e / ITEMS, j = e - line * ITEMS;
+                lv[q] = line;
+                jv[q] = j;
+                float a = 0.f, b = 0.f;
+                if (e < total && line < nact && j >= 1) {
+                    const float* p = row0 + line * rstride;
+                    a = p[j - 1];
+                    b = p[n - j];
+                }
+                av[q] = a;
+                bv[q] = b;
+            }
+#pragma unroll
+            for (int q = 0; q < 4; q++) {
+                const int e = e0 + q * nthr;
+                if (e < total) {
+                    const int j = jv[q];
+                    float* base = Sr + 2 * lv[q] * LS2;
+                    if (j == 0) {
+                        base[0] = 0.f;
+                    } else {
+                        const float w = ldg(tb.wpre + j);
+                        const float sm = w * (av[q] + bv[q]), df = 0.5f * (av[q] - bv[q]);
+                        base[j] = sm + df;
+                        if (j != M) base[N - j] = sm - df;
+                    }
+                }
+            }
+        }
+    }
+    __syncthreads();
+    rg_line_fft<float, N, 0>(S + l * LS2, g, tb);
+    __syncthreads();
+
+    // ---- 2. z blocks: thread t owns x-mode i = t+1 of every local block.
+    // Entry i of row q sits at Sr[2*(q*LS2 + sk(i>>1)) + (i&1)].
+    const int t = tid;
+    const bool mode_ok = t < n;
+    const int i = t + 1;
+    const int fo = 2 * sk(i >> 1) + (i & 1);
+    const int modes = geo.modes;
+    const int tmode = ky * nx + (mode_ok ? t : 0);
+    constexpr int RS = 2 * LS2;  // floats between rows
+    if (mode_ok) {
+        float cp[m];
+#pragma unroll
+        for (int k = 0; k < m; k++) cp[k] = tab[(size_t)k * modes + tmode];
+#pragma unroll
+        for (int b = 0; b < B; b++) {
+            const int gb = r * B + b;
+            float* col = Sr + fo + 16 * b * RS;
+            float v[m];
+#pragma unroll
+            for (int k = 0; k < m; k++) v[k] = col[k * RS];
+            float prev = 0.f;
+#pragma unroll
+            for (int k = 0; k < m; k++) {
+                prev = (v[k] * gs - prev) * cp[k];
+                v[k] = prev;
+            }
+#pragma unroll
+            for (int k = m - 2; k >= 0; k--) v[k] = v[k] - cp[k] * v[k + 1];
+#pragma unroll
+            for (int k = 0; k < m; k++) col[k * RS] = v[k];
+            xf[b * XS + t] = v[0];
+            xl[b * XS + t] = v[m - 1];
+            xg[b * XS + t] = gb < P - 1 ? col[m * RS] * gs : 0.f;
+        }
+    }
+    // the plane's outer ends: s[-1] = s[P-1] = 0
+    if (r == 0) xs[tid] = 0.f;
+    if (r == C - 1) xs[B * XS + tid] = 0.f;
+    cl.sync();
+
+    // ---- 3. separator systems of this CTA's x-modes
+    if (P > 1 && tid < MPC) {
+        const int tm = r * MPC + tid;
+        if (tm < n) {
+            const int mm = ky * nx + tm;
+            float d[P > 1 ? P - 1 : 1];
+#pragma unroll
+            for (int q = 0; q < P - 1; q++) {
+                // separator q lies between block q and block q + 1
+                const int c1 = q / B, b1 = q % B, c2 = (q + 1) / B, b2 = (q + 1) % B;
+                const float* g1 = cl.map_shared_rank(xg, c1);
+                const float* l1 = cl.map_shared_rank(xl, c1);
+                const float* f2 = cl.map_shared_rank(xf, c2);
+                d[q] = g1[b1 * XS + tm] - l1[b1 * XS + tm] - f2[b2 * XS + tm];
+            }
+            const float lo = tab[(size_t)m * modes + mm];
+            float acc = 0.f;
+#pragma unroll
+            for (int q = 0; q < P - 1; q++) {
+                acc = (d[q] - lo * acc) * tab[(size_t)(2 * m + q) * modes + mm];
+                d[q] = acc;
+            }
+            float u = 0.f;
+#pragma unroll
+            for (int q = P - 2; q >= 0; q--) {
+                u = d[q] - tab[(size_t)(2 * m + P - 1 + q) * modes + mm] * u;
+                d[q] = u;
+            }
+            // s[q] ends block q on the right and block q+1 on the left: slot
+            // q - (c B - 1) of xs in the CTA c that holds each of them
+#pragma unroll
+            for (int q = 0; q < P - 1; q++) {
+                const int c1 = q / B, c2 = (q + 1) / B;
+                cl.map_shared_rank(xs, c1)[(q - (c1 * B - 1)) * XS + tm] = d[q];
+                if (c2 != c1) cl.map_shared_rank(xs, c2)[(q - (c2 * B - 1)) * XS + tm] = d[q];
+            }
+        }
+    }
+    cl.sync();
+
+    // ---- 4. finish the blocks: u = v + beta_rev * s_left + beta * s_right
+    if (mode_ok) {
+        float be[m];
+#pragma unroll
+        for (int k = 0; k < m; k++) be[k] = tab[(size_t)(m + k) * modes + tmode];
+#pragma unroll
+        for (int b = 0; b < B; b++) {
+            const int gb = r * B + b;
+            const float ul = xs[b * XS + t], ur = xs[(b + 1) * XS + t];
+            float* col = Sr + fo + 16 * b * RS;
+#pragma unroll
+            for (int k = 0; k < m; k++) col[k * RS] = col[k * RS] + be[m - 1 - k] * ul + be[k] * ur;
+            if (gb < P - 1) col[m * RS] = ur;
+        }
+    }
+    __syncthreads();
+
+    // ---- 5. inverse DST along x: fold from the transform layout into the
+    // linear one (every read before any write: the two layouts overlap)
+    {
+        constexpr int total = L * ITEMS;
+        constexpr int PER = (total + nthr - 1) / nthr;
+        float av[PER], bv[PER];
+#pragma unroll
+        for (int q = 0; q < PER; q++) {
+            const int e = tid + q * nthr;
+            const int line = e / ITEMS, j = e - line * ITEMS;
+            float a = 0.f, b = 0.f;
+            if (e < total && j >= 1) {
+                const float* base = Sr + line * RS;
+                const int jm = N - j;
+                a = base[2 * sk(j >> 1) + (j & 1)];
+                b = base[2 * sk(jm >> 1) + (jm & 1)];
+            }
+            av[q] = a;
+            bv[q] = b;
+        }
+        __syncthreads();
+#pragma unroll
+        for (int q = 0; q < PER; q++) {
+            const int e = tid + q * nthr;
+            if (e < total) {
+                const int line = e / ITEMS, j = e - line * ITEMS;
+                float* base = Sr + line * RS;
+                if (j == 0) {
+                    base[0] = 0.f;
+                } else {
+                    const float w = ldg(tb.wpre + j);
+                    const float sm = w * (av[q] + bv[q]), df = 0.5f * (av[q] - bv[q]);
+                    base[j] = sm + df;
+                    if (j != M) base[N - j] = sm - df;
+                }
+            }
+        }
+    }
+    __syncthreads();
+    rg_line_fft<float, N, 0>(S + l * LS2, g, tb);
+    __syncthreads();
+
+    // ---- 6. store the rows
+    const int total = nact * n;
+    for (int e = tid; e < total; e += nthr) {
+        const int q = e / n, ii = e - q * n + 1;
+        row0[q * rstride + ii - 1] = sc_inv * Sr[q * RS + 2 * sk(ii >> 1) + (ii & 1)];
+    }
+}
+
+}  // namespace fdmgpu

@@ -25,6 +25,7 @@
 #include "sine.cuh"
 #include "sine_rg.cuh"
 #include "sine_tc.cuh"
+#include "plane_xz.cuh"
 #include "pfft.cuh"
 #include "solve_kernels.cuh"
 
@@ -108,16 +109,15 @@ static void upload_plambda(DevBuf& buf, int n, double h) {
     FDM_CUDA(cudaMemcpy(buf.get(n * sizeof(T)), v.data(), n * sizeof(T), cudaMemcpyHostToDevice));
 }
 
-// streaming multiprocessors of the current device (cached per process;
-// the function-local static is initialised once, thread-safely)
+// streaming multiprocessors of the current device (looked up once per
+// device)
 static int sm_count() {
-    static const int sms = [] {
-        int dev = 0, v = 0;
-        FDM_CUDA(cudaGetDevice(&dev));
-        FDM_CUDA(cudaDeviceGetAttribute(&v, cudaDevAttrMultiProcessorCount, dev));
+    static PerDevice<int> sms;
+    return sms.get([] {
+        int v = 0;
+        FDM_CUDA(cudaDeviceGetAttribute(&v, cudaDevAttrMultiProcessorCount, current_device()));
         return v > 0 ? v : 1;
-    }();
-    return sms;
+    });
 }
 
 template <typename T, bool INV>
@@ -157,7 +157,11 @@ static int pick_lines(int N) {
 
 template <typename Tin, typename T, typename Tout, int AXIS, int MODE>
 constexpr const char* sine_name() {
-    return AXIS == 1 ? (sizeof(T) == 8 ? "sine_y_f64" : "sine_y_f32")
+    return AXIS == 1 ? (MODE == kRound      ? "sine_y_round"
+                        : MODE == kCombine ? "sine_y_combine"
+                        : sizeof(T) == 8   ? "sine_y_f64"
+                        : sizeof(Tout) == 8 ? "sine_y_f32_out64"
+                                            : "sine_y_f32")
            : MODE == kRound    ? "sine_x_round"
            : MODE == kResidual ? "sine_x_resid"
            : MODE == kCombine  ? "sine_x_combine"
@@ -176,11 +180,11 @@ static void launch_rg(const Tin* in, Tout* out, int nx, int ny, int nz, int nvol
         else if constexpr (rg_use_occ<T, AXIS, N>()) return k_sine_rg_occ<Tin, T, Tout, AXIS, MODE, N>;
         else return k_sine_rg<Tin, T, Tout, AXIS, MODE, N>;
     }();
-    static const bool attr_set = [kern] {
+    static PerDevice<bool> attr_set;
+    attr_set.get([kern] {
         FDM_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
         return true;
-    }();
-    (void)attr_set;
+    });
     unsigned gx;
     if (AXIS == 0) gx = (unsigned)((ny * (long long)nz + L - 1) / L);
     else gx = (unsigned)(nz * ((nx + L - 1) / L));
@@ -225,13 +229,14 @@ static void launch_tc_n(const float* in, float* out, const SineTcGeom& g, const 
                         cudaStream_t st) {
     using C = TcCfg<N>;
     const auto kern = tc_kernel<N, AXIS>();
-    static const int grid_cap = [kern] {
+    static PerDevice<int> grid_caps;
+    const int grid_cap = grid_caps.get([kern] {
         FDM_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, C::kSmem));
         FDM_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributePreferredSharedMemoryCarveout, 100));
         // resident CTAs per SM from the kernel's own registers and shared
         // memory, and tensor memory (512 columns per SM across CTAs)
-        int dev = 0, sms = 0, smem_sm = 0, regs_sm = 0;
-        FDM_CUDA(cudaGetDevice(&dev));
+        const int dev = current_device();
+        int sms = 0, smem_sm = 0, regs_sm = 0;
         FDM_CUDA(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
         FDM_CUDA(cudaDeviceGetAttribute(&smem_sm, cudaDevAttrMaxSharedMemoryPerMultiprocessor, dev));
         FDM_CUDA(cudaDeviceGetAttribute(&regs_sm, cudaDevAttrMaxRegistersPerMultiprocessor, dev));
@@ -242,7 +247,7 @@ static void launch_tc_n(const float* in, float* out, const SineTcGeom& g, const 
         int per_sm = std::min(smem_sm / smem_cta, regs_sm / std::max(regs_cta, 1));
         per_sm = std::max(1, std::min(per_sm, 512 / N));
         return per_sm * sms;
-    }();
+    });
     // as many CTAs as the tiles need in the fewest rounds, spread evenly
     const long long tiles = (g.lines + C::M - 1) / C::M;
     const long long rounds = (tiles + grid_cap - 1) / grid_cap;
@@ -294,12 +299,12 @@ static void launch_sine(const Tin* in, Tout* out, int nx, int ny, int nz, int nv
     int Lshift = 0;
     while ((1 << Lshift) < L) Lshift++;
     const size_t smem = sine_smem_bytes<T>(tb.N, L);
-    static const bool attr_set = [] {
+    static PerDevice<bool> attr_set;
+    attr_set.get([] {
         FDM_CUDA(cudaFuncSetAttribute(k_sine_pass<Tin, T, Tout, AXIS, MODE>,
                                       cudaFuncAttributeMaxDynamicSharedMemorySize, (int)(kSineSmemBudget + 1024)));
         return true;
-    }();
-    (void)attr_set;
+    });
     unsigned gx;
     if (AXIS == 0) gx = (unsigned)((ny * (long long)nz + L - 1) / L);
     else gx = (unsigned)(nz * ((nx + L - 1) / L));
@@ -436,6 +441,88 @@ static void zsolve_tab_launch(T* W, int nx, int ny, int nz, int nvol, const T* t
     FDM_LAUNCH_CHECK();
 }
 
+// Fused plane pass (k_plane_xz): rows per CTA and cluster size for an
+// x-line of N points and nz rows; false when the plane does not split into
+// 1, 2, 4 or 8 CTAs of whole z blocks.
+static bool plane_split(int N, int nz, int* C) {
+    int L = 0;
+    switch (N) {
+        case 64: L = PlaneCfg<64>::L; break;
+        case 128: L = PlaneCfg<128>::L; break;
+        case 256: L = PlaneCfg<256>::L; break;
+        default: return false;
+    }
+    if ((nz + 1) % L != 0 || nz + 1 > 256) return false;  // at most 16 z blocks of 16 rows
+    const int c = (nz + 1) / L;
+    if (c != 1 && c != 2 && c != 4 && c != 8) return false;
+    *C = c;
+    return true;
+}
+
+template <int N, int C>
+static void launch_plane_n(float* W, const PlaneGeom& g, int nvol, const SineTables<float>& tb, float gs, float sci,
+                           const float* tab, cudaStream_t st) {
+  if constexpr (PlaneCfg<N>::B * C > 16) {
+    FDM_FAIL(FDMGPU_ESIZE, "plane pass: more than 16 z blocks");
+  } else {
+    // 4 CTAs of 256 threads per SM (64 registers) fit next to their shared
+    // memory (47 KB at N = 256)
+    const auto kern = k_plane_xz<N, C, 4>;
+    constexpr size_t smem = PlaneCfg<N>::smem();
+    static PerDevice<bool> attr_set;
+    attr_set.get([kern] {
+        FDM_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+        return true;
+    });
+    cudaLaunchConfig_t cfg = {};
+    cfg.gridDim = dim3((unsigned)(C * g.ny), (unsigned)nvol, 1);
+    cfg.blockDim = dim3(256, 1, 1);
+    cfg.dynamicSmemBytes = smem;
+    cfg.stream = st;
+    cudaLaunchAttribute at[1];
+    at[0].id = cudaLaunchAttributeClusterDimension;
+    at[0].val.clusterDim.x = C;
+    at[0].val.clusterDim.y = 1;
+    at[0].val.clusterDim.z = 1;
+    cfg.attrs = at;
+    cfg.numAttrs = 1;
+    FDM_TIMED("plane_xz_f32", st);
+    FDM_CUDA(cudaLaunchKernelEx(&cfg, kern, W, g, tb, gs, sci, tab));
+  }
+}
+
+template <int N>
+static void launch_plane_c(int C, float* W, const PlaneGeom& g, int nvol, const SineTables<float>& tb, float gs,
+                           float sci, const float* tab, cudaStream_t st) {
+    switch (C) {
+        case 1: return launch_plane_n<N, 1>(W, g, nvol, tb, gs, sci, tab, st);
+        case 2: return launch_plane_n<N, 2>(W, g, nvol, tb, gs, sci, tab, st);
+        case 4: return launch_plane_n<N, 4>(W, g, nvol, tb, gs, sci, tab, st);
+        case 8: return launch_plane_n<N, 8>(W, g, nvol, tb, gs, sci, tab, st);
+        default: FDM_FAIL(FDMGPU_ESIZE, "plane pass: cluster of %d CTAs", C);
+    }
+}
+
+// Forward DST along x, z solve and inverse DST along x of every y-mode plane
+// of nvol FP32 volumes in place (scales: fwd along x times gscale of the z
+// right-hand side, inv along x).
+static void launch_plane(float* W, int nx, int ny, int nz, int nvol, const SineTables<float>& tb, double fwd,
+                         double gscale, double inv, const float* tab, cudaStream_t st) {
+    int C = 0;
+    if (!plane_split(nx + 1, nz, &C)) FDM_FAIL(FDMGPU_ESIZE, "plane pass: unsupported %dx%d", nx, nz);
+    PlaneGeom g;
+    g.nx = nx; g.ny = ny; g.nz = nz;
+    g.vstride = (long long)nx * ny * nz;
+    g.modes = nx * ny;
+    const float gs = (float)(fwd * gscale), sci = (float)inv;
+    switch (nx + 1) {
+        case 64: return launch_plane_c<64>(C, W, g, nvol, tb, gs, sci, tab, st);
+        case 128: return launch_plane_c<128>(C, W, g, nvol, tb, gs, sci, tab, st);
+        case 256: return launch_plane_c<256>(C, W, g, nvol, tb, gs, sci, tab, st);
+        default: FDM_FAIL(FDMGPU_ESIZE, "plane pass: x line of %d points", nx + 1);
+    }
+}
+
 static std::vector<double> lambda_host(int n, double h) {
     std::vector<double> v(n);
     for (int j = 1; j <= n; j++) {
@@ -493,6 +580,8 @@ struct CubePlan {
     int zmode = 1;          // 1: table-driven z-solve when the line splits, 0: factors computed per solve
     int dst_tc = 0;         // bit 0 / bit 1: plain FP32 DST passes along x / y on the tensor cores (32-, 64-,
                             // 128-point axes)
+    int pipeline = 1;       // mixed form: 1 = DST-y, fused x-z plane pass, DST-y where the plane splits
+                            // (plane_split); 0 = the five passes x, y, z, y, x
     bool periodic = false;  // all three axes periodic (real FFTs, divide, inverse FFTs)
     bool mixed_ok = true;   // within the mixed solve's conditioning limit (kMixedKappaMax)
     DevBuf ptw_x, ptw_y, ptw_z, plam_x, plam_y, plam_z;
@@ -692,6 +781,25 @@ struct CubePlan {
                         zfac * hz_eff * hz_eff, st);
     }
 
+    // the FP32 z factor table (built on first use); false when the z line
+    // does not split into blocks
+    bool ztab32_ready() {
+        if (!ztab32.p && zm32 == 0) {
+            if (!zsolve_table_host<float>(ztab32, nx, ny, nz, lambda_host(nx, hx_eff), lambda_host(ny, dy),
+                                          hz_eff * hz_eff, &zm32, &zP32))
+                zm32 = -1;
+        }
+        return zm32 > 0;
+    }
+
+    // whether the mixed solve runs the three-pass pipeline with the fused
+    // x-z plane pass
+    bool plane_ok() {
+        int C = 0;
+        return pipeline == 1 && zmode == 1 && !(dst_tc & 1) && plane_split(nx + 1, nz, &C) && ztab32_ready() &&
+               zm32 == 15;
+    }
+
     void solve_device(void* ans, const void* rhs, int nrhs, cudaStream_t st) {
         check_grid_y(nrhs);
         last_stream = st;
@@ -735,9 +843,66 @@ struct CubePlan {
     // Mixed solve of nrhs volumes.  With vin / vout (device arrays of nrhs
     // user pointers) the FP64 input and output volumes are addressed through
     // them and rhs / ans are not used; the FP32 scratch stays contiguous.
+    // Mixed solve with the fused plane pass: per sweep DST-y, the x-z plane
+    // pass, inverse DST-y.  The x and y transforms commute, so this is the
+    // same operator as run_mixed's x, y, z, y, x order.
+    void run_mixed_planes(double* ans, const double* rhs, int nrhs, cudaStream_t st, const void* const* vin,
+                          void* const* vout) {
+        const long long V = vol() * nrhs;
+        const int sweeps = sweeps_for_tol();
+        last_sweeps = sweeps;
+        float* W = (float*)work32.get(V * sizeof(float));
+        const float* tab = (const float*)ztab32.p;
+        const double gscale = zfac * hz_eff * hz_eff;
+        SineFused fin;
+        memset(&fin, 0, sizeof(fin));
+        fin.vin = vin;
+        launch_sine<double, float, float, 1, kRound>(rhs, W, nx, ny, nz, nrhs, ty32.view(), scy, st, &fin);
+        launch_plane(W, nx, ny, nz, nrhs, tx32.view(), scx, gscale, slx, tab, st);
+        if (sweeps == 0) {
+            SineFused fo;
+            memset(&fo, 0, sizeof(fo));
+            fo.vout = vout;
+            launch_sine<float, float, double, 1>(W, ans, nx, ny, nz, nrhs, ty32.view(), sly, st, &fo);
+            return;
+        }
+        float* UH = (float*)uhi.get(V * sizeof(float));
+        float* UL = sweeps > 1 ? (float*)ulo.get(V * sizeof(float)) : nullptr;
+        double* NR = (double*)norms.get((size_t)2 * nrhs * sweeps * sizeof(double));
+        FDM_CUDA(cudaMemsetAsync(NR, 0, (size_t)2 * nrhs * sweeps * sizeof(double), st));
+        launch_sine<float, float, float, 1>(W, UH, nx, ny, nz, nrhs, ty32.view(), sly, st);
+        const double cx = 1.0 / (hx_eff * hx_eff) / S, cy = 1.0 / (dy * dy) / S, cz = 1.0 / (hz_eff * hz_eff) / S;
+        for (int s = 1; s <= sweeps; s++) {
+            SineFused fr;
+            memset(&fr, 0, sizeof(fr));
+            fr.f = rhs;
+            fr.vin = vin;
+            fr.uhi = UH;
+            fr.ulo = s >= 2 ? UL : nullptr;
+            fr.cx = split_host(cx); fr.cy = split_host(cy); fr.cz = split_host(cz);
+            fr.cxf = (float)cx; fr.cyf = (float)cy; fr.czf = (float)cz;
+            fr.iso = (cx == cy && cy == cz) ? 1 : 0;
+            launch_residual(fr, W, nx, ny, nz, nrhs, st);
+            launch_sine<float, float, float, 1>(W, W, nx, ny, nz, nrhs, ty32.view(), scy, st);
+            launch_plane(W, nx, ny, nz, nrhs, tx32.view(), scx, gscale, slx, tab, st);
+            SineFused fc;
+            memset(&fc, 0, sizeof(fc));
+            fc.uhi = UH;
+            fc.ulo = s >= 2 ? UL : nullptr;
+            fc.out64 = ans;
+            fc.vout = vout;
+            fc.ulo_out = UL;
+            fc.last = s == sweeps ? 1 : 0;
+            fc.norms = NR + (size_t)2 * nrhs * (s - 1);
+            launch_sine<float, float, float, 1, kCombine>(W, (float*)nullptr, nx, ny, nz, nrhs, ty32.view(), sly,
+                                                          st, &fc);
+        }
+    }
+
     void run_mixed(double* ans, const double* rhs, int nrhs, cudaStream_t st, const void* const* vin = nullptr,
                    void* const* vout = nullptr) {
         ensure_mixed_tables();
+        if (plane_ok()) return run_mixed_planes(ans, rhs, nrhs, st, vin, vout);
         const long long V = vol() * nrhs;
         const int sweeps = sweeps_for_tol();
         last_sweeps = sweeps;
@@ -1345,17 +1510,14 @@ namespace fdmgpu {
 // ---------------------------------------------------------------------------
 static __device__ __align__(256) unsigned char g_noalloc_scratch[FDMGPU_NOALLOC_SCRATCH_BYTES];
 
-constexpr int kNoallocMaxDevices = 64;
 static std::mutex g_noalloc_mu;
-static void* g_noalloc_ptr[kNoallocMaxDevices];
+static void* g_noalloc_ptr[kMaxDevices];
 
 // Device address of the array on the current device.  The first call on a
 // device looks it up with cudaGetSymbolAddress (which also loads the module
 // there); later calls reuse the address.
 static unsigned char* noalloc_scratch() {
-    int dev = 0;
-    FDM_CUDA(cudaGetDevice(&dev));
-    if (dev < 0 || dev >= kNoallocMaxDevices) FDM_FAIL(FDMGPU_EINVAL, "device ordinal %d out of range", dev);
+    const int dev = current_device();
     std::lock_guard<std::mutex> lk(g_noalloc_mu);
     if (!g_noalloc_ptr[dev]) {
         void* p = nullptr;
@@ -1384,6 +1546,53 @@ __global__ void k_noalloc_tables(float2* tw, float2* post, float* wpre, float* l
         const double sv = sinpi((i + 1) * 0.5 / (n + 1));
         lam[i] = (float)(4.0 / (h * h) * (sv * sv));
     }
+}
+
+// Per-mode factors of the partitioned z-solve, the table zsolve_table_host
+// builds for a handle (layout of k_zsolve_tab: block pivot reciprocals,
+// right-end responses, separator pivot reciprocals and multipliers, value
+// major), computed here on the device in FP64 and stored in FP32.  The
+// eigenvalues are 4/h^2 sin^2(j pi / (2(n+1))) of x (spacing hx) and y
+// (spacing hy); h2 is the z spacing squared.  Products and sums are rounded
+// one by one (no contraction), as the host computes them.
+__global__ void k_noalloc_ztable(float* tab, int nx, int ny, int m, int P, double hx, double hy, double h2) {
+    const int modes = nx * ny;
+    const int mode = blockIdx.x * blockDim.x + threadIdx.x;
+    if (mode >= modes) return;
+    const int j = mode % nx, k = mode / nx;
+    const double sx = sinpi((j + 1) * 0.5 / (nx + 1)), sy = sinpi((k + 1) * 0.5 / (ny + 1));
+    const double lx = __dmul_rn(4. / (hx * hx), __dmul_rn(sx, sx));
+    const double ly = __dmul_rn(4. / (hy * hy), __dmul_rn(sy, sy));
+    const double b = __dsub_rn(-2.0, __dmul_rn(__dadd_rn(lx, ly), h2));
+    double cp[15], be[15];
+    double c = 0.0;
+    for (int i = 0; i < m; i++) {
+        c = 1.0 / __dsub_rn(b, c);
+        cp[i] = c;
+    }
+    be[m - 1] = -cp[m - 1];
+    for (int i = m - 2; i >= 0; i--) be[i] = __dmul_rn(-cp[i], be[i + 1]);
+    for (int i = 0; i < m; i++) {
+        tab[(size_t)i * modes + mode] = (float)cp[i];
+        tab[(size_t)(m + i) * modes + mode] = (float)be[i];
+    }
+    const double lo = be[0], dg = __dadd_rn(b, __dmul_rn(2.0, be[m - 1]));
+    double pc = 0.0;
+    for (int q = 0; q < P - 1; q++) {
+        const double r = 1.0 / __dsub_rn(dg, __dmul_rn(lo, pc));
+        pc = __dmul_rn(lo, r);
+        tab[(size_t)(2 * m + q) * modes + mode] = (float)r;
+        tab[(size_t)(2 * m + P - 1 + q) * modes + mode] = (float)pc;
+    }
+}
+
+// Block length m and block count P of the table-driven z-solve for nz rows
+// (the split zsolve_table_host uses); false when the line does not split
+// into at most 16 blocks of 2^k - 1 rows.
+static bool ztable_split(int nz, int* m, int* P) {
+    *m = nz < 15 ? nz : 15;
+    *P = (nz + 1) / (*m + 1);
+    return (*m + 1) * *P == nz + 1 && *P <= 16;
 }
 
 struct NoallocAxis {
@@ -1425,7 +1634,12 @@ static void noalloc_solve(double dx, double dy, double dz, double lx, double ly,
                  nx, ny, nz, lapl_kappa(nx, ny, nz, hx_eff, dy, hz_eff), kMixedKappaMax);
 
     const long long V = (long long)nx * ny * nz * nrhs;
-    const size_t need = noalloc_axis_bytes(nx + 1) + noalloc_axis_bytes(ny + 1) +
+    // the per-mode z factor table of a handle's mixed plan, when the line
+    // splits (otherwise both solve with factors computed per solve)
+    int zm = 0, zP = 0;
+    const bool ztab = ztable_split(nz, &zm, &zP);
+    const size_t tab_bytes = ztab ? noalloc_align((size_t)(2 * zm + 2 * (zP - 1)) * nx * ny * sizeof(float)) : 0;
+    const size_t need = noalloc_axis_bytes(nx + 1) + noalloc_axis_bytes(ny + 1) + tab_bytes +
                         noalloc_align((size_t)2 * nrhs * (sweeps > 0 ? sweeps : 1) * sizeof(double)) +
                         noalloc_align((size_t)V * sizeof(float)) * (sweeps == 0 ? 1 : (sweeps > 1 ? 3 : 2));
     if (need > (size_t)FDMGPU_NOALLOC_SCRATCH_BYTES)
@@ -1436,6 +1650,8 @@ static void noalloc_solve(double dx, double dy, double dz, double lx, double ly,
     unsigned char* p = noalloc_scratch();
     NoallocAxis ax = noalloc_axis(p, nx + 1);
     NoallocAxis ay = noalloc_axis(p, ny + 1);
+    float* ZT = ztab ? (float*)p : nullptr;
+    p += tab_bytes;
     double* NR = (double*)p;
     p += noalloc_align((size_t)2 * nrhs * (sweeps > 0 ? sweeps : 1) * sizeof(double));
     float* W = (float*)p;
@@ -1454,6 +1670,11 @@ static void noalloc_solve(double dx, double dy, double dz, double lx, double ly,
         k_noalloc_tables<<<(ny + 1 + 255) / 256, 256, 0, st>>>(ay.tw, ay.post, ay.wpre, ay.lam, ny + 1, dy);
         FDM_LAUNCH_CHECK();
     }
+    if (ztab) {
+        FDM_TIMED("noalloc_tables", st);
+        k_noalloc_ztable<<<(nx * ny + 127) / 128, 128, 0, st>>>(ZT, nx, ny, zm, zP, hx_eff, dy, hz_eff * hz_eff);
+        FDM_LAUNCH_CHECK();
+    }
     auto view = [](const NoallocAxis& a, int N) {
         SineTables<float> v;
         v.tw = a.tw; v.post = a.post; v.wpre = a.wpre; v.N = N; v.M = N / 2;
@@ -1461,10 +1682,14 @@ static void noalloc_solve(double dx, double dy, double dz, double lx, double ly,
     };
     const SineTables<float> tx = view(ax, nx + 1), ty = view(ay, ny + 1);
     const double h2 = hz_eff * hz_eff, gscale = zfac * hz_eff * hz_eff;
+    auto zsolve = [&](float* w) {
+        if (ztab) zsolve_tab_launch<float>(w, nx, ny, nz, nrhs, ZT, zm, zP, gscale, st);
+        else zsolve_lines<float>(w, nx, ny, nz, nrhs, ax.lam, ay.lam, h2, gscale, st);
+    };
 
     launch_sine<double, float, float, 0, kRound>(rhs, W, nx, ny, nz, nrhs, tx, scx, st);
     launch_sine<float, float, float, 1>(W, W, nx, ny, nz, nrhs, ty, scy, st);
-    zsolve_lines<float>(W, nx, ny, nz, nrhs, ax.lam, ay.lam, h2, gscale, st);
+    zsolve(W);
     launch_sine<float, float, float, 1>(W, W, nx, ny, nz, nrhs, ty, sly, st);
     if (sweeps == 0) {
         launch_sine<float, float, double, 0>(W, ans, nx, ny, nz, nrhs, tx, slx, st);
@@ -1487,7 +1712,7 @@ static void noalloc_solve(double dx, double dy, double dz, double lx, double ly,
         launch_residual(fr, W, nx, ny, nz, nrhs, st);
         launch_sine<float, float, float, 0>(W, W, nx, ny, nz, nrhs, tx, scx, st);
         launch_sine<float, float, float, 1>(W, W, nx, ny, nz, nrhs, ty, scy, st);
-        zsolve_lines<float>(W, nx, ny, nz, nrhs, ax.lam, ay.lam, h2, gscale, st);
+        zsolve(W);
         launch_sine<float, float, float, 1>(W, W, nx, ny, nz, nrhs, ty, sly, st);
         SineFused fc;
         memset(&fc, 0, sizeof(fc));
@@ -1980,6 +2205,25 @@ int fdmgpu_lapl_cube_set_schedule(fdmgpu_lapl_cube* h, int ztable, int dst_tc) {
     if ((ztable != 0 && ztable != 1) || dst_tc < 0 || dst_tc > 3) FDM_FAIL(FDMGPU_EINVAL, "ztable 0/1, dst_tc 0..3");
     h->plan.zmode = ztable;
     h->plan.dst_tc = dst_tc;
+    FDM_API_END
+}
+
+int fdmgpu_lapl_cube_set_pipeline(fdmgpu_lapl_cube* h, int pipeline) {
+    FDM_API_BEGIN
+    if (!h) FDM_FAIL(FDMGPU_EINVAL, "null handle");
+    if (pipeline != FDMGPU_PIPE_FIVE_PASS && pipeline != FDMGPU_PIPE_PLANES)
+        FDM_FAIL(FDMGPU_EINVAL, "pipeline must be FDMGPU_PIPE_FIVE_PASS or FDMGPU_PIPE_PLANES");
+    h->plan.pipeline = pipeline;
+    FDM_API_END
+}
+
+int fdmgpu_lapl_cube_pipeline_in_use(fdmgpu_lapl_cube* h, int* pipeline) {
+    FDM_API_BEGIN
+    if (!h || !pipeline) FDM_FAIL(FDMGPU_EINVAL, "null argument");
+    CubePlan& p = h->plan;
+    *pipeline = (!p.periodic && p.dtype == FDMGPU_F64 && p.precision == FDMGPU_MIXED && p.mixed_ok && p.plane_ok())
+                    ? FDMGPU_PIPE_PLANES
+                    : FDMGPU_PIPE_FIVE_PASS;
     FDM_API_END
 }
 

@@ -115,116 +115,16 @@ __device__ __forceinline__ void dft_reg(vec2_t<T>* v) {
 // skewed slot of entry k of C / the packed output: one pad slot per 16
 __device__ __forceinline__ int sk(int k) { return k + (k >> 4); }
 
-template <typename Tin, typename T, typename Tout, int AXIS, int MODE, int N>
-__device__ __forceinline__ void sine_rg_body(const Tin* in, Tout* out, const SineGeom& geo, const SineTables<T>& tb,
-                                             T scale, const SineFused& fu) {
+// The transform of one line held in its slots Ls (AXIS's layout): on entry
+// the folded values y_0..y_{N-1} as M complex slots c_m = (y_{2m}, y_{2m+1}),
+// on exit the unscaled F_1..F_n with entry i as component i&1 of slot
+// sk(i>>1).  Called by the G threads of the line (g = 0..G-1), which must
+// belong to one warp; the phases inside need only warp synchronisation.
+template <typename T, int N, int AXIS>
+__device__ __forceinline__ void rg_line_fft(vec2_t<T>* Ls, int g, const SineTables<T>& tb) {
     using T2 = vec2_t<T>;
     using Gm = RgGeom<N, AXIS>;
-    constexpr int M = Gm::M, R1 = Gm::R1, R2 = Gm::R2, G = Gm::G, L = Gm::L, D2 = Gm::D2, E = Gm::E;
-    constexpr int LS2 = Gm::LS2;
-    constexpr int n = N - 1;
-    constexpr int ITEMS = M + 1;  // fold items per line: j = 0..M
-    extern __shared__ __align__(16) unsigned char smem_raw[];
-    T2* S = reinterpret_cast<T2*>(smem_raw);
-    T* Sr = reinterpret_cast<T*>(smem_raw);
-    const int nx = geo.nx, ny = geo.ny, nz = geo.nz;
-    const int tid = threadIdx.x;
-    constexpr int nthr = L * G;
-    const int l = tid / G, g = tid % G;
-    const long long voff = (long long)blockIdx.y * geo.vstride;
-
-    int row0 = 0, nact, x0 = 0, z = 0;
-    if (AXIS == 0) {
-        row0 = blockIdx.x * L;
-        nact = min(L, ny * nz - row0);
-    } else {
-        const int ntx = (nx + L - 1) / L;
-        z = blockIdx.x / ntx;
-        x0 = (blockIdx.x - z * ntx) * L;
-        nact = min(L, nx - x0);
-    }
-
-    // ---- load + fold: item (line, j) reads x_j and x_{N-j} and writes
-    // y_j = w_j (a+b) + (a-b)/2 and y_{N-j} = w_j (a+b) - (a-b)/2
-    {
-        const T half = T(0.5);
-        constexpr int total = L * ITEMS;
-        for (int e0 = tid; e0 < total; e0 += 4 * nthr) {
-            T av[4], bv[4];
-            int lv[4], jv[4];
-#pragma unroll
-            for (int q = 0; q < 4; q++) {
-                const int e = e0 + q * nthr;
-                int line, j;
-                if (AXIS == 0) {
-                    line = e / ITEMS;
-                    j = e - line * ITEMS;
-                } else {
-                    j = e / L;
-                    line = e - j * L;
-                }
-                lv[q] = line;
-                jv[q] = j;
-                T a = T(0), b = T(0);
-                if (e < total && line < nact && j >= 1) {
-                    if (AXIS == 0) {
-                        const int R = row0 + line;
-                        if (MODE == kResidual) {
-                            const int zz = geo.div_ny.div(R), yy = R - zz * ny;
-                            SineFused f2 = fu;
-                            f2.f = fu.vin ? (const double*)fu.vin[blockIdx.y] : fu.f + voff;
-                            f2.uhi += voff;
-                            if (f2.ulo) f2.ulo += voff;
-                            const long long rb = (long long)R * n;
-                            a = T(residual_at(f2, rb + j - 1, j - 1, yy, zz, nx, ny, nz));
-                            b = T(residual_at(f2, rb + n - j, n - j, yy, zz, nx, ny, nz));
-                        } else {
-                            const Tin* p = (fu.vin ? (const Tin*)fu.vin[blockIdx.y] : in + voff) + (long long)R * n;
-                            if (MODE == kRound) {
-                                a = T(f64_to_f32((double)p[j - 1]));
-                                b = T(f64_to_f32((double)p[n - j]));
-                            } else {
-                                a = T(p[j - 1]);
-                                b = T(p[n - j]);
-                            }
-                        }
-                    } else {
-                        const Tin* p = (fu.vin ? (const Tin*)fu.vin[blockIdx.y] : in + voff) + ((long long)z * ny) * nx + x0 +
-                                       line;
-                        if (MODE == kRound) {
-                            a = T(f64_to_f32((double)p[(long long)(j - 1) * nx]));
-                            b = T(f64_to_f32((double)p[(long long)(n - j) * nx]));
-                        } else {
-                            a = T(p[(long long)(j - 1) * nx]);
-                            b = T(p[(long long)(n - j) * nx]);
-                        }
-                    }
-                }
-                av[q] = a;
-                bv[q] = b;
-            }
-#pragma unroll
-            for (int q = 0; q < 4; q++) {
-                const int e = e0 + q * nthr;
-                if (e < total) {
-                    const int line = lv[q], j = jv[q];
-                    T* base = Sr + 2 * (size_t)line * LS2;
-                    if (j == 0) {
-                        base[0] = T(0);
-                    } else {
-                        const T w = ldg(tb.wpre + j);
-                        const T sm = w * (av[q] + bv[q]), df = half * (av[q] - bv[q]);
-                        base[j] = sm + df;
-                        if (j != M) base[N - j] = sm - df;
-                    }
-                }
-            }
-        }
-    }
-    __syncthreads();
-
-    T2* Ls = S + (size_t)l * LS2;  // this line's slots
-
+    constexpr int M = Gm::M, R1 = Gm::R1, R2 = Gm::R2, G = Gm::G, D2 = Gm::D2, E = Gm::E;
     // ---- pass 1: DFT_R1 + twiddle
     T2 v[R1];
 #pragma unroll
@@ -332,82 +232,196 @@ __device__ __forceinline__ void sine_rg_body(const Tin* in, Tout* out, const Sin
         fm.y = s1 + rmid;
         Ls[sk(M / 2)] = fm;
     }
-    __syncthreads();
+}
 
-    // ---- store phase: entry i of line l is component i&1 of slot sk(i>>1)
+template <typename Tin, typename T, typename Tout, int AXIS, int MODE, int N>
+__device__ __forceinline__ void sine_rg_body(const Tin* in, Tout* out, const SineGeom& geo, const SineTables<T>& tb,
+                                             T scale, const SineFused& fu) {
+    using T2 = vec2_t<T>;
+    using Gm = RgGeom<N, AXIS>;
+    constexpr int M = Gm::M, G = Gm::G, L = Gm::L;
+    constexpr int LS2 = Gm::LS2;
+    constexpr int n = N - 1;
+    constexpr int ITEMS = M + 1;  // fold items per line: j = 0..M
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    T2* S = reinterpret_cast<T2*>(smem_raw);
+    T* Sr = reinterpret_cast<T*>(smem_raw);
+    const int nx = geo.nx, ny = geo.ny, nz = geo.nz;
+    const int tid = threadIdx.x;
+    constexpr int nthr = L * G;
+    const int l = tid / G, g = tid % G;
+    const long long voff = (long long)blockIdx.y * geo.vstride;
+
+    int row0 = 0, nact, x0 = 0, z = 0;
     if (AXIS == 0) {
-        const int total = nact * n;
-        const long long base = voff + (long long)row0 * n;
-        if (MODE == kCombine) {
-            float cc = 0.f, uu = 0.f;
-            // batches of 4 elements per thread: the uhi / ulo loads of a
-            // batch are issued before any of them is used
-            for (int e0 = tid; e0 < total; e0 += 4 * nthr) {
-                float hv[4], lv[4];
+        row0 = blockIdx.x * L;
+        nact = min(L, ny * nz - row0);
+    } else {
+        const int ntx = (nx + L - 1) / L;
+        z = blockIdx.x / ntx;
+        x0 = (blockIdx.x - z * ntx) * L;
+        nact = min(L, nx - x0);
+    }
+
+    // ---- load + fold: item (line, j) reads x_j and x_{N-j} and writes
+    // y_j = w_j (a+b) + (a-b)/2 and y_{N-j} = w_j (a+b) - (a-b)/2
+    {
+        const T half = T(0.5);
+        constexpr int total = L * ITEMS;
+        for (int e0 = tid; e0 < total; e0 += 4 * nthr) {
+            T av[4], bv[4];
+            int lv[4], jv[4];
 #pragma unroll
-                for (int q = 0; q < 4; q++) {
-                    const int e = e0 + q * nthr;
-                    hv[q] = 0.f;
-                    lv[q] = 0.f;
-                    if (e < total) {
-                        hv[q] = fu.uhi[base + e];
-                        if (fu.ulo) lv[q] = fu.ulo[base + e];
+            for (int q = 0; q < 4; q++) {
+                const int e = e0 + q * nthr;
+                int line, j;
+                if (AXIS == 0) {
+                    line = e / ITEMS;
+                    j = e - line * ITEMS;
+                } else {
+                    j = e / L;
+                    line = e - j * L;
+                }
+                lv[q] = line;
+                jv[q] = j;
+                T a = T(0), b = T(0);
+                if (e < total && line < nact && j >= 1) {
+                    if (AXIS == 0) {
+                        const int R = row0 + line;
+                        if (MODE == kResidual) {
+                            const int zz = geo.div_ny.div(R), yy = R - zz * ny;
+                            SineFused f2 = fu;
+                            f2.f = fu.vin ? (const double*)fu.vin[blockIdx.y] : fu.f + voff;
+                            f2.uhi += voff;
+                            if (f2.ulo) f2.ulo += voff;
+                            const long long rb = (long long)R * n;
+                            a = T(residual_at(f2, rb + j - 1, j - 1, yy, zz, nx, ny, nz));
+                            b = T(residual_at(f2, rb + n - j, n - j, yy, zz, nx, ny, nz));
+                        } else {
+                            const Tin* p = (fu.vin ? (const Tin*)fu.vin[blockIdx.y] : in + voff) + (long long)R * n;
+                            if (MODE == kRound) {
+                                a = T(f64_to_f32((double)p[j - 1]));
+                                b = T(f64_to_f32((double)p[n - j]));
+                            } else {
+                                a = T(p[j - 1]);
+                                b = T(p[n - j]);
+                            }
+                        }
+                    } else {
+                        const Tin* p = (fu.vin ? (const Tin*)fu.vin[blockIdx.y] : in + voff) + ((long long)z * ny) * nx + x0 +
+                                       line;
+                        if (MODE == kRound) {
+                            a = T(f64_to_f32((double)p[(long long)(j - 1) * nx]));
+                            b = T(f64_to_f32((double)p[(long long)(n - j) * nx]));
+                        } else {
+                            a = T(p[(long long)(j - 1) * nx]);
+                            b = T(p[(long long)(n - j) * nx]);
+                        }
                     }
                 }
+                av[q] = a;
+                bv[q] = b;
+            }
 #pragma unroll
-                for (int q = 0; q < 4; q++) {
-                    const int e = e0 + q * nthr;
-                    if (e < total) {
-                        const int r = e / n, i = e - r * n + 1;
-                        const float cv = (float)(scale * Sr[2 * ((size_t)r * LS2 + sk(i >> 1)) + (i & 1)]);
-                        const long long idx = base + e;
-                        ff s2 = two_sum(hv[q], lv[q]);
-                        s2 = ff_add_f(s2, cv);
-                        if (fu.last) {
-                            double* o64 = fu.vout ? (double*)fu.vout[blockIdx.y] : fu.out64 + voff;
-                            o64[idx - voff] = ff_to_f64(s2);
-                        }
-                        else fu.ulo_out[idx] = lv[q] + cv;
-                        cc += cv * cv;
-                        uu += s2.h * s2.h;
+            for (int q = 0; q < 4; q++) {
+                const int e = e0 + q * nthr;
+                if (e < total) {
+                    const int line = lv[q], j = jv[q];
+                    T* base = Sr + 2 * (size_t)line * LS2;
+                    if (j == 0) {
+                        base[0] = T(0);
+                    } else {
+                        const T w = ldg(tb.wpre + j);
+                        const T sm = w * (av[q] + bv[q]), df = half * (av[q] - bv[q]);
+                        base[j] = sm + df;
+                        if (j != M) base[N - j] = sm - df;
                     }
                 }
             }
+        }
+    }
+    __syncthreads();
+
+    rg_line_fft<T, N, AXIS>(S + (size_t)l * LS2, g, tb);
+    __syncthreads();
+
+    // ---- store phase: entry i of line l is component i&1 of slot sk(i>>1).
+    // Element e of the CTA's output goes to point idx of the volume (x
+    // fastest); so is its offset in shared memory.
+    const int total = AXIS == 0 ? nact * n : n * L;
+    auto locate = [&](int e, long long& idx, int& so) -> bool {
+        if (AXIS == 0) {
+            const int r = e / n, i = e - r * n + 1;
+            idx = (long long)row0 * n + e;
+            so = 2 * (r * LS2 + sk(i >> 1)) + (i & 1);
+            return e < total;
+        } else {
+            const int y = e / L, c = e - y * L, i = y + 1;
+            idx = ((long long)z * ny + y) * nx + x0 + c;
+            so = 2 * (c * LS2 + sk(i >> 1)) + (i & 1);
+            return e < total && c < nact;
+        }
+    };
+    if (MODE == kCombine) {
+        float cc = 0.f, uu = 0.f;
+        double* o64 = fu.vout ? (double*)fu.vout[blockIdx.y] : fu.out64 + voff;
+        // batches of 4 elements per thread: the uhi / ulo loads of a batch
+        // are issued before any of them is used
+        for (int e0 = tid; e0 < total; e0 += 4 * nthr) {
+            float hv[4], lv[4];
+            long long ix[4];
+            int so[4];
+            bool ok[4];
+#pragma unroll
+            for (int q = 0; q < 4; q++) {
+                ok[q] = locate(e0 + q * nthr, ix[q], so[q]);
+                hv[q] = 0.f;
+                lv[q] = 0.f;
+                if (ok[q]) {
+                    hv[q] = fu.uhi[voff + ix[q]];
+                    if (fu.ulo) lv[q] = fu.ulo[voff + ix[q]];
+                }
+            }
+#pragma unroll
+            for (int q = 0; q < 4; q++) {
+                if (ok[q]) {
+                    const float cv = (float)(scale * Sr[so[q]]);
+                    ff s2 = two_sum(hv[q], lv[q]);
+                    s2 = ff_add_f(s2, cv);
+                    if (fu.last) o64[ix[q]] = ff_to_f64(s2);
+                    else fu.ulo_out[voff + ix[q]] = lv[q] + cv;
+                    cc += cv * cv;
+                    uu += s2.h * s2.h;
+                }
+            }
+        }
+        for (int o = 16; o > 0; o >>= 1) {
+            cc += __shfl_down_sync(0xffffffffu, cc, o);
+            uu += __shfl_down_sync(0xffffffffu, uu, o);
+        }
+        __shared__ float red[2][32];
+        const int w = tid >> 5, ln = tid & 31;
+        if (ln == 0) { red[0][w] = cc; red[1][w] = uu; }
+        __syncthreads();
+        if (w == 0) {
+            constexpr int nw = nthr >> 5;
+            cc = ln < nw ? red[0][ln] : 0.f;
+            uu = ln < nw ? red[1][ln] : 0.f;
             for (int o = 16; o > 0; o >>= 1) {
                 cc += __shfl_down_sync(0xffffffffu, cc, o);
                 uu += __shfl_down_sync(0xffffffffu, uu, o);
             }
-            __shared__ float red[2][32];
-            const int w = tid >> 5, ln = tid & 31;
-            if (ln == 0) { red[0][w] = cc; red[1][w] = uu; }
-            __syncthreads();
-            if (w == 0) {
-                constexpr int nw = nthr >> 5;
-                cc = ln < nw ? red[0][ln] : 0.f;
-                uu = ln < nw ? red[1][ln] : 0.f;
-                for (int o = 16; o > 0; o >>= 1) {
-                    cc += __shfl_down_sync(0xffffffffu, cc, o);
-                    uu += __shfl_down_sync(0xffffffffu, uu, o);
-                }
-                if (ln == 0 && fu.norms) {
-                    atomicAdd(&fu.norms[2 * blockIdx.y], (double)cc);
-                    atomicAdd(&fu.norms[2 * blockIdx.y + 1], (double)uu);
-                }
-            }
-        } else {
-            Tout* ob = (fu.vout ? (Tout*)fu.vout[blockIdx.y] : out + voff) + (long long)row0 * n;
-            for (int e = tid; e < total; e += nthr) {
-                const int r = e / n, i = e - r * n + 1;
-                ob[e] = Tout(scale * Sr[2 * ((size_t)r * LS2 + sk(i >> 1)) + (i & 1)]);
+            if (ln == 0 && fu.norms) {
+                atomicAdd(&fu.norms[2 * blockIdx.y], (double)cc);
+                atomicAdd(&fu.norms[2 * blockIdx.y + 1], (double)uu);
             }
         }
     } else {
-        const int total = n * L;
-        const long long base = voff + ((long long)z * ny) * nx + x0;
+        Tout* ob = fu.vout ? (Tout*)fu.vout[blockIdx.y] : out + voff;
         for (int e = tid; e < total; e += nthr) {
-            const int y = e / L, c = e - y * L, i = y + 1;
-            if (c < nact)
-                out[base + (long long)y * nx + c] = Tout(scale * Sr[2 * ((size_t)c * LS2 + sk(i >> 1)) + (i & 1)]);
+            long long idx;
+            int so;
+            if (locate(e, idx, so)) ob[idx] = Tout(scale * Sr[so]);
         }
     }
 }

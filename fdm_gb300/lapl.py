@@ -121,6 +121,18 @@ class LaplCube:
         mask = 3 if dst_tc is True else int(dst_tc)
         N.check(self._lib.fdmgpu_lapl_cube_set_schedule(self._h, int(bool(ztable)), mask))
 
+    def set_pipeline(self, planes: bool = True) -> None:
+        """Mixed-form pass structure: the fused x-z plane pass between two
+        DSTs along y (default, where the sizes allow it) or the five passes
+        x, y, z, y, x."""
+        N.check(self._lib.fdmgpu_lapl_cube_set_pipeline(self._h, 1 if planes else 0))
+
+    def pipeline_in_use(self) -> str:
+        """'planes' or 'five_pass': what a solve of this handle runs."""
+        p = c_int()
+        N.check(self._lib.fdmgpu_lapl_cube_pipeline_in_use(self._h, byref(p)))
+        return "planes" if p.value == 1 else "five_pass"
+
     def device_failed(self) -> bool:
         """True if a tensor-core pass of this solver gave up waiting for its
         MMAs (synchronises the device)."""

@@ -91,3 +91,19 @@ def random_sizes(count: int, seed: int, choices=(31, 63, 127)):
     """count (nx, ny, nz) triples drawn independently from choices."""
     rng = np.random.default_rng(seed)
     return [tuple(int(c) for c in rng.choice(choices, size=3)) for _ in range(count)]
+
+
+def uneven_batch_torch(count: int, seed: int, choices=(31, 63, 127), device="cuda"):
+    """The uneven batch's right-hand sides: count volumes whose sizes per axis
+    are drawn from choices (random_sizes), volume i manufactured like the
+    single solves (8 terms, no noise) with k along each axis uniform in
+    [1, (n+1)/4] for that axis's n, seeded by seed and i.  Returns (shapes,
+    f list, u list) of float64 device tensors of shape (nz, ny, nx)."""
+    shapes = random_sizes(count, seed)
+    fs, us = [], []
+    for i, (nx, ny, nz) in enumerate(shapes):
+        f, u = manufactured_torch(nx, ny, nz, seed=seed * 100003 + i,
+                                  kmax=((nx + 1) // 4, (ny + 1) // 4, (nz + 1) // 4), device=device)
+        fs.append(f)
+        us.append(u)
+    return shapes, fs, us

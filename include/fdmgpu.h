@@ -122,24 +122,33 @@ int fdmgpu_lapl_cube_solve_device(fdmgpu_lapl_cube* h, void* d_ans, const void* 
  * callers that must not allocate device memory while they solve: programs
  * whose device memory belongs to their own pool or to another framework's
  * allocator, loops that must not wait on the allocator after start-up, and
- * hosts that forbid device allocation once initialised.  Same arguments and
- * result as a handle created with these sizes and set to FDMGPU_MIXED with
- * `tol`, called through fdmgpu_lapl_cube_solve_device (FP64 device arrays,
- * nrhs volumes back to back, asynchronous on stream), but no handle: its
- * tables, FP32 work volumes and norms live in one array of
- * FDMGPU_NOALLOC_SCRATCH_BYTES that the library holds on every device it is
- * loaded on, until the process exits.  A solve needs about
- * 4*nx*ny*nz*nrhs bytes per FP32 volume (2 volumes for one refinement sweep,
- * 3 for two) plus a few KB; larger requests return FDMGPU_EBUDGET with the
- * byte counts in the message, and sizes beyond the mixed solve's conditioning
+ * hosts that forbid device allocation once initialised.  Same arguments as a
+ * handle created with these sizes and set to FDMGPU_MIXED with `tol`, called
+ * through fdmgpu_lapl_cube_solve_device (FP64 device arrays, nrhs volumes
+ * back to back, asynchronous on stream), but no handle.  It runs the same
+ * kernels with the same schedule: sweeps chosen by tol, the per-mode z factor
+ * table when the z line splits into blocks.  Its tables are computed on the
+ * device in FP64 (a handle builds them on the host), so an FP32 table entry
+ * can differ in its last bit and the answer agrees with the handle's to
+ * round-off of the refined solve, not bit for bit.  The tables, FP32 work
+ * volumes and norms live in one array of FDMGPU_NOALLOC_SCRATCH_BYTES that
+ * the library holds on every device it is loaded on, until the process
+ * exits.  Limit: 4*nx*ny*nz*nrhs bytes per FP32 volume, 1 volume for
+ * tol >= 1e-5 (no sweep), 2 for 1e-11 <= tol < 1e-5 (one sweep), 3 below
+ * (two sweeps), plus the z table, 4*(2m + 2(P-1)) bytes per (x,y) mode (m =
+ * min(nz,15) rows per block, P = (nz+1)/(m+1) blocks; 2.8 MB at 127x127,
+ * 15.6 MB at 255x255), plus a few KB: about 8.3M, 4.1M and 2.7M points
+ * less the table.  Larger requests return FDMGPU_EBUDGET with the byte
+ * counts in the message, and sizes beyond the mixed solve's conditioning
  * limit (see fdmgpu_lapl_cube_set_precision) return FDMGPU_ENOTSUP.  The
- * first call on a device looks up the
- * array's device address (and loads the module there); make that first call
- * before any stream capture.  All calls on a device share the array: calls
- * that overlap on the GPU (other streams, other host threads) race on it, so
- * serialise them.  No cudaMalloc, cudaFree or other allocating routine is
- * called (with fdmgpu_profile_enable(1) the library creates timing events for
- * every launch, this entry point's included). */
+ * first call on a device looks up the array's device address (and loads the
+ * module there) and keeps it: make that first call before any stream
+ * capture, and do not call the library again on a device after
+ * cudaDeviceReset (the kept address would be stale).  All calls on a device
+ * share the array: calls that overlap on the GPU (other streams, other host
+ * threads) race on it, so serialise them.  No cudaMalloc, cudaFree or other
+ * allocating routine is called (with fdmgpu_profile_enable(1) the library
+ * creates timing events for every launch, this entry point's included). */
 #define FDMGPU_NOALLOC_SCRATCH_BYTES (32u * 1024u * 1024u)
 int fdmgpu_lapl_cube_solve_mixed_noalloc(double dx, double dy, double dz, double lx, double ly, double lz,
                                          int nx, int ny, int nz, double tol, void* d_ans, const void* d_rhs,
@@ -157,6 +166,21 @@ int fdmgpu_lapl_cube_scratch_bytes(fdmgpu_lapl_cube* h, size_t* bytes);
  * plain FP32 DST passes along x / y on the tensor cores when that axis has
  * 32, 64 or 128 points (default 0: FFTs) */
 int fdmgpu_lapl_cube_set_schedule(fdmgpu_lapl_cube* h, int ztable, int dst_tc);
+/* pass structure of the mixed form (no counterpart in the reference, which
+ * transforms x, y and z in turn, src/lapl_cube.cpp:13-141).
+ * FDMGPU_PIPE_PLANES (default): per sweep the DST along y, one fused pass per
+ * y-mode plane (DST along x, tridiagonal z solve, inverse DST along x; a
+ * cluster of CTAs per plane) and the inverse DST along y: three passes over
+ * the volume instead of five.  It applies when the x line has 64, 128 or
+ * 256 points, nz + 1 is 1, 2, 4 or 8 times the plane pass's rows per CTA (32
+ * at 128 and 256 points, 64 at 64 points), the z factor table is in use and
+ * the x DST is not on the tensor cores; otherwise, and with
+ * FDMGPU_PIPE_FIVE_PASS, the solve runs DST x, DST y, z solve, inverse DST
+ * y, inverse DST x.  Both give the same answer to the mixed tolerance.
+ * fdmgpu_lapl_cube_pipeline_in_use reports which one a solve would run. */
+enum { FDMGPU_PIPE_FIVE_PASS = 0, FDMGPU_PIPE_PLANES = 1 };
+int fdmgpu_lapl_cube_set_pipeline(fdmgpu_lapl_cube* h, int pipeline);
+int fdmgpu_lapl_cube_pipeline_in_use(fdmgpu_lapl_cube* h, int* pipeline);
 /* 1 in *failed if a tensor-core pass of this handle gave up waiting for its
  * MMAs (synchronises the device) */
 int fdmgpu_lapl_cube_device_status(fdmgpu_lapl_cube* h, int* failed);

@@ -99,6 +99,14 @@ NBODY_CASES = (
 )
 
 
+def _save(name: str, arrays: dict) -> None:
+    """Writes tests/golden/<name>.npz unless the command line names other
+    fixtures (`make_golden.py ns_cube` rewrites only ns_cube.npz)."""
+    only = set(sys.argv[1:])
+    if not only or name in only:
+        np.savez_compressed(OUT / (name + ".npz"), **arrays)
+
+
 def main():
     R = reference()
     if R is None:
@@ -132,7 +140,7 @@ def main():
             v1 = sfft32(sfft32(v, 1.0), 2.0 / N)
             worst = max(worst, float(np.abs(v1[1:] - v[1:]).max()))
         d["f32_roundtrip_err_%d" % N] = np.array(worst)
-    np.savez_compressed(OUT / "dst.npz", **d)
+    _save("dst", d)
 
     # LaplCube
     c = {}
@@ -161,7 +169,7 @@ def main():
     for k, v in checksums(out).items():
         c["ut31_ans_" + k] = v
     c["ut31_err"] = np.abs(out - exact).max() / np.abs(exact).max()
-    np.savez_compressed(OUT / "lapl_cube.npz", **c)
+    _save("lapl_cube", c)
 
     # periodic LaplCube<double,false,periodic^3> and its transforms
     # (FFT<T>::pFFT_1 / pFFT); arrays of n_z*n_y*n_x as the periodic callers
@@ -190,7 +198,7 @@ def main():
         per["fft3d_in_%d" % N] = cube
         per["fft3d_fwd_%d" % N] = R.pfft3d(cube, 1.0)
         per["fft3d_inv_%d" % N] = R.pfft3d(cube, 1.0, inverse=True)
-    np.savez_compressed(OUT / "lapl_cube_periodic.npz", **per)
+    _save("lapl_cube_periodic", per)
 
     # LaplCyl3FFT2<double,false,zflag> (src/lapl_cyl.cpp:10-166): arrays
     # (nphi, nz, nr), r fastest
@@ -242,7 +250,7 @@ def main():
         for f in ("u", "v", "w", "p"):
             cyl["lin_%s_s10_%s" % (name, f)] = m.get(f)
         m.close()
-    np.savez_compressed(OUT / "lapl_cyl.npz", **cyl)
+    _save("lapl_cyl", cyl)
 
     # LaplRect / LaplRectFFT2
     r = {}
@@ -268,7 +276,7 @@ def main():
         r["rhs_" + tag] = rhs
         r["args_" + tag] = np.array(args)
         r["ans_" + tag] = R.lapl_rect_flags(rhs, *args, fft2, flags)
-    np.savez_compressed(OUT / "lapl_rect.npz", **r)
+    _save("lapl_rect", r)
 
     # tridiagonal: Thomas and cyclic reduction on U(-1,1) systems with a
     # dominant diagonal
@@ -287,7 +295,7 @@ def main():
         t["crg_%d" % n] = R.cyclic_reduction(dg, lo, up, b, general=True)
         if (n + 1) & n == 0:
             t["cr_%d" % n] = R.cyclic_reduction(dg, lo, up, b, general=False)
-    np.savez_compressed(OUT / "tdiag.npz", **t)
+    _save("tdiag", t)
 
     # NSCube lid-driven cavity, Re=250, dt=0.01, [-pi,pi]^3
     ns = {}
@@ -306,6 +314,15 @@ def main():
         for k, v in checksums(m.get(name)).items():
             ns["n31_s10_%s_%s" % (name, k)] = v
     m.close()
+    # the 1000-step cavity's own size, 63^3 (64 intervals): the first 10 and
+    # 50 steps, checksums plus values at seeded positions
+    m = R.nscube(63, 63, 250.0, 0.01)
+    for steps, done in ((10, 10), (40, 50)):
+        m.step(steps)
+        for name in ("u", "v", "w", "p", "x"):
+            for k, v in checksums(m.get(name), nsamp=512).items():
+                ns["n63_s%d_%s_%s" % (done, name, k)] = v
+    m.close()
     # NSCube<float> (src/ns_cube.cpp:281-282), same cavity
     m = R.nscube_float(15, 15, 250.0, 0.01)
     m.step(20)
@@ -316,7 +333,7 @@ def main():
         for k, v in checksums(m.get(name)).items():
             ns["f32_n15_s100_%s_%s" % (name, k)] = v
     m.close()
-    np.savez_compressed(OUT / "ns_cube.npz", **ns)
+    _save("ns_cube", ns)
 
     # particle-mesh N-body driver, NBody<T,false,CIC3<T>> (test/nbody.cpp):
     # the constructor's bodies, then the state after 1 and 5 steps
@@ -339,7 +356,7 @@ def main():
         for k in ("x", "v", "a", "aprev"):
             nb["%s_s5_%s" % (tag, k)] = b[k].astype(T)
         m.close()
-    np.savez_compressed(OUT / "nbody.npz", **nb)
+    _save("nbody", nb)
     for p in sorted(OUT.glob("*.npz")):
         print(p.name, p.stat().st_size)
 

@@ -51,6 +51,25 @@ def test_batch_uneven_vs_single_fp64(cuda, tol):
         assert _rel(ans[i], ref) <= tol, (i, s)
 
 
+def test_batch_config3_inputs(cuda):
+    """The uneven batch's own inputs (sizes per axis from {31, 63, 127},
+    manufactured solutions with k in [1, (n+1)/4] per axis, tol 1e-8), 48 of
+    them: every answer against its FP64 single solve and the manufactured u."""
+    import torch
+    shapes, rhs, exact = workloads.uneven_batch_torch(48, seed=2024)
+    args = [workloads.solver_args(*s) for s in shapes]
+    ans = [torch.empty_like(r) for r in rhs]
+    b = BatchSolver(shapes, [a[0:3] for a in args], [a[3:6] for a in args], precision="mixed", tol=1e-8)
+    b.tune(ans, rhs)
+    b.solve(ans, rhs)
+    torch.cuda.synchronize()
+    for i, s in enumerate(shapes):
+        ref = _single_plain(s, args[i][0:3], args[i][3:6], rhs[i])
+        assert _rel(ans[i], ref) <= 1e-8, (i, s)
+        assert _rel(ans[i], exact[i]) <= 1e-8, (i, s)
+        assert _rel(ref, exact[i]) <= 1e-13, (i, s)
+
+
 def test_batch_plain_equals_single(cuda):
     """Plain FP64 through pointer tables equals the contiguous FP64 solve."""
     import torch

@@ -64,6 +64,28 @@ def test_plain_f64_vs_oracle(cuda, port, shape):
     assert rel_l2(ans, ref) <= TOL_PLAIN
 
 
+def test_plain_f64_config2_size_vs_oracle(cuda, port):
+    """The metric's own size, 255^3 interior, with its inputs (k in [1,60],
+    N(0,1e-3) noise): the plain FP64 GPU solve against the oracle's
+    LaplCube::solve, and the mixed form against both; without noise the
+    manufactured u comes back to round-off (the discretisation error of
+    these exact discrete modes is zero)."""
+    n = 255
+    args = workloads.solver_args(n, n, n)
+    f, _ = workloads.manufactured(n, n, n, seed=0, kmax=60, noise=1e-3)
+    ref = port.lapl_cube(f, *args[:6])
+    ans, _ = solve_host(args, f)
+    assert rel_l2(ans, ref) <= TOL_PLAIN
+    mixed, m = solve_host(args, f, precision="mixed", tol=1e-10)
+    assert m.last_info(1)[0] == 1
+    assert rel_l2(mixed, ref) <= TOL_MIXED
+    assert rel_l2(mixed, ans) <= TOL_MIXED
+    f0, u0 = workloads.manufactured(n, n, n, seed=1, kmax=60)
+    ans0, _ = solve_host(args, f0)
+    assert rel_l2(ans0, u0) <= 1e-13
+    assert rel_l2(ans0, port.lapl_cube(f0, *args[:6])) <= TOL_PLAIN
+
+
 def test_plain_f32_vs_oracle(cuda, port):
     n = 31
     f, u = workloads.manufactured(n, n, n, seed=4, kmax=8)
@@ -166,6 +188,51 @@ def test_mixed_tolerance_levels(cuda):
         assert s == want_sweeps
         err = (torch.linalg.norm(b - a) / torch.linalg.norm(a)).item()
         assert err <= max(tol, 1e-13), (tol, err)
+
+
+@pytest.mark.parametrize("shape", [(63, 63, 63), (127, 127, 127), (255, 255, 255), (127, 63, 255), (255, 31, 127),
+                                   (63, 127, 63), (255, 255, 31), (127, 15, 31)])
+def test_mixed_plane_pipeline(cuda, shape):
+    """The three-pass pipeline (DST-y, the fused x-z plane pass on clusters
+    of 1 to 8 CTAs, inverse DST-y) against the FP64 form and the five-pass
+    pipeline, for every refinement schedule (no sweep, one, two), two
+    right-hand sides at once (white noise plus smooth modes)."""
+    import torch
+    nx, ny, nz = shape
+    f = torch.stack([workloads.manufactured_torch(nx, ny, nz, seed=31 + s, kmax=min(shape) // 4 + 1,
+                                                  noise=1e-3)[0] for s in (0, 1)]).contiguous()
+    g = torch.Generator(device="cuda").manual_seed(5)
+    f[1] += torch.randn(f[1].shape, dtype=torch.float64, device="cuda", generator=g)
+    args = workloads.solver_args(nx, ny, nz)
+    a = torch.empty_like(f)
+    LaplCube(*args).solve_device(a, f, nrhs=2)
+    for tol in (1e-4, 1e-10, 1e-13):
+        planes = LaplCube(*args, precision="mixed", tol=tol)
+        assert planes.pipeline_in_use() == "planes"
+        five = LaplCube(*args, precision="mixed", tol=tol)
+        five.set_pipeline(False)
+        assert five.pipeline_in_use() == "five_pass"
+        b = torch.empty_like(f)
+        c = torch.empty_like(f)
+        planes.solve_device(b, f, nrhs=2)
+        five.solve_device(c, f, nrhs=2)
+        torch.cuda.synchronize()
+        for i in range(2):
+            eb = (torch.linalg.norm(b[i] - a[i]) / torch.linalg.norm(a[i])).item()
+            ec = (torch.linalg.norm(c[i] - a[i]) / torch.linalg.norm(a[i])).item()
+            assert eb <= max(tol, 1e-12), (shape, tol, i, eb, ec)
+            assert ec <= max(tol, 1e-12), (shape, tol, i, eb, ec)
+
+
+def test_plane_pipeline_applicability(cuda):
+    """Sizes the plane pass does not cover run the five-pass pipeline."""
+    for shape in ((31, 31, 31), (63, 63, 31), (127, 127, 7), (255, 255, 511)):
+        m = LaplCube(*workloads.solver_args(*shape), precision="mixed", tol=1e-10)
+        assert m.pipeline_in_use() == "five_pass", shape
+    m = LaplCube(*workloads.solver_args(127, 127, 127), precision="mixed", tol=1e-10)
+    m.set_schedule(ztable=False)
+    assert m.pipeline_in_use() == "five_pass"
+    assert LaplCube(*workloads.solver_args(127, 127, 127)).pipeline_in_use() == "five_pass"  # plain FP64
 
 
 @pytest.mark.parametrize("pinned", [True, False])

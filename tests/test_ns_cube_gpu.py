@@ -47,6 +47,23 @@ def test_golden_31_cube(cuda, golden):
         assert np.abs(got[g["n31_s10_%s_idx" % name]] - g["n31_s10_%s_vals" % name]).max() <= 1e-12 * scale, name
 
 
+def test_golden_63_cube(cuda, golden):
+    """63^3 (the 1000-step case's size) against the reference's own fields
+    after 10 and 50 steps (checksums and 512 sampled values per field), so
+    the 1000-step comparison with the restatement has a link to the
+    reference at this size."""
+    g = golden("ns_cube")
+    m = make(63)
+    for steps, done in ((10, 10), (40, 50)):
+        m.step(steps)
+        for name in ("u", "v", "w", "p", "x"):
+            got = m.get(name).data.ravel()
+            pre = "n63_s%d_%s_" % (done, name)
+            scale = max(1.0, float(g[pre + "maxabs"]))
+            assert np.abs(got[g[pre + "idx"]] - g[pre + "vals"]).max() <= 1e-12 * scale, (done, name)
+            assert abs(np.linalg.norm(got) - float(g[pre + "l2"])) <= 1e-12 * float(g[pre + "l2"]), (done, name)
+
+
 def test_all_fields_vs_oracle_31(cuda, port):
     m = make(31)
     o = port.nscube(31, 31, 250.0, 0.01)

@@ -148,6 +148,28 @@ def test_nscube_matches_reference(port, golden):
     m.close()
 
 
+def _check_n63(get, g, done):
+    for name in ("u", "v", "w", "p", "x"):
+        a = get(name).ravel()
+        pre = "n63_s%d_%s_" % (done, name)
+        scale = max(1.0, float(g[pre + "maxabs"]))
+        assert np.abs(a[g[pre + "idx"]] - g[pre + "vals"]).max() <= 1e-12 * scale, (done, name)
+        assert abs(np.linalg.norm(a) - float(g[pre + "l2"])) <= 1e-12 * float(g[pre + "l2"]), (done, name)
+
+
+def test_nscube_63_matches_reference(port, golden):
+    """The 1000-step cavity's size (63^3): the restatement against the
+    reference's fields after 10 and 50 steps (checksums and 512 sampled
+    values per field)."""
+    g = golden("ns_cube")
+    m = port.nscube(63, 63, 250.0, 0.01)
+    m.step(10)
+    _check_n63(m.get, g, 10)
+    m.step(40)
+    _check_n63(m.get, g, 50)
+    m.close()
+
+
 def test_nscube_rejects_bad_size(port):
     with pytest.raises(ValueError):
         port.nscube(32, 32, 250.0, 0.01)
