@@ -89,43 +89,47 @@ __global__ void __launch_bounds__(256, MINB) k_plane_xz(float* __restrict__ W, P
     const long long rstride = (long long)ny * nx;  // between consecutive z rows
     float* row0 = W + (long long)blockIdx.y * geo.vstride + ((long long)z0 * ny + ky) * nx;
 
-    // ---- 1. load + fold (item (line, j) reads x_j and x_{N-j}), DST along x
-    {
-        constexpr int total = L * ITEMS;
-        for (int e0 = tid; e0 < total; e0 += 4 * nthr) {
-            float av[4], bv[4];
-            int lv[4], jv[4];
+    // The fold and store phases run one warp per line: lane c takes the
+    // items j = c + 32k (and lane 0 also j = M), so every global and shared
+    // address is a per-thread base plus a compile-time offset.  In the fold
+    // input entry j of line l is float 2 l LS2 + j; in the packed output
+    // entry i is float 2 l LS2 + 2 sk(i>>1) + (i&1), which is c + 34k for
+    // i = c + 32k and fb - 34k for i = N - c - 32k (fb below).
+    const int lane = tid & 31, wid = tid >> 5;
+    constexpr int KJ = M / 32;  // full rounds of 32 items per line (j < M)
+    constexpr int LPW = L / 8;  // lines per warp
+    const int hh = (lane + 1) >> 1;
+    const int fb = 2 * (M + M / 16 - hh - (hh > 0 ? 1 : 0)) + (lane & 1);
+    static_assert(M % 32 == 0 && L % 8 == 0, "warp-per-line phases");
+
+    // ---- 1. load + fold, then the DST along x
 #pragma unroll
-            for (int q = 0; q < 4; q++) {
-                const int e = e0 + q * nthr;
-                const int line = e / ITEMS, j = e - line * ITEMS;
-                lv[q] = line;
-                jv[q] = j;
-                float a = 0.f, b = 0.f;
-                if (e < total && line < nact && j >= 1) {
-                    const float* p = row0 + line * rstride;
-                    a = p[j - 1];
-                    b = p[n - j];
-                }
-                av[q] = a;
-                bv[q] = b;
-            }
+    for (int li = 0; li < LPW; li++) {
+        const int line = wid + 8 * li;
+        float* xo = Sr + 2 * line * LS2;
+        if (line < nact) {
+            const float* p = row0 + line * rstride;
+            float a[KJ], b[KJ];
 #pragma unroll
-            for (int q = 0; q < 4; q++) {
-                const int e = e0 + q * nthr;
-                if (e < total) {
-                    const int j = jv[q];
-                    float* base = Sr + 2 * lv[q] * LS2;
-                    if (j == 0) {
-                        base[0] = 0.f;
-                    } else {
-                        const float w = ldg(tb.wpre + j);
-                        const float sm = w * (av[q] + bv[q]), df = 0.5f * (av[q] - bv[q]);
-                        base[j] = sm + df;
-                        if (j != M) base[N - j] = sm - df;
-                    }
-                }
+            for (int k = 0; k < KJ; k++) {
+                const bool ok = k > 0 || lane > 0;
+                a[k] = ok ? p[lane + 32 * k - 1] : 0.f;
+                b[k] = ok ? p[n - lane - 32 * k] : 0.f;
             }
+            const float am = p[M - 1];
+#pragma unroll
+            for (int k = 0; k < KJ; k++) {
+                const int j = lane + 32 * k;
+                const float w = ldg(tb.wpre + j);
+                const float sm = w * (a[k] + b[k]), df = 0.5f * (a[k] - b[k]);
+                xo[j] = sm + df;  // j = 0: both are 0
+                if (k > 0 || lane > 0) xo[N - j] = sm - df;
+            }
+            if (lane == 0) xo[M] = ldg(tb.wpre + M) * (am + am);
+        } else {
+            // the row past the plane's end (last CTA): a zero line
+#pragma unroll
+            for (int k = 0; k < 2 * KJ; k++) xo[lane + 32 * k] = 0.f;
         }
     }
     __syncthreads();
@@ -229,53 +233,50 @@ __global__ void __launch_bounds__(256, MINB) k_plane_xz(float* __restrict__ W, P
     }
     __syncthreads();
 
-    // ---- 5. inverse DST along x: fold from the transform layout into the
-    // linear one (every read before any write: the two layouts overlap)
-    {
-        constexpr int total = L * ITEMS;
-        constexpr int PER = (total + nthr - 1) / nthr;
-        float av[PER], bv[PER];
+    // ---- 5. inverse DST along x: fold from the packed output into the fold
+    // input of the same line (a warp reads the whole line first: the two
+    // layouts overlap)
 #pragma unroll
-        for (int q = 0; q < PER; q++) {
-            const int e = tid + q * nthr;
-            const int line = e / ITEMS, j = e - line * ITEMS;
-            float a = 0.f, b = 0.f;
-            if (e < total && j >= 1) {
-                const float* base = Sr + line * RS;
-                const int jm = N - j;
-                a = base[2 * sk(j >> 1) + (j & 1)];
-                b = base[2 * sk(jm >> 1) + (jm & 1)];
-            }
-            av[q] = a;
-            bv[q] = b;
-        }
-        __syncthreads();
+    for (int li = 0; li < LPW; li++) {
+        const int line = wid + 8 * li;
+        float* base = Sr + 2 * line * LS2;
+        float a[KJ], b[KJ];
 #pragma unroll
-        for (int q = 0; q < PER; q++) {
-            const int e = tid + q * nthr;
-            if (e < total) {
-                const int line = e / ITEMS, j = e - line * ITEMS;
-                float* base = Sr + line * RS;
-                if (j == 0) {
-                    base[0] = 0.f;
-                } else {
-                    const float w = ldg(tb.wpre + j);
-                    const float sm = w * (av[q] + bv[q]), df = 0.5f * (av[q] - bv[q]);
-                    base[j] = sm + df;
-                    if (j != M) base[N - j] = sm - df;
-                }
-            }
+        for (int k = 0; k < KJ; k++) {
+            const bool ok = k > 0 || lane > 0;
+            a[k] = ok ? base[lane + 34 * k] : 0.f;
+            b[k] = ok ? base[fb - 34 * k] : 0.f;
         }
+        const float am = base[2 * (M / 2 + M / 32)];
+        __syncwarp();
+#pragma unroll
+        for (int k = 0; k < KJ; k++) {
+            const int j = lane + 32 * k;
+            const float w = ldg(tb.wpre + j);
+            const float sm = w * (a[k] + b[k]), df = 0.5f * (a[k] - b[k]);
+            base[j] = sm + df;
+            if (k > 0 || lane > 0) base[N - j] = sm - df;
+        }
+        if (lane == 0) base[M] = ldg(tb.wpre + M) * (am + am);
     }
     __syncthreads();
     rg_line_fft<float, N, 0>(S + l * LS2, g, tb);
     __syncthreads();
 
-    // ---- 6. store the rows
-    const int total = nact * n;
-    for (int e = tid; e < total; e += nthr) {
-        const int q = e / n, ii = e - q * n + 1;
-        row0[q * rstride + ii - 1] = sc_inv * Sr[q * RS + 2 * sk(ii >> 1) + (ii & 1)];
+    // ---- 6. store the rows: slot k = c + 32q of a line holds F_2k and
+    // F_2k+1, which go to x = 2k-1 and 2k
+#pragma unroll
+    for (int li = 0; li < LPW; li++) {
+        const int line = wid + 8 * li;
+        if (line >= nact) continue;
+        const T2* src = S + line * LS2 + lane + (lane >> 4);
+        float* dst = row0 + line * rstride + 2 * lane;
+#pragma unroll
+        for (int q = 0; q < M / 32; q++) {
+            const T2 f2 = src[34 * q];
+            if (q > 0 || lane > 0) dst[64 * q - 1] = sc_inv * f2.x;
+            dst[64 * q] = sc_inv * f2.y;
+        }
     }
 }
 

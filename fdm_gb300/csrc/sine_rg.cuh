@@ -234,6 +234,35 @@ __device__ __forceinline__ void rg_line_fft(vec2_t<T>* Ls, int g, const SineTabl
     }
 }
 
+// Adds the CTA's sums of ||c||^2 and ||u||^2 to norms[2v], norms[2v+1]
+// (v = blockIdx.y).  All threads of the CTA call it.
+__device__ __forceinline__ void norms_reduce(float cc, float uu, double* norms, int tid, int nthr) {
+    for (int o = 16; o > 0; o >>= 1) {
+        cc += __shfl_down_sync(0xffffffffu, cc, o);
+        uu += __shfl_down_sync(0xffffffffu, uu, o);
+    }
+    __shared__ float red[2][32];
+    const int w = tid >> 5, ln = tid & 31;
+    if (ln == 0) {
+        red[0][w] = cc;
+        red[1][w] = uu;
+    }
+    __syncthreads();
+    if (w == 0) {
+        const int nw = nthr >> 5;
+        cc = ln < nw ? red[0][ln] : 0.f;
+        uu = ln < nw ? red[1][ln] : 0.f;
+        for (int o = 16; o > 0; o >>= 1) {
+            cc += __shfl_down_sync(0xffffffffu, cc, o);
+            uu += __shfl_down_sync(0xffffffffu, uu, o);
+        }
+        if (ln == 0 && norms) {
+            atomicAdd(&norms[2 * blockIdx.y], (double)cc);
+            atomicAdd(&norms[2 * blockIdx.y + 1], (double)uu);
+        }
+    }
+}
+
 template <typename Tin, typename T, typename Tout, int AXIS, int MODE, int N>
 __device__ __forceinline__ void sine_rg_body(const Tin* in, Tout* out, const SineGeom& geo, const SineTables<T>& tb,
                                              T scale, const SineFused& fu) {
@@ -265,7 +294,50 @@ __device__ __forceinline__ void sine_rg_body(const Tin* in, Tout* out, const Sin
 
     // ---- load + fold: item (line, j) reads x_j and x_{N-j} and writes
     // y_j = w_j (a+b) + (a-b)/2 and y_{N-j} = w_j (a+b) - (a-b)/2
-    {
+    constexpr bool kCol32 = AXIS == 1 && L == 32 && MODE != kResidual;
+    const int lane = tid & 31, wid = tid >> 5;
+    if constexpr (kCol32) {
+        // column pass with one line per lane: warp w takes the items j =
+        // w + 8q of its 32 lines, so an address is a per-thread base plus q
+        // steps of 8 rows
+        constexpr int QN = (ITEMS + 7) / 8;
+        const bool act = lane < nact;
+        const Tin* p = (fu.vin ? (const Tin*)fu.vin[blockIdx.y] : in + voff) + ((long long)z * ny) * nx + x0 + lane;
+        T* xo = Sr + 2 * lane * LS2;  // this lane's line: folded entry j at xo[j]
+        const long long s8 = 8LL * nx;
+        const Tin* pa = p + (long long)(wid - 1) * nx;  // x_j sits in row j - 1
+        const Tin* pb = p + (long long)(n - wid) * nx;  // x_{N-j} in row n - j
+#pragma unroll
+        for (int q0 = 0; q0 < QN; q0 += 4) {
+            T av[4], bv[4];
+#pragma unroll
+            for (int qq = 0; qq < 4; qq++) {
+                const int q = q0 + qq, j = wid + 8 * q;
+                T a = T(0), b = T(0);
+                if (q < QN && j <= M && (q > 0 || wid > 0) && act) {
+                    if (MODE == kRound) {
+                        a = T(f64_to_f32((double)pa[q * s8]));
+                        b = T(f64_to_f32((double)pb[-q * s8]));
+                    } else {
+                        a = T(pa[q * s8]);
+                        b = T(pb[-q * s8]);
+                    }
+                }
+                av[qq] = a;
+                bv[qq] = b;
+            }
+#pragma unroll
+            for (int qq = 0; qq < 4; qq++) {
+                const int q = q0 + qq, j = wid + 8 * q;
+                if (q < QN && j <= M) {
+                    const T w = ldg(tb.wpre + j);
+                    const T sm = w * (av[qq] + bv[qq]), df = T(0.5) * (av[qq] - bv[qq]);
+                    xo[j] = sm + df;  // j = 0: w_0 = 0 and a = b = 0
+                    if (j != M && j != 0) xo[N - j] = sm - df;
+                }
+            }
+        }
+    } else {
         const T half = T(0.5);
         constexpr int total = L * ITEMS;
         for (int e0 = tid; e0 < total; e0 += 4 * nthr) {
@@ -362,7 +434,85 @@ __device__ __forceinline__ void sine_rg_body(const Tin* in, Tout* out, const Sin
             return e < total && c < nact;
         }
     };
-    if (MODE == kCombine) {
+    // FP32 lines of 128 and 256 points read F_2k and F_2k+1 of a line as one
+    // float2 (packed slot k) and store the two entries
+    constexpr bool kPair = sizeof(T) == 4 && (N == 128 || N == 256);
+    if constexpr (kCol32 && kPair) {
+        // column pass, one line per lane: warp w stores the packed slots k =
+        // w + 8q (slot sk(k) = w + 8q + q/2), entries 2k and 2k+1 to rows
+        // y = 2k-1 and 2k
+        constexpr int QS = M / 8;
+        const bool act = lane < nact;
+        const T2* src = S + lane * LS2 + wid;
+        const long long s16 = 16LL * nx;
+        const long long base = ((long long)z * ny + 2 * wid - 1) * nx + x0 + lane;  // row 2k-1 at q = 0
+        if constexpr (MODE == kCombine) {
+            float cc = 0.f, uu = 0.f;
+            double* o64 = (fu.vout ? (double*)fu.vout[blockIdx.y] : fu.out64 + voff) + base;
+            const float* uh = fu.uhi + voff + base;
+            const float* ul = fu.ulo ? fu.ulo + voff + base : nullptr;
+            float* ulo_out = fu.last ? nullptr : fu.ulo_out + voff + base;
+#pragma unroll
+            for (int q0 = 0; q0 < QS; q0 += 2) {
+                float hv[4], lw[4];
+#pragma unroll
+                for (int a = 0; a < 4; a++) {
+                    const int q = q0 + (a >> 1), h = a & 1;
+                    const long long o = q * s16 + h * nx;
+                    const bool ok = act && (h || q > 0 || wid > 0);
+                    hv[a] = ok ? uh[o] : 0.f;
+                    lw[a] = (ok && ul) ? ul[o] : 0.f;
+                }
+#pragma unroll
+                for (int qq = 0; qq < 2; qq++) {
+                    const int q = q0 + qq;
+                    if (!act) continue;
+                    const T2 f2 = src[8 * q + (q >> 1)];
+#pragma unroll
+                    for (int h = 0; h < 2; h++) {
+                        if (!h && q == 0 && wid == 0) continue;
+                        const int a = 2 * qq + h;
+                        const long long o = q * s16 + h * nx;
+                        const float cv = (float)(scale * (h ? f2.y : f2.x));
+                        ff s2 = two_sum(hv[a], lw[a]);
+                        s2 = ff_add_f(s2, cv);
+                        if (fu.last) o64[o] = ff_to_f64(s2);
+                        else ulo_out[o] = lw[a] + cv;
+                        cc += cv * cv;
+                        uu += s2.h * s2.h;
+                    }
+                }
+            }
+            norms_reduce(cc, uu, fu.norms, tid, nthr);
+        } else {
+            Tout* ob = (fu.vout ? (Tout*)fu.vout[blockIdx.y] : out + voff) + base;
+            if (act) {
+#pragma unroll
+                for (int q = 0; q < QS; q++) {
+                    const T2 f2 = src[8 * q + (q >> 1)];
+                    if (q > 0 || wid > 0) ob[q * s16] = Tout(scale * f2.x);
+                    ob[q * s16 + nx] = Tout(scale * f2.y);
+                }
+            }
+        }
+    } else if constexpr (AXIS == 0 && kPair && MODE != kCombine) {
+        // row pass: warp w stores lines w, w+8, ...; lane c the packed slots
+        // k = c + 32q (slot sk(k) = c + c/16 + 34q), entries to x = 2k-1, 2k
+        Tout* ob = (fu.vout ? (Tout*)fu.vout[blockIdx.y] : out + voff) + (long long)row0 * n + 2 * lane;
+#pragma unroll
+        for (int li = 0; li < L / 8; li++) {
+            const int r = wid + 8 * li;
+            if (r >= nact) continue;
+            const T2* src = S + r * LS2 + lane + (lane >> 4);
+            Tout* dst = ob + (long long)r * n;
+#pragma unroll
+            for (int q = 0; q < M / 32; q++) {
+                const T2 f2 = src[34 * q];
+                if (q > 0 || lane > 0) dst[64 * q - 1] = Tout(scale * f2.x);
+                dst[64 * q] = Tout(scale * f2.y);
+            }
+        }
+    } else if (MODE == kCombine) {
         float cc = 0.f, uu = 0.f;
         double* o64 = fu.vout ? (double*)fu.vout[blockIdx.y] : fu.out64 + voff;
         // batches of 4 elements per thread: the uhi / ulo loads of a batch
@@ -395,27 +545,7 @@ __device__ __forceinline__ void sine_rg_body(const Tin* in, Tout* out, const Sin
                 }
             }
         }
-        for (int o = 16; o > 0; o >>= 1) {
-            cc += __shfl_down_sync(0xffffffffu, cc, o);
-            uu += __shfl_down_sync(0xffffffffu, uu, o);
-        }
-        __shared__ float red[2][32];
-        const int w = tid >> 5, ln = tid & 31;
-        if (ln == 0) { red[0][w] = cc; red[1][w] = uu; }
-        __syncthreads();
-        if (w == 0) {
-            constexpr int nw = nthr >> 5;
-            cc = ln < nw ? red[0][ln] : 0.f;
-            uu = ln < nw ? red[1][ln] : 0.f;
-            for (int o = 16; o > 0; o >>= 1) {
-                cc += __shfl_down_sync(0xffffffffu, cc, o);
-                uu += __shfl_down_sync(0xffffffffu, uu, o);
-            }
-            if (ln == 0 && fu.norms) {
-                atomicAdd(&fu.norms[2 * blockIdx.y], (double)cc);
-                atomicAdd(&fu.norms[2 * blockIdx.y + 1], (double)uu);
-            }
-        }
+        norms_reduce(cc, uu, fu.norms, tid, nthr);
     } else {
         Tout* ob = fu.vout ? (Tout*)fu.vout[blockIdx.y] : out + voff;
         for (int e = tid; e < total; e += nthr) {
