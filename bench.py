@@ -48,7 +48,37 @@ KERNEL_BYTES = {
     "sine_x_round": 12, "sine_x_resid": 16, "sine_x_combine": 16, "sine_x_f32": 8, "sine_x_f32_out64": 12,
     "sine_y_f32": 8, "sine_x_f64": 16, "sine_y_f64": 16, "zsolve_f32": 8, "zsolve_f64": 16,
     "tridiag_f32": 8, "tridiag_f64": 16, "residual_ff": 16,
+    "plane_xz_f32": 8, "sine_y_round": 12, "sine_y_combine": 16, "sine_y_f32_out64": 12,
 }
+
+
+def unixbench_score(samples):
+    """The reference's own summary of repeated timings (src/unixbench_score.cpp:9-20):
+    the geometric mean of the fastest two thirds of the samples."""
+    data = sorted(samples)
+    keep = (2 * len(data)) // 3
+    if keep == 0:
+        return None
+    return math.exp(sum(math.log(d) for d in data[:keep]) / keep)
+
+
+def cpu_model():
+    """The host CPU's model name (lscpu, else /proc/cpuinfo)."""
+    try:
+        out = subprocess.run(["lscpu"], stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True,
+                             timeout=10).stdout
+        for ln in out.splitlines():
+            if ln.strip().startswith("Model name:"):
+                return ln.split(":", 1)[1].strip()
+    except (OSError, subprocess.SubprocessError):
+        pass
+    try:
+        for ln in open("/proc/cpuinfo"):
+            if ln.lower().startswith("model name"):
+                return ln.split(":", 1)[1].strip()
+    except OSError:
+        pass
+    return "unknown"
 
 
 def peaks():
@@ -170,6 +200,7 @@ def cpu_reference_rate(sample_solves: int, n: int = N_INT, time_budget: float = 
     cores = port().threads()
     sample = "%d single-RHS %d^3 LaplCube<double> solves (median %.3f s each), OpenMP threads=%d" % (
         len(times), n, med, cores)
+    cpu_reference_rate.last_times = times
     return 1.0 / med, kind, cores, sample
 
 
@@ -183,7 +214,9 @@ def run_reference_arm(args, world, rank):
         "vs_baseline": None, "dtype": "f64", "data": "synthetic",
         "config": {"workload": "poisson_dirichlet_255^3_x16rhs", "grid": [N_INT] * 3, "nrhs": NRHS,
                    "kmax": KMAX, "noise": NOISE, "tol": TOL},
-        "cpu_baseline": {"value": rate, "unit": UNIT, "cores": cores, "kind": kind, "sample": sample},
+        "cpu_baseline": {"value": rate, "unit": UNIT, "cores": cores, "kind": kind, "sample": sample,
+                         "cpu_model": cpu_model(),
+                         "unixbench_ms_per_solve": 1e3 * unixbench_score(cpu_reference_rate.last_times)},
         "e2e": {"value": rate, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
     }
     print(json.dumps(line), flush=True)
@@ -698,16 +731,18 @@ def main():
         barrier(world)
         torch.cuda.synchronize()
         l0 = _native.launch_count()
-        e0 = torch.cuda.Event(enable_timing=True)
-        e1 = torch.cuda.Event(enable_timing=True)
-        e0.record(stream)
-        for _ in range(args.steps):
+        ev = [torch.cuda.Event(enable_timing=True) for _ in range(args.steps + 1)]
+        ev[0].record(stream)
+        for k in range(args.steps):
             step()
-        e1.record(stream)
+            ev[k + 1].record(stream)
         torch.cuda.synchronize()
         barrier(world)
         launches = _native.launch_count() - l0
-        ms = e0.elapsed_time(e1)
+        ms = ev[0].elapsed_time(ev[-1])
+        step_ms = [ev[k].elapsed_time(ev[k + 1]) for k in range(args.steps)]
+        e0 = torch.cuda.Event(enable_timing=True)
+        e1 = torch.cuda.Event(enable_timing=True)
         ms = allreduce_max(world, ms)
 
         # ---- e2e: host-pointer batch entry point, pinned host buffers
@@ -755,13 +790,14 @@ def main():
     e1.record(stream)
     stream.synchronize()
     plain_rate = 2 * NRHS / (e0.elapsed_time(e1) * 1e-3)
+    # the 1000-step cavity (63^3, Re 250, dt 0.01) from the zero state, as
+    # the CPU baseline runs it
     ns = fdm_gb300.NSCube(nx=63, nz=63, Re=250.0, dt=0.01, u0=1.0)
-    ns.step(20)
     torch.cuda.synchronize()
     t0 = time.perf_counter()
-    ns.step(200)
+    ns.step(1000)
     torch.cuda.synchronize()
-    ns_ms = (time.perf_counter() - t0) * 1e3 / 200
+    ns_ms = (time.perf_counter() - t0) * 1e3 / 1000
     ns.close()
     # the cylindrical step at the reference's defaults (nr 32, nz 31, nphi 32)
     cyl = fdm_gb300.NSCyl(Re=100.0, dt=0.001)
@@ -786,6 +822,7 @@ def main():
     solves = args.steps * NRHS * world
     value = solves / (ms * 1e-3)
     e2e_value = e2e_steps * NRHS * world / e2e_s
+    step_ms_samples = step_ms
     step_ms = ms / args.steps
     line = {
         "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
@@ -798,6 +835,8 @@ def main():
         "accuracy": {"rel_l2_vs_fp64_gpu_max": max(errs), "rel_l2_vs_fp64_gpu_median": statistics.median(errs),
                      "sweeps": sweeps, "correction_estimate_max": max(est)},
         "latency_ms_per_solve": step_ms / NRHS,
+        "unixbench_ms_per_step": unixbench_score(step_ms_samples),
+        "pipeline": mixed.pipeline_in_use(),
         "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": NRHS * vol * 8,
                 "d2h_bytes_per_step": NRHS * vol * 8},
         "gpu_launches": launches,
@@ -810,7 +849,8 @@ def main():
                            "bytes_per_point": SOLVE_BYTES_PER_POINT},
         "kernels_ms_per_step": {k: v[1] / 2 for k, v in sorted(prof.items(), key=lambda kv: -kv[1][1])},
         "plain_fp64_gpu": {"value": plain_rate, "unit": UNIT},
-        "nscube_63cubed": {"ms_per_step": ns_ms, "steps_timed": 200, "Re": 250.0, "dt": 0.01},
+        "nscube_63cubed": {"ms_per_step": ns_ms, "steps_timed": 1000, "Re": 250.0, "dt": 0.01,
+                           "clock": "host clock around 1000 graph-launched steps from the zero state"},
         "nscyl_32x31x32": {"ms_per_step": cyl_ms, "steps_timed": 200, "Re": 100.0, "dt": 0.001},
         "uneven_batch": uneven,
         "periodic_poisson": periodic,
@@ -820,14 +860,23 @@ def main():
     }
     if rank == 0 and not args.no_cpu_baseline:
         rate, kind, cores, sample = cpu_reference_rate(5)
-        line["cpu_baseline"] = {"value": rate, "unit": UNIT, "cores": cores, "kind": kind, "sample": sample}
+        line["cpu_baseline"] = {"value": rate, "unit": UNIT, "cores": cores, "kind": kind, "sample": sample,
+                                "cpu_model": cpu_model(),
+                                "unixbench_ms_per_solve": 1e3 * unixbench_score(cpu_reference_rate.last_times)}
+        # the cavity of the 1000-step case (63^3, Re 250, dt 0.01), every
+        # step timed: mean and the reference's unixbench summary
         from oracle.oracle import port
         o = port().nscube(63, 63, 250.0, 0.01)
-        o.step(2)
-        t0 = time.perf_counter()
-        o.step(10)
-        line["cpu_baseline"]["nscube_63cubed_ms_per_step"] = (time.perf_counter() - t0) * 1e3 / 10
+        nst = []
+        for _ in range(1000):
+            t0 = time.perf_counter()
+            o.step(1)
+            nst.append((time.perf_counter() - t0) * 1e3)
         o.close()
+        line["cpu_baseline"]["nscube_63cubed_1000_steps"] = {
+            "ms_per_step": statistics.fmean(nst), "unixbench_ms_per_step": unixbench_score(nst),
+            "total_s": sum(nst) / 1e3, "kind": "port", "threads": cores}
+        line["cpu_baseline"]["nscube_63cubed_ms_per_step"] = statistics.fmean(nst)
         # the same solve on one host thread (one 255^3 solve)
         pt = port()
         threads = pt.threads()
