@@ -20,7 +20,8 @@ CSRC = PKG / "csrc"
 BUILD = PKG / "_build"
 LIB = PKG / "libfdmgpu.so"
 ORACLE = ROOT / "oracle"
-REF_SRC = Path(os.environ.get("FDM_REF_SRC", "/root/reference/src"))
+# the reference's src/ directory, for the compiled checker only (optional)
+REF_SRC = Path(os.environ["FDM_REF_SRC"]) if os.environ.get("FDM_REF_SRC") else None
 
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 # host code rounds as written (no contraction into fused multiply-adds), so
@@ -82,8 +83,11 @@ def build_oracle(with_reference: bool = True) -> None:
     """Builds oracle/liboracle.so; also oracle/_ref/libfdm_ref.so from the
     reference sources when that tree exists on this machine."""
     _run(["make", "-s", "-C", str(ORACLE), "liboracle.so"])
-    if with_reference and REF_SRC.is_dir():
-        _run(["make", "-s", "-C", str(ORACLE), "ref", "REF_SRC=%s" % REF_SRC])
+    if with_reference:
+        # the recipe builds it where the reference tree exists (its own default
+        # location, or FDM_REF_SRC)
+        extra = ["REF_SRC=%s" % REF_SRC] if REF_SRC is not None else []
+        _run(["make", "-s", "-C", str(ORACLE), "ref-if-present", *extra])
 
 
 def build_all(force: bool = False) -> None:

@@ -70,20 +70,6 @@ __device__ __forceinline__ double sub_rn(double a, double b) { return __dsub_rn(
 template <>
 __device__ __forceinline__ float sub_rn(float a, float b) { return __fsub_rn(a, b); }
 
-// a / b for finite operands through the correctly rounded reciprocal y of b
-// and two remainder corrections (Markstein's theorem: the result equals the
-// IEEE quotient bit for bit); five FP64 operations instead of a division
-struct CDiv {
-    double b, y;
-};
-static inline CDiv cdiv_of(double b) { return CDiv{b, 1.0 / b}; }
-__device__ __forceinline__ double cdiv(double a, CDiv d) {
-    const double q0 = a * d.y;
-    double q = fma(fma(-q0, d.b, a), d.y, q0);
-    q = fma(fma(-q, d.b, a), d.y, q);
-    return (__double_as_longlong(a) << 1) == 0 ? q0 : q;
-}
-__device__ __forceinline__ CDiv cdiv_dev(double b) { return CDiv{b, 1.0 / b}; }
 // a / b in T: FP64 through cdiv, FP32 by the (fast) IEEE float division
 __device__ __forceinline__ double tdiv(double a, CDiv d) { return cdiv(a, d); }
 __device__ __forceinline__ float tdiv(float a, CDiv d) { return a / (float)d.b; }

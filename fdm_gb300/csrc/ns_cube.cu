@@ -45,36 +45,12 @@ static FieldT<T> make_field(int z1, int z2, int y1, int y2, int x1, int x2) {
     return f;
 }
 
-// A divisor fixed for the whole run and its correctly rounded reciprocal
-// (computed on the host).
-struct CDiv {
-    double b, y;
-};
-
-static CDiv cdiv_of(double b) { return CDiv{b, 1.0 / b}; }
-
 struct NSParams {
     int nx, ny, nz;
     double U0, Re, dt, dx, dy, dz, dx2, dy2, dz2;
     CDiv dRe, ddx, ddy, ddz, ddx2, ddy2, ddz2, ddt;
     double dt_dx, dt_dy, dt_dz;  // dt/dx etc., correctly rounded on the host
 };
-
-// a / d.b correctly rounded, for finite a and quotients and remainders in
-// the normal range: q0 = a*y within two ulps, then two remainder
-// corrections r = a - b q (exact through the fused multiply-add) and
-// q <- q + r y.  After the first q is faithful, and a faithful q with
-// y = RN(1/b) corrects to RN(a/b) (P. Markstein, "Computation of elementary
-// functions on the IBM RISC System/6000 processor", IBM J. Res. Dev. 34,
-// 1990; the correction theorem as stated in J.-M. Muller et al., Handbook
-// of Floating-Point Arithmetic, ch. on division).  Five FP64 operations and
-// no data-dependent slow path; a zero dividend returns its signed zero.
-__device__ __forceinline__ double cdiv(double a, CDiv d) {
-    const double q0 = a * d.y;
-    double q = fma(fma(-q0, d.b, a), d.y, q0);
-    q = fma(fma(-q, d.b, a), d.y, q);
-    return (__double_as_longlong(a) << 1) == 0 ? q0 : q;
-}
 
 __device__ __forceinline__ double sq(double x) { return x * x; }  // asp::sq, src/asp_misc.h:295
 

@@ -27,20 +27,6 @@ namespace fdmgpu {
 
 namespace cyl {
 
-struct CDiv {
-    double b, y;
-};
-static CDiv cdiv_of(double b) { return CDiv{b, 1.0 / b}; }
-
-// a / d.b correctly rounded (Markstein's remainder corrections, as in the
-// NSCube stencils)
-__device__ __forceinline__ double cdiv(double a, CDiv d) {
-    const double q0 = a * d.y;
-    double q = fma(fma(-q0, d.b, a), d.y, q0);
-    q = fma(fma(-q, d.b, a), d.y, q);
-    return (__double_as_longlong(a) << 1) == 0 ? q0 : q;
-}
-
 __device__ __forceinline__ double sq(double x) { return x * x; }  // asp::sq, src/asp_misc.h:295
 
 template <typename T>
@@ -439,10 +425,10 @@ struct NSCylPlan {
             q.rc1 = (q.rc - 0.5 * P.dr) / q.rc;
             q.rcr = q.rc * q.rc;
             q.dtdphi_r = P.dt / P.dphi / q.rc;
-            q.drf = cyl::cdiv_of(q.rf);
-            q.drfr = cyl::cdiv_of(q.rfr);
-            q.drc = cyl::cdiv_of(q.rc);
-            q.drcr = cyl::cdiv_of(q.rcr);
+            q.drf = cdiv_of(q.rf);
+            q.drfr = cdiv_of(q.rfr);
+            q.drc = cdiv_of(q.rc);
+            q.drcr = cdiv_of(q.rcr);
         }
         FDM_CUDA(cudaMemcpy(radii.get(rv.size() * sizeof(cyl::Radii)), rv.data(), rv.size() * sizeof(cyl::Radii),
                             cudaMemcpyHostToDevice));
@@ -576,10 +562,10 @@ void setup_cyl(NSCylPlan<T>& s, int zper, double R, double r0, double h1, double
     P.dr = (R - r0) / nr; P.dz = (h2 - h1) / nz; P.dphi = 2 * M_PI / nphi;
     P.dr2 = P.dr * P.dr; P.dz2 = P.dz * P.dz; P.dphi2 = P.dphi * P.dphi;
     P.Re = Re; P.dt = dt; P.U0 = u0;
-    P.dRe = cyl::cdiv_of(Re);
-    P.ddr = cyl::cdiv_of(P.dr); P.ddz = cyl::cdiv_of(P.dz); P.ddphi = cyl::cdiv_of(P.dphi);
-    P.ddr2 = cyl::cdiv_of(P.dr2); P.ddz2 = cyl::cdiv_of(P.dz2); P.ddphi2 = cyl::cdiv_of(P.dphi2);
-    P.ddt = cyl::cdiv_of(dt);
+    P.dRe = cdiv_of(Re);
+    P.ddr = cdiv_of(P.dr); P.ddz = cdiv_of(P.dz); P.ddphi = cdiv_of(P.dphi);
+    P.ddr2 = cdiv_of(P.dr2); P.ddz2 = cdiv_of(P.dz2); P.ddphi2 = cdiv_of(P.dphi2);
+    P.ddt = cdiv_of(dt);
     P.dt_dr = dt / P.dr; P.dt_dz = dt / P.dz;
     s.init(R, r0, h1, h2);
 }
