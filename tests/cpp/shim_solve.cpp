@@ -6,8 +6,10 @@
 //   shim_solve dirichlet <nx> <ny> <nz> <dx> <dy> <dz> <lx> <ly> <lz> <rhs> <ans>
 //   shim_solve periodic  <nx> <ny> <nz> <dx> <dy> <dz> <lx> <ly> <lz> <rhs> <ans>
 //   shim_solve nscube    <n> <steps> <out_u>
+//   shim_solve nsdriver  <double|float> <n> <steps> <out>   (the cavity driver)
 //   shim_solve cyl       <periodic_z> <nr> <nz> <nphi> <dr> <dz> <r0> <lr> <lz> <rhs> <ans>
 //   shim_solve nscyl     <periodic_z> <nr> <nz> <nphi> <steps> <out_u>
+#include <chrono>
 #include <cstdio>
 #include <cstdlib>
 #include <cstring>
@@ -46,12 +48,14 @@ struct Cfg {
     int n;
     double Re = 250.0;
     int nr = 0, nz = 0, nphi = 0;
+    int steps = 1;
     double get(const char*, const char* key, double def) const {
         if (!strcmp(key, "Re")) return Re;
         if (!strcmp(key, "dt")) return 0.01;
         return def;
     }
     int get(const char*, const char* key, int def) const {
+        if (!strcmp(key, "steps")) return steps;
         if (nr) {
             if (!strcmp(key, "nr")) return nr;
             if (!strcmp(key, "nz")) return nz;
@@ -63,11 +67,38 @@ struct Cfg {
     }
 };
 
+// The reference's cavity driver (test/test_ns_cube.cpp:21-69) without its
+// plotter (plplot): construct from the config, hand the velocity arrays to a
+// consumer, step, time.  Writes time_index, dx, dy, dz, the step count and
+// ns.u.vec (as doubles) to `out`.
+template <typename T, bool check>
+void calc(const Cfg& c, const char* out) {
+    using namespace std::chrono;
+    fdm::NSCube<T, true> ns(c);
+    const int steps = c.get("ns", "steps", 1);
+    const T* uvec = ns.u.vec;  // what the driver gives plot.use(ns.u.vec, ...)
+    auto t1 = steady_clock::now();
+    for (int i = 0; i < steps; i++) ns.step();
+    auto t2 = steady_clock::now();
+    printf("It took me '%f' seconds\n", duration_cast<duration<double>>(t2 - t1).count());
+    std::vector<double> o = {(double)ns.time_index, ns.dx, ns.dy, ns.dz, (double)steps,
+                             (double)ns.u[ns.nz + 1][3][3]};
+    for (int e = 0; e < ns.u.size; e++) o.push_back((double)uvec[e]);
+    write_all(out, o);
+}
+
 }  // namespace
 
 int main(int argc, char** argv) {
     if (argc < 2) return 1;
     const std::string mode = argv[1];
+    if (mode == "nsdriver" && argc == 6) {
+        Cfg c{atoi(argv[3])};
+        c.steps = atoi(argv[4]);
+        if (!strcmp(argv[2], "float")) calc<float, false>(c, argv[5]);
+        else calc<double, false>(c, argv[5]);
+        return 0;
+    }
     if (mode == "nscube" && argc == 5) {
         Cfg c{atoi(argv[2])};
         fdm::NSCube<double, false> ns(c);

@@ -54,6 +54,35 @@ def test_shim_program_matches_reference(tmp_path, native, cuda, golden):
 
 
 @pytest.mark.gpu
+@pytest.mark.parametrize("dtype", ["double", "float"])
+def test_shim_cavity_driver_matches_reference(tmp_path, native, cuda, golden, dtype):
+    """A caller written like the reference's cavity driver (reads ns.dx,
+    ns.u.vec, ns.time_index and ns.u[i][k][j]) compiles against the NSCube
+    shim unchanged and gives the reference's fields after 20 steps, for
+    NSCube<double> and NSCube<float>."""
+    exe = _build(tmp_path, native)
+    ns = golden("ns_cube")
+    out = subprocess.run([str(exe), "nsdriver", dtype, "15", "20", str(tmp_path / "drv")], check=True,
+                         capture_output=True, text=True)
+    assert "It took me" in out.stdout
+    o = np.frombuffer((tmp_path / "drv").read_bytes())
+    assert o[0] == 20 and o[4] == 20  # time_index, steps
+    assert o[1] == o[2] == o[3] == 2 * np.pi / 15  # dx = (x2 - x1) / nx
+    u = o[6:]
+    ref64 = ns["n15_s20_u"]
+    assert u.size == ref64.size
+    if dtype == "double":
+        assert np.abs(u - ref64).max() <= 1e-12 * max(1.0, np.abs(ref64).max())
+    else:
+        # the float cavity's own criterion (test_ns_cube_gpu.py): within ten
+        # times the reference's float-vs-double gap
+        ref32 = ns["f32_n15_s20_u"].astype(np.float64)
+        gap = np.linalg.norm(ref32 - ref64)
+        assert np.linalg.norm(u - ref32) <= 10 * gap + 1e-6 * np.linalg.norm(ref64)
+    assert o[5] == u[(16 * 17 + 3) * 18 + 4]  # ns.u[nz+1][3][3]: z 16, y 3, x 3 (x runs from -1, 18 wide)
+
+
+@pytest.mark.gpu
 def test_shim_cylindrical_matches_reference(tmp_path, native, cuda, golden):
     """fdm::LaplCyl3FFT2 and fdm::NSCyl through the C++ shims against the
     reference's own answers (Dirichlet and periodic z)."""
