@@ -505,10 +505,11 @@ def measure_serving(torch, fdm_gb300, workloads, dev, rates=SERVE_RATES, seconds
 
     ref_sq = {sh: float(np.sum(np.square(r))) for sh, r in ref.items()}
 
-    def check(sh, buf):
-        # relative L2 error of one answer against the FP64 form
+    def check(sh, buf, est):
+        # relative L2 error of one answer against the FP64 form, beside the
+        # server's own estimate of it
         d = buf.numpy() - ref[sh]
-        return sh, buf, math.sqrt(float(np.sum(d * d)) / ref_sq[sh])
+        return sh, buf, math.sqrt(float(np.sum(d * d)) / ref_sq[sh]), est
 
     srv = Server(150e9, lanes=lanes, max_batch=max_batch)
     sess = [srv.session_create(63, 63, Re=(100.0, 250.0, 400.0)[i % 3], dt=0.01) for i in range(64)]
@@ -537,7 +538,7 @@ def measure_serving(torch, fdm_gb300, workloads, dev, rates=SERVE_RATES, seconds
         ks = rng.integers(1, 51, n)
         srv.stats_reset()
         live = {}
-        lat, lat_solve, lat_adv, errs, futs = [], [], [], [], []
+        lat, lat_solve, lat_adv, errs, ests, futs = [], [], [], [], [], []
         i = 0
         t0 = time.perf_counter()
         t_last = t0
@@ -565,22 +566,24 @@ def measure_serving(torch, fdm_gb300, workloads, dev, rates=SERVE_RATES, seconds
                 t_last = time.perf_counter()
                 if sh:
                     lat_solve.append(l_ms)
-                    futs.append(pool.submit(check, sh, b))
+                    futs.append(pool.submit(check, sh, b, rec["err_est"]))
                 else:
                     lat_adv.append(l_ms)
                 rec = srv.next_done(0.0) if live else None
             keep = []
             for fu in futs:
                 if fu.done():
-                    sh, b, e = fu.result()
+                    sh, b, e, es = fu.result()
                     errs.append(e)
+                    ests.append(es)
                     free[sh].append(b)
                 else:
                     keep.append(fu)
             futs = keep
         for fu in futs:
-            sh, b, e = fu.result()
+            sh, b, e, es = fu.result()
             errs.append(e)
+            ests.append(es)
             free[sh].append(b)
         wall = t_last - t0
         st = srv.stats()
@@ -594,6 +597,9 @@ def measure_serving(torch, fdm_gb300, workloads, dev, rates=SERVE_RATES, seconds
             "p50_advance_ms": pct(lat_adv, 50), "p99_advance_ms": pct(lat_adv, 99),
             "solve_err_vs_fp64_max": max(errs) if errs else None,
             "solve_err_vs_fp64_median": pct(errs, 50), "solves_checked": len(errs),
+            "solve_err_est_max": max(ests) if ests else None,
+            "solve_err_est_bounds_fraction": (sum(1 for e, es in zip(errs, ests) if es >= e) / len(errs))
+            if errs else None,
             "solve_launches": st["batches"], "solves_batched": st["batched_requests"],
             "peak_device_gb": st["peak_bytes"] / 1e9, "mean_queue_ms": st["mean_queue_ms"],
         })
@@ -712,6 +718,13 @@ def main():
     stream.synchronize()
     errs = [(torch.linalg.norm(out[i] - ref64[i]) / torch.linalg.norm(ref64[i])).item() for i in range(NRHS)]
     sweeps, est = mixed.last_info(NRHS)
+    # the closed loop: a handle that checks every right-hand side's estimate
+    # and sweeps again while one exceeds tol (the estimates bound the errors)
+    adaptive = fdm_gb300.LaplCube(*sargs, precision="mixed", tol=TOL, adaptive=True)
+    out2 = torch.empty_like(out)
+    adaptive.solve_device(out2, f, nrhs=NRHS, stream=stream)
+    a_sweeps, a_est = adaptive.last_info(NRHS)
+    del out2, adaptive
     del ref64
     torch.cuda.empty_cache()
 
@@ -833,7 +846,10 @@ def main():
                    "l2_flush": "inputs 2.1 GB per step > 135 MB L2", "parallelism": "replicas%d" % world,
                    "rhs_per_call": chunk},
         "accuracy": {"rel_l2_vs_fp64_gpu_max": max(errs), "rel_l2_vs_fp64_gpu_median": statistics.median(errs),
-                     "sweeps": sweeps, "correction_estimate_max": max(est)},
+                     "sweeps": sweeps, "error_estimate_max": max(est),
+                     "error_estimate_per_rhs": est, "error_per_rhs": errs,
+                     "estimate_bounds_error": all(e >= x for e, x in zip(est, errs)),
+                     "adaptive": {"sweeps": a_sweeps, "error_estimate_max": max(a_est)}},
         "latency_ms_per_solve": step_ms / NRHS,
         "unixbench_ms_per_step": unixbench_score(step_ms_samples),
         "pipeline": mixed.pipeline_in_use(),

@@ -69,6 +69,7 @@ _SIGS = [
     ("fdmgpu_lapl_cube_scratch_bytes", c_int, [c_void_p, POINTER(c_size_t)]),
     ("fdmgpu_lapl_cube_set_schedule", c_int, [c_void_p, c_int, c_int]),
     ("fdmgpu_lapl_cube_set_pipeline", c_int, [c_void_p, c_int]),
+    ("fdmgpu_lapl_cube_set_refinement", c_int, [c_void_p, c_int]),
     ("fdmgpu_lapl_cube_pipeline_in_use", c_int, [c_void_p, POINTER(c_int)]),
     ("fdmgpu_lapl_cube_device_status", c_int, [c_void_p, POINTER(c_int)]),
     ("fdmgpu_lapl_cube_destroy", c_int, [c_void_p]),
@@ -142,13 +143,14 @@ _SIGS = [
     ("fdmgpu_server_session_create", c_int, [c_void_p, POINTER(c_int), c_int, c_int] + [c_double] * 9),
     ("fdmgpu_server_submit_advance", c_int, [c_void_p, POINTER(c_ulonglong), c_int, c_int]),
     ("fdmgpu_server_poll", c_int,
-     [c_void_p, c_ulonglong, POINTER(c_int), POINTER(c_int), POINTER(c_double), POINTER(c_double), POINTER(c_int)]),
+     [c_void_p, c_ulonglong, POINTER(c_int), POINTER(c_int), POINTER(c_double), POINTER(c_double), POINTER(c_int),
+      POINTER(c_double)]),
     ("fdmgpu_server_wait", c_int,
      [c_void_p, c_ulonglong, c_double, POINTER(c_int), POINTER(c_int), POINTER(c_double), POINTER(c_double),
-      POINTER(c_int)]),
+      POINTER(c_int), POINTER(c_double)]),
     ("fdmgpu_server_next_done", c_int,
      [c_void_p, c_double, POINTER(c_ulonglong), POINTER(c_int), POINTER(c_int), POINTER(c_double),
-      POINTER(c_double), POINTER(c_int)]),
+      POINTER(c_double), POINTER(c_int), POINTER(c_double)]),
     ("fdmgpu_server_cancel", c_int, [c_void_p, c_ulonglong]),
     ("fdmgpu_server_session_get_field", c_int,
      [c_void_p, c_int, c_int, c_void_p, c_size_t, POINTER(c_longlong), c_double]),

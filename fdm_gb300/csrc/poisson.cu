@@ -709,7 +709,8 @@ struct CubePlan {
         hz_eff = (nz == ny) ? dy : dz;
         zfac = dz * slz * slz * (nz + 1) / 2.0;
         S = (dx * slx * slx * (nx + 1) / 2.0) * (dy * sly * sly * (ny + 1) / 2.0) * zfac;
-        mixed_ok = lapl_kappa(nx, ny, nz, hx_eff, dy, hz_eff) <= kMixedKappaMax;
+        kappa = lapl_kappa(nx, ny, nz, hx_eff, dy, hz_eff);
+        mixed_ok = kappa <= kMixedKappaMax;
         if (dtype == FDMGPU_F64) {
             tx64.build(nx + 1);
             ty64.build(ny + 1);
@@ -802,6 +803,7 @@ struct CubePlan {
 
     void solve_device(void* ans, const void* rhs, int nrhs, cudaStream_t st) {
         check_grid_y(nrhs);
+        last_est.clear();
         last_stream = st;
         last_nrhs = nrhs;
         if (periodic) {
@@ -840,96 +842,92 @@ struct CubePlan {
         return ff{h, (float)(v - (double)h)};
     }
 
-    // Mixed solve of nrhs volumes.  With vin / vout (device arrays of nrhs
-    // user pointers) the FP64 input and output volumes are addressed through
-    // them and rhs / ans are not used; the FP32 scratch stays contiguous.
-    // Mixed solve with the fused plane pass: per sweep DST-y, the x-z plane
-    // pass, inverse DST-y.  The x and y transforms commute, so this is the
-    // same operator as run_mixed's x, y, z, y, x order.
-    void run_mixed_planes(double* ans, const double* rhs, int nrhs, cudaStream_t st, const void* const* vin,
-                          void* const* vout) {
-        const long long V = vol() * nrhs;
-        const int sweeps = sweeps_for_tol();
-        last_sweeps = sweeps;
-        float* W = (float*)work32.get(V * sizeof(float));
-        const float* tab = (const float*)ztab32.p;
-        const double gscale = zfac * hz_eff * hz_eff;
-        SineFused fin;
-        memset(&fin, 0, sizeof(fin));
-        fin.vin = vin;
-        launch_sine<double, float, float, 1, kRound>(rhs, W, nx, ny, nz, nrhs, ty32.view(), scy, st, &fin);
-        launch_plane(W, nx, ny, nz, nrhs, tx32.view(), scx, gscale, slx, tab, st);
-        if (sweeps == 0) {
-            SineFused fo;
-            memset(&fo, 0, sizeof(fo));
-            fo.vout = vout;
-            launch_sine<float, float, double, 1>(W, ans, nx, ny, nz, nrhs, ty32.view(), sly, st, &fo);
-            return;
-        }
-        float* UH = (float*)uhi.get(V * sizeof(float));
-        float* UL = sweeps > 1 ? (float*)ulo.get(V * sizeof(float)) : nullptr;
-        double* NR = (double*)norms.get((size_t)2 * nrhs * sweeps * sizeof(double));
-        FDM_CUDA(cudaMemsetAsync(NR, 0, (size_t)2 * nrhs * sweeps * sizeof(double), st));
-        launch_sine<float, float, float, 1>(W, UH, nx, ny, nz, nrhs, ty32.view(), sly, st);
-        const double cx = 1.0 / (hx_eff * hx_eff) / S, cy = 1.0 / (dy * dy) / S, cz = 1.0 / (hz_eff * hz_eff) / S;
-        for (int s = 1; s <= sweeps; s++) {
-            SineFused fr;
-            memset(&fr, 0, sizeof(fr));
-            fr.f = rhs;
-            fr.vin = vin;
-            fr.uhi = UH;
-            fr.ulo = s >= 2 ? UL : nullptr;
-            fr.cx = split_host(cx); fr.cy = split_host(cy); fr.cz = split_host(cz);
-            fr.cxf = (float)cx; fr.cyf = (float)cy; fr.czf = (float)cz;
-            fr.iso = (cx == cy && cy == cz) ? 1 : 0;
-            launch_residual(fr, W, nx, ny, nz, nrhs, st);
-            launch_sine<float, float, float, 1>(W, W, nx, ny, nz, nrhs, ty32.view(), scy, st);
-            launch_plane(W, nx, ny, nz, nrhs, tx32.view(), scx, gscale, slx, tab, st);
-            SineFused fc;
-            memset(&fc, 0, sizeof(fc));
-            fc.uhi = UH;
-            fc.ulo = s >= 2 ? UL : nullptr;
-            fc.out64 = ans;
-            fc.vout = vout;
-            fc.ulo_out = UL;
-            fc.last = s == sweeps ? 1 : 0;
-            fc.norms = NR + (size_t)2 * nrhs * (s - 1);
-            launch_sine<float, float, float, 1, kCombine>(W, (float*)nullptr, nx, ny, nz, nrhs, ty32.view(), sly,
-                                                          st, &fc);
+    // Model of the error left after a refinement sweep.  Sweep k measures
+    // e_k = ||c_k|| / ||u||, the relative size of its correction, which is
+    // the error of the solution before it.  The error after it is the larger
+    // of rho e_k, rho the contraction of a sweep, and the floor the
+    // float-float residual allows, kFloorPerKappa times the operator's
+    // eigenvalue ratio kappa.  From two sweeps rho = e_k / e_{k-1}; after the
+    // first, rho = kRhoPerErr e_1 (an FP32 inner solve that leaves a relative
+    // error e on u leaves a multiple of e on the rougher correction).
+    // Measured on GB300 over 16 cases (31^3 to 255^3, anisotropic spacings,
+    // smooth and white-noise data; relative L2 against the FP64 form): error
+    // after one sweep / e_1^2 between 2.5 and 44, error after two sweeps /
+    // kappa between 1.1e-17 and 6.7e-17.  The constants keep a margin of 2.3
+    // and 1.5 over those.
+    static constexpr double kRhoPerErr = 100.0;
+    static constexpr double kFloorPerKappa = 1e-16;
+    double kappa = 0.0;  // largest over smallest eigenvalue, summed over the axes
+    double est_after(double ek, double ekm1, int k) const {
+        if (ek <= 0.0) return kFloorPerKappa * kappa;
+        const double rho = k >= 2 && ekm1 > 0.0 ? std::min(1.0, ek / ekm1) : std::min(1.0, kRhoPerErr * ek);
+        return std::max(rho * ek, kFloorPerKappa * kappa);
+    }
+    // estimates of the nrhs right-hand sides from their norms after `sweeps`
+    // sweeps (host copy of the norms buffer, layout [sweep][rhs][c2, u2])
+    void estimates_from_norms(const double* v, int nrhs, int sweeps, double* est) const {
+        for (int i = 0; i < nrhs; i++) {
+            if (sweeps <= 0) {
+                est[i] = -1.0;
+                continue;
+            }
+            auto e = [&](int k) {  // e_k, k = 1..sweeps
+                const double c2 = v[(size_t)2 * nrhs * (k - 1) + 2 * i], u2 = v[(size_t)2 * nrhs * (k - 1) + 2 * i + 1];
+                return u2 > 0 ? std::sqrt(c2 / u2) : 0.0;
+            };
+            est[i] = est_after(e(sweeps), sweeps >= 2 ? e(sweeps - 1) : 0.0, sweeps);
         }
     }
+    int refine_adaptive = 0;       // 1: extra sweeps while an estimate exceeds tol (synchronises)
+    std::vector<double> last_est;  // per RHS, filled by an adaptive solve
 
-    void run_mixed(double* ans, const double* rhs, int nrhs, cudaStream_t st, const void* const* vin = nullptr,
-                   void* const* vout = nullptr) {
-        ensure_mixed_tables();
-        if (plane_ok()) return run_mixed_planes(ans, rhs, nrhs, st, vin, vout);
+    // final estimates of the last solve (synchronises st)
+    std::vector<double> final_estimates(int nrhs, int sweeps, cudaStream_t st) const {
+        std::vector<double> out(nrhs, -1.0);
+        if (sweeps <= 0 || !norms.p) return out;
+        std::vector<double> v((size_t)2 * nrhs * sweeps);
+        FDM_CUDA(cudaStreamSynchronize(st));
+        FDM_CUDA(cudaMemcpy(v.data(), norms.p, v.size() * sizeof(double), cudaMemcpyDeviceToHost));
+        estimates_from_norms(v.data(), nrhs, sweeps, out.data());
+        return out;
+    }
+
+    // The passes of one mixed pipeline: `first` takes the FP64 right-hand
+    // sides to the FP32 work volume one pass short of the solution, `last`
+    // applies that final pass (T_out = the FP64 output or UH), `inner` takes
+    // the residual in W to the correction one pass short, `combine` applies
+    // the final pass and adds the correction.
+    template <typename First, typename Last, typename Inner, typename Combine>
+    void sweep_loop(double* ans, const double* rhs, int nrhs, cudaStream_t st, const void* const* vin,
+                    void* const* vout, First first, Last last, Inner inner, Combine combine) {
         const long long V = vol() * nrhs;
         const int sweeps = sweeps_for_tol();
         last_sweeps = sweeps;
+        last_est.clear();
         float* W = (float*)work32.get(V * sizeof(float));
-        SineFused fin;
-        memset(&fin, 0, sizeof(fin));
-        fin.vin = vin;
-        launch_sine<double, float, float, 0, kRound>(rhs, W, nx, ny, nz, nrhs, tx32.view(), scx, st, &fin);
-        sine32<1>(W, W, nrhs, scy, st);
-        zsolve<float>(W, nrhs, lamx32, lamy32, st);
-        sine32<1>(W, W, nrhs, sly, st);
+        first(W);
         if (sweeps == 0) {
             SineFused fo;
             memset(&fo, 0, sizeof(fo));
             fo.vout = vout;
-            launch_sine<float, float, double, 0>(W, ans, nx, ny, nz, nrhs, tx32.view(), slx, st, &fo);
+            last(W, (double*)ans, (float*)nullptr, fo);
             return;
         }
+        const bool adaptive = refine_adaptive && max_sweeps > sweeps;
+        const int cap = adaptive ? max_sweeps : sweeps;
         float* UH = (float*)uhi.get(V * sizeof(float));
-        float* UL = sweeps > 1 ? (float*)ulo.get(V * sizeof(float)) : nullptr;
-        double* NR = (double*)norms.get((size_t)2 * nrhs * sweeps * sizeof(double));
-        FDM_CUDA(cudaMemsetAsync(NR, 0, (size_t)2 * nrhs * sweeps * sizeof(double), st));
-        sine32<0>(W, UH, nrhs, slx, st);
+        float* UL = (sweeps > 1 || adaptive) ? (float*)ulo.get(V * sizeof(float)) : nullptr;
+        double* NR = (double*)norms.get((size_t)2 * nrhs * cap * sizeof(double));
+        FDM_CUDA(cudaMemsetAsync(NR, 0, (size_t)2 * nrhs * cap * sizeof(double), st));
+        {
+            SineFused fo;
+            memset(&fo, 0, sizeof(fo));
+            last(W, (double*)nullptr, UH, fo);
+        }
         // r = f - A u / S: the inner solve multiplies by S again, so it
         // returns the correction S A^-1 f - u
         const double cx = 1.0 / (hx_eff * hx_eff) / S, cy = 1.0 / (dy * dy) / S, cz = 1.0 / (hz_eff * hz_eff) / S;
-        for (int s = 1; s <= sweeps; s++) {
+        auto sweep = [&](int s, bool is_last, bool keep) {
             SineFused fr;
             memset(&fr, 0, sizeof(fr));
             fr.f = rhs;
@@ -940,22 +938,93 @@ struct CubePlan {
             fr.cxf = (float)cx; fr.cyf = (float)cy; fr.czf = (float)cz;
             fr.iso = (cx == cy && cy == cz) ? 1 : 0;
             launch_residual(fr, W, nx, ny, nz, nrhs, st);
-            sine32<0>(W, W, nrhs, scx, st);
-            sine32<1>(W, W, nrhs, scy, st);
-            zsolve<float>(W, nrhs, lamx32, lamy32, st);
-            sine32<1>(W, W, nrhs, sly, st);
+            inner(W);
             SineFused fc;
             memset(&fc, 0, sizeof(fc));
             fc.uhi = UH;
             fc.ulo = s >= 2 ? UL : nullptr;
             fc.out64 = ans;
             fc.vout = vout;
-            fc.ulo_out = UL;
-            fc.last = s == sweeps ? 1 : 0;
+            fc.ulo_out = (!is_last || keep) ? UL : nullptr;
+            fc.last = is_last ? 1 : 0;
             fc.norms = NR + (size_t)2 * nrhs * (s - 1);
-            launch_sine<float, float, float, 0, kCombine>(W, (float*)nullptr, nx, ny, nz, nrhs, tx32.view(), slx,
-                                                          st, &fc);
+            combine(W, fc);
+        };
+        for (int s = 1; s <= sweeps; s++) sweep(s, s == sweeps, adaptive);
+        if (!adaptive) return;
+        // closed loop: more sweeps while a right-hand side's estimated
+        // remaining error exceeds tol
+        int done = sweeps;
+        for (;;) {
+            last_est = final_estimates(nrhs, done, st);
+            const double worst = *std::max_element(last_est.begin(), last_est.end());
+            if (worst <= tol || done >= cap) break;
+            done++;
+            sweep(done, true, done < cap);
+            last_sweeps = done;
         }
+    }
+
+    // Mixed solve of nrhs volumes.  With vin / vout (device arrays of nrhs
+    // user pointers) the FP64 input and output volumes are addressed through
+    // them and rhs / ans are not used; the FP32 scratch stays contiguous.
+    // With the fused plane pass: DST-y, the x-z plane pass, inverse DST-y
+    // (the x and y transforms commute, so it is the same operator as the x,
+    // y, z, y, x order of the five-pass form).
+    void run_mixed(double* ans, const double* rhs, int nrhs, cudaStream_t st, const void* const* vin = nullptr,
+                   void* const* vout = nullptr) {
+        ensure_mixed_tables();
+        if (plane_ok()) {
+            const float* tab = (const float*)ztab32.p;
+            const double gscale = zfac * hz_eff * hz_eff;
+            sweep_loop(
+                ans, rhs, nrhs, st, vin, vout,
+                [&](float* W) {
+                    SineFused fin;
+                    memset(&fin, 0, sizeof(fin));
+                    fin.vin = vin;
+                    launch_sine<double, float, float, 1, kRound>(rhs, W, nx, ny, nz, nrhs, ty32.view(), scy, st, &fin);
+                    launch_plane(W, nx, ny, nz, nrhs, tx32.view(), scx, gscale, slx, tab, st);
+                },
+                [&](float* W, double* o64, float* o32, const SineFused& fo) {
+                    if (o64) launch_sine<float, float, double, 1>(W, o64, nx, ny, nz, nrhs, ty32.view(), sly, st, &fo);
+                    else launch_sine<float, float, float, 1>(W, o32, nx, ny, nz, nrhs, ty32.view(), sly, st);
+                },
+                [&](float* W) {
+                    launch_sine<float, float, float, 1>(W, W, nx, ny, nz, nrhs, ty32.view(), scy, st);
+                    launch_plane(W, nx, ny, nz, nrhs, tx32.view(), scx, gscale, slx, tab, st);
+                },
+                [&](float* W, const SineFused& fc) {
+                    launch_sine<float, float, float, 1, kCombine>(W, (float*)nullptr, nx, ny, nz, nrhs, ty32.view(),
+                                                                  sly, st, &fc);
+                });
+            return;
+        }
+        sweep_loop(
+            ans, rhs, nrhs, st, vin, vout,
+            [&](float* W) {
+                SineFused fin;
+                memset(&fin, 0, sizeof(fin));
+                fin.vin = vin;
+                launch_sine<double, float, float, 0, kRound>(rhs, W, nx, ny, nz, nrhs, tx32.view(), scx, st, &fin);
+                sine32<1>(W, W, nrhs, scy, st);
+                zsolve<float>(W, nrhs, lamx32, lamy32, st);
+                sine32<1>(W, W, nrhs, sly, st);
+            },
+            [&](float* W, double* o64, float* o32, const SineFused& fo) {
+                if (o64) launch_sine<float, float, double, 0>(W, o64, nx, ny, nz, nrhs, tx32.view(), slx, st, &fo);
+                else sine32<0>(W, o32, nrhs, slx, st);
+            },
+            [&](float* W) {
+                sine32<0>(W, W, nrhs, scx, st);
+                sine32<1>(W, W, nrhs, scy, st);
+                zsolve<float>(W, nrhs, lamx32, lamy32, st);
+                sine32<1>(W, W, nrhs, sly, st);
+            },
+            [&](float* W, const SineFused& fc) {
+                launch_sine<float, float, float, 0, kCombine>(W, (float*)nullptr, nx, ny, nz, nrhs, tx32.view(), slx,
+                                                              st, &fc);
+            });
     }
 
     // Plain FP64 solve through pointer tables: first pass from the user
@@ -1719,7 +1788,7 @@ static void noalloc_solve(double dx, double dy, double dz, double lx, double ly,
         fc.uhi = UH;
         fc.ulo = s >= 2 ? UL : nullptr;
         fc.out64 = ans;
-        fc.ulo_out = UL;
+        fc.ulo_out = s < sweeps ? UL : nullptr;
         fc.last = s == sweeps ? 1 : 0;
         fc.norms = NR + (size_t)2 * nrhs * (s - 1);
         launch_sine<float, float, float, 0, kCombine>(W, (float*)nullptr, nx, ny, nz, nrhs, tx, slx, st, &fc);
@@ -1728,6 +1797,18 @@ static void noalloc_solve(double dx, double dy, double dz, double lx, double ly,
 
 void cube_solve_device(fdmgpu_lapl_cube* h, void* ans, const void* rhs, int nrhs, cudaStream_t st) {
     h->plan.solve_device(ans, rhs, nrhs, st);
+}
+
+int cube_norms_async(fdmgpu_lapl_cube* h, double* host, int nrhs, cudaStream_t st) {
+    const CubePlan& c = h->plan;
+    if (c.last_sweeps <= 0 || !c.norms.p) return c.last_sweeps;
+    FDM_CUDA(cudaMemcpyAsync(host, c.norms.p, (size_t)2 * nrhs * c.last_sweeps * sizeof(double),
+                             cudaMemcpyDeviceToHost, st));
+    return c.last_sweeps;
+}
+
+void cube_estimates(const fdmgpu_lapl_cube* h, const double* norms_host, int sweeps, int nrhs, double* est) {
+    h->plan.estimates_from_norms(norms_host, nrhs, sweeps, est);
 }
 
 void cyl_solve_device(fdmgpu_lapl_cyl* h, void* ans, const void* rhs, int nrhs, cudaStream_t st) {
@@ -1867,14 +1948,10 @@ int fdmgpu_lapl_cube_last_info(fdmgpu_lapl_cube* h, int* sweeps, double* est, in
     if (sweeps) *sweeps = c.last_sweeps;
     if (est) {
         if (nrhs > c.last_nrhs) FDM_FAIL(FDMGPU_EINVAL, "asked for %d estimates, last solve had %d", nrhs, c.last_nrhs);
-        if (c.last_sweeps <= 0) {
-            for (int i = 0; i < nrhs; i++) est[i] = -1.0;
-        } else {
-            std::vector<double> v((size_t)2 * c.last_nrhs);
-            FDM_CUDA(cudaMemcpy(v.data(), (double*)c.norms.p + (size_t)2 * c.last_nrhs * (c.last_sweeps - 1),
-                                v.size() * sizeof(double), cudaMemcpyDeviceToHost));
-            for (int i = 0; i < nrhs; i++) est[i] = v[2 * i + 1] > 0 ? std::sqrt(v[2 * i] / v[2 * i + 1]) : 0.0;
-        }
+        const std::vector<double> e = (int)c.last_est.size() == c.last_nrhs
+                                          ? c.last_est
+                                          : c.final_estimates(c.last_nrhs, c.last_sweeps, c.last_stream);
+        for (int i = 0; i < nrhs; i++) est[i] = e[i];
     }
     FDM_API_END
 }
@@ -2205,6 +2282,14 @@ int fdmgpu_lapl_cube_set_schedule(fdmgpu_lapl_cube* h, int ztable, int dst_tc) {
     if ((ztable != 0 && ztable != 1) || dst_tc < 0 || dst_tc > 3) FDM_FAIL(FDMGPU_EINVAL, "ztable 0/1, dst_tc 0..3");
     h->plan.zmode = ztable;
     h->plan.dst_tc = dst_tc;
+    FDM_API_END
+}
+
+int fdmgpu_lapl_cube_set_refinement(fdmgpu_lapl_cube* h, int adaptive) {
+    FDM_API_BEGIN
+    if (!h) FDM_FAIL(FDMGPU_EINVAL, "null handle");
+    if (adaptive != 0 && adaptive != 1) FDM_FAIL(FDMGPU_EINVAL, "adaptive must be 0 or 1");
+    h->plan.refine_adaptive = adaptive;
     FDM_API_END
 }
 

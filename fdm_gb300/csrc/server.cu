@@ -32,6 +32,7 @@
 #include <algorithm>
 
 #include "internal.h"
+#include "poisson.h"
 
 namespace fdmgpu {
 namespace serve {
@@ -76,6 +77,7 @@ struct Request {
     int steps = 0;
     double t_submit = 0, t_start = 0, t_done = 0;
     int batch = 1;  // requests in the launch this one ran in
+    double err_est = -1.0;  // solves: estimated relative error of the answer (-1: none)
 };
 
 struct Plan {
@@ -113,6 +115,8 @@ struct Lane {
     std::unique_ptr<Plan> plan;  // plan in use (solves)
     size_t staged = 0;           // staging bytes reserved by this launch
     double t_done = 0;
+    double* norms_host = nullptr;  // page-locked copy of the launch's refinement norms
+    int sweeps = 0;                // sweeps of the launch's solve (0: none, -1: FP64)
 };
 
 struct Server {
@@ -170,6 +174,20 @@ struct Server {
     }
 
     void finish_lane(Lane* L) {  // under mq; no CUDA calls
+        // per-request error estimates of a solve launch from the norms the
+        // lane copied back (host arithmetic)
+        if (L->plan && !L->reqs.empty() && L->reqs[0]->kind == FDMGPU_REQ_SOLVE) {
+            const int nb = (int)L->reqs.size();
+            double est[64];
+            if (L->sweeps > 0 && nb <= 64) {
+                cube_estimates(L->plan->h, L->norms_host, L->sweeps, nb, est);
+                for (int i = 0; i < nb; i++) L->reqs[i]->err_est = est[i];
+            } else {
+                // FP64 solves (tol <= 0, or a mixed plan beyond its
+                // conditioning limit) carry no refinement error
+                for (Request* r : L->reqs) r->err_est = (r->key.sweeps < 0 || L->sweeps < 0) ? 0.0 : -1.0;
+            }
+        }
         for (Request* r : L->reqs) {
             r->t_done = L->t_done;
             finished.push_back(r->id);
@@ -405,6 +423,15 @@ struct Server {
         }
         code = fdmgpu_lapl_cube_solve_device(a.plan->h, dout, din, nb, L->st);
         if (code) err = fdmgpu_last_error();
+        L->sweeps = 0;
+        if (!code) {
+            try {
+                L->sweeps = cube_norms_async(a.plan->h, L->norms_host, nb, L->st);
+            } catch (const Error& ex) {
+                code = ex.code;
+                err = fdmgpu_last_error();
+            }
+        }
         for (int i = 0; !code && i < nb; i++) {
             e = cudaMemcpyAsync(a.batch[i]->ans, (char*)dout + vb * i, vb, cudaMemcpyDeviceToHost, L->st);
             if (e != cudaSuccess) {
@@ -454,6 +481,10 @@ struct Server {
             lanes[i].srv = this;
             lanes[i].index = i;
             FDM_CUDA(cudaStreamCreateWithFlags(&lanes[i].st, cudaStreamNonBlocking));
+            // refinement norms of one launch: 2 doubles per right-hand side
+            // per sweep (at most 3 sweeps)
+            FDM_CUDA(cudaHostAlloc(&lanes[i].norms_host, sizeof(double) * 2 * 3 * (size_t)max_batch,
+                                   cudaHostAllocDefault));
         }
         thread = std::thread([this] { loop(); });
     }
@@ -473,8 +504,10 @@ struct Server {
         if (thread.joinable()) thread.join();
         idle.clear();
         sessions.clear();
-        for (auto& L : lanes)
+        for (auto& L : lanes) {
             if (L.st) cudaStreamDestroy(L.st);
+            if (L.norms_host) cudaFreeHost(L.norms_host);
+        }
         if (pool) cudaMemPoolDestroy(pool);
     }
 
@@ -504,7 +537,8 @@ struct fdmgpu_server {
 };
 
 static void read_request(const Request& r, int* state, int* status, double* latency_ms, double* queue_ms,
-                         int* batch) {
+                         int* batch, double* err_est) {
+    if (err_est) *err_est = r.state == FDMGPU_REQ_DONE ? r.err_est : -1.0;
     if (state) *state = r.state;
     if (status) *status = r.status;
     const bool fin = r.state == FDMGPU_REQ_DONE || r.state == FDMGPU_REQ_FAILED;
@@ -668,20 +702,20 @@ int fdmgpu_server_submit_advance(fdmgpu_server* h, unsigned long long* id, int s
 }
 
 int fdmgpu_server_poll(fdmgpu_server* h, unsigned long long id, int* state, int* status, double* latency_ms,
-                       double* queue_ms, int* batch) {
+                       double* queue_ms, int* batch, double* err_est) {
     FDM_API_BEGIN
     if (!h) FDM_FAIL(FDMGPU_EINVAL, "null handle");
     Server& s = h->s;
     std::lock_guard<std::mutex> g(s.mq);
     auto it = s.reqs.find(id);
     if (it == s.reqs.end()) FDM_FAIL(FDMGPU_EINVAL, "no request %llu (finished requests are reported once)", id);
-    read_request(*it->second, state, status, latency_ms, queue_ms, batch);
+    read_request(*it->second, state, status, latency_ms, queue_ms, batch, err_est);
     if (final_state(it->second->state)) retire(s, id);
     FDM_API_END
 }
 
 int fdmgpu_server_wait(fdmgpu_server* h, unsigned long long id, double timeout_ms, int* state, int* status,
-                       double* latency_ms, double* queue_ms, int* batch) {
+                       double* latency_ms, double* queue_ms, int* batch, double* err_est) {
     FDM_API_BEGIN
     if (!h) FDM_FAIL(FDMGPU_EINVAL, "null handle");
     Server& s = h->s;
@@ -692,11 +726,11 @@ int fdmgpu_server_wait(fdmgpu_server* h, unsigned long long id, double timeout_m
     const auto until = std::chrono::steady_clock::now() + std::chrono::duration<double, std::milli>(timeout_ms);
     while (!final_state(r->state)) {
         if (s.cv_done.wait_until(lk, until) == std::cv_status::timeout && !final_state(r->state)) {
-            read_request(*r, state, status, latency_ms, queue_ms, batch);
+            read_request(*r, state, status, latency_ms, queue_ms, batch, err_est);
             FDM_FAIL(FDMGPU_ETIMEOUT, "request %llu not finished after %.0f ms", id, timeout_ms);
         }
     }
-    read_request(*r, state, status, latency_ms, queue_ms, batch);
+    read_request(*r, state, status, latency_ms, queue_ms, batch, err_est);
     retire(s, id);
     FDM_API_END
 }
@@ -719,7 +753,7 @@ int fdmgpu_server_cancel(fdmgpu_server* h, unsigned long long id) {
 }
 
 int fdmgpu_server_next_done(fdmgpu_server* h, double timeout_ms, unsigned long long* id, int* state, int* status,
-                            double* latency_ms, double* queue_ms, int* batch) {
+                            double* latency_ms, double* queue_ms, int* batch, double* err_est) {
     FDM_API_BEGIN
     if (!h || !id) FDM_FAIL(FDMGPU_EINVAL, "null argument");
     Server& s = h->s;
@@ -732,7 +766,7 @@ int fdmgpu_server_next_done(fdmgpu_server* h, double timeout_ms, unsigned long l
             auto it = s.reqs.find(f);
             if (it == s.reqs.end()) continue;  // already reported by poll or wait
             *id = f;
-            read_request(*it->second, state, status, latency_ms, queue_ms, batch);
+            read_request(*it->second, state, status, latency_ms, queue_ms, batch, err_est);
             retire(s, f);
             return FDMGPU_OK;
         }

@@ -228,8 +228,8 @@ struct SineFused {
     int iso;              // cx == cy == cz: one coefficient times the 6-neighbour sum
     // kCombine
     double* out64;
-    float* ulo_out;
-    int last;
+    float* ulo_out;  // when set: ulo += c (the float low part of u, kept for a further sweep)
+    int last;        // write u = uhi + ulo + c to the FP64 output
     double* norms;  // per volume: ||c||^2, ||u||^2
     // optional per-volume pointers (device arrays indexed by blockIdx.y) for
     // the user-facing input (kRound / kPlain loads, the residual's f) and
@@ -497,7 +497,7 @@ __global__ void __launch_bounds__(256) k_sine_pass(const Tin* in, Tout* out, Sin
                 ff s = two_sum(h, lo);
                 s = ff_add_f(s, cv);
                 if (fu.last) (fu.vout ? (double*)fu.vout[blockIdx.y] - voff : fu.out64)[idx] = ff_to_f64(s);
-                else fu.ulo_out[idx] = lo + cv;
+                if (fu.ulo_out) fu.ulo_out[idx] = lo + cv;
                 cc += cv * cv;
                 uu += s.h * s.h;
             }

@@ -49,7 +49,14 @@ struct RgGeom {
     static constexpr int RS0 = TR > CS ? (TR > M ? TR : M) : (CS > M ? CS : M);
     // line stride in slots: 8 (mod 16) for the row pass so the two lines of
     // a half-warp use disjoint bank pairs; odd for the column pass, whose
-    // load and store walk across lines
+    // load and store walk across lines.  Pass 2 and the unpack still meet
+    // two-way conflicts between the two lines of a half-warp (they want an
+    // odd, resp. 4 (mod 8), offset between them).  A layout without padding
+    // whose views XOR the slot with a per-line mask removes most of them
+    // (37 % fewer shared-memory wavefronts at 256 points in a bank model),
+    // but measured slower on GB300 (x pass 1.56 -> 1.72 ms, y pass 1.45 ->
+    // 1.52 ms per 16 x 255^3 pair) while the passes were bound by integer
+    // index arithmetic.
     static constexpr int LS2 = AXIS == 0 ? ((RS0 + 7) / 16 * 16 + 8) : (RS0 | 1);
 };
 
@@ -451,7 +458,7 @@ __device__ __forceinline__ void sine_rg_body(const Tin* in, Tout* out, const Sin
             double* o64 = (fu.vout ? (double*)fu.vout[blockIdx.y] : fu.out64 + voff) + base;
             const float* uh = fu.uhi + voff + base;
             const float* ul = fu.ulo ? fu.ulo + voff + base : nullptr;
-            float* ulo_out = fu.last ? nullptr : fu.ulo_out + voff + base;
+            float* ulo_out = fu.ulo_out ? fu.ulo_out + voff + base : nullptr;
 #pragma unroll
             for (int q0 = 0; q0 < QS; q0 += 2) {
                 float hv[4], lw[4];
@@ -477,7 +484,7 @@ __device__ __forceinline__ void sine_rg_body(const Tin* in, Tout* out, const Sin
                         ff s2 = two_sum(hv[a], lw[a]);
                         s2 = ff_add_f(s2, cv);
                         if (fu.last) o64[o] = ff_to_f64(s2);
-                        else ulo_out[o] = lw[a] + cv;
+                        if (ulo_out) ulo_out[o] = lw[a] + cv;
                         cc += cv * cv;
                         uu += s2.h * s2.h;
                     }
@@ -539,7 +546,7 @@ __device__ __forceinline__ void sine_rg_body(const Tin* in, Tout* out, const Sin
                     ff s2 = two_sum(hv[q], lv[q]);
                     s2 = ff_add_f(s2, cv);
                     if (fu.last) o64[ix[q]] = ff_to_f64(s2);
-                    else fu.ulo_out[voff + ix[q]] = lv[q] + cv;
+                    if (fu.ulo_out) fu.ulo_out[voff + ix[q]] = lv[q] + cv;
                     cc += cv * cv;
                     uu += s2.h * s2.h;
                 }

@@ -65,11 +65,14 @@ class LaplCube:
     """3-D Dirichlet Poisson solver, fdm::LaplCube<T,check,F> (src/lapl_cube.h:9-106).
 
     precision: "plain" (every stage in `dtype`) or "mixed" (float64 arrays;
-    FP32 inner solves with refinement to `tol`).
+    FP32 inner solves with refinement to `tol`).  adaptive: after the sweeps
+    `tol` asks for, run further sweeps (up to max_sweeps) while a right-hand
+    side's estimated remaining error exceeds `tol` (the solve then waits for
+    the device).
     """
 
     def __init__(self, dx, dy, dz, lx, ly, lz, nx, ny, nz, dtype=np.float64, precision="plain",
-                 tol=1e-10, max_sweeps=3, periodic=False):
+                 tol=1e-10, max_sweeps=3, periodic=False, adaptive=False):
         self._lib = N.load()
         self.dtype = np.dtype(dtype)
         self.nx, self.ny, self.nz = int(nx), int(ny), int(nz)
@@ -86,6 +89,8 @@ class LaplCube:
             raise N.FdmError(N.EINVAL, "precision must be 'plain' or 'mixed'")
         N.check(self._lib.fdmgpu_lapl_cube_set_precision(self._h, N.MIXED if precision == "mixed" else N.PLAIN,
                                                          float(tol), int(max_sweeps)))
+        if adaptive:
+            N.check(self._lib.fdmgpu_lapl_cube_set_refinement(self._h, 1))
 
     def solve(self, ans: np.ndarray, rhs: np.ndarray) -> None:
         """ans <- solution for rhs (host arrays, synchronous)."""
@@ -141,7 +146,7 @@ class LaplCube:
         return bool(f.value)
 
     def last_info(self, nrhs: int = 1):
-        """(sweeps, [relative size of the last correction per RHS])."""
+        """(sweeps, [estimated relative error left per RHS]); -1 without a sweep."""
         s = c_int()
         est = (c_double * nrhs)()
         N.check(self._lib.fdmgpu_lapl_cube_last_info(self._h, byref(s), est, int(nrhs)))

@@ -78,36 +78,38 @@ class Server:
         return rid.value
 
     @staticmethod
-    def _record(rid, state, status, lat, queue, batch):
+    def _record(rid, state, status, lat, queue, batch, est):
         return {"id": rid, "state": STATE_NAMES[state.value], "status": status.value, "latency_ms": lat.value,
-                "queue_ms": queue.value, "batch": batch.value}
+                "queue_ms": queue.value, "batch": batch.value, "err_est": est.value}
 
     def _out(self):
-        return c_int(), c_int(), c_double(), c_double(), c_int()
+        return c_int(), c_int(), c_double(), c_double(), c_int(), c_double()
 
     def poll(self, rid: int) -> dict:
-        """State of a request; a finished one is reported once."""
-        st, status, lat, q, b = self._out()
+        """State of a request; a finished one is reported once.  err_est: a
+        finished mixed solve's estimated relative error (0 for FP64, -1
+        otherwise)."""
+        st, status, lat, q, b, e = self._out()
         N.check(self._lib.fdmgpu_server_poll(self._h, int(rid), byref(st), byref(status), byref(lat), byref(q),
-                                             byref(b)))
-        return self._record(rid, st, status, lat, q, b)
+                                             byref(b), byref(e)))
+        return self._record(rid, st, status, lat, q, b, e)
 
     def wait(self, rid: int, timeout_ms: float = 60000.0) -> dict:
-        st, status, lat, q, b = self._out()
+        st, status, lat, q, b, e = self._out()
         N.check(self._lib.fdmgpu_server_wait(self._h, int(rid), float(timeout_ms), byref(st), byref(status),
-                                             byref(lat), byref(q), byref(b)))
-        return self._record(rid, st, status, lat, q, b)
+                                             byref(lat), byref(q), byref(b), byref(e)))
+        return self._record(rid, st, status, lat, q, b, e)
 
     def next_done(self, timeout_ms: float = 1000.0):
         """The next finished request, or None after timeout_ms."""
         rid = c_ulonglong()
-        st, status, lat, q, b = self._out()
+        st, status, lat, q, b, e = self._out()
         rc = self._lib.fdmgpu_server_next_done(self._h, float(timeout_ms), byref(rid), byref(st), byref(status),
-                                               byref(lat), byref(q), byref(b))
+                                               byref(lat), byref(q), byref(b), byref(e))
         if rc == N.ETIMEOUT:
             return None
         N.check(rc)
-        return self._record(rid.value, st, status, lat, q, b)
+        return self._record(rid.value, st, status, lat, q, b, e)
 
     def cancel(self, rid: int) -> None:
         N.check(self._lib.fdmgpu_server_cancel(self._h, int(rid)))

@@ -154,11 +154,23 @@ int fdmgpu_lapl_cube_solve_mixed_noalloc(double dx, double dy, double dz, double
                                          int nx, int ny, int nz, double tol, void* d_ans, const void* d_rhs,
                                          int nrhs, void* stream);
 /* refinement report of the last solve: sweeps done (-1: a mixed plan that
- * solved in FP64) and, per RHS, the relative size of the last correction
- * ||c||_2/||u||_2 (an upper estimate of the remaining relative error; -1 when
- * no sweep ran).  est may be NULL; it receives nrhs values.
- * Synchronises the handle's last stream. */
+ * solved in FP64) and, per RHS, the estimated relative L2 error left in the
+ * answer (-1 when no sweep ran).  Sweep k measures e_k = ||c_k||/||u||, the
+ * size of its correction; the estimate after the last sweep is rho e_k with
+ * the observed contraction rho = e_k/e_{k-1}, or rho = 100 e_1 after a single
+ * sweep (a margin over the FP32 inner solve's contraction measured on GB300),
+ * and never below 1e-16 times the operator's eigenvalue ratio (the floor of
+ * the float-float residual).
+ * est may be NULL; it receives nrhs values.  Synchronises the handle's last
+ * stream.  (No reference counterpart: the reference solves exactly in T.) */
 int fdmgpu_lapl_cube_last_info(fdmgpu_lapl_cube* h, int* sweeps, double* est, int nrhs);
+/* adaptive = 1: after the sweeps that tol asks for, the mixed solve checks
+ * every right-hand side's estimate (as last_info reports it) and runs
+ * further sweeps, up to max_sweeps, while one exceeds tol; each check
+ * synchronises the solve's stream, so the call returns after the device
+ * finished.  0 (default): the sweep count follows tol alone and the solve
+ * stays asynchronous.  No reference counterpart. */
+int fdmgpu_lapl_cube_set_refinement(fdmgpu_lapl_cube* h, int adaptive);
 /* bytes of device scratch the handle holds */
 int fdmgpu_lapl_cube_scratch_bytes(fdmgpu_lapl_cube* h, size_t* bytes);
 /* schedule of the mixed form: ztable = 1 uses the per-mode z factor table
@@ -391,17 +403,20 @@ int fdmgpu_server_submit_advance(fdmgpu_server* h, unsigned long long* id, int s
 /* state of a request; a finished (done, failed, cancelled) request is
  * reported once and then forgotten.  latency_ms: submit to completion
  * (-1 while unfinished); queue_ms: submit to launch; batch: requests in its
- * launch.  A failed request's message is left in fdmgpu_last_error(). */
+ * launch; err_est (may be NULL): for a finished mixed-precision solve the
+ * estimated relative L2 error of its answer (the model of
+ * fdmgpu_lapl_cube_last_info), 0 for an FP64 solve, -1 otherwise.  A failed
+ * request's message is left in fdmgpu_last_error(). */
 int fdmgpu_server_poll(fdmgpu_server* h, unsigned long long id, int* state, int* status, double* latency_ms,
-                       double* queue_ms, int* batch);
+                       double* queue_ms, int* batch, double* err_est);
 /* as poll, blocking until the request finishes or timeout_ms passes
  * (FDMGPU_ETIMEOUT) */
 int fdmgpu_server_wait(fdmgpu_server* h, unsigned long long id, double timeout_ms, int* state, int* status,
-                       double* latency_ms, double* queue_ms, int* batch);
+                       double* latency_ms, double* queue_ms, int* batch, double* err_est);
 /* the next finished request (any), reported as poll does; FDMGPU_ETIMEOUT
  * when none finishes within timeout_ms */
 int fdmgpu_server_next_done(fdmgpu_server* h, double timeout_ms, unsigned long long* id, int* state,
-                            int* status, double* latency_ms, double* queue_ms, int* batch);
+                            int* status, double* latency_ms, double* queue_ms, int* batch, double* err_est);
 /* cancels a queued request (FDMGPU_EINVAL once it has started) */
 int fdmgpu_server_cancel(fdmgpu_server* h, unsigned long long id);
 /* copies a session field (FDMGPU_NS_*) once its queued advances are done */

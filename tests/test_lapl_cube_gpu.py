@@ -235,6 +235,66 @@ def test_plane_pipeline_applicability(cuda):
     assert LaplCube(*workloads.solver_args(127, 127, 127)).pipeline_in_use() == "five_pass"  # plain FP64
 
 
+def _white_or_smooth(shape, white, seed):
+    import torch
+    nx, ny, nz = shape
+    if white:
+        g = torch.Generator(device="cuda").manual_seed(seed)
+        return torch.randn((nz, ny, nx), dtype=torch.float64, device="cuda", generator=g)
+    return workloads.manufactured_torch(nx, ny, nz, seed=seed, kmax=min(shape) // 4, noise=1e-3)[0]
+
+
+@pytest.mark.parametrize("shape,white", [((255, 255, 255), True), ((255, 255, 31), True), ((127, 63, 255), False),
+                                         ((63, 31, 63), True), ((31, 31, 31), False)])
+def test_error_estimate_bounds_error(cuda, shape, white):
+    """last_info's per-RHS estimate of the remaining error is at least the
+    error against the FP64 form, after one sweep and after two."""
+    import torch
+    f = _white_or_smooth(shape, white, 3)
+    args = workloads.solver_args(*shape)
+    u = torch.empty_like(f)
+    LaplCube(*args).solve_device(u, f)
+    for tol, sweeps in ((1e-10, 1), (1e-12, 2)):
+        m = LaplCube(*args, precision="mixed", tol=tol)
+        a = torch.empty_like(f)
+        m.solve_device(a, f)
+        s, est = m.last_info(1)
+        err = (torch.linalg.norm(a - u) / torch.linalg.norm(u)).item()
+        assert s == sweeps
+        assert err <= est[0] <= 1e-8, (shape, tol, err, est)
+
+
+def test_adaptive_refinement_adds_a_sweep(cuda):
+    """A case the tolerance alone under-serves: 255 x 255 x 31 white noise at
+    tol 2e-11 gets one sweep from the schedule and misses the tolerance
+    (error ~5e-11); the closed loop sees the estimate above tol, runs a
+    second sweep and meets it."""
+    import torch
+    shape, tol = (255, 255, 31), 2e-11
+    f = _white_or_smooth(shape, True, 3)
+    args = workloads.solver_args(*shape)
+    u = torch.empty_like(f)
+    LaplCube(*args).solve_device(u, f)
+    fixed = LaplCube(*args, precision="mixed", tol=tol)
+    a = torch.empty_like(f)
+    fixed.solve_device(a, f)
+    s, est = fixed.last_info(1)
+    err = (torch.linalg.norm(a - u) / torch.linalg.norm(u)).item()
+    assert s == 1 and est[0] > tol and err <= est[0]
+    closed = LaplCube(*args, precision="mixed", tol=tol, adaptive=True)
+    b = torch.empty_like(f)
+    closed.solve_device(b, f)
+    s2, est2 = closed.last_info(1)
+    err2 = (torch.linalg.norm(b - u) / torch.linalg.norm(u)).item()
+    assert s2 == 2
+    assert err2 <= est2[0] <= tol, (err2, est2)
+    # the host-array call runs the same loop
+    h = np.zeros(f.shape)
+    closed.solve(h, f.cpu().numpy())
+    assert closed.last_info(1)[0] == 2
+    assert rel_l2(h, u.cpu().numpy()) <= tol
+
+
 @pytest.mark.parametrize("pinned", [True, False])
 def test_host_batch_pipeline_equals_device(cuda, pinned):
     """The pipelined host-pointer batch (ring of 3 device slots) gives the
