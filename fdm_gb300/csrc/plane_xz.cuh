@@ -58,6 +58,10 @@ struct PlaneCfg {
 // right-hand-side scale; sc_inv: the inverse x scale; tab: the per-mode z
 // factor table of k_zsolve_tab (block pivots, right-end responses,
 // separator pivots and multipliers, value-major over nx*ny modes).
+// The x transforms use the row swizzles of RgSwz (layouts B and C only, so
+// the plane's own views of the folded input and packed output are plain).
+constexpr bool kPlaneSwz = true;
+
 template <int N, int C, int MINB>
 __global__ void __launch_bounds__(256, MINB) k_plane_xz(float* __restrict__ W, PlaneGeom geo, SineTables<float> tb,
                                                         float gs, float sc_inv, const float* __restrict__ tab) {
@@ -133,7 +137,7 @@ __global__ void __launch_bounds__(256, MINB) k_plane_xz(float* __restrict__ W, P
         }
     }
     __syncthreads();
-    rg_line_fft<float, N, 0>(S + l * LS2, g, tb);
+    rg_line_fft<float, N, 0, kPlaneSwz>(S + l * LS2, g, l, tb);
     __syncthreads();
 
     // ---- 2. z blocks: thread t owns x-mode i = t+1 of every local block.
@@ -260,7 +264,7 @@ __global__ void __launch_bounds__(256, MINB) k_plane_xz(float* __restrict__ W, P
         if (lane == 0) base[M] = ldg(tb.wpre + M) * (am + am);
     }
     __syncthreads();
-    rg_line_fft<float, N, 0>(S + l * LS2, g, tb);
+    rg_line_fft<float, N, 0, kPlaneSwz>(S + l * LS2, g, l, tb);
     __syncthreads();
 
     // ---- 6. store the rows: slot k = c + 32q of a line holds F_2k and

@@ -60,6 +60,49 @@ struct RgGeom {
     static constexpr int LS2 = AXIS == 0 ? ((RS0 + 7) / 16 * 16 + 8) : (RS0 | 1);
 };
 
+// Slot swizzles of the two layouts private to the line transform, FP32
+// only (chosen for 8-byte slots): B, the transpose between its passes
+// (entry (k1, j) at slot k1 (R2+1) + (j ^ mask): the XOR stays inside the
+// row of R2 entries), and C (entry k at slot sk(k) ^ mask, pass 2 to the
+// unpack).  The masks are keyed on bits 0 and 1 of the line's index.  The
+// lines that share a half-warp want different offsets between them in
+// different phases (pass 1 and its transpose write 16 banks, pass 2 an odd
+// number of slots, the unpack 8 (mod 16) slots), which no single line
+// stride gives; these masks give the fewest shared-memory wavefronts in a
+// bank model of every phase (FP32 rows of 256 points: 1792 -> 1168 for the
+// two layouts), and on GB300 the plane pass of 255^3 x 16 went from 2.88
+// to 2.81 ms, the x passes about 1 % faster.  Column passes keep plain
+// layouts: a swizzled column layout at the row stride (3328 -> 2450
+// modelled wavefronts) needed more than 48 registers and ran 3-5 % slower
+// at 4 CTAs per SM than the plain one at 5.
+template <typename T, int N, int AXIS>
+struct RgSwz {
+    static constexpr int B0 = 0, B1 = 0, C0 = 0, C1 = 0;
+};
+template <int N>
+struct RgSwzRow {
+    static constexpr int B0 = N == 256 ? 1 : 0, B1 = N == 64 ? 1 : 0;
+    static constexpr int C0 = N == 256 ? 5 : (N == 128 || N == 64) ? 2 : 0, C1 = N == 64 ? 1 : N == 32 ? 5 : 0;
+};
+template <> struct RgSwz<float, 256, 0> : RgSwzRow<256> {};
+template <> struct RgSwz<float, 128, 0> : RgSwzRow<128> {};
+template <> struct RgSwz<float, 64, 0> : RgSwzRow<64> {};
+template <> struct RgSwz<float, 32, 0> : RgSwzRow<32> {};
+template <> struct RgSwz<float, 32, 1> {
+    static constexpr int B0 = 1, B1 = 2, C0 = 0, C1 = 0;
+};
+
+// largest s ^ m over s < n and every mask m whose bits lie within those of
+// mmax rounded up to 2^k - 1
+__host__ __device__ constexpr int swz_max(int n, int mmax) {
+    int cover = 0;
+    while (cover < mmax) cover = 2 * cover + 1;
+    int r = 0;
+    for (int s = 0; s < n; s++)
+        for (int m = 0; m <= cover; m++) r = (s ^ m) > r ? (s ^ m) : r;
+    return r;
+}
+
 // cos / sin of 2 pi m / 16
 __device__ __forceinline__ constexpr double c16(int m) {
     return m == 0 ? 1.0 : m == 1 ? 0.92387953251128674 : m == 2 ? 0.70710678118654757 : m == 3 ? 0.38268343236508984
@@ -127,11 +170,18 @@ __device__ __forceinline__ int sk(int k) { return k + (k >> 4); }
 // on exit the unscaled F_1..F_n with entry i as component i&1 of slot
 // sk(i>>1).  Called by the G threads of the line (g = 0..G-1), which must
 // belong to one warp; the phases inside need only warp synchronisation.
-template <typename T, int N, int AXIS>
-__device__ __forceinline__ void rg_line_fft(vec2_t<T>* Ls, int g, const SineTables<T>& tb) {
+// line: the line's index in the CTA (selects the swizzle of RgSwz; SWZ =
+// false keeps both private layouts plain).
+template <typename T, int N, int AXIS, bool SWZ = true>
+__device__ __forceinline__ void rg_line_fft(vec2_t<T>* Ls, int g, int line, const SineTables<T>& tb) {
     using T2 = vec2_t<T>;
     using Gm = RgGeom<N, AXIS>;
+    using Sw = RgSwz<T, N, AXIS>;
     constexpr int M = Gm::M, R1 = Gm::R1, R2 = Gm::R2, G = Gm::G, D2 = Gm::D2, E = Gm::E;
+    static_assert(swz_max(R2, Sw::B0 | Sw::B1) < R2 && swz_max(Gm::CS, Sw::C0 | Sw::C1) < Gm::LS2,
+                  "a swizzled slot stays inside its row of the transpose (B) and inside its line (C)");
+    const int mB = SWZ ? (((line & 1) ? Sw::B0 : 0) ^ ((line & 2) ? Sw::B1 : 0)) : 0;
+    const int mC = SWZ ? (((line & 1) ? Sw::C0 : 0) ^ ((line & 2) ? Sw::C1 : 0)) : 0;
     // ---- pass 1: DFT_R1 + twiddle
     T2 v[R1];
 #pragma unroll
@@ -143,7 +193,7 @@ __device__ __forceinline__ void rg_line_fft(vec2_t<T>* Ls, int g, const SineTabl
     }
     __syncwarp();
 #pragma unroll
-    for (int k1 = 0; k1 < R1; k1++) Ls[k1 * (R2 + 1) + g] = v[k1];
+    for (int k1 = 0; k1 < R1; k1++) Ls[k1 * (R2 + 1) + (g ^ mB)] = v[k1];
     __syncwarp();
 
     // ---- pass 2: D2 DFTs of length R2 per thread
@@ -152,7 +202,7 @@ __device__ __forceinline__ void rg_line_fft(vec2_t<T>* Ls, int g, const SineTabl
     for (int d = 0; d < D2; d++) {
         const int k1 = g * D2 + d;
 #pragma unroll
-        for (int j2 = 0; j2 < R2; j2++) u[d][j2] = Ls[k1 * (R2 + 1) + j2];
+        for (int j2 = 0; j2 < R2; j2++) u[d][j2] = Ls[k1 * (R2 + 1) + (j2 ^ mB)];
         dft_reg<T, R2>(u[d]);
     }
     __syncwarp();
@@ -160,7 +210,7 @@ __device__ __forceinline__ void rg_line_fft(vec2_t<T>* Ls, int g, const SineTabl
     for (int d = 0; d < D2; d++) {
         const int k1 = g * D2 + d;
 #pragma unroll
-        for (int k2 = 0; k2 < R2; k2++) Ls[sk(k1 + R1 * k2)] = u[d][k2];
+        for (int k2 = 0; k2 < R2; k2++) Ls[sk(k1 + R1 * k2) ^ mC] = u[d][k2];
     }
     __syncwarp();
 
@@ -170,17 +220,17 @@ __device__ __forceinline__ void rg_line_fft(vec2_t<T>* Ls, int g, const SineTabl
 #pragma unroll
     for (int t = 0; t < E; t++) {
         const int k = g * E + t;
-        const T2 ck = Ls[sk(k)];
+        const T2 ck = Ls[sk(k) ^ mC];
         if (k == 0) {
             ra[t] = T(0.5) * (ck.x + ck.y);  // Re Y_0, halved in the running sum
             ia[t] = T(0);
-            const T2 cmid = Ls[sk(M / 2)];
+            const T2 cmid = Ls[sk(M / 2) ^ mC];
             rmid = cmid.x;
             imid = -cmid.y;
             rb[t] = T(0);
             ib[t] = T(0);
         } else {
-            const T2 cm = Ls[sk(M - k)];
+            const T2 cm = Ls[sk(M - k) ^ mC];
             const T ex = T(0.5) * (ck.x + cm.x), ey = T(0.5) * (ck.y - cm.y);
             const T ox = T(0.5) * (ck.y + cm.y), oy = T(-0.5) * (ck.x - cm.x);
             const T2 w = ldg(tb.post + k);
@@ -421,7 +471,7 @@ __device__ __forceinline__ void sine_rg_body(const Tin* in, Tout* out, const Sin
     }
     __syncthreads();
 
-    rg_line_fft<T, N, AXIS>(S + (size_t)l * LS2, g, tb);
+    rg_line_fft<T, N, AXIS>(S + (size_t)l * LS2, g, l, tb);
     __syncthreads();
 
     // ---- store phase: entry i of line l is component i&1 of slot sk(i>>1).
