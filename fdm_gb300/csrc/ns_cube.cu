@@ -12,6 +12,10 @@
 // RHS, the five passes of the plain FP64 Poisson solve, update).  After the
 // first eager step the sequence is captured once into a CUDA graph and
 // replayed, which removes the host launch cost that dominates at 63^3.
+// Quotients by the run constants (Re, h, h^2, dt) are, by default, products
+// with reciprocals computed on the host; the exact form (set_exact) rounds
+// each one as the reference's division does.  Every kernel is bound by the
+// FP64 pipe, which GB300 runs at a small fraction of its FP32 rate.
 #include <cmath>
 #include <cstdio>
 #include <memory>
@@ -50,23 +54,81 @@ struct NSParams {
     double U0, Re, dt, dx, dy, dz, dx2, dy2, dz2;
     CDiv dRe, ddx, ddy, ddz, ddx2, ddy2, ddz2, ddt;
     double dt_dx, dt_dy, dt_dz;  // dt/dx etc., correctly rounded on the host
+    // reciprocals of the run constants for the fast form (FAST = true): a
+    // quotient x / a / b becomes x * (1 / (a b)), one FP64 multiply instead
+    // of two correctly rounded divisions (five operations each)
+    double rRe_dx2, rRe_dy2, rRe_dz2, rRe_dx, rRe_dy, rRe_dz;
+    double rdx, rdy, rdz, rdx2, rdy2, rdz2, rdt;
 };
+
+// x / d (FAST: x * r, r = 1 / d computed on the host; otherwise the
+// correctly rounded quotient of cdiv)
+template <bool FAST>
+__device__ __forceinline__ double qdiv(double x, CDiv d, double r) {
+    if constexpr (FAST) return x * r;
+    else return cdiv(x, d);
+}
+
+// (x / Re) / h^2, or x * (1 / (Re h^2)) in the fast form
+template <bool FAST>
+__device__ __forceinline__ double qdiv2(double x, CDiv dRe, CDiv d2, double r) {
+    if constexpr (FAST) return x * r;
+    else return cdiv(cdiv(x, dRe), d2);
+}
+
+// Point e of the surface of a W x H x D box (x fastest): the two z faces,
+// the two y faces without their z edges, the two x faces without either.
+// Returns false past the surface's 2(WH + W(D-2) + (H-2)(D-2)) points.
+__device__ __forceinline__ bool surface_point(long long e, int W, int H, int D, int& i, int& k, int& j) {
+    const long long zf = (long long)W * H;
+    if (e < 2 * zf) {
+        i = e < zf ? 0 : D - 1;
+        const long long r = e < zf ? e : e - zf;
+        k = (int)(r / W);
+        j = (int)(r - (long long)k * W);
+        return true;
+    }
+    e -= 2 * zf;
+    const long long yf = (long long)W * (D - 2);
+    if (e < 2 * yf) {
+        k = e < yf ? 0 : H - 1;
+        const long long r = e < yf ? e : e - yf;
+        i = 1 + (int)(r / W);
+        j = (int)(r % W);
+        return true;
+    }
+    e -= 2 * yf;
+    const long long xf = (long long)(H - 2) * (D - 2);
+    if (e < 2 * xf) {
+        j = e < xf ? 0 : W - 1;
+        const long long r = e < xf ? e : e - xf;
+        i = 1 + (int)(r / (H - 2));
+        k = 1 + (int)(r % (H - 2));
+        return true;
+    }
+    return false;
+}
+
+__host__ __device__ inline long long surface_points(int W, int H, int D) {
+    return 2 * ((long long)W * H + (long long)W * (D - 2) + (long long)(H - 2) * (D - 2));
+}
 
 __device__ __forceinline__ double sq(double x) { return x * x; }  // asp::sq, src/asp_misc.h:295
 
 // init_bound, first phase: the lid (without the two x-ghost columns that the
 // mirror below overwrites anyway), the x-mirror of u below the lid, and the
-// y-/z-mirrors of v and w.  None of these reads what another writes.
-// Thread grid covers a (z,y,x) box of (nz+3) x (ny+3) x (nx+3).
+// y-/z-mirrors of v and w.  None of these reads what another writes.  Every
+// point written lies on the surface of the (z,y,x) box [-1, nz+1] x
+// [-1, ny+1] x [-1, nx+1]; one thread per surface point.
 template <typename T>
 __global__ void k_ns_bound1(FieldT<T> u, FieldT<T> v, FieldT<T> w, NSParams P) {
     const int nx = P.nx, ny = P.ny, nz = P.nz;
     const long long e = (long long)blockIdx.x * blockDim.x + threadIdx.x;
-    const int W = nx + 3, H = ny + 3, D = nz + 3;
-    if (e >= (long long)W * H * D) return;
-    const int j = (int)(e % W) - 1;
-    const int k = (int)((e / W) % H) - 1;
-    const int i = (int)(e / ((long long)W * H)) - 1;
+    int i, k, j;
+    if (!surface_point(e, nx + 3, ny + 3, nz + 3, i, k, j)) return;
+    i -= 1;
+    k -= 1;
+    j -= 1;
     // lid (src/ns_cube.cpp:67-72): u[nz+1][k][j] = 2U0 - u[nz][k][j], j in [-1, nz+1]
     if (i == nz + 1 && k >= 0 && k <= ny + 1 && j >= 0 && j <= min(nz + 1, nx)) u(nz + 1, k, j) = 2 * P.U0 - u(nz, k, j);
     // u x-mirror for i <= nz (:76-81)
@@ -87,41 +149,43 @@ __global__ void k_ns_bound1(FieldT<T> u, FieldT<T> v, FieldT<T> w, NSParams P) {
 }
 
 // init_bound, second phase: u x-mirror of the lid row (reads the lid values
-// written by phase one) and the Neumann pressure ghosts (:98-121).
-template <typename T>
+// written by phase one) and the Neumann pressure ghosts (:98-121).  Every
+// point written lies on the surface of the box [0, nz+1] x [0, ny+1] x
+// [0, nx+1]; one thread per surface point.
+template <typename T, bool FAST>
 __global__ void k_ns_bound2(FieldT<T> u, FieldT<T> v, FieldT<T> w, FieldT<T> p, NSParams P) {
     const int nx = P.nx, ny = P.ny, nz = P.nz;
     const long long e = (long long)blockIdx.x * blockDim.x + threadIdx.x;
-    const int W = nx + 2, H = ny + 2, D = nz + 2;
-    if (e >= (long long)W * H * D) return;
-    const int j = (int)(e % W);
-    const int k = (int)((e / W) % H);
-    const int i = (int)(e / ((long long)W * H));
+    int i, k, j;
+    if (!surface_point(e, nx + 2, ny + 2, nz + 2, i, k, j)) return;
+    auto g = [&](double x, CDiv d, double r) { return qdiv2<FAST>(x, P.dRe, d, r); };
     if (i == nz + 1 && k <= ny + 1) {
         if (j == 0) u(nz + 1, k, -1) = u(nz + 1, k, 1);
         if (j == nx + 1) u(nz + 1, k, nx + 1) = u(nz + 1, k, nx - 1);
     }
     if (i >= 1 && i <= nz && k >= 1 && k <= ny) {
-        if (j == 0) p(i, k, 0) = p(i, k, 1) - cdiv(cdiv(u(i, k, 1) - 2 * u(i, k, 0) + u(i, k, -1), P.dRe), P.ddx);
+        if (j == 0) p(i, k, 0) = p(i, k, 1) - g(u(i, k, 1) - 2 * u(i, k, 0) + u(i, k, -1), P.ddx, P.rRe_dx);
         if (j == nx + 1)
-            p(i, k, nx + 1) = p(i, k, nx) - cdiv(cdiv(u(i, k, nx + 1) - 2 * u(i, k, nx) + u(i, k, nx - 1), P.dRe), P.ddx);
+            p(i, k, nx + 1) = p(i, k, nx) - g(u(i, k, nx + 1) - 2 * u(i, k, nx) + u(i, k, nx - 1), P.ddx, P.rRe_dx);
     }
     if (i >= 1 && i <= nz && j >= 1 && j <= nx) {
-        if (k == 0) p(i, 0, j) = p(i, 1, j) - cdiv(cdiv(v(i, 1, j) - 2 * v(i, 0, j) + v(i, -1, j), P.dRe), P.ddy);
+        if (k == 0) p(i, 0, j) = p(i, 1, j) - g(v(i, 1, j) - 2 * v(i, 0, j) + v(i, -1, j), P.ddy, P.rRe_dy);
         if (k == ny + 1)
-            p(i, ny + 1, j) = p(i, ny, j) - cdiv(cdiv(v(i, ny + 1, j) - 2 * v(i, ny, j) + v(i, ny - 1, j), P.dRe), P.ddy);
+            p(i, ny + 1, j) = p(i, ny, j) - g(v(i, ny + 1, j) - 2 * v(i, ny, j) + v(i, ny - 1, j), P.ddy, P.rRe_dy);
     }
     if (k >= 1 && k <= ny && j >= 1 && j <= nx) {
-        if (i == 0) p(0, k, j) = p(1, k, j) - cdiv(cdiv(w(1, k, j) - 2 * w(0, k, j) + w(-1, k, j), P.dRe), P.ddz);
+        if (i == 0) p(0, k, j) = p(1, k, j) - g(w(1, k, j) - 2 * w(0, k, j) + w(-1, k, j), P.ddz, P.rRe_dz);
         if (i == nz + 1)
-            p(nz + 1, k, j) = p(nz, k, j) - cdiv(cdiv(w(nz + 1, k, j) - 2 * w(nz, k, j) + w(nz - 1, k, j), P.dRe), P.ddz);
+            p(nz + 1, k, j) = p(nz, k, j) - g(w(nz + 1, k, j) - 2 * w(nz, k, j) + w(nz - 1, k, j), P.ddz, P.rRe_dz);
     }
 }
 
 // FGH (src/ns_cube.cpp:126-200), one thread per (i,k,j) of the box
 // [0,nz] x [0,ny] x [0,nx]; each thread writes whichever of F, G, H has that
-// point in its range.
-template <typename T>
+// point in its range.  FAST: quotients by the run constants as products with
+// their reciprocals (about half the FP64 operations; results within a few
+// units in the last place of the exact form's).
+template <typename T, bool FAST>
 __global__ void __launch_bounds__(256)
     k_ns_fgh(FieldT<T> u, FieldT<T> v, FieldT<T> w, FieldT<T> F, FieldT<T> G, FieldT<T> H, NSParams P) {
     const int nx = P.nx, ny = P.ny, nz = P.nz;
@@ -132,46 +196,56 @@ __global__ void __launch_bounds__(256)
     const int k = (int)((e / W) % Hh);
     const int i = (int)(e / ((long long)W * Hh));
     const double dt = P.dt;
-    // x / Re / h^2 and x / h, each quotient rounded as the reference's
-    auto dif = [&](double x, CDiv d2) { return cdiv(cdiv(x, P.dRe), d2); };
-    if (i >= 1 && k >= 1) {
-        F(i, k, j) = u(i, k, j) + dt * (
-            dif(u(i, k, j + 1) - 2 * u(i, k, j) + u(i, k, j - 1), P.ddx2) +
-            dif(u(i, k + 1, j) - 2 * u(i, k, j) + u(i, k - 1, j), P.ddy2) +
-            dif(u(i + 1, k, j) - 2 * u(i, k, j) + u(i - 1, k, j), P.ddz2) -
-            cdiv(sq(0.5 * (u(i, k, j) + u(i, k, j + 1))) - sq(0.5 * (u(i, k, j - 1) + u(i, k, j))), P.ddx) -
-            cdiv(0.25 * ((u(i, k, j) + u(i, k + 1, j)) * (v(i, k, j + 1) + v(i, k, j)) -
-                         (u(i, k - 1, j) + u(i, k, j)) * (v(i, k - 1, j + 1) + v(i, k - 1, j))), P.ddy) -
-            cdiv(0.25 * ((u(i, k, j) + u(i + 1, k, j)) * (w(i, k, j + 1) + w(i, k, j)) -
-                         (u(i - 1, k, j) + u(i, k, j)) * (w(i - 1, k, j + 1) + w(i - 1, k, j))), P.ddz));
+    // x / Re / h^2 and x / h (exact form: each quotient rounded as the
+    // reference's)
+    auto dif = [&](double x, CDiv d2, double r) { return qdiv2<FAST>(x, P.dRe, d2, r); };
+    auto qd = [&](double x, CDiv d, double r) { return qdiv<FAST>(x, d, r); };
+    // the three components are formed before any is stored, so that the
+    // compiler may share the loads and the cross products they have in
+    // common (the stores could alias the velocity fields)
+    double fv = 0.0, gv = 0.0, hv = 0.0;
+    const bool doF = i >= 1 && k >= 1, doG = i >= 1 && j >= 1, doH = k >= 1 && j >= 1;
+    if (doF) {
+        fv = u(i, k, j) + dt * (
+            dif(u(i, k, j + 1) - 2 * u(i, k, j) + u(i, k, j - 1), P.ddx2, P.rRe_dx2) +
+            dif(u(i, k + 1, j) - 2 * u(i, k, j) + u(i, k - 1, j), P.ddy2, P.rRe_dy2) +
+            dif(u(i + 1, k, j) - 2 * u(i, k, j) + u(i - 1, k, j), P.ddz2, P.rRe_dz2) -
+            qd(sq(0.5 * (u(i, k, j) + u(i, k, j + 1))) - sq(0.5 * (u(i, k, j - 1) + u(i, k, j))), P.ddx, P.rdx) -
+            qd(0.25 * ((u(i, k, j) + u(i, k + 1, j)) * (v(i, k, j + 1) + v(i, k, j)) -
+                         (u(i, k - 1, j) + u(i, k, j)) * (v(i, k - 1, j + 1) + v(i, k - 1, j))), P.ddy, P.rdy) -
+            qd(0.25 * ((u(i, k, j) + u(i + 1, k, j)) * (w(i, k, j + 1) + w(i, k, j)) -
+                         (u(i - 1, k, j) + u(i, k, j)) * (w(i - 1, k, j + 1) + w(i - 1, k, j))), P.ddz, P.rdz));
     }
-    if (i >= 1 && j >= 1) {
-        G(i, k, j) = v(i, k, j) + dt * (
-            dif(v(i, k, j + 1) - 2 * v(i, k, j) + v(i, k, j - 1), P.ddx2) +
-            dif(v(i, k + 1, j) - 2 * v(i, k, j) + v(i, k - 1, j), P.ddy2) +
-            dif(v(i + 1, k, j) - 2 * v(i, k, j) + v(i - 1, k, j), P.ddz2) -
-            cdiv(sq(0.5 * (v(i, k, j) + v(i, k + 1, j))) - sq(0.5 * (v(i, k - 1, j) + v(i, k, j))), P.ddy) -
-            cdiv(0.25 * ((u(i, k, j) + u(i, k + 1, j)) * (v(i, k, j + 1) + v(i, k, j)) -
-                         (u(i, k, j - 1) + u(i, k + 1, j - 1)) * (v(i, k, j) + v(i, k, j - 1))), P.ddx) -
-            cdiv(0.25 * ((w(i, k, j) + w(i, k + 1, j)) * (v(i, k, j) + v(i + 1, k, j)) -
-                         (w(i - 1, k, j) + w(i - 1, k + 1, j)) * (v(i - 1, k, j) + v(i, k, j))), P.ddz));
+    if (doG) {
+        gv = v(i, k, j) + dt * (
+            dif(v(i, k, j + 1) - 2 * v(i, k, j) + v(i, k, j - 1), P.ddx2, P.rRe_dx2) +
+            dif(v(i, k + 1, j) - 2 * v(i, k, j) + v(i, k - 1, j), P.ddy2, P.rRe_dy2) +
+            dif(v(i + 1, k, j) - 2 * v(i, k, j) + v(i - 1, k, j), P.ddz2, P.rRe_dz2) -
+            qd(sq(0.5 * (v(i, k, j) + v(i, k + 1, j))) - sq(0.5 * (v(i, k - 1, j) + v(i, k, j))), P.ddy, P.rdy) -
+            qd(0.25 * ((u(i, k, j) + u(i, k + 1, j)) * (v(i, k, j + 1) + v(i, k, j)) -
+                         (u(i, k, j - 1) + u(i, k + 1, j - 1)) * (v(i, k, j) + v(i, k, j - 1))), P.ddx, P.rdx) -
+            qd(0.25 * ((w(i, k, j) + w(i, k + 1, j)) * (v(i, k, j) + v(i + 1, k, j)) -
+                         (w(i - 1, k, j) + w(i - 1, k + 1, j)) * (v(i - 1, k, j) + v(i, k, j))), P.ddz, P.rdz));
     }
-    if (k >= 1 && j >= 1) {
-        H(i, k, j) = w(i, k, j) + dt * (
-            dif(w(i, k, j + 1) - 2 * w(i, k, j) + w(i, k, j - 1), P.ddx2) +
-            dif(w(i, k + 1, j) - 2 * w(i, k, j) + w(i, k - 1, j), P.ddy2) +
-            dif(w(i + 1, k, j) - 2 * w(i, k, j) + w(i - 1, k, j), P.ddz2) -
-            cdiv(sq(0.5 * (w(i + 1, k, j) + w(i, k, j))) - sq(0.5 * (w(i - 1, k, j) + w(i, k, j))), P.ddz) -
-            cdiv(0.25 * ((u(i + 1, k, j) + u(i, k, j)) * (w(i, k, j + 1) + w(i, k, j)) -
-                         (u(i + 1, k, j - 1) + u(i, k, j - 1)) * (w(i, k, j) + w(i, k, j - 1))), P.ddx) -
-            cdiv(0.25 * ((w(i, k, j) + w(i, k + 1, j)) * (v(i, k, j) + v(i + 1, k, j)) -
-                         (w(i, k - 1, j) + w(i, k, j)) * (v(i, k - 1, j) + v(i + 1, k - 1, j))), P.ddy));
+    if (doH) {
+        hv = w(i, k, j) + dt * (
+            dif(w(i, k, j + 1) - 2 * w(i, k, j) + w(i, k, j - 1), P.ddx2, P.rRe_dx2) +
+            dif(w(i, k + 1, j) - 2 * w(i, k, j) + w(i, k - 1, j), P.ddy2, P.rRe_dy2) +
+            dif(w(i + 1, k, j) - 2 * w(i, k, j) + w(i - 1, k, j), P.ddz2, P.rRe_dz2) -
+            qd(sq(0.5 * (w(i + 1, k, j) + w(i, k, j))) - sq(0.5 * (w(i - 1, k, j) + w(i, k, j))), P.ddz, P.rdz) -
+            qd(0.25 * ((u(i + 1, k, j) + u(i, k, j)) * (w(i, k, j + 1) + w(i, k, j)) -
+                         (u(i + 1, k, j - 1) + u(i, k, j - 1)) * (w(i, k, j) + w(i, k, j - 1))), P.ddx, P.rdx) -
+            qd(0.25 * ((w(i, k, j) + w(i, k + 1, j)) * (v(i, k, j) + v(i + 1, k, j)) -
+                         (w(i, k - 1, j) + w(i, k, j)) * (v(i, k - 1, j) + v(i + 1, k - 1, j))), P.ddy, P.rdy));
     }
+    if (doF) F(i, k, j) = fv;
+    if (doG) G(i, k, j) = gv;
+    if (doH) H(i, k, j) = hv;
 }
 
 // Divergence RHS with the Dirichlet pressure ghosts folded in
 // (src/ns_cube.cpp:206-235).
-template <typename T>
+template <typename T, bool FAST>
 __global__ void k_ns_rhs(FieldT<T> F, FieldT<T> G, FieldT<T> H, FieldT<T> p, FieldT<T> RHS, NSParams P) {
     const int nx = P.nx, ny = P.ny, nz = P.nz;
     const long long e = (long long)blockIdx.x * blockDim.x + threadIdx.x;
@@ -180,14 +254,15 @@ __global__ void k_ns_rhs(FieldT<T> F, FieldT<T> G, FieldT<T> H, FieldT<T> p, Fie
     const int k = (int)((e / nx) % ny) + 1;
     const int i = (int)(e / ((long long)nx * ny)) + 1;
     // T-typed like the reference RHS element: rounded after each update
-    T r = cdiv(cdiv(F(i, k, j) - F(i, k, j - 1), P.ddx) + cdiv(G(i, k, j) - G(i, k - 1, j), P.ddy) +
-                    cdiv(H(i, k, j) - H(i - 1, k, j), P.ddz), P.ddt);
-    if (i <= 1) r -= cdiv(p(i - 1, k, j), P.ddz2);
-    if (k <= 1) r -= cdiv(p(i, k - 1, j), P.ddy2);
-    if (j <= 1) r -= cdiv(p(i, k, j - 1), P.ddx2);
-    if (j >= nx) r -= cdiv(p(i, k, j + 1), P.ddx2);
-    if (k >= ny) r -= cdiv(p(i, k + 1, j), P.ddy2);
-    if (i >= nz) r -= cdiv(p(i + 1, k, j), P.ddz2);
+    auto qd = [&](double x, CDiv d, double rc) { return qdiv<FAST>(x, d, rc); };
+    T r = qd(qd(F(i, k, j) - F(i, k, j - 1), P.ddx, P.rdx) + qd(G(i, k, j) - G(i, k - 1, j), P.ddy, P.rdy) +
+                 qd(H(i, k, j) - H(i - 1, k, j), P.ddz, P.rdz), P.ddt, P.rdt);
+    if (i <= 1) r -= qd(p(i - 1, k, j), P.ddz2, P.rdz2);
+    if (k <= 1) r -= qd(p(i, k - 1, j), P.ddy2, P.rdy2);
+    if (j <= 1) r -= qd(p(i, k, j - 1), P.ddx2, P.rdx2);
+    if (j >= nx) r -= qd(p(i, k, j + 1), P.ddx2, P.rdx2);
+    if (k >= ny) r -= qd(p(i, k + 1, j), P.ddy2, P.rdy2);
+    if (i >= nz) r -= qd(p(i + 1, k, j), P.ddz2, P.rdz2);
     RHS(i, k, j) = r;
 }
 
@@ -247,6 +322,7 @@ struct NSPlanT {
     cudaGraphExec_t gexec = nullptr;
     int time_index = 0;
     int steps_run = 0;
+    bool exact = false;  // quotients correctly rounded as the reference's (slower)
 
     ~NSPlanT() {
         if (gexec) cudaGraphExecDestroy(gexec);
@@ -285,29 +361,36 @@ struct NSPlanT {
     }
 
     void enqueue_step() {
+        if (exact) enqueue_step_t<false>();
+        else enqueue_step_t<true>();
+    }
+
+    template <bool FAST>
+    void enqueue_step_t() {
         const int nx = P.nx, ny = P.ny, nz = P.nz;
         const int B = 256;
         auto blocks = [&](long long n) { return (unsigned)((n + B - 1) / B); };
         const long long vol = (long long)nx * ny * nz;
         {
             FDM_TIMED("ns_bound1", st);
-            k_ns_bound1<T><<<blocks((long long)(nx + 3) * (ny + 3) * (nz + 3)), B, 0, st>>>(f[0], f[1], f[2], P);
+            k_ns_bound1<T><<<blocks(surface_points(nx + 3, ny + 3, nz + 3)), B, 0, st>>>(f[0], f[1], f[2], P);
             FDM_LAUNCH_CHECK();
         }
         {
             FDM_TIMED("ns_bound2", st);
-            k_ns_bound2<T><<<blocks((long long)(nx + 2) * (ny + 2) * (nz + 2)), B, 0, st>>>(f[0], f[1], f[2], f[3], P);
+            k_ns_bound2<T, FAST><<<blocks(surface_points(nx + 2, ny + 2, nz + 2)), B, 0, st>>>(f[0], f[1], f[2], f[3],
+                                                                                             P);
             FDM_LAUNCH_CHECK();
         }
         {
             FDM_TIMED("ns_fgh", st);
-            k_ns_fgh<T><<<blocks((long long)(nx + 1) * (ny + 1) * (nz + 1)), B, 0, st>>>(f[0], f[1], f[2], f[5], f[6],
-                                                                                      f[7], P);
+            k_ns_fgh<T, FAST><<<blocks((long long)(nx + 1) * (ny + 1) * (nz + 1)), B, 0, st>>>(f[0], f[1], f[2], f[5],
+                                                                                            f[6], f[7], P);
             FDM_LAUNCH_CHECK();
         }
         {
             FDM_TIMED("ns_rhs", st);
-            k_ns_rhs<T><<<blocks(vol), B, 0, st>>>(f[5], f[6], f[7], f[3], f[8], P);
+            k_ns_rhs<T, FAST><<<blocks(vol), B, 0, st>>>(f[5], f[6], f[7], f[3], f[8], P);
             FDM_LAUNCH_CHECK();
         }
         cube_solve_device(lapl, f[4].p, f[8].p, 1, st);
@@ -375,6 +458,11 @@ void setup_plan(NSPlanT<T>& s, int nx, int nz, double x1, double y1, double z1, 
     s.P.ddx2 = cdiv_of(s.P.dx2); s.P.ddy2 = cdiv_of(s.P.dy2); s.P.ddz2 = cdiv_of(s.P.dz2);
     s.P.ddt = cdiv_of(dt);
     s.P.dt_dx = dt / s.P.dx; s.P.dt_dy = dt / s.P.dy; s.P.dt_dz = dt / s.P.dz;
+    s.P.rRe_dx2 = 1.0 / (Re * s.P.dx2); s.P.rRe_dy2 = 1.0 / (Re * s.P.dy2); s.P.rRe_dz2 = 1.0 / (Re * s.P.dz2);
+    s.P.rRe_dx = 1.0 / (Re * s.P.dx); s.P.rRe_dy = 1.0 / (Re * s.P.dy); s.P.rRe_dz = 1.0 / (Re * s.P.dz);
+    s.P.rdx = 1.0 / s.P.dx; s.P.rdy = 1.0 / s.P.dy; s.P.rdz = 1.0 / s.P.dz;
+    s.P.rdx2 = 1.0 / s.P.dx2; s.P.rdy2 = 1.0 / s.P.dy2; s.P.rdz2 = 1.0 / s.P.dz2;
+    s.P.rdt = 1.0 / dt;
     s.init();
 }
 }  // namespace
@@ -410,6 +498,23 @@ int fdmgpu_nscube_step(fdmgpu_nscube* h, int k) {
     if (!h) FDM_FAIL(FDMGPU_EINVAL, "null handle");
     if (k < 0) FDM_FAIL(FDMGPU_EINVAL, "negative step count");
     with_plan(h, [&](auto& s) { s.step(k); });
+    FDM_API_END
+}
+
+int fdmgpu_nscube_set_exact(fdmgpu_nscube* h, int exact) {
+    FDM_API_BEGIN
+    if (!h) FDM_FAIL(FDMGPU_EINVAL, "null handle");
+    if (exact != 0 && exact != 1) FDM_FAIL(FDMGPU_EINVAL, "exact must be 0 or 1");
+    with_plan(h, [&](auto& s) {
+        if (s.exact == (exact == 1)) return;
+        FDM_CUDA(cudaStreamSynchronize(s.st));
+        s.exact = exact == 1;
+        // the captured step holds the other form's kernels
+        if (s.gexec) cudaGraphExecDestroy(s.gexec);
+        if (s.graph) cudaGraphDestroy(s.graph);
+        s.gexec = nullptr;
+        s.graph = nullptr;
+    });
     FDM_API_END
 }
 

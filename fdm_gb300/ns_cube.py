@@ -77,6 +77,12 @@ class NSCube:
     def step(self, k: int = 1) -> None:
         N.check(self._lib.fdmgpu_nscube_step(self._h, int(k)))
 
+    def set_exact(self, exact: bool = True) -> None:
+        """exact=True: quotients by the run constants correctly rounded, as
+        the reference's divisions are; False (default): products with
+        precomputed reciprocals (faster, last-bit differences)."""
+        N.check(self._lib.fdmgpu_nscube_set_exact(self._h, 1 if exact else 0))
+
     @property
     def time_index(self) -> int:
         t = c_int()
