@@ -70,6 +70,8 @@ _SIGS = [
     ("fdmgpu_lapl_cube_set_schedule", c_int, [c_void_p, c_int, c_int]),
     ("fdmgpu_lapl_cube_set_pipeline", c_int, [c_void_p, c_int]),
     ("fdmgpu_lapl_cube_set_refinement", c_int, [c_void_p, c_int]),
+    ("fdmgpu_lapl_cube_tune", c_int, [c_void_p, c_void_p, c_void_p, c_int, c_void_p, POINTER(c_double)]),
+    ("fdmgpu_lapl_cube_get_schedule", c_int, [c_void_p, POINTER(c_int), POINTER(c_int), POINTER(c_int)]),
     ("fdmgpu_lapl_cube_pipeline_in_use", c_int, [c_void_p, POINTER(c_int)]),
     ("fdmgpu_lapl_cube_device_status", c_int, [c_void_p, POINTER(c_int)]),
     ("fdmgpu_lapl_cube_destroy", c_int, [c_void_p]),

@@ -578,8 +578,8 @@ struct CubePlan {
     DevBuf work32, uhi, ulo, norms, work64;
     DevBuf ztab64, ztab32;  // partitioned z-solve factors per mode
     int zmode = 1;          // 1: table-driven z-solve when the line splits, 0: factors computed per solve
-    int dst_tc = 0;         // bit 0 / bit 1: plain FP32 DST passes along x / y on the tensor cores (32-, 64-,
-                            // 128-point axes)
+    int dst_tc = -1;        // bit 0 / bit 1: plain FP32 DST passes along x / y on the tensor cores (32-, 64-,
+                            // 128-point axes); -1: default_tc_mask()
     int pipeline = 1;       // mixed form: 1 = DST-y, fused x-z plane pass, DST-y where the plane splits
                             // (plane_split); 0 = the five passes x, y, z, y, x
     bool periodic = false;  // all three axes periodic (real FFTs, divide, inverse FFTs)
@@ -740,7 +740,7 @@ struct CubePlan {
     template <int AXIS>
     void sine32(const float* in, float* out, int nrhs, double scale, cudaStream_t st) {
         const int N = (AXIS == 0 ? nx : ny) + 1;
-        if (((dst_tc >> AXIS) & 1) && tc_supported(N)) {
+        if (((tc_mask() >> AXIS) & 1) && tc_supported(N)) {
             DevBuf& img = AXIS == 0 ? tc_img_x : tc_img_y;
             if (!img.p) {
                 std::vector<float> h = tc_sine_image(N);
@@ -797,8 +797,87 @@ struct CubePlan {
     // x-z plane pass
     bool plane_ok() {
         int C = 0;
-        return pipeline == 1 && zmode == 1 && !(dst_tc & 1) && plane_split(nx + 1, nz, &C) && ztab32_ready() &&
+        return pipeline == 1 && zmode == 1 && !(tc_mask() & 1) && plane_split(nx + 1, nz, &C) && ztab32_ready() &&
                zm32 == 15;
+    }
+
+    // Tensor-core DST passes of a mixed plan whose schedule was not set:
+    // 32-point x axes (they never take the plane pipeline, whose x lines
+    // have 64 to 256 points) and 32-point y axes of plans that run the five
+    // passes.  Measured on GB300 (mixed, tol 1e-10): 31^3 x 64 at 522 k
+    // solves/s with both axes on the tensor cores against 449 k with FFTs,
+    // and the batch tuner kept the x axis on the tensor cores for every
+    // 31-point-x group of its 512-volume batch; with the plane pipeline the
+    // y axis ties (63^3 x 16: 95.1 k against 95.0 k), so the FFT stays.
+    int default_tc_mask() const {
+        if (precision != FDMGPU_MIXED || dtype != FDMGPU_F64 || periodic) return 0;
+        int m = nx + 1 == 32 ? 1 : 0;
+        int C = 0;
+        const bool planes = pipeline == 1 && zmode == 1 && !(m & 1) && plane_split(nx + 1, nz, &C);
+        if (ny + 1 == 32 && !planes) m |= 2;
+        return m;
+    }
+    int tc_mask() const { return dst_tc >= 0 ? dst_tc : default_tc_mask(); }
+
+    // Times every schedule of the mixed form on the caller's right-hand
+    // sides (pipeline, z-solve variant, tensor-core axes) and keeps the
+    // fastest whose accuracy is assured: with a refinement sweep, a variant
+    // with per-solve z factors or tensor-core passes must predict
+    // 10 e^(sweeps+1) <= tol from its measured first-sweep estimate e (as the
+    // batch tuner does); without a sweep (tol >= 1e-5, above the FP32 and
+    // split-TF32 inner solves' errors) per-solve factors do not qualify.
+    // Synchronises st.  Returns the chosen schedule's time per call in ms.
+    double tune(void* ans, const void* rhs, int nrhs, cudaStream_t st) {
+        if (precision != FDMGPU_MIXED || !mixed_ok || periodic) return 0.0;
+        ensure_mixed_tables();
+        const int tc_axes = (tc_supported(nx + 1) ? 1 : 0) | (tc_supported(ny + 1) ? 2 : 0);
+        const int sweeps = sweeps_for_tol();
+        cudaEvent_t a, b;
+        FDM_CUDA(cudaEventCreate(&a));
+        FDM_CUDA(cudaEventCreate(&b));
+        double best = 1e30;
+        int bp = pipeline, bz = zmode, bt = tc_mask();
+        try {
+            for (int pl = 1; pl >= 0; pl--)
+                for (int zm = 1; zm >= 0; zm--)
+                    for (int tc = 0; tc <= 3; tc++) {
+                        if (tc & ~tc_axes) continue;
+                        int C = 0;
+                        // a plane schedule that cannot take planes is the five-pass one
+                        if (pl == 1 && (zm == 0 || (tc & 1) || !plane_split(nx + 1, nz, &C))) continue;
+                        if (zm == 0 && sweeps == 0) continue;
+                        pipeline = pl;
+                        zmode = zm;
+                        dst_tc = tc;
+                        solve_device(ans, rhs, nrhs, st);  // warm-up: tables and scratch of this schedule
+                        FDM_CUDA(cudaEventRecord(a, st));
+                        solve_device(ans, rhs, nrhs, st);
+                        FDM_CUDA(cudaEventRecord(b, st));
+                        FDM_CUDA(cudaEventSynchronize(b));
+                        float ms = 0.f;
+                        FDM_CUDA(cudaEventElapsedTime(&ms, a, b));
+                        if ((zm == 0 || tc != 0) && sweeps > 0) {
+                            const double e = first_sweep_est(nrhs, st);
+                            if (10.0 * std::pow(e, sweeps + 1) > tol) continue;
+                        }
+                        if (ms < best) {
+                            best = ms;
+                            bp = pl;
+                            bz = zm;
+                            bt = tc;
+                        }
+                    }
+        } catch (...) {
+            cudaEventDestroy(a);
+            cudaEventDestroy(b);
+            throw;
+        }
+        cudaEventDestroy(a);
+        cudaEventDestroy(b);
+        pipeline = bp;
+        zmode = bz;
+        dst_tc = bt;
+        return best;
     }
 
     void solve_device(void* ans, const void* rhs, int nrhs, cudaStream_t st) {
@@ -852,11 +931,13 @@ struct CubePlan {
     // error e on u leaves a multiple of e on the rougher correction).
     // Measured on GB300 over 16 cases (31^3 to 255^3, anisotropic spacings,
     // smooth and white-noise data; relative L2 against the FP64 form): error
-    // after one sweep / e_1^2 between 2.5 and 44, error after two sweeps /
-    // kappa between 1.1e-17 and 6.7e-17.  The constants keep a margin of 2.3
-    // and 1.5 over those.
+    // after one sweep / e_1^2 between 2.5 and 44.  Error after two sweeps /
+    // kappa: 1.1e-17 to 6.7e-17 on those cases, but up to 2.0e-16 over 44
+    // more (elongated boxes such as 31 x 255 x 31 and 255 x 31 x 31, with FFT
+    // and with tensor-core DST passes).  The constants keep a margin of 2.3
+    // and 1.5 over the largest.
     static constexpr double kRhoPerErr = 100.0;
-    static constexpr double kFloorPerKappa = 1e-16;
+    static constexpr double kFloorPerKappa = 3e-16;
     double kappa = 0.0;  // largest over smallest eigenvalue, summed over the axes
     double est_after(double ek, double ekm1, int k) const {
         if (ek <= 0.0) return kFloorPerKappa * kappa;
@@ -2025,7 +2106,7 @@ int fdmgpu_batch_schedule(fdmgpu_batch* h, int group, int* n3, int* members, int
     if (members) *members = (int)gr.members.size();
     if (chunk) *chunk = gr.chunk;
     if (ztable) *ztable = gr.zmode;
-    if (dst_tc) *dst_tc = gr.plan->dst_tc;
+    if (dst_tc) *dst_tc = gr.plan->tc_mask();
     if (tuned_ms) *tuned_ms = gr.tuned_ms;
     FDM_API_END
 }
@@ -2282,6 +2363,25 @@ int fdmgpu_lapl_cube_set_schedule(fdmgpu_lapl_cube* h, int ztable, int dst_tc) {
     if ((ztable != 0 && ztable != 1) || dst_tc < 0 || dst_tc > 3) FDM_FAIL(FDMGPU_EINVAL, "ztable 0/1, dst_tc 0..3");
     h->plan.zmode = ztable;
     h->plan.dst_tc = dst_tc;
+    FDM_API_END
+}
+
+int fdmgpu_lapl_cube_tune(fdmgpu_lapl_cube* h, void* d_ans, const void* d_rhs, int nrhs, void* stream,
+                          double* ms) {
+    FDM_API_BEGIN
+    if (!h || !d_ans || !d_rhs) FDM_FAIL(FDMGPU_EINVAL, "null argument");
+    if (nrhs < 1) FDM_FAIL(FDMGPU_EINVAL, "nrhs must be positive");
+    const double t = h->plan.tune(d_ans, d_rhs, nrhs, (cudaStream_t)stream);
+    if (ms) *ms = t;
+    FDM_API_END
+}
+
+int fdmgpu_lapl_cube_get_schedule(fdmgpu_lapl_cube* h, int* pipeline, int* ztable, int* dst_tc) {
+    FDM_API_BEGIN
+    if (!h) FDM_FAIL(FDMGPU_EINVAL, "null handle");
+    if (pipeline) *pipeline = h->plan.pipeline;
+    if (ztable) *ztable = h->plan.zmode;
+    if (dst_tc) *dst_tc = h->plan.tc_mask();
     FDM_API_END
 }
 

@@ -126,6 +126,24 @@ class LaplCube:
         mask = 3 if dst_tc is True else int(dst_tc)
         N.check(self._lib.fdmgpu_lapl_cube_set_schedule(self._h, int(bool(ztable)), mask))
 
+    def tune(self, ans, rhs, nrhs: int = 1, stream=None) -> float:
+        """Times every mixed-form schedule (pipeline, z-solve variant,
+        tensor-core axes) on these device arrays and keeps the fastest whose
+        accuracy is assured; returns its time per call in ms."""
+        eb = self.dtype.itemsize
+        ms = c_double()
+        N.check(self._lib.fdmgpu_lapl_cube_tune(self._h, _dev_ptr(ans, eb, self.count * nrhs),
+                                                _dev_ptr(rhs, eb, self.count * nrhs), int(nrhs),
+                                                _stream_ptr(stream), byref(ms)))
+        return ms.value
+
+    def schedule(self) -> dict:
+        """The mixed form's schedule: pipeline asked for ('planes' or
+        'five_pass'), table-driven z-solve, tensor-core axes (bit 0 x, 1 y)."""
+        p, z, t = c_int(), c_int(), c_int()
+        N.check(self._lib.fdmgpu_lapl_cube_get_schedule(self._h, byref(p), byref(z), byref(t)))
+        return {"pipeline": "planes" if p.value == 1 else "five_pass", "ztable": bool(z.value), "dst_tc": t.value}
+
     def set_pipeline(self, planes: bool = True) -> None:
         """Mixed-form pass structure: the fused x-z plane pass between two
         DSTs along y (default, where the sizes allow it) or the five passes

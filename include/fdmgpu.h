@@ -125,9 +125,11 @@ int fdmgpu_lapl_cube_solve_device(fdmgpu_lapl_cube* h, void* d_ans, const void* 
  * hosts that forbid device allocation once initialised.  Same arguments as a
  * handle created with these sizes and set to FDMGPU_MIXED with `tol`, called
  * through fdmgpu_lapl_cube_solve_device (FP64 device arrays, nrhs volumes
- * back to back, asynchronous on stream), but no handle.  It runs the same
- * kernels with the same schedule: sweeps chosen by tol, the per-mode z factor
- * table when the z line splits into blocks.  Its tables are computed on the
+ * back to back, asynchronous on stream), but no handle.  It runs the
+ * handle's kernels in the five-pass order with FFT DST passes (a handle may
+ * instead take the fused plane pass, or the tensor cores for 32-point axes;
+ * the answers agree to the mixed tolerance), sweeps chosen by tol, the
+ * per-mode z factor table when the z line splits into blocks.  Its tables are computed on the
  * device in FP64 (a handle builds them on the host), so an FP32 table entry
  * can differ in its last bit and the answer agrees with the handle's to
  * round-off of the refined solve, not bit for bit.  The tables, FP32 work
@@ -159,7 +161,7 @@ int fdmgpu_lapl_cube_solve_mixed_noalloc(double dx, double dy, double dz, double
  * size of its correction; the estimate after the last sweep is rho e_k with
  * the observed contraction rho = e_k/e_{k-1}, or rho = 100 e_1 after a single
  * sweep (a margin over the FP32 inner solve's contraction measured on GB300),
- * and never below 1e-16 times the operator's eigenvalue ratio (the floor of
+ * and never below 3e-16 times the operator's eigenvalue ratio (the floor of
  * the float-float residual).
  * est may be NULL; it receives nrhs values.  Synchronises the handle's last
  * stream.  (No reference counterpart: the reference solves exactly in T.) */
@@ -176,8 +178,24 @@ int fdmgpu_lapl_cube_scratch_bytes(fdmgpu_lapl_cube* h, size_t* bytes);
 /* schedule of the mixed form: ztable = 1 uses the per-mode z factor table
  * (default), 0 computes the factors per solve; dst_tc bit 0 / bit 1 runs the
  * plain FP32 DST passes along x / y on the tensor cores when that axis has
- * 32, 64 or 128 points (default 0: FFTs) */
+ * 32, 64 or 128 points.  Until this is called, a mixed plan puts 32-point x
+ * axes on the tensor cores, and 32-point y axes when it runs the five-pass
+ * pipeline (the faster schedules measured on GB300); every other axis runs
+ * FFTs. */
 int fdmgpu_lapl_cube_set_schedule(fdmgpu_lapl_cube* h, int ztable, int dst_tc);
+/* Times every schedule of the mixed form (pipeline, z-solve variant,
+ * tensor-core axes) on nrhs right-hand sides at d_rhs (answers to d_ans)
+ * and keeps the fastest whose accuracy is assured: with a refinement sweep,
+ * a variant without the z factor table or with tensor-core passes must show,
+ * from its measured first-sweep correction e, that 10 e^(sweeps+1) <= tol;
+ * without a sweep, variants without the table are not kept.  Synchronous on
+ * stream; *ms (may be NULL) receives the kept schedule's time per call.  A
+ * plain or FP64-fallback plan is left as it is.  No reference counterpart. */
+int fdmgpu_lapl_cube_tune(fdmgpu_lapl_cube* h, void* d_ans, const void* d_rhs, int nrhs, void* stream, double* ms);
+/* the mixed form's schedule: the pipeline asked for (FDMGPU_PIPE_*;
+ * fdmgpu_lapl_cube_pipeline_in_use reports the one a solve runs), ztable and
+ * the tensor-core axes (dst_tc bits) */
+int fdmgpu_lapl_cube_get_schedule(fdmgpu_lapl_cube* h, int* pipeline, int* ztable, int* dst_tc);
 /* pass structure of the mixed form (no counterpart in the reference, which
  * transforms x, y and z in turn, src/lapl_cube.cpp:13-141).
  * FDMGPU_PIPE_PLANES (default): per sweep the DST along y, one fused pass per

@@ -235,6 +235,58 @@ def test_plane_pipeline_applicability(cuda):
     assert LaplCube(*workloads.solver_args(127, 127, 127)).pipeline_in_use() == "five_pass"  # plain FP64
 
 
+def test_default_tensor_core_axes(cuda):
+    """A mixed plan puts 32-point x axes on the tensor cores, and 32-point y
+    axes where it runs the five passes; its answers stay within the mixed
+    tolerance of the FP64 form, and set_schedule overrides the default."""
+    import torch
+    cases = {(31, 31, 31): 3, (31, 63, 63): 1, (63, 31, 63): 0, (63, 31, 31): 2, (127, 127, 127): 0,
+             (63, 63, 63): 0}
+    for shape, mask in cases.items():
+        args = workloads.solver_args(*shape)
+        m = LaplCube(*args, precision="mixed", tol=1e-10)
+        assert m.schedule()["dst_tc"] == mask, shape
+        f = workloads.manufactured_torch(*shape, seed=5, kmax=min(shape) // 4, noise=1e-3)[0]
+        f = torch.stack([f, torch.flip(f, dims=[0])]).contiguous()
+        a, u = torch.empty_like(f), torch.empty_like(f)
+        m.solve_device(a, f, nrhs=2)
+        LaplCube(*args).solve_device(u, f, nrhs=2)
+        s, est = m.last_info(2)
+        for i in range(2):
+            err = (torch.linalg.norm(a[i] - u[i]) / torch.linalg.norm(u[i])).item()
+            assert err <= TOL_MIXED and err <= est[i], (shape, i, err, est[i])
+    assert LaplCube(*workloads.solver_args(31, 31, 31)).schedule()["dst_tc"] == 0  # plain FP64
+    m = LaplCube(*workloads.solver_args(31, 31, 31), precision="mixed", tol=1e-10)
+    m.set_schedule(ztable=True, dst_tc=0)
+    assert m.schedule()["dst_tc"] == 0
+
+
+@pytest.mark.parametrize("shape,nrhs,tol", [((31, 31, 31), 8, 1e-10), ((63, 31, 127), 2, 1e-10),
+                                            ((63, 63, 63), 4, 1e-12), ((31, 63, 31), 4, 1e-4)])
+def test_tune_keeps_an_accurate_schedule(cuda, shape, nrhs, tol):
+    """tune() times the mixed schedules on the caller's data and keeps one
+    whose answers meet the tolerance against the FP64 form."""
+    import torch
+    args = workloads.solver_args(*shape)
+    f = torch.stack([workloads.manufactured_torch(*shape, seed=s, kmax=min(shape) // 4, noise=1e-3)[0]
+                     for s in range(nrhs)]).contiguous()
+    u, a = torch.empty_like(f), torch.empty_like(f)
+    LaplCube(*args).solve_device(u, f, nrhs=nrhs)
+    m = LaplCube(*args, precision="mixed", tol=tol)
+    ms = m.tune(a, f, nrhs=nrhs)
+    assert ms > 0.0
+    sch = m.schedule()
+    assert sch["dst_tc"] in (0, 1, 2, 3)
+    a.fill_(float("nan"))
+    m.solve_device(a, f, nrhs=nrhs)
+    for i in range(nrhs):
+        err = (torch.linalg.norm(a[i] - u[i]) / torch.linalg.norm(u[i])).item()
+        assert err <= max(tol, 1e-12), (shape, sch, i, err)
+    # a plain plan is left as it is
+    p = LaplCube(*args)
+    assert p.tune(a, f, nrhs=nrhs) == 0.0
+
+
 def _white_or_smooth(shape, white, seed):
     import torch
     nx, ny, nz = shape
@@ -245,7 +297,8 @@ def _white_or_smooth(shape, white, seed):
 
 
 @pytest.mark.parametrize("shape,white", [((255, 255, 255), True), ((255, 255, 31), True), ((127, 63, 255), False),
-                                         ((63, 31, 63), True), ((31, 31, 31), False)])
+                                         ((63, 31, 63), True), ((31, 31, 31), False), ((31, 31, 31), True),
+                                         ((31, 255, 31), True), ((255, 31, 31), False), ((63, 31, 31), True)])
 def test_error_estimate_bounds_error(cuda, shape, white):
     """last_info's per-RHS estimate of the remaining error is at least the
     error against the FP64 form, after one sweep and after two."""
