@@ -471,7 +471,7 @@ SERVE_RATES = (100, 300, 1000, 3000, 5000)
 
 
 def measure_serving(torch, fdm_gb300, workloads, dev, rates=SERVE_RATES, seconds=4.0, max_requests=20000,
-                    max_outstanding=1024, lanes=16, max_batch=8):
+                    max_outstanding=1024, lanes=32, max_batch=8):
     """Serving loop under Poisson arrivals at each rate: 70% single solves
     (each axis from {31,63,127}, 5% at 255^3, tol 1e-6 or 1e-10 half and
     half), 30% advances of k ~ U{1..50} steps on 64 resident 63^3 cavity
