@@ -170,13 +170,14 @@ constexpr const char* sine_name() {
                                : "sine_x_f32";
 }
 
-template <typename Tin, typename T, typename Tout, int AXIS, int MODE, int N>
-static void launch_rg(const Tin* in, Tout* out, int nx, int ny, int nz, int nvol, const SineTables<T>& tb,
-                      double scale, cudaStream_t st, const SineFused& fu, SineGeom geo) {
-    constexpr int L = RgGeom<N, AXIS>::L;
-    constexpr size_t smem = rg_smem_bytes<T, N, AXIS>();
+template <typename Tin, typename T, typename Tout, int AXIS, int MODE, int N, int NT = 256>
+static void launch_rg_nt(const Tin* in, Tout* out, int nx, int ny, int nz, int nvol, const SineTables<T>& tb,
+                         double scale, cudaStream_t st, const SineFused& fu, const SineGeom& geo) {
+    constexpr int L = RgGeom<N, AXIS, NT>::L;
+    constexpr size_t smem = rg_smem_bytes<T, N, AXIS, NT>();
     const auto kern = [] {
-        if constexpr (rg_use_occ5<T, AXIS, N>()) return k_sine_rg_occ5<Tin, T, Tout, AXIS, MODE, N>;
+        if constexpr (NT != 256) return k_sine_rg<Tin, T, Tout, AXIS, MODE, N, NT>;
+        else if constexpr (rg_use_occ5<T, AXIS, N>()) return k_sine_rg_occ5<Tin, T, Tout, AXIS, MODE, N>;
         else if constexpr (rg_use_occ<T, AXIS, N>()) return k_sine_rg_occ<Tin, T, Tout, AXIS, MODE, N>;
         else return k_sine_rg<Tin, T, Tout, AXIS, MODE, N>;
     }();
@@ -190,8 +191,27 @@ static void launch_rg(const Tin* in, Tout* out, int nx, int ny, int nz, int nvol
     else gx = (unsigned)(nz * ((nx + L - 1) / L));
     dim3 grid(gx, nvol);
     FDM_TIMED((sine_name<Tin, T, Tout, AXIS, MODE>()), st);
-    kern<<<grid, 256, smem, st>>>(in, out, geo, tb, (T)scale, fu);
+    kern<<<grid, NT, smem, st>>>(in, out, geo, tb, (T)scale, fu);
     FDM_LAUNCH_CHECK();
+}
+
+// Lines of up to 64 points in volumes too small to give every SM two CTAs
+// of 256 threads run in CTAs of 128 or 64 (fewer lines per CTA, more CTAs):
+// a 63^3 volume's 3969 lines make 62 CTAs of 64 lines, on 62 of 152 SMs.
+template <typename Tin, typename T, typename Tout, int AXIS, int MODE, int N>
+static void launch_rg(const Tin* in, Tout* out, int nx, int ny, int nz, int nvol, const SineTables<T>& tb,
+                      double scale, cudaStream_t st, const SineFused& fu, SineGeom geo) {
+    if constexpr (N <= 64) {
+        const long long lines = (AXIS == 0 ? (long long)ny * nz : (long long)nx * nz) * nvol;
+        const long long want = 2LL * sm_count();
+        if (lines / RgGeom<N, AXIS, 256>::L < want) {
+            if (lines / RgGeom<N, AXIS, 128>::L >= want)
+                return launch_rg_nt<Tin, T, Tout, AXIS, MODE, N, 128>(in, out, nx, ny, nz, nvol, tb, scale, st, fu,
+                                                                      geo);
+            return launch_rg_nt<Tin, T, Tout, AXIS, MODE, N, 64>(in, out, nx, ny, nz, nvol, tb, scale, st, fu, geo);
+        }
+    }
+    launch_rg_nt<Tin, T, Tout, AXIS, MODE, N, 256>(in, out, nx, ny, nz, nvol, tb, scale, st, fu, geo);
 }
 
 // ---------------------------------------------------------------------------

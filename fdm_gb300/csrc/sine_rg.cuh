@@ -36,12 +36,14 @@ template <> struct RgCfg<128> { static constexpr int R1 = 8, R2 = 8; };
 template <> struct RgCfg<256> { static constexpr int R1 = 16, R2 = 8; };
 template <> struct RgCfg<512> { static constexpr int R1 = 16, R2 = 16; };
 
-template <int N, int AXIS>
+// NT: threads per CTA (256; 128 or 64 for the lines of up to 64 points of
+// volumes too small to give every SM two CTAs of 256)
+template <int N, int AXIS, int NT = 256>
 struct RgGeom {
     static constexpr int M = N / 2;
     static constexpr int R1 = RgCfg<N>::R1, R2 = RgCfg<N>::R2;
     static constexpr int G = R2;              // threads per line
-    static constexpr int L = 256 / G;         // lines per CTA
+    static constexpr int L = NT / G;          // lines per CTA
     static constexpr int D2 = R1 / G;         // length-R2 DFTs per thread in pass 2
     static constexpr int E = M / (2 * G);     // unpack pairs per thread
     static constexpr int TR = R1 * (R2 + 1);  // transpose slots
@@ -320,11 +322,13 @@ __device__ __forceinline__ void norms_reduce(float cc, float uu, double* norms, 
     }
 }
 
-template <typename Tin, typename T, typename Tout, int AXIS, int MODE, int N>
+template <typename Tin, typename T, typename Tout, int AXIS, int MODE, int N, int NT = 256>
 __device__ __forceinline__ void sine_rg_body(const Tin* in, Tout* out, const SineGeom& geo, const SineTables<T>& tb,
                                              T scale, const SineFused& fu) {
     using T2 = vec2_t<T>;
-    using Gm = RgGeom<N, AXIS>;
+    using Gm = RgGeom<N, AXIS, NT>;
+    // the lane-per-line column path and the paired row store walk 8 warps
+    static_assert(NT == 256 || N <= 64, "CTAs of fewer than 256 threads are for lines of up to 64 points");
     constexpr int M = Gm::M, G = Gm::G, L = Gm::L;
     constexpr int LS2 = Gm::LS2;
     constexpr int n = N - 1;
@@ -351,7 +355,7 @@ __device__ __forceinline__ void sine_rg_body(const Tin* in, Tout* out, const Sin
 
     // ---- load + fold: item (line, j) reads x_j and x_{N-j} and writes
     // y_j = w_j (a+b) + (a-b)/2 and y_{N-j} = w_j (a+b) - (a-b)/2
-    constexpr bool kCol32 = AXIS == 1 && L == 32 && MODE != kResidual;
+    constexpr bool kCol32 = AXIS == 1 && L == 32 && NT == 256 && MODE != kResidual;
     const int lane = tid & 31, wid = tid >> 5;
     if constexpr (kCol32) {
         // column pass with one line per lane: warp w takes the items j =
@@ -613,10 +617,10 @@ __device__ __forceinline__ void sine_rg_body(const Tin* in, Tout* out, const Sin
     }
 }
 
-template <typename Tin, typename T, typename Tout, int AXIS, int MODE, int N>
-__global__ void __launch_bounds__(256) k_sine_rg(const Tin* in, Tout* out, SineGeom geo, SineTables<T> tb, T scale,
-                                                 SineFused fu) {
-    sine_rg_body<Tin, T, Tout, AXIS, MODE, N>(in, out, geo, tb, scale, fu);
+template <typename Tin, typename T, typename Tout, int AXIS, int MODE, int N, int NT = 256>
+__global__ void __launch_bounds__(NT) k_sine_rg(const Tin* in, Tout* out, SineGeom geo, SineTables<T> tb, T scale,
+                                                SineFused fu) {
+    sine_rg_body<Tin, T, Tout, AXIS, MODE, N, NT>(in, out, geo, tb, scale, fu);
 }
 
 // The same kernel held to 64 registers (4 CTAs of 256 threads per SM): for
@@ -648,9 +652,9 @@ constexpr bool rg_use_occ5() {
     return sizeof(T) == 4 && AXIS == 1 && N == 256;
 }
 
-template <typename T, int N, int AXIS>
+template <typename T, int N, int AXIS, int NT = 256>
 constexpr size_t rg_smem_bytes() {
-    return (size_t)RgGeom<N, AXIS>::L * RgGeom<N, AXIS>::LS2 * sizeof(vec2_t<T>);
+    return (size_t)RgGeom<N, AXIS, NT>::L * RgGeom<N, AXIS, NT>::LS2 * sizeof(vec2_t<T>);
 }
 
 }  // namespace fdmgpu
