@@ -96,12 +96,18 @@ __global__ void __launch_bounds__(256, MINB) k_plane_xz(float* __restrict__ W, P
     // The fold and store phases run one warp per line: lane c takes the
     // items j = c + 32k (and lane 0 also j = M), so every global and shared
     // address is a per-thread base plus a compile-time offset.  In the fold
-    // input entry j of line l is float 2 l LS2 + j; in the packed output
-    // entry i is float 2 l LS2 + 2 sk(i>>1) + (i&1), which is c + 34k for
-    // i = c + 32k and fb - 34k for i = N - c - 32k (fb below).
+    // input entry j of the line at position p is float 2 p LS2 + j; in the
+    // packed output entry i is float 2 p LS2 + 2 sk(i>>1) + (i&1), which is
+    // c + 34k for i = c + 32k and fb - 34k for i = N - c - 32k (fb below).
+    // Warp w folds, transforms and stores the rows w + 8j (j < LPW), kept at
+    // positions LPW w + j: the transform's G threads of position p belong to
+    // warp p / LPW, so between fold, transform and store only the warp
+    // synchronises.  Row q of the CTA sits at position rowpos(q).
     const int lane = tid & 31, wid = tid >> 5;
     constexpr int KJ = M / 32;  // full rounds of 32 items per line (j < M)
     constexpr int LPW = L / 8;  // lines per warp
+    static_assert(LPW * G == 32, "a warp's transform threads hold its own rows");
+    auto rowpos = [](int q) { return LPW * (q & 7) + (q >> 3); };
     const int hh = (lane + 1) >> 1;
     const int fb = 2 * (M + M / 16 - hh - (hh > 0 ? 1 : 0)) + (lane & 1);
     static_assert(M % 32 == 0 && L % 8 == 0, "warp-per-line phases");
@@ -110,7 +116,7 @@ __global__ void __launch_bounds__(256, MINB) k_plane_xz(float* __restrict__ W, P
 #pragma unroll
     for (int li = 0; li < LPW; li++) {
         const int line = wid + 8 * li;
-        float* xo = Sr + 2 * line * LS2;
+        float* xo = Sr + 2 * (LPW * wid + li) * LS2;
         if (line < nact) {
             const float* p = row0 + line * rstride;
             float a[KJ], b[KJ];
@@ -136,12 +142,12 @@ __global__ void __launch_bounds__(256, MINB) k_plane_xz(float* __restrict__ W, P
             for (int k = 0; k < 2 * KJ; k++) xo[lane + 32 * k] = 0.f;
         }
     }
-    __syncthreads();
+    __syncwarp();
     rg_line_fft<float, N, 0, kPlaneSwz>(S + l * LS2, g, l, tb);
     __syncthreads();
 
     // ---- 2. z blocks: thread t owns x-mode i = t+1 of every local block.
-    // Entry i of row q sits at Sr[2*(q*LS2 + sk(i>>1)) + (i&1)].
+    // Entry i of row q sits at Sr[2*(rowpos(q)*LS2 + sk(i>>1)) + (i&1)].
     const int t = tid;
     const bool mode_ok = t < n;
     const int i = t + 1;
@@ -156,10 +162,10 @@ __global__ void __launch_bounds__(256, MINB) k_plane_xz(float* __restrict__ W, P
 #pragma unroll
         for (int b = 0; b < B; b++) {
             const int gb = r * B + b;
-            float* col = Sr + fo + 16 * b * RS;
+            float* col = Sr + fo;
             float v[m];
 #pragma unroll
-            for (int k = 0; k < m; k++) v[k] = col[k * RS];
+            for (int k = 0; k < m; k++) v[k] = col[rowpos(16 * b + k) * RS];
             float prev = 0.f;
 #pragma unroll
             for (int k = 0; k < m; k++) {
@@ -169,10 +175,10 @@ __global__ void __launch_bounds__(256, MINB) k_plane_xz(float* __restrict__ W, P
 #pragma unroll
             for (int k = m - 2; k >= 0; k--) v[k] = v[k] - cp[k] * v[k + 1];
 #pragma unroll
-            for (int k = 0; k < m; k++) col[k * RS] = v[k];
+            for (int k = 0; k < m; k++) col[rowpos(16 * b + k) * RS] = v[k];
             xf[b * XS + t] = v[0];
             xl[b * XS + t] = v[m - 1];
-            xg[b * XS + t] = gb < P - 1 ? col[m * RS] * gs : 0.f;
+            xg[b * XS + t] = gb < P - 1 ? col[rowpos(16 * b + m) * RS] * gs : 0.f;
         }
     }
     // the plane's outer ends: s[-1] = s[P-1] = 0
@@ -229,10 +235,13 @@ __global__ void __launch_bounds__(256, MINB) k_plane_xz(float* __restrict__ W, P
         for (int b = 0; b < B; b++) {
             const int gb = r * B + b;
             const float ul = xs[b * XS + t], ur = xs[(b + 1) * XS + t];
-            float* col = Sr + fo + 16 * b * RS;
+            float* col = Sr + fo;
 #pragma unroll
-            for (int k = 0; k < m; k++) col[k * RS] = col[k * RS] + be[m - 1 - k] * ul + be[k] * ur;
-            if (gb < P - 1) col[m * RS] = ur;
+            for (int k = 0; k < m; k++) {
+                float& e = col[rowpos(16 * b + k) * RS];
+                e = e + be[m - 1 - k] * ul + be[k] * ur;
+            }
+            if (gb < P - 1) col[rowpos(16 * b + m) * RS] = ur;
         }
     }
     __syncthreads();
@@ -242,8 +251,7 @@ __global__ void __launch_bounds__(256, MINB) k_plane_xz(float* __restrict__ W, P
     // layouts overlap)
 #pragma unroll
     for (int li = 0; li < LPW; li++) {
-        const int line = wid + 8 * li;
-        float* base = Sr + 2 * line * LS2;
+        float* base = Sr + 2 * (LPW * wid + li) * LS2;
         float a[KJ], b[KJ];
 #pragma unroll
         for (int k = 0; k < KJ; k++) {
@@ -263,9 +271,9 @@ __global__ void __launch_bounds__(256, MINB) k_plane_xz(float* __restrict__ W, P
         }
         if (lane == 0) base[M] = ldg(tb.wpre + M) * (am + am);
     }
-    __syncthreads();
+    __syncwarp();
     rg_line_fft<float, N, 0, kPlaneSwz>(S + l * LS2, g, l, tb);
-    __syncthreads();
+    __syncwarp();
 
     // ---- 6. store the rows: slot k = c + 32q of a line holds F_2k and
     // F_2k+1, which go to x = 2k-1 and 2k
@@ -273,7 +281,7 @@ __global__ void __launch_bounds__(256, MINB) k_plane_xz(float* __restrict__ W, P
     for (int li = 0; li < LPW; li++) {
         const int line = wid + 8 * li;
         if (line >= nact) continue;
-        const T2* src = S + line * LS2 + lane + (lane >> 4);
+        const T2* src = S + (LPW * wid + li) * LS2 + lane + (lane >> 4);
         float* dst = row0 + line * rstride + 2 * lane;
 #pragma unroll
         for (int q = 0; q < M / 32; q++) {
