@@ -59,6 +59,10 @@ struct NSParams {
     // of two correctly rounded divisions (five operations each)
     double rRe_dx2, rRe_dy2, rRe_dz2, rRe_dx, rRe_dy, rRe_dz;
     double rdx, rdy, rdz, rdx2, rdy2, rdz2, rdt;
+    // the fast FGH's constants with dt folded in: dt / (Re h^2) for the
+    // diffusion terms, dt / (4 h) for the convection terms (whose 0.5 and
+    // 0.25 factors they absorb); the fast divergence's 1 / (h dt)
+    double kCx, kCy, kCz, kAx, kAy, kAz, kRx, kRy, kRz;
 };
 
 // x / d (FAST: x * r, r = 1 / d computed on the host; otherwise the
@@ -183,8 +187,11 @@ __global__ void k_ns_bound2(FieldT<T> u, FieldT<T> v, FieldT<T> w, FieldT<T> p, 
 // FGH (src/ns_cube.cpp:126-200), one thread per (i,k,j) of the box
 // [0,nz] x [0,ny] x [0,nx]; each thread writes whichever of F, G, H has that
 // point in its range.  FAST: quotients by the run constants as products with
-// their reciprocals (about half the FP64 operations; results within a few
-// units in the last place of the exact form's).
+// their reciprocals, and for FP64 fields dt and the convection terms' 0.5 /
+// 0.25 folded into per-axis constants so that each component is one chain of
+// fused multiply-adds (about a quarter of the exact form's FP64 operations;
+// results within a few units in the last place of the exact form's).  The
+// float cavity keeps the reference's expressions and promotions.
 template <typename T, bool FAST>
 __global__ void __launch_bounds__(256)
     k_ns_fgh(FieldT<T> u, FieldT<T> v, FieldT<T> w, FieldT<T> F, FieldT<T> G, FieldT<T> H, NSParams P) {
@@ -205,6 +212,50 @@ __global__ void __launch_bounds__(256)
     // common (the stores could alias the velocity fields)
     double fv = 0.0, gv = 0.0, hv = 0.0;
     const bool doF = i >= 1 && k >= 1, doG = i >= 1 && j >= 1, doH = k >= 1 && j >= 1;
+    if constexpr (FAST && sizeof(T) == 8) {
+        // FP64 fields: u + dt (diffusion - convection) as one chain of fused
+        // multiply-adds
+        // per component: sq(a/2) - sq(b/2) = (a^2 - b^2) / 4 and the
+        // cross terms' 0.25 go into dt / (4 h); the three cross products
+        // that two components share (F's y term and G's x term, F's z term
+        // and H's x term, G's z term and H's y term) are formed once.  Every
+        // read below is inside its field's range for any point of the box.
+        const double uc = u(i, k, j), vc = v(i, k, j), wc = w(i, k, j);
+        const double puv = (uc + u(i, k + 1, j)) * (v(i, k, j + 1) + vc);
+        const double puw = (uc + u(i + 1, k, j)) * (w(i, k, j + 1) + wc);
+        const double pwv = (wc + w(i, k + 1, j)) * (vc + v(i + 1, k, j));
+        auto lap = [](double m, double c, double pl) { return (m + pl) - 2.0 * c; };
+        if (doF) {
+            const double a = uc + u(i, k, j + 1), b = u(i, k, j - 1) + uc;
+            double acc = uc + P.kCx * lap(u(i, k, j - 1), uc, u(i, k, j + 1));
+            acc += P.kCy * lap(u(i, k - 1, j), uc, u(i, k + 1, j));
+            acc += P.kCz * lap(u(i - 1, k, j), uc, u(i + 1, k, j));
+            acc -= P.kAx * (a * a - b * b);
+            acc -= P.kAy * (puv - (u(i, k - 1, j) + uc) * (v(i, k - 1, j + 1) + v(i, k - 1, j)));
+            acc -= P.kAz * (puw - (u(i - 1, k, j) + uc) * (w(i - 1, k, j + 1) + w(i - 1, k, j)));
+            fv = acc;
+        }
+        if (doG) {
+            const double a = vc + v(i, k + 1, j), b = v(i, k - 1, j) + vc;
+            double acc = vc + P.kCx * lap(v(i, k, j - 1), vc, v(i, k, j + 1));
+            acc += P.kCy * lap(v(i, k - 1, j), vc, v(i, k + 1, j));
+            acc += P.kCz * lap(v(i - 1, k, j), vc, v(i + 1, k, j));
+            acc -= P.kAy * (a * a - b * b);
+            acc -= P.kAx * (puv - (u(i, k, j - 1) + u(i, k + 1, j - 1)) * (vc + v(i, k, j - 1)));
+            acc -= P.kAz * (pwv - (w(i - 1, k, j) + w(i - 1, k + 1, j)) * (v(i - 1, k, j) + vc));
+            gv = acc;
+        }
+        if (doH) {
+            const double a = w(i + 1, k, j) + wc, b = w(i - 1, k, j) + wc;
+            double acc = wc + P.kCx * lap(w(i, k, j - 1), wc, w(i, k, j + 1));
+            acc += P.kCy * lap(w(i, k - 1, j), wc, w(i, k + 1, j));
+            acc += P.kCz * lap(w(i - 1, k, j), wc, w(i + 1, k, j));
+            acc -= P.kAz * (a * a - b * b);
+            acc -= P.kAx * (puw - (u(i + 1, k, j - 1) + u(i, k, j - 1)) * (wc + w(i, k, j - 1)));
+            acc -= P.kAy * (pwv - (w(i, k - 1, j) + wc) * (v(i, k - 1, j) + v(i + 1, k - 1, j)));
+            hv = acc;
+        }
+    } else {
     if (doF) {
         fv = u(i, k, j) + dt * (
             dif(u(i, k, j + 1) - 2 * u(i, k, j) + u(i, k, j - 1), P.ddx2, P.rRe_dx2) +
@@ -238,6 +289,7 @@ __global__ void __launch_bounds__(256)
             qd(0.25 * ((w(i, k, j) + w(i, k + 1, j)) * (v(i, k, j) + v(i + 1, k, j)) -
                          (w(i, k - 1, j) + w(i, k, j)) * (v(i, k - 1, j) + v(i + 1, k - 1, j))), P.ddy, P.rdy));
     }
+    }
     if (doF) F(i, k, j) = fv;
     if (doG) G(i, k, j) = gv;
     if (doH) H(i, k, j) = hv;
@@ -255,8 +307,13 @@ __global__ void k_ns_rhs(FieldT<T> F, FieldT<T> G, FieldT<T> H, FieldT<T> p, Fie
     const int i = (int)(e / ((long long)nx * ny)) + 1;
     // T-typed like the reference RHS element: rounded after each update
     auto qd = [&](double x, CDiv d, double rc) { return qdiv<FAST>(x, d, rc); };
-    T r = qd(qd(F(i, k, j) - F(i, k, j - 1), P.ddx, P.rdx) + qd(G(i, k, j) - G(i, k - 1, j), P.ddy, P.rdy) +
-                 qd(H(i, k, j) - H(i - 1, k, j), P.ddz, P.rdz), P.ddt, P.rdt);
+    T r;
+    if constexpr (FAST)  // 1 / (h dt) per axis
+        r = (F(i, k, j) - F(i, k, j - 1)) * P.kRx + (G(i, k, j) - G(i, k - 1, j)) * P.kRy +
+            (H(i, k, j) - H(i - 1, k, j)) * P.kRz;
+    else
+        r = qd(qd(F(i, k, j) - F(i, k, j - 1), P.ddx, P.rdx) + qd(G(i, k, j) - G(i, k - 1, j), P.ddy, P.rdy) +
+                   qd(H(i, k, j) - H(i - 1, k, j), P.ddz, P.rdz), P.ddt, P.rdt);
     if (i <= 1) r -= qd(p(i - 1, k, j), P.ddz2, P.rdz2);
     if (k <= 1) r -= qd(p(i, k - 1, j), P.ddy2, P.rdy2);
     if (j <= 1) r -= qd(p(i, k, j - 1), P.ddx2, P.rdx2);
@@ -463,6 +520,9 @@ void setup_plan(NSPlanT<T>& s, int nx, int nz, double x1, double y1, double z1, 
     s.P.rdx = 1.0 / s.P.dx; s.P.rdy = 1.0 / s.P.dy; s.P.rdz = 1.0 / s.P.dz;
     s.P.rdx2 = 1.0 / s.P.dx2; s.P.rdy2 = 1.0 / s.P.dy2; s.P.rdz2 = 1.0 / s.P.dz2;
     s.P.rdt = 1.0 / dt;
+    s.P.kCx = dt / (Re * s.P.dx2); s.P.kCy = dt / (Re * s.P.dy2); s.P.kCz = dt / (Re * s.P.dz2);
+    s.P.kAx = dt / (4.0 * s.P.dx); s.P.kAy = dt / (4.0 * s.P.dy); s.P.kAz = dt / (4.0 * s.P.dz);
+    s.P.kRx = 1.0 / (s.P.dx * dt); s.P.kRy = 1.0 / (s.P.dy * dt); s.P.kRz = 1.0 / (s.P.dz * dt);
     s.init();
 }
 }  // namespace
