@@ -467,11 +467,11 @@ def measure_periodic(torch, fdm_gb300, stream, reps=50):
     return out
 
 
-SERVE_RATES = (100, 300, 1000, 3000, 5000)
+SERVE_RATES = (100, 300, 1000, 1500, 3000, 5000)
 
 
 def measure_serving(torch, fdm_gb300, workloads, dev, rates=SERVE_RATES, seconds=4.0, max_requests=20000,
-                    max_outstanding=1024, lanes=32, max_batch=8):
+                    max_outstanding=1024, lanes=48, max_batch=8):
     """Serving loop under Poisson arrivals at each rate: 70% single solves
     (each axis from {31,63,127}, 5% at 255^3, tol 1e-6 or 1e-10 half and
     half), 30% advances of k ~ U{1..50} steps on 64 resident 63^3 cavity
@@ -667,7 +667,7 @@ def main():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-serving", action="store_true", help="skip the serving-loop sweep")
     ap.add_argument("--serve-rates", default=None,
-                    help="comma-separated arrival rates (req/s) of the serving sweep (default 100,300,1000,3000,5000)")
+                    help="comma-separated arrival rates (req/s) of the serving sweep (default 100,300,1000,1500,3000,5000)")
     ap.add_argument("--ncu-case", nargs="?", const="solve", default=None,
                     choices=["solve", "nscube", "tc", "nbody", "nbody_pp"],
                     help="run only a small case for profiler captures: 'solve' (two mixed solves of 2 RHS at "
