@@ -856,6 +856,7 @@ struct CubePlan {
         FDM_CUDA(cudaEventCreate(&a));
         FDM_CUDA(cudaEventCreate(&b));
         double best = 1e30;
+        const int p0 = pipeline, z0 = zmode, t0 = dst_tc;  // restored if a candidate fails
         int bp = pipeline, bz = zmode, bt = tc_mask();
         try {
             for (int pl = 1; pl >= 0; pl--)
@@ -890,6 +891,9 @@ struct CubePlan {
         } catch (...) {
             cudaEventDestroy(a);
             cudaEventDestroy(b);
+            pipeline = p0;
+            zmode = z0;
+            dst_tc = t0;
             throw;
         }
         cudaEventDestroy(a);

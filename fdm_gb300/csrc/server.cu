@@ -178,9 +178,9 @@ struct Server {
         // lane copied back (host arithmetic)
         if (L->plan && !L->reqs.empty() && L->reqs[0]->kind == FDMGPU_REQ_SOLVE) {
             const int nb = (int)L->reqs.size();
-            double est[64];
-            if (L->sweeps > 0 && nb <= 64) {
-                cube_estimates(L->plan->h, L->norms_host, L->sweeps, nb, est);
+            if (L->sweeps > 0) {
+                std::vector<double> est((size_t)nb);
+                cube_estimates(L->plan->h, L->norms_host, L->sweeps, nb, est.data());
                 for (int i = 0; i < nb; i++) L->reqs[i]->err_est = est[i];
             } else {
                 // FP64 solves (tol <= 0, or a mixed plan beyond its
