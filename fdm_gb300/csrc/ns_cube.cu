@@ -16,6 +16,7 @@
 // with reciprocals computed on the host; the exact form (set_exact) rounds
 // each one as the reference's division does.  Every kernel is bound by the
 // FP64 pipe, which GB300 runs at a small fraction of its FP32 rate.
+#include <algorithm>
 #include <cmath>
 #include <cstdio>
 #include <memory>
@@ -125,7 +126,7 @@ __device__ __forceinline__ double sq(double x) { return x * x; }  // asp::sq, sr
 // point written lies on the surface of the (z,y,x) box [-1, nz+1] x
 // [-1, ny+1] x [-1, nx+1]; one thread per surface point.
 template <typename T>
-__global__ void k_ns_bound1(FieldT<T> u, FieldT<T> v, FieldT<T> w, NSParams P) {
+__device__ __forceinline__ void ns_bound1_body(FieldT<T> u, FieldT<T> v, FieldT<T> w, const NSParams& P) {
     const int nx = P.nx, ny = P.ny, nz = P.nz;
     const long long e = (long long)blockIdx.x * blockDim.x + threadIdx.x;
     int i, k, j;
@@ -157,7 +158,7 @@ __global__ void k_ns_bound1(FieldT<T> u, FieldT<T> v, FieldT<T> w, NSParams P) {
 // point written lies on the surface of the box [0, nz+1] x [0, ny+1] x
 // [0, nx+1]; one thread per surface point.
 template <typename T, bool FAST>
-__global__ void k_ns_bound2(FieldT<T> u, FieldT<T> v, FieldT<T> w, FieldT<T> p, NSParams P) {
+__device__ __forceinline__ void ns_bound2_body(FieldT<T> u, FieldT<T> v, FieldT<T> w, FieldT<T> p, const NSParams& P) {
     const int nx = P.nx, ny = P.ny, nz = P.nz;
     const long long e = (long long)blockIdx.x * blockDim.x + threadIdx.x;
     int i, k, j;
@@ -193,8 +194,8 @@ __global__ void k_ns_bound2(FieldT<T> u, FieldT<T> v, FieldT<T> w, FieldT<T> p, 
 // results within a few units in the last place of the exact form's).  The
 // float cavity keeps the reference's expressions and promotions.
 template <typename T, bool FAST>
-__global__ void __launch_bounds__(256)
-    k_ns_fgh(FieldT<T> u, FieldT<T> v, FieldT<T> w, FieldT<T> F, FieldT<T> G, FieldT<T> H, NSParams P) {
+__device__ __forceinline__ void ns_fgh_body(FieldT<T> u, FieldT<T> v, FieldT<T> w, FieldT<T> F, FieldT<T> G,
+                                            FieldT<T> H, const NSParams& P) {
     const int nx = P.nx, ny = P.ny, nz = P.nz;
     const long long e = (long long)blockIdx.x * blockDim.x + threadIdx.x;
     const int W = nx + 1, Hh = ny + 1, D = nz + 1;
@@ -298,7 +299,8 @@ __global__ void __launch_bounds__(256)
 // Divergence RHS with the Dirichlet pressure ghosts folded in
 // (src/ns_cube.cpp:206-235).
 template <typename T, bool FAST>
-__global__ void k_ns_rhs(FieldT<T> F, FieldT<T> G, FieldT<T> H, FieldT<T> p, FieldT<T> RHS, NSParams P) {
+__device__ __forceinline__ void ns_rhs_body(FieldT<T> F, FieldT<T> G, FieldT<T> H, FieldT<T> p, FieldT<T> RHS,
+                                            const NSParams& P) {
     const int nx = P.nx, ny = P.ny, nz = P.nz;
     const long long e = (long long)blockIdx.x * blockDim.x + threadIdx.x;
     if (e >= (long long)nx * ny * nz) return;
@@ -326,8 +328,8 @@ __global__ void k_ns_rhs(FieldT<T> F, FieldT<T> G, FieldT<T> H, FieldT<T> p, Fie
 // update_uvwp (src/ns_cube.cpp:241-277): pressure-gradient correction of the
 // interior faces, then p = x on the interior (src/tensor.h:280-283).
 template <typename T>
-__global__ void k_ns_update(FieldT<T> u, FieldT<T> v, FieldT<T> w, FieldT<T> p, FieldT<T> x, FieldT<T> F, FieldT<T> G,
-                            FieldT<T> H, NSParams P) {
+__device__ __forceinline__ void ns_update_body(FieldT<T> u, FieldT<T> v, FieldT<T> w, FieldT<T> p, FieldT<T> x, FieldT<T> F, FieldT<T> G,
+                            FieldT<T> H, const NSParams& P) {
     const int nx = P.nx, ny = P.ny, nz = P.nz;
     const long long e = (long long)blockIdx.x * blockDim.x + threadIdx.x;
     if (e >= (long long)nx * ny * nz) return;
@@ -339,6 +341,60 @@ __global__ void k_ns_update(FieldT<T> u, FieldT<T> v, FieldT<T> w, FieldT<T> p, 
     if (k < ny) v(i, k, j) = G(i, k, j) - P.dt_dy * (x(i, k + 1, j) - xc);
     if (i < nz) w(i, k, j) = H(i, k, j) - P.dt_dz * (x(i + 1, k, j) - xc);
     p(i, k, j) = xc;
+}
+
+// Per-session state of a step: the nine fields' storage and the run
+// constants.  One step kernel serves one session or several of the same
+// geometry: blockIdx.y picks the session from a device table of these, the
+// ranges and strides of the fields (the same for all) come as an argument.
+template <typename T>
+struct NSSessionT {
+    T* f[9];  // u v w p x F G H RHS
+    NSParams P;
+};
+template <typename T>
+struct NSGeomT {
+    FieldT<T> f[9];  // ranges and strides (p not used)
+};
+template <typename T>
+__device__ __forceinline__ FieldT<T> ns_field(const NSGeomT<T>& g, const NSSessionT<T>& s, int i) {
+    FieldT<T> r = g.f[i];
+    r.p = s.f[i];
+    return r;
+}
+
+template <typename T>
+__global__ void k_ns_bound1(NSGeomT<T> g, const NSSessionT<T>* __restrict__ ss) {
+    const NSSessionT<T>& S = ss[blockIdx.y];
+    const NSParams P = S.P;
+    ns_bound1_body<T>(ns_field(g, S, 0), ns_field(g, S, 1), ns_field(g, S, 2), P);
+}
+template <typename T, bool FAST>
+__global__ void k_ns_bound2(NSGeomT<T> g, const NSSessionT<T>* __restrict__ ss) {
+    const NSSessionT<T>& S = ss[blockIdx.y];
+    const NSParams P = S.P;
+    ns_bound2_body<T, FAST>(ns_field(g, S, 0), ns_field(g, S, 1), ns_field(g, S, 2), ns_field(g, S, 3), P);
+}
+template <typename T, bool FAST>
+__global__ void __launch_bounds__(256) k_ns_fgh(NSGeomT<T> g, const NSSessionT<T>* __restrict__ ss) {
+    const NSSessionT<T>& S = ss[blockIdx.y];
+    const NSParams P = S.P;
+    ns_fgh_body<T, FAST>(ns_field(g, S, 0), ns_field(g, S, 1), ns_field(g, S, 2), ns_field(g, S, 5),
+                         ns_field(g, S, 6), ns_field(g, S, 7), P);
+}
+template <typename T, bool FAST>
+__global__ void k_ns_rhs(NSGeomT<T> g, const NSSessionT<T>* __restrict__ ss) {
+    const NSSessionT<T>& S = ss[blockIdx.y];
+    const NSParams P = S.P;
+    ns_rhs_body<T, FAST>(ns_field(g, S, 5), ns_field(g, S, 6), ns_field(g, S, 7), ns_field(g, S, 3),
+                         ns_field(g, S, 8), P);
+}
+template <typename T>
+__global__ void k_ns_update(NSGeomT<T> g, const NSSessionT<T>* __restrict__ ss) {
+    const NSSessionT<T>& S = ss[blockIdx.y];
+    const NSParams P = S.P;
+    ns_update_body<T>(ns_field(g, S, 0), ns_field(g, S, 1), ns_field(g, S, 2), ns_field(g, S, 3), ns_field(g, S, 4),
+                      ns_field(g, S, 5), ns_field(g, S, 6), ns_field(g, S, 7), P);
 }
 
 // Cell-centred velocity of the interior cells for the VTK snapshot
@@ -378,8 +434,24 @@ struct NSPlanT {
     cudaGraph_t graph = nullptr;
     cudaGraphExec_t gexec = nullptr;
     int time_index = 0;
-    int steps_run = 0;
+    // a step of its own ran eagerly: kernel attributes are set and the
+    // pressure solve's scratch exists, so later steps can be captured (steps
+    // shared with other cavities use neither)
+    bool warm = false;
     bool exact = false;  // quotients correctly rounded as the reference's (slower)
+    // the step kernels' view of this session: field geometry, and on the
+    // device the session table of one entry and, for the FP64 pressure
+    // solve through pointer tables, {&RHS, &x}
+    NSGeomT<T> geo;
+    DevBuf sess_dev, io_dev;
+    const void* io_host[2] = {nullptr, nullptr};  // {RHS, x}: the FP32 pressure solve's arguments
+
+    NSSessionT<T> session() const {
+        NSSessionT<T> s;
+        for (int i = 0; i < 9; i++) s.f[i] = f[i].p;
+        s.P = P;
+        return s;
+    }
 
     ~NSPlanT() {
         if (gexec) cudaGraphExecDestroy(gexec);
@@ -415,6 +487,16 @@ struct NSPlanT {
         int rc = fdmgpu_lapl_cube_create(&lapl, sizeof(T) == 8 ? FDMGPU_F64 : FDMGPU_F32, FDMGPU_DIRICHLET, P.dx, P.dy, P.dz, x2 - x1 + P.dx,
                                          y2 - y1 + P.dy, z2 - z1 + P.dz, nx, ny, nz);
         if (rc) throw Error{rc};
+        // the transforms' CTA size as for one volume however many sessions
+        // a step serves, so that a session's fields come out the same alone
+        // and stepped together with others
+        cube_set_rule_volumes(lapl, 1);
+        for (int i = 0; i < 9; i++) geo.f[i] = f[i];
+        const NSSessionT<T> h = session();
+        FDM_CUDA(cudaMemcpy(sess_dev.get(sizeof(h)), &h, sizeof(h), cudaMemcpyHostToDevice));
+        io_host[0] = f[8].p;
+        io_host[1] = f[4].p;
+        FDM_CUDA(cudaMemcpy(io_dev.get(sizeof(io_host)), io_host, sizeof(io_host), cudaMemcpyHostToDevice));
     }
 
     void enqueue_step() {
@@ -424,44 +506,61 @@ struct NSPlanT {
 
     template <bool FAST>
     void enqueue_step_t() {
-        const int nx = P.nx, ny = P.ny, nz = P.nz;
+        enqueue_steps<FAST>(geo, (const NSSessionT<T>*)sess_dev.p,
+                            sizeof(T) == 8 ? (const void* const*)io_dev.p : io_host, 1, 1, lapl, nullptr, st);
+    }
+
+    // One step of nsess sessions of this geometry: the session table ss
+    // and, for FP64 fields, io = {&RHS of every session, then &x of every
+    // session} (nsess pointers each, on the device; for FP32 fields, one
+    // session, the host pair {RHS, x}); scratch: FP64 work volumes for the
+    // pressure solve (null: the plan's own).
+    template <bool FAST>
+    static void enqueue_steps(const NSGeomT<T>& g, const NSSessionT<T>* ss, const void* const* io, int nsess,
+                              int io_stride, fdmgpu_lapl_cube* lapl, double* scratch, cudaStream_t st) {
+        const int nx = g.f[4].x2, ny = g.f[4].y2, nz = g.f[4].z2;  // x: {1..nz, 1..ny, 1..nx}
         const int B = 256;
-        auto blocks = [&](long long n) { return (unsigned)((n + B - 1) / B); };
+        auto grid = [&](long long n) { return dim3((unsigned)((n + B - 1) / B), (unsigned)nsess); };
         const long long vol = (long long)nx * ny * nz;
         {
             FDM_TIMED("ns_bound1", st);
-            k_ns_bound1<T><<<blocks(surface_points(nx + 3, ny + 3, nz + 3)), B, 0, st>>>(f[0], f[1], f[2], P);
+            k_ns_bound1<T><<<grid(surface_points(nx + 3, ny + 3, nz + 3)), B, 0, st>>>(g, ss);
             FDM_LAUNCH_CHECK();
         }
         {
             FDM_TIMED("ns_bound2", st);
-            k_ns_bound2<T, FAST><<<blocks(surface_points(nx + 2, ny + 2, nz + 2)), B, 0, st>>>(f[0], f[1], f[2], f[3],
-                                                                                             P);
+            k_ns_bound2<T, FAST><<<grid(surface_points(nx + 2, ny + 2, nz + 2)), B, 0, st>>>(g, ss);
             FDM_LAUNCH_CHECK();
         }
         {
             FDM_TIMED("ns_fgh", st);
-            k_ns_fgh<T, FAST><<<blocks((long long)(nx + 1) * (ny + 1) * (nz + 1)), B, 0, st>>>(f[0], f[1], f[2], f[5],
-                                                                                            f[6], f[7], P);
+            k_ns_fgh<T, FAST><<<grid((long long)(nx + 1) * (ny + 1) * (nz + 1)), B, 0, st>>>(g, ss);
             FDM_LAUNCH_CHECK();
         }
         {
             FDM_TIMED("ns_rhs", st);
-            k_ns_rhs<T, FAST><<<blocks(vol), B, 0, st>>>(f[5], f[6], f[7], f[3], f[8], P);
+            k_ns_rhs<T, FAST><<<grid(vol), B, 0, st>>>(g, ss);
             FDM_LAUNCH_CHECK();
         }
-        cube_solve_device(lapl, f[4].p, f[8].p, 1, st);
+        if constexpr (sizeof(T) == 8) {
+            cube_solve_ptrs(lapl, io, (void* const*)(io + io_stride), nsess, scratch, st);
+        } else {
+            // NSCube<float>: one session per step (the FP32 plan solves
+            // contiguous volumes); io = {RHS, x} are the data pointers
+            cube_solve_device(lapl, (void*)io[1], io[0], 1, st);
+        }
         {
             FDM_TIMED("ns_update", st);
-            k_ns_update<T><<<blocks(vol), B, 0, st>>>(f[0], f[1], f[2], f[3], f[4], f[5], f[6], f[7], P);
+            k_ns_update<T><<<grid(vol), B, 0, st>>>(g, ss);
             FDM_LAUNCH_CHECK();
         }
     }
 
     void step(int k) {
         for (int s = 0; s < k; s++) {
-            if (steps_run == 0) {
-                enqueue_step();  // eager first step: sets kernel attributes
+            if (!warm) {
+                enqueue_step();  // eager first step
+                warm = true;
             } else {
                 if (!gexec) {
                     FDM_CUDA(cudaStreamBeginCapture(st, cudaStreamCaptureModeThreadLocal));
@@ -478,7 +577,6 @@ struct NSPlanT {
                 }
                 FDM_CUDA(cudaGraphLaunch(gexec, st));
             }
-            steps_run++;
             time_index++;
         }
     }
@@ -493,6 +591,71 @@ struct fdmgpu_nscube {
     std::unique_ptr<NSPlanT<double>> d;
     std::unique_ptr<NSPlanT<float>> f;
 };
+
+namespace fdmgpu {
+
+bool nscube_mergeable(const fdmgpu_nscube* a, const fdmgpu_nscube* b) {
+    if (!a || !b || !a->d || !b->d) return false;
+    const NSPlanT<double>& p = *a->d;
+    const NSPlanT<double>& q = *b->d;
+    return p.P.nx == q.P.nx && p.P.ny == q.P.ny && p.P.nz == q.P.nz && p.P.dx == q.P.dx && p.P.dy == q.P.dy &&
+           p.P.dz == q.P.dz && p.x2 - p.x1 == q.x2 - q.x1 && p.y2 - p.y1 == q.y2 - q.y1 &&
+           p.z2 - p.z1 == q.z2 - q.z1 && p.exact == q.exact;
+}
+
+void nscube_step_many(fdmgpu_nscube* const* hs, const int* steps, int n, cudaStream_t st) {
+    if (n < 1) return;
+    for (int i = 0; i < n; i++) {
+        if (!hs[i] || !hs[i]->d) FDM_FAIL(FDMGPU_ENOTSUP, "shared steps are for FP64 cavities");
+        if (steps[i] < 0) FDM_FAIL(FDMGPU_EINVAL, "negative step count");
+        if (i > 0 && !nscube_mergeable(hs[0], hs[i])) FDM_FAIL(FDMGPU_EINVAL, "cavities of different geometry");
+    }
+    // most steps first: round r steps the prefix of cavities with steps > r
+    std::vector<int> idx(n);
+    for (int i = 0; i < n; i++) idx[i] = i;
+    std::stable_sort(idx.begin(), idx.end(), [&](int a, int b) { return steps[a] > steps[b]; });
+    const int rounds = steps[idx[0]];
+    NSPlanT<double>& p0 = *hs[idx[0]]->d;
+    std::vector<NSSessionT<double>> ss(n);
+    std::vector<const void*> io((size_t)2 * n);
+    for (int k = 0; k < n; k++) {
+        const NSPlanT<double>& pk = *hs[idx[k]]->d;
+        ss[k] = pk.session();
+        io[k] = pk.io_host[0];      // RHS
+        io[n + k] = pk.io_host[1];  // x
+    }
+    if (rounds > 0) {
+        // the tables and the pressure solve's work volumes, stream-ordered
+        // (the cavities' own plans and captured steps keep their buffers)
+        const size_t bs = (ss.size() * sizeof(NSSessionT<double>) + 255) / 256 * 256;
+        const size_t bio = (io.size() * sizeof(void*) + 255) / 256 * 256;
+        const size_t bw = (size_t)n * p0.P.nx * p0.P.ny * p0.P.nz * sizeof(double);
+        char* d = nullptr;
+        FDM_CUDA(cudaMallocAsync((void**)&d, bs + bio + bw, st));
+        try {
+            FDM_CUDA(cudaMemcpyAsync(d, ss.data(), ss.size() * sizeof(NSSessionT<double>), cudaMemcpyHostToDevice, st));
+            FDM_CUDA(cudaMemcpyAsync(d + bs, io.data(), io.size() * sizeof(void*), cudaMemcpyHostToDevice, st));
+            const auto* dss = (const NSSessionT<double>*)d;
+            const auto* dio = (const void* const*)(d + bs);
+            double* W = (double*)(d + bs + bio);
+            for (int r = 0; r < rounds; r++) {
+                int count = 0;
+                while (count < n && steps[idx[count]] > r) count++;
+                if (p0.exact) NSPlanT<double>::enqueue_steps<false>(p0.geo, dss, dio, count, n, p0.lapl, W, st);
+                else NSPlanT<double>::enqueue_steps<true>(p0.geo, dss, dio, count, n, p0.lapl, W, st);
+            }
+        } catch (...) {
+            cudaFreeAsync(d, st);
+            throw;
+        }
+        FDM_CUDA(cudaFreeAsync(d, st));
+    }
+    for (int i = 0; i < n; i++) {
+        hs[i]->d->time_index += steps[i];
+    }
+}
+
+}  // namespace fdmgpu
 
 namespace {
 // runs fn on the handle's plan, whichever element type it has

@@ -198,11 +198,15 @@ static void launch_rg_nt(const Tin* in, Tout* out, int nx, int ny, int nz, int n
 // Lines of up to 64 points in volumes too small to give every SM two CTAs
 // of 256 threads run in CTAs of 128 or 64 (fewer lines per CTA, more CTAs):
 // a 63^3 volume's 3969 lines make 62 CTAs of 64 lines, on 62 of 152 SMs.
+// rule_vols > 0: decide as for that many volumes (a caller whose launches
+// serve varying numbers of volumes keeps one CTA size, and so the same
+// rounding, for all).
 template <typename Tin, typename T, typename Tout, int AXIS, int MODE, int N>
 static void launch_rg(const Tin* in, Tout* out, int nx, int ny, int nz, int nvol, const SineTables<T>& tb,
-                      double scale, cudaStream_t st, const SineFused& fu, SineGeom geo) {
+                      double scale, cudaStream_t st, const SineFused& fu, SineGeom geo, int rule_vols) {
     if constexpr (N <= 64) {
-        const long long lines = (AXIS == 0 ? (long long)ny * nz : (long long)nx * nz) * nvol;
+        const long long lines =
+            (AXIS == 0 ? (long long)ny * nz : (long long)nx * nz) * (rule_vols > 0 ? rule_vols : nvol);
         const long long want = 2LL * sm_count();
         if (lines / RgGeom<N, AXIS, 256>::L < want) {
             if (lines / RgGeom<N, AXIS, 128>::L >= want)
@@ -296,7 +300,7 @@ static void launch_sine_tc(int N, const float* in, float* out, long long lines, 
 
 template <typename Tin, typename T, typename Tout, int AXIS, int MODE = kPlain>
 static void launch_sine(const Tin* in, Tout* out, int nx, int ny, int nz, int nvol, const SineTables<T>& tb,
-                        double scale, cudaStream_t st, const SineFused* fused = nullptr) {
+                        double scale, cudaStream_t st, const SineFused* fused = nullptr, int rule_vols = 0) {
     SineGeom geo;
     geo.nx = nx; geo.ny = ny; geo.nz = nz;
     geo.vstride = (long long)nx * ny * nz;
@@ -306,12 +310,12 @@ static void launch_sine(const Tin* in, Tout* out, int nx, int ny, int nz, int nv
     memset(&fu, 0, sizeof(fu));
     if (fused) fu = *fused;
     switch (tb.N) {
-        case 16: return launch_rg<Tin, T, Tout, AXIS, MODE, 16>(in, out, nx, ny, nz, nvol, tb, scale, st, fu, geo);
-        case 32: return launch_rg<Tin, T, Tout, AXIS, MODE, 32>(in, out, nx, ny, nz, nvol, tb, scale, st, fu, geo);
-        case 64: return launch_rg<Tin, T, Tout, AXIS, MODE, 64>(in, out, nx, ny, nz, nvol, tb, scale, st, fu, geo);
-        case 128: return launch_rg<Tin, T, Tout, AXIS, MODE, 128>(in, out, nx, ny, nz, nvol, tb, scale, st, fu, geo);
-        case 256: return launch_rg<Tin, T, Tout, AXIS, MODE, 256>(in, out, nx, ny, nz, nvol, tb, scale, st, fu, geo);
-        case 512: return launch_rg<Tin, T, Tout, AXIS, MODE, 512>(in, out, nx, ny, nz, nvol, tb, scale, st, fu, geo);
+        case 16: return launch_rg<Tin, T, Tout, AXIS, MODE, 16>(in, out, nx, ny, nz, nvol, tb, scale, st, fu, geo, rule_vols);
+        case 32: return launch_rg<Tin, T, Tout, AXIS, MODE, 32>(in, out, nx, ny, nz, nvol, tb, scale, st, fu, geo, rule_vols);
+        case 64: return launch_rg<Tin, T, Tout, AXIS, MODE, 64>(in, out, nx, ny, nz, nvol, tb, scale, st, fu, geo, rule_vols);
+        case 128: return launch_rg<Tin, T, Tout, AXIS, MODE, 128>(in, out, nx, ny, nz, nvol, tb, scale, st, fu, geo, rule_vols);
+        case 256: return launch_rg<Tin, T, Tout, AXIS, MODE, 256>(in, out, nx, ny, nz, nvol, tb, scale, st, fu, geo, rule_vols);
+        case 512: return launch_rg<Tin, T, Tout, AXIS, MODE, 512>(in, out, nx, ny, nz, nvol, tb, scale, st, fu, geo, rule_vols);
         default: break;
     }
     // other lengths: the shared-memory Stockham kernel
@@ -984,6 +988,7 @@ struct CubePlan {
         }
     }
     int refine_adaptive = 0;       // 1: extra sweeps while an estimate exceeds tol (synchronises)
+    int rule_vols = 0;             // > 0: line transforms choose their CTA size as for this many volumes
     std::vector<double> last_est;  // per RHS, filled by an adaptive solve
 
     // final estimates of the last solve (synchronises st)
@@ -1134,20 +1139,21 @@ struct CubePlan {
 
     // Plain FP64 solve through pointer tables: first pass from the user
     // volumes into contiguous FP64 scratch, last pass back out.
-    void run_plain_ptrs(const void* const* vin, void* const* vout, int nrhs, cudaStream_t st) {
+    void run_plain_ptrs(const void* const* vin, void* const* vout, int nrhs, cudaStream_t st, double* Wext = nullptr) {
         const long long V = vol() * nrhs;
-        double* W = (double*)work64.get(V * sizeof(double));
+        double* W = Wext ? Wext : (double*)work64.get(V * sizeof(double));
+        const int rv = rule_vols;
         SineFused fin;
         memset(&fin, 0, sizeof(fin));
         fin.vin = vin;
-        launch_sine<double, double, double, 0>(nullptr, W, nx, ny, nz, nrhs, tx64.view(), scx, st, &fin);
-        launch_sine<double, double, double, 1>(W, W, nx, ny, nz, nrhs, ty64.view(), scy, st);
+        launch_sine<double, double, double, 0>(nullptr, W, nx, ny, nz, nrhs, tx64.view(), scx, st, &fin, rv);
+        launch_sine<double, double, double, 1>(W, W, nx, ny, nz, nrhs, ty64.view(), scy, st, nullptr, rv);
         zsolve<double>(W, nrhs, lamx64, lamy64, st);
-        launch_sine<double, double, double, 1>(W, W, nx, ny, nz, nrhs, ty64.view(), sly, st);
+        launch_sine<double, double, double, 1>(W, W, nx, ny, nz, nrhs, ty64.view(), sly, st, nullptr, rv);
         SineFused fo;
         memset(&fo, 0, sizeof(fo));
         fo.vout = vout;
-        launch_sine<double, double, double, 0>(W, nullptr, nx, ny, nz, nrhs, tx64.view(), slx, st, &fo);
+        launch_sine<double, double, double, 0>(W, nullptr, nx, ny, nz, nrhs, tx64.view(), slx, st, &fo, rv);
     }
 
     // Largest first-sweep correction estimate ||c||/||u|| over the nrhs
@@ -1903,6 +1909,19 @@ static void noalloc_solve(double dx, double dy, double dz, double lx, double ly,
 void cube_solve_device(fdmgpu_lapl_cube* h, void* ans, const void* rhs, int nrhs, cudaStream_t st) {
     h->plan.solve_device(ans, rhs, nrhs, st);
 }
+
+void cube_solve_ptrs(fdmgpu_lapl_cube* h, const void* const* d_in, void* const* d_out, int nvol, double* scratch,
+                     cudaStream_t st) {
+    CubePlan& c = h->plan;
+    if (c.dtype != FDMGPU_F64 || c.periodic) FDM_FAIL(FDMGPU_ENOTSUP, "pointer-table solves are FP64 Dirichlet");
+    check_grid_y(nvol);
+    c.last_stream = st;
+    c.last_nrhs = nvol;
+    c.last_sweeps = 0;
+    c.run_plain_ptrs(d_in, d_out, nvol, st, scratch);
+}
+
+void cube_set_rule_volumes(fdmgpu_lapl_cube* h, int vols) { h->plan.rule_vols = vols > 0 ? vols : 0; }
 
 int cube_norms_async(fdmgpu_lapl_cube* h, double* host, int nrhs, cudaStream_t st) {
     const CubePlan& c = h->plan;

@@ -116,6 +116,7 @@ struct Lane {
     size_t staged = 0;           // staging bytes reserved by this launch
     double t_done = 0;
     double* norms_host = nullptr;  // page-locked copy of the launch's refinement norms
+    cudaEvent_t ev = nullptr;      // orders shared cavity steps against the sessions' streams
     int sweeps = 0;                // sweeps of the launch's solve (0: none, -1: FP64)
 };
 
@@ -231,6 +232,8 @@ struct Server {
         Lane* lane = nullptr;
         std::vector<Request*> batch;
         std::unique_ptr<Plan> plan;  // pooled plan to reuse (solves)
+        std::vector<fdmgpu_nscube*> cavities;  // advances: the sessions' cavities
+        std::vector<cudaStream_t> streams;     // and their streams
         std::vector<std::unique_ptr<Plan>> evict;
         double plan_grow = 0;
     };
@@ -243,7 +246,9 @@ struct Server {
 
     // Picks the next launch: the oldest admissible request, plus for a
     // solve the later waiting solves of the same plan key (up to max_batch)
-    // that still fit.  Returns false when nothing can start now.
+    // that still fit, and for an advance the first waiting advance of each
+    // other idle session of the same cavity geometry (up to max_batch): their
+    // steps share launches.  Returns false when nothing can start now.
     bool pick(Action& a) {
         Lane* L = free_lane();
         if (!L) return false;
@@ -262,7 +267,22 @@ struct Server {
                 s->second->busy = true;
                 a.lane = L;
                 a.batch.push_back(r);
-                pending.erase(it);
+                a.cavities.push_back(s->second->h);
+                auto next = pending.erase(it);
+                for (auto j = next; j != pending.end() && (int)a.batch.size() < max_batch;) {
+                    Request* q = *j;
+                    auto t = q->kind == FDMGPU_REQ_ADVANCE ? sessions.find(q->session) : sessions.end();
+                    if (t == sessions.end() || t->second->busy || !nscube_mergeable(a.cavities[0], t->second->h)) {
+                        ++j;
+                        continue;
+                    }
+                    t->second->busy = true;  // one advance per session and launch
+                    a.batch.push_back(q);
+                    a.cavities.push_back(t->second->h);
+                    a.streams.push_back(t->second->st);
+                    j = pending.erase(j);
+                }
+                a.streams.insert(a.streams.begin(), s->second->st);
                 return true;
             }
             // solve: first come first served on memory
@@ -333,17 +353,13 @@ struct Server {
         std::string err;
         int code = FDMGPU_OK;
         cudaStream_t cb = L->st;
-        if (a.batch[0]->kind == FDMGPU_REQ_ADVANCE) {
+        if (a.batch[0]->kind == FDMGPU_REQ_ADVANCE && a.batch.size() == 1) {
             // the session's own stream; the lane is the concurrency slot
-            Request* r = a.batch[0];
-            fdmgpu_nscube* h = nullptr;
-            {
-                std::lock_guard<std::mutex> g(mq);
-                h = sessions[r->session]->h;
-                cb = sessions[r->session]->st;
-            }
-            code = fdmgpu_nscube_step(h, r->steps);
+            cb = a.streams[0];
+            code = fdmgpu_nscube_step(a.cavities[0], a.batch[0]->steps);
             if (code) err = fdmgpu_last_error();
+        } else if (a.batch[0]->kind == FDMGPU_REQ_ADVANCE) {
+            code = run_advances(a, err);
         } else {
             code = run_solves(a, err);
         }
@@ -387,6 +403,43 @@ struct Server {
             L->t_done = now_ms();
             finish_lane(L);
         }
+    }
+
+    // Advances of several sessions of one cavity geometry: each step's
+    // kernels take all the cavities that still have steps to go, on the
+    // lane's stream, ordered after and before the sessions' own streams.
+    int run_advances(Action& a, std::string& err) {
+        Lane* L = a.lane;
+        const int n = (int)a.batch.size();
+        std::vector<int> steps((size_t)n);
+        for (int i = 0; i < n; i++) steps[i] = a.batch[i]->steps;
+        cudaError_t e = cudaSuccess;
+        for (int i = 0; e == cudaSuccess && i < n; i++) {
+            e = cudaEventRecord(L->ev, a.streams[i]);
+            if (e == cudaSuccess) e = cudaStreamWaitEvent(L->st, L->ev, 0);
+        }
+        if (e != cudaSuccess) {
+            err = std::string("ordering the sessions' streams failed: ") + cudaGetErrorString(e);
+            return FDMGPU_ECUDA;
+        }
+        int code = FDMGPU_OK;
+        try {
+            nscube_step_many(a.cavities.data(), steps.data(), n, L->st);
+        } catch (const Error& x) {
+            err = fdmgpu_last_error();
+            code = x.code;
+        } catch (const std::bad_alloc&) {
+            err = "host allocation failed";
+            code = FDMGPU_ENOMEM;
+        }
+        // the sessions' later work follows the shared steps
+        e = cudaEventRecord(L->ev, L->st);
+        for (int i = 0; e == cudaSuccess && i < n; i++) e = cudaStreamWaitEvent(a.streams[i], L->ev, 0);
+        if (e != cudaSuccess && !code) {
+            err = std::string("ordering the sessions' streams failed: ") + cudaGetErrorString(e);
+            code = FDMGPU_ECUDA;
+        }
+        return code;
     }
 
     int run_solves(Action& a, std::string& err) {
@@ -485,6 +538,7 @@ struct Server {
             // per sweep (at most 3 sweeps)
             FDM_CUDA(cudaHostAlloc(&lanes[i].norms_host, sizeof(double) * 2 * 3 * (size_t)max_batch,
                                    cudaHostAllocDefault));
+            FDM_CUDA(cudaEventCreateWithFlags(&lanes[i].ev, cudaEventDisableTiming));
         }
         thread = std::thread([this] { loop(); });
     }
@@ -507,6 +561,7 @@ struct Server {
         for (auto& L : lanes) {
             if (L.st) cudaStreamDestroy(L.st);
             if (L.norms_host) cudaFreeHost(L.norms_host);
+            if (L.ev) cudaEventDestroy(L.ev);
         }
         if (pool) cudaMemPoolDestroy(pool);
     }
@@ -647,7 +702,9 @@ int fdmgpu_server_session_create(fdmgpu_server* h, int* session, int nx, int nz,
     FDM_API_BEGIN
     if (!h || !session) FDM_FAIL(FDMGPU_EINVAL, "null argument");
     Server& s = h->s;
-    const double bytes = 10.0 * (nx + 3.0) * (nx + 3.0) * (nz + 3.0) * sizeof(double);
+    // nine fields and the pressure solve's work volume, plus the work volume
+    // of steps shared with other sessions
+    const double bytes = 11.0 * (nx + 3.0) * (nx + 3.0) * (nz + 3.0) * sizeof(double);
     {
         std::lock_guard<std::mutex> g(s.mq);
         if (s.used + bytes > s.budget) FDM_FAIL(FDMGPU_EBUDGET, "session state does not fit in the budget");

@@ -424,7 +424,10 @@ int fdmgpu_server_submit_solve(fdmgpu_server* h, unsigned long long* id, const i
 /* a resident lid-driven cavity (parameters of fdmgpu_nscube_create, FP64) */
 int fdmgpu_server_session_create(fdmgpu_server* h, int* session, int nx, int nz, double x1, double y1,
                                  double z1, double x2, double y2, double z2, double u0, double Re, double dt);
-/* advances run in submission order per session */
+/* advances run in submission order per session; waiting advances of
+ * sessions whose cavities have one geometry (grid, spacing, box extents) run
+ * their steps as shared launches (up to max_batch sessions), with results
+ * bit for bit those of steps run alone */
 int fdmgpu_server_submit_advance(fdmgpu_server* h, unsigned long long* id, int session, int steps);
 /* state of a request; a finished (done, failed, cancelled) request is
  * reported once and then forgotten.  latency_ms: submit to completion

@@ -87,6 +87,41 @@ def test_results_same_alone_and_in_the_mix(cuda):
     ns.close()
 
 
+def test_advances_of_one_geometry_share_launches(cuda):
+    """Waiting advances of sessions of one cavity geometry run as one launch
+    per step over all of them; each session still matches a standalone
+    NSCube advanced as far, whatever its Re and step count."""
+    box = (-math.pi, -math.pi, -math.pi, math.pi, math.pi, math.pi)
+    cases = [(250.0, 5), (100.0, 9), (400.0, 0), (250.0, 2)]
+    with Server(budget_bytes=8e9, lanes=1, max_batch=8) as srv:
+        sids = [srv.session_create(31, 31, Re=re, dt=0.01) for re, _ in cases]
+        other = srv.session_create(15, 15)  # another geometry: launches of its own
+        busy = srv.submit_advance(srv.session_create(63, 63), 200)  # holds the one lane
+        ids = [srv.submit_advance(s, k) for s, (_, k) in zip(sids, cases)]
+        alone = srv.submit_advance(other, 3)
+        assert srv.wait(busy)["state"] == "done"
+        recs = [srv.wait(i) for i in ids]
+        assert all(r["state"] == "done" and r["batch"] == len(cases) for r in recs), recs
+        rec = srv.wait(alone)
+        assert rec["state"] == "done" and rec["batch"] == 1
+        # steps of their own (the first captures the cavity's step), then
+        # shared steps again, continue from the shared ones
+        for s in sids:
+            assert srv.wait(srv.submit_advance(s, 2))["batch"] == 1
+        busy = srv.submit_advance(srv.session_create(63, 63), 200)
+        more = [srv.submit_advance(s, 1) for s in sids]
+        assert srv.wait(busy)["state"] == "done"
+        assert all(srv.wait(i)["batch"] == len(cases) for i in more)
+        fields = [srv.session_field(s, "u") for s in sids]
+    for (re, k), (u, steps) in zip(cases, fields):
+        assert steps == k + 3
+        ns = NSCube(nx=31, nz=31, Re=re, dt=0.01, u0=1.0, x1=box[0], y1=box[1], z1=box[2], x2=box[3], y2=box[4],
+                    z2=box[5])
+        ns.step(k + 3)
+        assert np.array_equal(ns.get("u").data.ravel(), u.ravel()), (re, k)
+        ns.close()
+
+
 def test_waiting_solves_share_a_launch(cuda):
     """Solves of one geometry that wait behind a busy lane go out as one
     launch; their answers equal the ones they get alone."""
