@@ -471,15 +471,18 @@ SERVE_RATES = (100, 300, 1000, 1500, 3000, 5000)
 
 
 def measure_serving(torch, fdm_gb300, workloads, dev, rates=SERVE_RATES, seconds=4.0, max_requests=20000,
-                    max_outstanding=1024, lanes=48, max_batch=8):
+                    max_outstanding=1024, lanes=48, max_batch=8, max_wait_ms=0.0):
     """Serving loop under Poisson arrivals at each rate: 70% single solves
     (each axis from {31,63,127}, 5% at 255^3, tol 1e-6 or 1e-10 half and
     half), 30% advances of k ~ U{1..50} steps on 64 resident 63^3 cavity
     sessions (Re in {100,250,400}, dt 0.01), 150 GB budget.  Each rate runs
     min(20000, rate x seconds) requests; at most max_outstanding are held by
     the client, later arrivals wait and that wait counts in their latency.
-    Every solve's answer is checked against the FP64 form."""
+    Every solve's answer is checked against the FP64 form.  max_wait_ms > 0:
+    the server sheds requests not started within that time of submission
+    (status EBUSY); they count as shed, not in the latencies."""
     import concurrent.futures as cf
+    from fdm_gb300 import _native as N
     import numpy as np
     from fdm_gb300.serve import Server
     rng = np.random.default_rng(4242)
@@ -525,6 +528,8 @@ def measure_serving(torch, fdm_gb300, workloads, dev, rates=SERVE_RATES, seconds
         srv.wait(rid)
         if sh:
             free[sh].append(b)
+    if max_wait_ms > 0:
+        srv.set_admission(0, max_wait_ms)
     pool = cf.ThreadPoolExecutor(8)
     out = []
     for lam in rates:
@@ -539,6 +544,7 @@ def measure_serving(torch, fdm_gb300, workloads, dev, rates=SERVE_RATES, seconds
         srv.stats_reset()
         live = {}
         lat, lat_solve, lat_adv, errs, ests, futs = [], [], [], [], [], []
+        shed = 0
         i = 0
         t0 = time.perf_counter()
         t_last = t0
@@ -559,6 +565,13 @@ def measure_serving(torch, fdm_gb300, workloads, dev, rates=SERVE_RATES, seconds
             rec = srv.next_done(wait_ms) if live else None
             while rec is not None:
                 a_t, s_t, sh, b = live.pop(rec["id"])
+                if rec["state"] == "failed" and rec["status"] == N.EBUSY and max_wait_ms > 0:
+                    shed += 1
+                    if sh:
+                        free[sh].append(b)
+                    t_last = time.perf_counter()
+                    rec = srv.next_done(0.0) if live else None
+                    continue
                 if rec["state"] != "done":
                     raise RuntimeError("request failed: %s" % rec)
                 l_ms = rec["latency_ms"] + (s_t - a_t) * 1e3
@@ -591,7 +604,8 @@ def measure_serving(torch, fdm_gb300, workloads, dev, rates=SERVE_RATES, seconds
         def pct(v, q):
             return float(np.percentile(v, q)) if v else None
         out.append({
-            "offered_req_per_s": lam, "requests": n, "achieved_req_per_s": n / wall,
+            "offered_req_per_s": lam, "requests": n, "achieved_req_per_s": (n - shed) / wall,
+            "shed": shed, "shed_fraction": shed / n,
             "p50_ms": pct(lat, 50), "p99_ms": pct(lat, 99),
             "p50_solve_ms": pct(lat_solve, 50), "p99_solve_ms": pct(lat_solve, 99),
             "p50_advance_ms": pct(lat_adv, 50), "p99_advance_ms": pct(lat_adv, 99),
@@ -602,12 +616,15 @@ def measure_serving(torch, fdm_gb300, workloads, dev, rates=SERVE_RATES, seconds
             if errs else None,
             "solve_launches": st["batches"], "solves_batched": st["batched_requests"],
             "peak_device_gb": st["peak_bytes"] / 1e9, "mean_queue_ms": st["mean_queue_ms"],
+            # the server's own clock, submit to completion (no client-side wait)
+            "server_p50_ms": st["p50_ms"], "server_p99_ms": st["p99_ms"], "server_shed": st["shed"],
         })
     pool.shutdown()
     srv.close()
     return {"workload": "70% solves {31,63,127}^3 + 5% 255^3, tol 1e-6/1e-10; 30% advance k~U[1,50] on 64 "
                         "resident 63^3 sessions; Poisson arrivals; 150 GB budget",
             "lanes": lanes, "max_batch": max_batch, "max_outstanding": max_outstanding,
+            "queue_deadline_ms": max_wait_ms if max_wait_ms > 0 else None,
             "latency": "arrival to answer in pinned host memory (server clock from submit, plus client wait)",
             "advance_error": "sessions are the plain FP64 NSCube (bit-identical to a lone NSCube)",
             "rates": out}
@@ -838,6 +855,11 @@ def main():
     nbody["published_configs"] = measure_nbody_published(torch, fdm_gb300)
     rates = tuple(int(x) for x in args.serve_rates.split(",")) if args.serve_rates else SERVE_RATES
     serving = measure_serving(torch, fdm_gb300, workloads, dev, rates=rates) if not args.no_serving else None
+    # the same load past saturation with a 100 ms queue deadline: what is
+    # not started in time is shed (EBUSY) and the served requests keep
+    # bounded latency
+    serving_shed = (measure_serving(torch, fdm_gb300, workloads, dev, rates=(1500, 3000, 5000), max_wait_ms=100.0)
+                    if not args.no_serving else None)
 
     solves = args.steps * NRHS * world
     value = solves / (ms * 1e-3)
@@ -881,6 +903,7 @@ def main():
         "periodic_poisson": periodic,
         "nbody": nbody,
         "serving": serving,
+        "serving_with_queue_deadline": serving_shed,
         "clocks": clocks,
     }
     if rank == 0 and not args.no_cpu_baseline:

@@ -11,7 +11,7 @@ from pathlib import Path
 
 LIB_PATH = Path(__file__).resolve().parent / "libfdmgpu.so"
 
-OK, EINVAL, ESIZE, ENOMEM, ECUDA, ETIMEOUT, ENOTSUP, EBUDGET = range(8)
+OK, EINVAL, ESIZE, ENOMEM, ECUDA, ETIMEOUT, ENOTSUP, EBUDGET, EBUSY = range(9)
 F64, F32 = 0, 1
 PLAIN, MIXED = 0, 1
 RECT_TRIDIAG, RECT_FFT2 = 0, 1
@@ -20,7 +20,7 @@ NOALLOC_SCRATCH_BYTES = 32 * 1024 * 1024
 
 _STATUS_NAMES = {
     OK: "OK", EINVAL: "EINVAL", ESIZE: "ESIZE", ENOMEM: "ENOMEM", ECUDA: "ECUDA",
-    ETIMEOUT: "ETIMEOUT", ENOTSUP: "ENOTSUP", EBUDGET: "EBUDGET",
+    ETIMEOUT: "ETIMEOUT", ENOTSUP: "ENOTSUP", EBUDGET: "EBUDGET", EBUSY: "EBUSY",
 }
 
 
@@ -34,7 +34,7 @@ class ServerStats(ctypes.Structure):
         [("queued", c_int), ("running", c_int), ("batches", c_ulonglong), ("batched_requests", c_ulonglong)] + \
         [(n, c_double) for n in ("used_bytes", "peak_bytes", "budget_bytes", "plan_bytes", "session_bytes",
                                  "p50_ms", "p99_ms", "p50_solve_ms", "p99_solve_ms", "p50_advance_ms",
-                                 "p99_advance_ms", "mean_queue_ms")]
+                                 "p99_advance_ms", "mean_queue_ms")] + [("shed", c_ulonglong)]
 
     def as_dict(self) -> dict:
         return {n: getattr(self, n) for n, _ in self._fields_}
@@ -160,6 +160,7 @@ _SIGS = [
     ("fdmgpu_server_session_close", c_int, [c_void_p, c_int, c_double]),
     ("fdmgpu_server_stats", c_int, [c_void_p, c_void_p]),
     ("fdmgpu_server_stats_reset", c_int, [c_void_p]),
+    ("fdmgpu_server_set_admission", c_int, [c_void_p, c_int, c_double]),
     ("fdmgpu_server_destroy", c_int, [c_void_p]),
 ]
 

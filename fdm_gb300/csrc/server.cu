@@ -144,6 +144,9 @@ struct Server {
     double used = 0, peak = 0, plan_bytes = 0, session_bytes = 0, staged_bytes = 0;
     int running = 0;
     unsigned long long n_submitted = 0, n_completed = 0, n_failed = 0, n_cancelled = 0, n_rejected = 0;
+    unsigned long long n_shed = 0;
+    int max_queued = 0;      // > 0: submits find the queue full at this length (EBUSY)
+    double max_wait_ms = 0;  // > 0: queued requests are shed after this wait (EBUSY)
     unsigned long long n_batches = 0, n_batched = 0;
     std::vector<float> lat_solve, lat_advance;
     double queue_sum = 0;
@@ -225,6 +228,26 @@ struct Server {
         r->status = code;
         r->error = msg;
         n_failed++;
+    }
+
+    // Sheds the queued requests that waited past max_wait_ms (under mq).
+    // The queue is in submission order, so the expired ones lead it.
+    // Returns the ms until the next one expires (< 0: none queued).
+    double shed_expired() {
+        if (max_wait_ms <= 0) return -1.0;
+        const double t = now_ms();
+        while (!pending.empty() && t - pending.front()->t_submit >= max_wait_ms) {
+            Request* r = pending.front();
+            pending.pop_front();
+            r->state = FDMGPU_REQ_FAILED;
+            r->status = FDMGPU_EBUSY;
+            r->error = "shed: not started within the queue deadline";
+            r->t_done = t;
+            n_shed++;
+            finished.push_back(r->id);
+        }
+        if (pending.empty()) return -1.0;
+        return pending.front()->t_submit + max_wait_ms - t;
     }
 
     // What the scheduler does next (chosen under mq, carried out without it)
@@ -506,6 +529,9 @@ struct Server {
                 finish_lane(L);
             }
             if (stop && running == 0) break;
+            const size_t nfin = finished.size();
+            const double next_expiry = shed_expired();
+            if (finished.size() != nfin) cv_done.notify_all();
             Action a;
             if (!stop && pick(a)) {
                 lk.unlock();
@@ -514,7 +540,10 @@ struct Server {
                 lk.lock();
                 continue;
             }
-            cv_sched.wait(lk);
+            if (next_expiry >= 0)
+                cv_sched.wait_for(lk, std::chrono::microseconds((long long)(next_expiry * 1e3) + 1));
+            else
+                cv_sched.wait(lk);
         }
     }
 
@@ -682,6 +711,10 @@ int fdmgpu_server_submit_solve(fdmgpu_server* h, unsigned long long* id, const i
     const double need = Server::staging_bytes(*r) + Server::plan_need(r->key, r->vol, 1);
     std::lock_guard<std::mutex> g(s.mq);
     if (s.stop) FDM_FAIL(FDMGPU_EINVAL, "server is shutting down");
+    if (s.max_queued > 0 && (int)s.pending.size() >= s.max_queued) {
+        s.n_shed++;
+        FDM_FAIL(FDMGPU_EBUSY, "queue full (%d requests)", s.max_queued);
+    }
     if (need + s.session_bytes > s.budget) {
         s.n_rejected++;
         FDM_FAIL(FDMGPU_EBUDGET, "request needs %.0f bytes, budget %.0f (%.0f held by sessions)", need, s.budget,
@@ -744,6 +777,10 @@ int fdmgpu_server_submit_advance(fdmgpu_server* h, unsigned long long* id, int s
     if (s.stop) FDM_FAIL(FDMGPU_EINVAL, "server is shutting down");
     auto it = s.sessions.find(session);
     if (it == s.sessions.end() || it->second->closing) FDM_FAIL(FDMGPU_EINVAL, "no session %d", session);
+    if (s.max_queued > 0 && (int)s.pending.size() >= s.max_queued) {
+        s.n_shed++;
+        FDM_FAIL(FDMGPU_EBUSY, "queue full (%d requests)", s.max_queued);
+    }
     std::unique_ptr<Request> r(new Request());
     r->kind = FDMGPU_REQ_ADVANCE;
     r->session = session;
@@ -886,6 +923,7 @@ int fdmgpu_server_stats(fdmgpu_server* h, fdmgpu_server_stats_t* out) {
         out->failed = s.n_failed;
         out->cancelled = s.n_cancelled;
         out->rejected = s.n_rejected;
+        out->shed = s.n_shed;
         out->queued = (int)s.pending.size();
         out->running = s.running;
         out->batches = s.n_batches;
@@ -912,13 +950,25 @@ int fdmgpu_server_stats_reset(fdmgpu_server* h) {
     if (!h) FDM_FAIL(FDMGPU_EINVAL, "null handle");
     Server& s = h->s;
     std::lock_guard<std::mutex> g(s.mq);
-    s.n_submitted = s.n_completed = s.n_failed = s.n_cancelled = s.n_rejected = 0;
+    s.n_submitted = s.n_completed = s.n_failed = s.n_cancelled = s.n_rejected = s.n_shed = 0;
     s.n_batches = s.n_batched = 0;
     s.lat_solve.clear();
     s.lat_advance.clear();
     s.queue_sum = 0;
     s.queue_n = 0;
     s.peak = s.used;
+    FDM_API_END
+}
+
+int fdmgpu_server_set_admission(fdmgpu_server* h, int max_queued, double max_wait_ms) {
+    FDM_API_BEGIN
+    if (!h) FDM_FAIL(FDMGPU_EINVAL, "null handle");
+    if (max_queued < 0 || !(max_wait_ms >= 0)) FDM_FAIL(FDMGPU_EINVAL, "negative admission limit");
+    Server& s = h->s;
+    std::lock_guard<std::mutex> g(s.mq);
+    s.max_queued = max_queued;
+    s.max_wait_ms = max_wait_ms;
+    s.cv_sched.notify_one();  // the scheduler picks up the new deadline
     FDM_API_END
 }
 

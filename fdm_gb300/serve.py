@@ -141,6 +141,12 @@ class Server:
     def stats_reset(self) -> None:
         N.check(self._lib.fdmgpu_server_stats_reset(self._h))
 
+    def set_admission(self, max_queued: int = 0, max_wait_ms: float = 0.0) -> None:
+        """Load shedding: submits beyond max_queued queued requests raise
+        FdmError(EBUSY); requests not started within max_wait_ms finish as
+        failed with status EBUSY.  0 turns either limit off."""
+        N.check(self._lib.fdmgpu_server_set_admission(self._h, int(max_queued), float(max_wait_ms)))
+
     def close(self) -> None:
         if getattr(self, "_h", None):
             self._lib.fdmgpu_server_destroy(self._h)

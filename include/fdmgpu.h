@@ -42,7 +42,9 @@ enum {
     FDMGPU_ECUDA = 4,     /* a CUDA runtime call failed                         */
     FDMGPU_ETIMEOUT = 5,  /* a bounded device-side wait gave up                 */
     FDMGPU_ENOTSUP = 6,   /* combination not supported (e.g. periodic flags)    */
-    FDMGPU_EBUDGET = 7    /* request exceeds the configured memory budget      */
+    FDMGPU_EBUDGET = 7,   /* request exceeds the configured memory budget      */
+    FDMGPU_EBUSY = 8      /* serving loop: queue full, or the request waited
+                             past its queue deadline and was shed               */
 };
 
 /* element type of user arrays */
@@ -414,6 +416,7 @@ typedef struct {
     double used_bytes, peak_bytes, budget_bytes, plan_bytes, session_bytes;
     double p50_ms, p99_ms, p50_solve_ms, p99_solve_ms, p50_advance_ms, p99_advance_ms;
     double mean_queue_ms;
+    unsigned long long shed; /* refused at a full queue or dropped at the queue deadline (FDMGPU_EBUSY) */
 } fdmgpu_server_stats_t;
 
 int fdmgpu_server_create(fdmgpu_server** h, double budget_bytes, int lanes, int max_batch);
@@ -454,6 +457,13 @@ int fdmgpu_server_session_get_field(fdmgpu_server* h, int session, int field, do
 int fdmgpu_server_session_close(fdmgpu_server* h, int session, double timeout_ms);
 int fdmgpu_server_stats(fdmgpu_server* h, fdmgpu_server_stats_t* out);
 int fdmgpu_server_stats_reset(fdmgpu_server* h);
+/* load shedding (both off by default): with max_queued > 0 a submit finds
+ * the queue holding max_queued requests and returns FDMGPU_EBUSY (nothing is
+ * queued); with max_wait_ms > 0 a request that has not started max_wait_ms
+ * after its submission finishes as FDMGPU_REQ_FAILED with status
+ * FDMGPU_EBUSY (a skipped advance leaves its session where it was; later
+ * advances of the session still run in order).  Both count in stats.shed. */
+int fdmgpu_server_set_admission(fdmgpu_server* h, int max_queued, double max_wait_ms);
 /* cancels queued requests, waits for running ones, frees everything */
 int fdmgpu_server_destroy(fdmgpu_server* h);
 

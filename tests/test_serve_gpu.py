@@ -122,6 +122,55 @@ def test_advances_of_one_geometry_share_launches(cuda):
         ns.close()
 
 
+def _wait_running(srv, rid):
+    import time
+    for _ in range(20000):
+        if srv.poll(rid)["state"] == "running":
+            return
+        time.sleep(0.0005)
+    raise AssertionError("request %d never started" % rid)
+
+
+def test_load_shedding(cuda):
+    """Requests that wait past the queue deadline finish as EBUSY without
+    running; a full queue refuses submits with EBUSY; with the limits off
+    everything runs again."""
+    shape = (63, 63, 63)
+    r = _pinned_rhs(shape, 3)
+    outs = [_pinned_like(r) for _ in range(3)]
+    with Server(budget_bytes=8e9, lanes=1, max_batch=1) as srv:
+        sid = srv.session_create(63, 63)
+        srv.wait(srv.submit_advance(sid, 2))
+        srv.set_admission(max_queued=0, max_wait_ms=5.0)
+        busy = srv.submit_advance(sid, 300)  # holds the one lane for ~40 ms
+        late = [srv.submit_solve(a, r, shape, tol=1e-10) for a in outs]
+        assert srv.wait(busy)["state"] == "done"
+        for i in late:
+            rec = srv.wait(i)
+            assert rec["state"] == "failed" and rec["status"] == N.EBUSY, rec
+            assert rec["latency_ms"] >= 5.0
+        st = srv.stats()
+        assert st["shed"] == 3 and st["failed"] == 0 and st["completed"] == 2
+        # a full queue refuses at submit and queues nothing
+        srv.set_admission(max_queued=2, max_wait_ms=0.0)
+        busy = srv.submit_advance(sid, 300)
+        _wait_running(srv, busy)
+        queued = [srv.submit_solve(a, r, shape, tol=1e-10) for a in outs[:2]]
+        with pytest.raises(FdmError) as e:
+            srv.submit_solve(outs[2], r, shape, tol=1e-10)
+        assert e.value.status == N.EBUSY
+        for i in [busy] + queued:
+            assert srv.wait(i)["state"] == "done"
+        assert srv.stats()["shed"] == 4
+        srv.set_admission(0, 0.0)
+        ids = [srv.submit_solve(a, r, shape, tol=1e-10) for a in outs]
+        assert all(srv.wait(i)["state"] == "done" for i in ids)
+        _, steps = srv.session_field(sid, "u")
+        assert steps == 602
+    ref = _fp64(shape, r)
+    assert _rel(outs[2].numpy(), ref) <= 1e-10
+
+
 def test_waiting_solves_share_a_launch(cuda):
     """Solves of one geometry that wait behind a busy lane go out as one
     launch; their answers equal the ones they get alone."""
