@@ -813,6 +813,11 @@ def main():
     tfile = ROOT / "profiles" / "ncu_traffic.json"
     if tfile.exists():
         traffic = json.loads(tfile.read_text()).get(dname)
+    # what bounds the dominant kernel when it is not HBM (ncu, committed)
+    limiter = None
+    lfile = ROOT / "profiles" / "ncu_limiters.json"
+    if lfile.exists():
+        limiter = json.loads(lfile.read_text()).get(dname)
 
     # ---- context numbers (untimed for the headline): the plain FP64 GPU form
     # on the same inputs, and the NSCube cavity step at 63^3
@@ -889,7 +894,7 @@ def main():
         "roofline": {"bound": "hbm", "kernel": dname, "achieved": achieved, "peak": hbm, "unit": "GB/s",
                      "frac": (achieved / hbm) if achieved else None, "traffic": traffic,
                      "peak_source": peak_kind, "algorithmic_bytes_per_point": bpp,
-                     "launch_ms": per_launch_ms},
+                     "launch_ms": per_launch_ms, "limiter": limiter},
         "solve_roofline": {"achieved_gbs": value / world * SOLVE_BYTES_PER_POINT * vol / 1e9, "peak": hbm,
                            "frac": value / world * SOLVE_BYTES_PER_POINT * vol / 1e9 / hbm,
                            "bytes_per_point": SOLVE_BYTES_PER_POINT},
