@@ -100,6 +100,7 @@ _SIGS = [
     ("fdmgpu_nscube_create", c_int,
      [POINTER(c_void_p), c_int, c_int, c_int] + [c_double] * 9),
     ("fdmgpu_nscube_step", c_int, [c_void_p, c_int]),
+    ("fdmgpu_nscube_step_many", c_int, [c_void_p, c_void_p, c_int]),
     ("fdmgpu_nscube_set_exact", c_int, [c_void_p, c_int]),
     ("fdmgpu_nscube_set_stream", c_int, [c_void_p, c_void_p]),
     ("fdmgpu_nscube_field_info", c_int, [c_void_p, c_int, POINTER(c_size_t), POINTER(c_int)]),

@@ -716,6 +716,42 @@ int fdmgpu_nscube_create(fdmgpu_nscube** h, int dtype, int nx, int nz, double x1
     FDM_API_END
 }
 
+int fdmgpu_nscube_step_many(fdmgpu_nscube* const* hs, const int* steps, int n) {
+    FDM_API_BEGIN
+    if (!hs || !steps || n < 1) FDM_FAIL(FDMGPU_EINVAL, "null argument or no cavity");
+    for (int i = 0; i < n; i++) {
+        if (!hs[i]) FDM_FAIL(FDMGPU_EINVAL, "null handle");
+        for (int j = 0; j < i; j++)
+            if (hs[j] == hs[i]) FDM_FAIL(FDMGPU_EINVAL, "cavity %d appears twice", i);
+    }
+    // nscube_step_many checks the element type, the step counts and the
+    // geometry before anything is enqueued
+    for (int i = 0; i < n; i++) {
+        if (!hs[i]->d) FDM_FAIL(FDMGPU_ENOTSUP, "shared steps are for FP64 cavities");
+        if (steps[i] < 0) FDM_FAIL(FDMGPU_EINVAL, "negative step count");
+        if (!nscube_mergeable(hs[0], hs[i])) FDM_FAIL(FDMGPU_EINVAL, "cavities of different geometry");
+    }
+    // the steps run on the first cavity's stream, after the work queued on
+    // every cavity's stream and before what is queued there later
+    const cudaStream_t st = hs[0]->d->st;
+    cudaEvent_t ev = nullptr;
+    FDM_CUDA(cudaEventCreateWithFlags(&ev, cudaEventDisableTiming));
+    try {
+        for (int i = 1; i < n; i++) {
+            FDM_CUDA(cudaEventRecord(ev, hs[i]->d->st));
+            FDM_CUDA(cudaStreamWaitEvent(st, ev, 0));
+        }
+        nscube_step_many(hs, steps, n, st);
+        FDM_CUDA(cudaEventRecord(ev, st));
+        for (int i = 1; i < n; i++) FDM_CUDA(cudaStreamWaitEvent(hs[i]->d->st, ev, 0));
+    } catch (...) {
+        cudaEventDestroy(ev);
+        throw;
+    }
+    FDM_CUDA(cudaEventDestroy(ev));
+    FDM_API_END
+}
+
 int fdmgpu_nscube_step(fdmgpu_nscube* h, int k) {
     FDM_API_BEGIN
     if (!h) FDM_FAIL(FDMGPU_EINVAL, "null handle");

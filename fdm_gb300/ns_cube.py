@@ -77,6 +77,19 @@ class NSCube:
     def step(self, k: int = 1) -> None:
         N.check(self._lib.fdmgpu_nscube_step(self._h, int(k)))
 
+    @staticmethod
+    def step_many(cavities, steps) -> None:
+        """steps[i] steps of each FP64 cavity, all of one geometry, as shared
+        launches (fdmgpu_nscube_step_many); the fields are bit for bit those
+        of stepping each cavity alone."""
+        cav = list(cavities)
+        ks = [int(k) for k in steps]
+        if len(cav) != len(ks) or not cav:
+            raise N.FdmError(N.EINVAL, "one step count per cavity")
+        hs = (c_void_p * len(cav))(*[c._h for c in cav])
+        arr = (c_int * len(ks))(*ks)
+        N.check(cav[0]._lib.fdmgpu_nscube_step_many(hs, arr, len(cav)))
+
     def set_exact(self, exact: bool = True) -> None:
         """exact=True: quotients by the run constants correctly rounded, as
         the reference's divisions are; False (default): products with

@@ -349,6 +349,17 @@ int fdmgpu_nscube_create(fdmgpu_nscube** h, int dtype, int nx, int nz,
                          double u0, double Re, double dt);
 /* k steps; asynchronous on the handle's stream */
 int fdmgpu_nscube_step(fdmgpu_nscube* h, int k);
+/* steps[i] steps of each of n distinct FP64 cavities of one geometry (grid,
+ * spacing, box extents, quotient form; Re, dt and u0 may differ): step r of
+ * every cavity with more than r steps to go is one launch per kernel, the
+ * cavity read from a table by the grid's y index.  The fields are bit for
+ * bit those of fdmgpu_nscube_step on each handle.  Asynchronous on the
+ * first handle's stream, ordered after the work queued on every handle's
+ * stream and before what is queued there later.  FDMGPU_EINVAL for a
+ * repeated handle or different geometries, FDMGPU_ENOTSUP for FP32.  No
+ * reference counterpart: the reference steps one NSCube per call
+ * (src/ns_cube.cpp:27-62). */
+int fdmgpu_nscube_step_many(fdmgpu_nscube* const* hs, const int* steps, int n);
 /* exact = 1: every quotient by a run constant (Re, dx, dx^2, dt, ...) in
  * the boundary ghosts, F/G/H and the divergence is correctly rounded, as the
  * reference's a / b is (five FP64 operations each).  exact = 0 (default):

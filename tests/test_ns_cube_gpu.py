@@ -8,6 +8,7 @@ import pytest
 
 from tests.helpers import rel_l2
 from fdm_gb300 import Config, FdmError, NSCube
+from fdm_gb300 import _native as N
 
 pytestmark = pytest.mark.gpu
 
@@ -58,6 +59,38 @@ def test_fast_and_exact_forms_agree(cuda):
         x, y = a.get(name).data, b.get(name).data
         scale = max(1.0, float(np.abs(y).max()))  # the lid velocity is 1
         assert np.abs(x - y).max() <= 1e-13 * scale, name
+
+
+def test_step_many_matches_steps_alone(cuda):
+    """Shared steps of several cavities (fdmgpu_nscube_step_many) leave each
+    cavity bit for bit where its own steps would, mixed with its own steps
+    before and after; repeated handles, other geometries and FP32 cavities
+    are refused."""
+    res = (250.0, 100.0, 400.0)
+    shared = [NSCube(nx=31, nz=31, Re=re, dt=0.01, u0=1.0) for re in res]
+    alone = [NSCube(nx=31, nz=31, Re=re, dt=0.01, u0=1.0) for re in res]
+    NSCube.step_many(shared, [4, 0, 7])
+    shared[0].step(2)
+    NSCube.step_many(shared, [1, 3, 1])
+    for a, k in zip(alone, (7, 3, 8)):
+        a.step(k)
+    for s, a in zip(shared, alone):
+        assert s.time_index == a.time_index
+        for name in ("u", "v", "w", "p"):
+            assert np.array_equal(s.get(name).data, a.get(name).data), name
+    with pytest.raises(FdmError) as e:
+        NSCube.step_many([shared[0], shared[0]], [1, 1])
+    assert e.value.status == N.EINVAL
+    other = NSCube(nx=15, nz=15, Re=250.0, dt=0.01, u0=1.0)
+    with pytest.raises(FdmError) as e:
+        NSCube.step_many([shared[0], other], [1, 1])
+    assert e.value.status == N.EINVAL
+    f32 = NSCube(nx=31, nz=31, Re=250.0, dt=0.01, u0=1.0, dtype=np.float32)
+    with pytest.raises(FdmError) as e:
+        NSCube.step_many([shared[0], f32], [1, 1])
+    assert e.value.status == N.ENOTSUP
+    for c in shared + alone + [other, f32]:
+        c.close()
 
 
 def test_golden_31_cube(cuda, golden):
