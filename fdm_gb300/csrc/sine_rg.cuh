@@ -513,6 +513,42 @@ __device__ __forceinline__ void sine_rg_body(const Tin* in, Tout* out, const Sin
             const float* uh = fu.uhi + voff + base;
             const float* ul = fu.ulo ? fu.ulo + voff + base : nullptr;
             float* ulo_out = fu.ulo_out ? fu.ulo_out + voff + base : nullptr;
+            if (!ul) {
+                // no low part (the first sweep): u = uhi + c as the float
+                // pair two_sum(uhi, c), the value the general form below
+                // gives with ulo = 0; the uhi loads of half the slots are
+                // issued before any is used
+                constexpr int QH = QS / 2;
+#pragma unroll
+                for (int q0 = 0; q0 < QS; q0 += QH) {
+                    float hv[2 * QH];
+#pragma unroll
+                    for (int a = 0; a < 2 * QH; a++) {
+                        const int q = q0 + (a >> 1), h = a & 1;
+                        const bool ok = act && (h || q > 0 || wid > 0);
+                        hv[a] = ok ? uh[q * s16 + h * nx] : 0.f;
+                    }
+#pragma unroll
+                    for (int qq = 0; qq < QH; qq++) {
+                        const int q = q0 + qq;
+                        if (!act) continue;
+                        const T2 f2 = src[8 * q + (q >> 1)];
+#pragma unroll
+                        for (int h = 0; h < 2; h++) {
+                            if (!h && q == 0 && wid == 0) continue;
+                            const long long o = q * s16 + h * nx;
+                            const float cv = (float)(scale * (h ? f2.y : f2.x));
+                            const ff s2 = two_sum(__fadd_rn(hv[2 * qq + h], 0.f), cv);
+                            if (fu.last) o64[o] = ff_to_f64(s2);
+                            if (ulo_out) ulo_out[o] = __fadd_rn(0.f, cv);
+                            cc += cv * cv;
+                            uu += s2.h * s2.h;
+                        }
+                    }
+                }
+                norms_reduce(cc, uu, fu.norms, tid, nthr);
+                return;
+            }
 #pragma unroll
             for (int q0 = 0; q0 < QS; q0 += 2) {
                 float hv[4], lw[4];
