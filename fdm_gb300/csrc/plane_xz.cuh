@@ -61,6 +61,8 @@ struct PlaneCfg {
 // The x transforms use the row swizzles of RgSwz (layouts B and C only, so
 // the plane's own views of the folded input and packed output are plain).
 constexpr bool kPlaneSwz = true;
+// rows whose loads a warp issues together in the fold phase
+constexpr int kPlaneFoldLines = 2;
 
 template <int N, int C, int MINB>
 __global__ void __launch_bounds__(256, MINB) k_plane_xz(float* __restrict__ W, PlaneGeom geo, SineTables<float> tb,
@@ -112,34 +114,46 @@ __global__ void __launch_bounds__(256, MINB) k_plane_xz(float* __restrict__ W, P
     const int fb = 2 * (M + M / 16 - hh - (hh > 0 ? 1 : 0)) + (lane & 1);
     static_assert(M % 32 == 0 && L % 8 == 0, "warp-per-line phases");
 
-    // ---- 1. load + fold, then the DST along x
+    // ---- 1. load + fold, then the DST along x; the loads of kPlaneFoldLines
+    // rows are issued before any of them is folded
+    constexpr int PL = kPlaneFoldLines;
+    static_assert(LPW % PL == 0, "rows per warp in whole load batches");
 #pragma unroll
-    for (int li = 0; li < LPW; li++) {
-        const int line = wid + 8 * li;
-        float* xo = Sr + 2 * (LPW * wid + li) * LS2;
-        if (line < nact) {
+    for (int l0 = 0; l0 < LPW; l0 += PL) {
+        float a[PL][KJ], b[PL][KJ], am[PL];
+#pragma unroll
+        for (int pl = 0; pl < PL; pl++) {
+            const int line = wid + 8 * (l0 + pl);
             const float* p = row0 + line * rstride;
-            float a[KJ], b[KJ];
+            const bool in = line < nact;
 #pragma unroll
             for (int k = 0; k < KJ; k++) {
-                const bool ok = k > 0 || lane > 0;
-                a[k] = ok ? p[lane + 32 * k - 1] : 0.f;
-                b[k] = ok ? p[n - lane - 32 * k] : 0.f;
+                const bool ok = in && (k > 0 || lane > 0);
+                a[pl][k] = ok ? p[lane + 32 * k - 1] : 0.f;
+                b[pl][k] = ok ? p[n - lane - 32 * k] : 0.f;
             }
-            const float am = p[M - 1];
+            am[pl] = in ? p[M - 1] : 0.f;
+        }
 #pragma unroll
-            for (int k = 0; k < KJ; k++) {
-                const int j = lane + 32 * k;
-                const float w = ldg(tb.wpre + j);
-                const float sm = w * (a[k] + b[k]), df = 0.5f * (a[k] - b[k]);
-                xo[j] = sm + df;  // j = 0: both are 0
-                if (k > 0 || lane > 0) xo[N - j] = sm - df;
+        for (int pl = 0; pl < PL; pl++) {
+            const int li = l0 + pl;
+            const int line = wid + 8 * li;
+            float* xo = Sr + 2 * (LPW * wid + li) * LS2;
+            if (line < nact) {
+#pragma unroll
+                for (int k = 0; k < KJ; k++) {
+                    const int j = lane + 32 * k;
+                    const float w = ldg(tb.wpre + j);
+                    const float sm = w * (a[pl][k] + b[pl][k]), df = 0.5f * (a[pl][k] - b[pl][k]);
+                    xo[j] = sm + df;  // j = 0: both are 0
+                    if (k > 0 || lane > 0) xo[N - j] = sm - df;
+                }
+                if (lane == 0) xo[M] = ldg(tb.wpre + M) * (am[pl] + am[pl]);
+            } else {
+                // the row past the plane's end (last CTA): a zero line
+#pragma unroll
+                for (int k = 0; k < 2 * KJ; k++) xo[lane + 32 * k] = 0.f;
             }
-            if (lane == 0) xo[M] = ldg(tb.wpre + M) * (am + am);
-        } else {
-            // the row past the plane's end (last CTA): a zero line
-#pragma unroll
-            for (int k = 0; k < 2 * KJ; k++) xo[lane + 32 * k] = 0.f;
         }
     }
     __syncwarp();

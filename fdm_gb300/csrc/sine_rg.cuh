@@ -322,6 +322,10 @@ __device__ __forceinline__ void norms_reduce(float cc, float uu, double* norms, 
     }
 }
 
+// column pass, one line per lane: item pairs loaded per batch of the fold
+constexpr int kColFoldBatch = 8;    // FP32 input
+constexpr int kColFoldBatch64 = 8;  // FP64 input (kRound)
+
 template <typename Tin, typename T, typename Tout, int AXIS, int MODE, int N, int NT = 256>
 __device__ __forceinline__ void sine_rg_body(const Tin* in, Tout* out, const SineGeom& geo, const SineTables<T>& tb,
                                              T scale, const SineFused& fu) {
@@ -368,11 +372,14 @@ __device__ __forceinline__ void sine_rg_body(const Tin* in, Tout* out, const Sin
         const long long s8 = 8LL * nx;
         const Tin* pa = p + (long long)(wid - 1) * nx;  // x_j sits in row j - 1
         const Tin* pb = p + (long long)(n - wid) * nx;  // x_{N-j} in row n - j
+        // loads in flight per thread: FB pairs (FP32 input: all but one
+        // batch of the line's items ahead of their use)
+        constexpr int FB = sizeof(Tin) == 4 ? kColFoldBatch : kColFoldBatch64;
 #pragma unroll
-        for (int q0 = 0; q0 < QN; q0 += 4) {
-            T av[4], bv[4];
+        for (int q0 = 0; q0 < QN; q0 += FB) {
+            T av[FB], bv[FB];
 #pragma unroll
-            for (int qq = 0; qq < 4; qq++) {
+            for (int qq = 0; qq < FB; qq++) {
                 const int q = q0 + qq, j = wid + 8 * q;
                 T a = T(0), b = T(0);
                 if (q < QN && j <= M && (q > 0 || wid > 0) && act) {
@@ -388,7 +395,7 @@ __device__ __forceinline__ void sine_rg_body(const Tin* in, Tout* out, const Sin
                 bv[qq] = b;
             }
 #pragma unroll
-            for (int qq = 0; qq < 4; qq++) {
+            for (int qq = 0; qq < FB; qq++) {
                 const int q = q0 + qq, j = wid + 8 * q;
                 if (q < QN && j <= M) {
                     const T w = ldg(tb.wpre + j);
