@@ -325,6 +325,8 @@ __device__ __forceinline__ void norms_reduce(float cc, float uu, double* norms, 
 // column pass, one line per lane: item pairs loaded per batch of the fold
 constexpr int kColFoldBatch = 8;    // FP32 input
 constexpr int kColFoldBatch64 = 8;  // FP64 input (kRound)
+// column combine pass with a low part: packed slots whose loads go ahead
+constexpr int kCombineAhead = 4;
 
 template <typename Tin, typename T, typename Tout, int AXIS, int MODE, int N, int NT = 256>
 __device__ __forceinline__ void sine_rg_body(const Tin* in, Tout* out, const SineGeom& geo, const SineTables<T>& tb,
@@ -556,19 +558,22 @@ __device__ __forceinline__ void sine_rg_body(const Tin* in, Tout* out, const Sin
                 norms_reduce(cc, uu, fu.norms, tid, nthr);
                 return;
             }
+            // with a low part: the loads of kCombineAhead slots issued
+            // before any of them is used
+            constexpr int QC = kCombineAhead;
 #pragma unroll
-            for (int q0 = 0; q0 < QS; q0 += 2) {
-                float hv[4], lw[4];
+            for (int q0 = 0; q0 < QS; q0 += QC) {
+                float hv[2 * QC], lw[2 * QC];
 #pragma unroll
-                for (int a = 0; a < 4; a++) {
+                for (int a = 0; a < 2 * QC; a++) {
                     const int q = q0 + (a >> 1), h = a & 1;
                     const long long o = q * s16 + h * nx;
                     const bool ok = act && (h || q > 0 || wid > 0);
                     hv[a] = ok ? uh[o] : 0.f;
-                    lw[a] = (ok && ul) ? ul[o] : 0.f;
+                    lw[a] = ok ? ul[o] : 0.f;
                 }
 #pragma unroll
-                for (int qq = 0; qq < 2; qq++) {
+                for (int qq = 0; qq < QC; qq++) {
                     const int q = q0 + qq;
                     if (!act) continue;
                     const T2 f2 = src[8 * q + (q >> 1)];
