@@ -645,8 +645,11 @@ __device__ __forceinline__ void sine_rg_body(const Tin* in, Tout* out, const Sin
             for (int q = 0; q < 4; q++) {
                 if (ok[q]) {
                     const float cv = (float)(scale * Sr[so[q]]);
-                    ff s2 = two_sum(hv[q], lv[q]);
-                    s2 = ff_add_f(s2, cv);
+                    // no low part: two_sum(u_hi, c), the value of the general
+                    // form with u_lo = 0, bit for bit
+                    ff s2;
+                    if (fu.ulo) s2 = ff_add_f(two_sum(hv[q], lv[q]), cv);
+                    else s2 = two_sum(__fadd_rn(hv[q], 0.f), cv);
                     if (fu.last) o64[ix[q]] = ff_to_f64(s2);
                     if (fu.ulo_out) fu.ulo_out[voff + ix[q]] = lv[q] + cv;
                     cc += cv * cv;
