@@ -160,14 +160,18 @@ __global__ void __launch_bounds__(256, MINB) k_plane_xz(float* __restrict__ W, P
     rg_line_fft<float, N, 0, kPlaneSwz>(S + l * LS2, g, l, tb);
     __syncthreads();
 
-    // ---- 2. z blocks: thread t owns x-mode i = t+1 of every local block.
-    // Entry i of row q sits at Sr[2*(rowpos(q)*LS2 + sk(i>>1)) + (i&1)].
+    // ---- 2. z blocks: thread t owns x-mode i = t of every local block
+    // (thread 0 none).  Entry i of row q sits at Sr[2*(rowpos(q)*LS2 +
+    // sk(i>>1)) + (i&1)], float i + 2 (i >> 5) of the row, so the 32 modes
+    // of a warp are 32 consecutive floats (one wavefront); tm = i - 1 indexes
+    // the mode's table column and its slots of xf, xl, xg and xs.
     const int t = tid;
-    const bool mode_ok = t < n;
-    const int i = t + 1;
+    const bool mode_ok = t >= 1 && t <= n;
+    const int i = t;
+    const int tm0 = mode_ok ? t - 1 : 0;
     const int fo = 2 * sk(i >> 1) + (i & 1);
     const int modes = geo.modes;
-    const int tmode = ky * nx + (mode_ok ? t : 0);
+    const int tmode = ky * nx + tm0;
     constexpr int RS = 2 * LS2;  // floats between rows
     if (mode_ok) {
         float cp[m];
@@ -190,9 +194,9 @@ __global__ void __launch_bounds__(256, MINB) k_plane_xz(float* __restrict__ W, P
             for (int k = m - 2; k >= 0; k--) v[k] = v[k] - cp[k] * v[k + 1];
 #pragma unroll
             for (int k = 0; k < m; k++) col[rowpos(16 * b + k) * RS] = v[k];
-            xf[b * XS + t] = v[0];
-            xl[b * XS + t] = v[m - 1];
-            xg[b * XS + t] = gb < P - 1 ? col[rowpos(16 * b + m) * RS] * gs : 0.f;
+            xf[b * XS + tm0] = v[0];
+            xl[b * XS + tm0] = v[m - 1];
+            xg[b * XS + tm0] = gb < P - 1 ? col[rowpos(16 * b + m) * RS] * gs : 0.f;
         }
     }
     // the plane's outer ends: s[-1] = s[P-1] = 0
@@ -248,7 +252,7 @@ __global__ void __launch_bounds__(256, MINB) k_plane_xz(float* __restrict__ W, P
 #pragma unroll
         for (int b = 0; b < B; b++) {
             const int gb = r * B + b;
-            const float ul = xs[b * XS + t], ur = xs[(b + 1) * XS + t];
+            const float ul = xs[b * XS + tm0], ur = xs[(b + 1) * XS + tm0];
             float* col = Sr + fo;
 #pragma unroll
             for (int k = 0; k < m; k++) {
