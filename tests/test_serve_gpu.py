@@ -171,6 +171,55 @@ def test_load_shedding(cuda):
     assert _rel(outs[2].numpy(), ref) <= 1e-10
 
 
+def test_submits_from_several_threads(cuda):
+    """Four client threads submit solves and advances at once, with the
+    queue deadline and a queue bound set high enough to shed nothing: every
+    request completes and every answer is the same as alone."""
+    import threading
+    import torch
+    shapes = [(31, 31, 31), (63, 31, 31), (31, 63, 63)]
+    rhs = {s: _pinned_rhs(s, 70 + k) for k, s in enumerate(shapes)}
+    alone = {}
+    with Server(budget_bytes=8e9, lanes=1, max_batch=1) as srv:
+        for s in shapes:
+            a = _pinned_like(rhs[s])
+            srv.wait(srv.submit_solve(a, rhs[s], s, tol=1e-10))
+            alone[s] = a
+    errors = []
+    with Server(budget_bytes=8e9, lanes=8, max_batch=4) as srv:
+        srv.set_admission(max_queued=10000, max_wait_ms=60000.0)
+        sids = [srv.session_create(31, 31, Re=250.0, dt=0.01) for _ in range(4)]
+
+        def client(k):
+            try:
+                mine = []
+                for j in range(30):
+                    s = shapes[(k + j) % len(shapes)]
+                    a = _pinned_like(rhs[s])
+                    mine.append((srv.submit_solve(a, rhs[s], s, tol=1e-10), s, a))
+                    if j % 5 == 0:
+                        mine.append((srv.submit_advance(sids[k], 2), None, None))
+                for rid, s, a in mine:
+                    rec = srv.wait(rid)
+                    if rec["state"] != "done":
+                        errors.append(rec)
+                    elif s is not None and not torch.equal(a, alone[s]):
+                        errors.append(("differs", s))
+            except Exception as e:  # noqa: BLE001 - reported below
+                errors.append(repr(e))
+
+        threads = [threading.Thread(target=client, args=(k,)) for k in range(4)]
+        for t in threads:
+            t.start()
+        for t in threads:
+            t.join()
+        assert not errors, errors[:3]
+        st = srv.stats()
+        assert st["completed"] == 4 * (30 + 6) and st["shed"] == 0 and st["failed"] == 0
+        for sid in sids:
+            assert srv.session_field(sid, "u")[1] == 12
+
+
 def test_waiting_solves_share_a_launch(cuda):
     """Solves of one geometry that wait behind a busy lane go out as one
     launch; their answers equal the ones they get alone."""
