@@ -603,7 +603,7 @@ bool nscube_mergeable(const fdmgpu_nscube* a, const fdmgpu_nscube* b) {
            p.z2 - p.z1 == q.z2 - q.z1 && p.exact == q.exact;
 }
 
-void nscube_step_many(fdmgpu_nscube* const* hs, const int* steps, int n, cudaStream_t st) {
+void nscube_step_many(fdmgpu_nscube* const* hs, const int* steps, int n, cudaStream_t st, cudaMemPool_t pool) {
     if (n < 1) return;
     for (int i = 0; i < n; i++) {
         if (!hs[i] || !hs[i]->d) FDM_FAIL(FDMGPU_ENOTSUP, "shared steps are for FP64 cavities");
@@ -631,7 +631,8 @@ void nscube_step_many(fdmgpu_nscube* const* hs, const int* steps, int n, cudaStr
         const size_t bio = (io.size() * sizeof(void*) + 255) / 256 * 256;
         const size_t bw = (size_t)n * p0.P.nx * p0.P.ny * p0.P.nz * sizeof(double);
         char* d = nullptr;
-        FDM_CUDA(cudaMallocAsync((void**)&d, bs + bio + bw, st));
+        if (pool) FDM_CUDA(cudaMallocFromPoolAsync((void**)&d, bs + bio + bw, pool, st));
+        else FDM_CUDA(cudaMallocAsync((void**)&d, bs + bio + bw, st));
         try {
             FDM_CUDA(cudaMemcpyAsync(d, ss.data(), ss.size() * sizeof(NSSessionT<double>), cudaMemcpyHostToDevice, st));
             FDM_CUDA(cudaMemcpyAsync(d + bs, io.data(), io.size() * sizeof(void*), cudaMemcpyHostToDevice, st));

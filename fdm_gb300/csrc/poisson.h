@@ -42,7 +42,10 @@ void cube_estimates(const fdmgpu_lapl_cube* h, const double* norms_host, int swe
 // a single cavity's step, so every field comes out as it would alone.  The
 // caller orders st after each cavity's earlier work.  Throws fdmgpu::Error.
 bool nscube_mergeable(const fdmgpu_nscube* a, const fdmgpu_nscube* b);
-void nscube_step_many(fdmgpu_nscube* const* hs, const int* steps, int n, cudaStream_t st);
+// pool: where the tables and work volumes of the shared steps come from
+// (stream-ordered; null = the device's default pool)
+void nscube_step_many(fdmgpu_nscube* const* hs, const int* steps, int n, cudaStream_t st,
+                      cudaMemPool_t pool = nullptr);
 
 // The same for a LaplCyl3FFT2 plan (fdmgpu_lapl_cyl_create), used by NSCyl.
 void cyl_solve_device(fdmgpu_lapl_cyl* h, void* ans, const void* rhs, int nrhs, cudaStream_t st);

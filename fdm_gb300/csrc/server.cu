@@ -447,7 +447,7 @@ struct Server {
         }
         int code = FDMGPU_OK;
         try {
-            nscube_step_many(a.cavities.data(), steps.data(), n, L->st);
+            nscube_step_many(a.cavities.data(), steps.data(), n, L->st, pool);
         } catch (const Error& x) {
             err = fdmgpu_last_error();
             code = x.code;
