@@ -94,3 +94,19 @@ def test_server_arguments_without_gpu(native):
     assert lib.fdmgpu_server_create(None, 1e9, 8, 8) == N.EINVAL
     assert lib.fdmgpu_server_destroy(None) == N.OK
     assert lib.fdmgpu_server_cancel(None, 1) == N.EINVAL
+    assert lib.fdmgpu_server_set_admission(None, 0, 0.0) == N.EINVAL
+
+
+def test_shared_steps_arguments_without_gpu(native):
+    from ctypes import c_int
+    from fdm_gb300 import FdmError, NSCube
+    from fdm_gb300 import _native as N
+    lib = N.load()
+    assert lib.fdmgpu_nscube_step_many(None, None, 0) == N.EINVAL
+    hs = (c_void_p * 2)(None, None)
+    ks = (c_int * 2)(1, 1)
+    assert lib.fdmgpu_nscube_step_many(hs, ks, 0) == N.EINVAL
+    assert lib.fdmgpu_nscube_step_many(hs, ks, 2) == N.EINVAL  # null handles
+    with pytest.raises(FdmError) as e:
+        NSCube.step_many([], [])
+    assert e.value.status == N.EINVAL
