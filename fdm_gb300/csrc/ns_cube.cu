@@ -64,6 +64,7 @@ struct NSParams {
     // diffusion terms, dt / (4 h) for the convection terms (whose 0.5 and
     // 0.25 factors they absorb); the fast divergence's 1 / (h dt)
     double kCx, kCy, kCz, kAx, kAy, kAz, kRx, kRy, kRz;
+    double kC0;  // 1 - 2 (kCx + kCy + kCz): the centre's weight in u + dt diffusion
 };
 
 // x / d (FAST: x * r, r = 1 / d computed on the host; otherwise the
@@ -215,43 +216,49 @@ __device__ __forceinline__ void ns_fgh_body(FieldT<T> u, FieldT<T> v, FieldT<T> 
     const bool doF = i >= 1 && k >= 1, doG = i >= 1 && j >= 1, doH = k >= 1 && j >= 1;
     if constexpr (FAST && sizeof(T) == 8) {
         // FP64 fields: u + dt (diffusion - convection) as one chain of fused
-        // multiply-adds
-        // per component: sq(a/2) - sq(b/2) = (a^2 - b^2) / 4 and the
-        // cross terms' 0.25 go into dt / (4 h); the three cross products
-        // that two components share (F's y term and G's x term, F's z term
-        // and H's x term, G's z term and H's y term) are formed once.  Every
-        // read below is inside its field's range for any point of the box.
+        // multiply-adds.  Per component: the diffusion is kC0 c + sum over
+        // the axes of kC (m + p), the centre's three -2c terms gathered in
+        // kC0 = 1 - 2 (kCx + kCy + kCz); along the component's own axis
+        // sq(a/2) - sq(b/2) = (a - b)(a + b) / 4 = (p - m)(m + p + 2c) / 4
+        // with a = c + p, b = m + c, so the neighbour sum m + p serves both
+        // terms; the cross terms' 0.25 go into dt / (4 h); the three cross
+        // products that two components share (F's y term and G's x term, F's
+        // z term and H's x term, G's z term and H's y term) are formed once.
+        // Every read below is inside its field's range for any point of the
+        // box.
         const double uc = u(i, k, j), vc = v(i, k, j), wc = w(i, k, j);
         const double puv = (uc + u(i, k + 1, j)) * (v(i, k, j + 1) + vc);
         const double puw = (uc + u(i + 1, k, j)) * (w(i, k, j + 1) + wc);
         const double pwv = (wc + w(i, k + 1, j)) * (vc + v(i + 1, k, j));
-        auto lap = [](double m, double c, double pl) { return (m + pl) - 2.0 * c; };
         if (doF) {
-            const double a = uc + u(i, k, j + 1), b = u(i, k, j - 1) + uc;
-            double acc = uc + P.kCx * lap(u(i, k, j - 1), uc, u(i, k, j + 1));
-            acc += P.kCy * lap(u(i, k - 1, j), uc, u(i, k + 1, j));
-            acc += P.kCz * lap(u(i - 1, k, j), uc, u(i + 1, k, j));
-            acc -= P.kAx * (a * a - b * b);
+            const double m = u(i, k, j - 1), pl = u(i, k, j + 1), sx = m + pl;
+            double acc = P.kC0 * uc;
+            acc += P.kCx * sx;
+            acc += P.kCy * (u(i, k - 1, j) + u(i, k + 1, j));
+            acc += P.kCz * (u(i - 1, k, j) + u(i + 1, k, j));
+            acc -= P.kAx * ((pl - m) * (sx + 2.0 * uc));
             acc -= P.kAy * (puv - (u(i, k - 1, j) + uc) * (v(i, k - 1, j + 1) + v(i, k - 1, j)));
             acc -= P.kAz * (puw - (u(i - 1, k, j) + uc) * (w(i - 1, k, j + 1) + w(i - 1, k, j)));
             fv = acc;
         }
         if (doG) {
-            const double a = vc + v(i, k + 1, j), b = v(i, k - 1, j) + vc;
-            double acc = vc + P.kCx * lap(v(i, k, j - 1), vc, v(i, k, j + 1));
-            acc += P.kCy * lap(v(i, k - 1, j), vc, v(i, k + 1, j));
-            acc += P.kCz * lap(v(i - 1, k, j), vc, v(i + 1, k, j));
-            acc -= P.kAy * (a * a - b * b);
+            const double m = v(i, k - 1, j), pl = v(i, k + 1, j), sy = m + pl;
+            double acc = P.kC0 * vc;
+            acc += P.kCx * (v(i, k, j - 1) + v(i, k, j + 1));
+            acc += P.kCy * sy;
+            acc += P.kCz * (v(i - 1, k, j) + v(i + 1, k, j));
+            acc -= P.kAy * ((pl - m) * (sy + 2.0 * vc));
             acc -= P.kAx * (puv - (u(i, k, j - 1) + u(i, k + 1, j - 1)) * (vc + v(i, k, j - 1)));
             acc -= P.kAz * (pwv - (w(i - 1, k, j) + w(i - 1, k + 1, j)) * (v(i - 1, k, j) + vc));
             gv = acc;
         }
         if (doH) {
-            const double a = w(i + 1, k, j) + wc, b = w(i - 1, k, j) + wc;
-            double acc = wc + P.kCx * lap(w(i, k, j - 1), wc, w(i, k, j + 1));
-            acc += P.kCy * lap(w(i, k - 1, j), wc, w(i, k + 1, j));
-            acc += P.kCz * lap(w(i - 1, k, j), wc, w(i + 1, k, j));
-            acc -= P.kAz * (a * a - b * b);
+            const double m = w(i - 1, k, j), pl = w(i + 1, k, j), sz = m + pl;
+            double acc = P.kC0 * wc;
+            acc += P.kCx * (w(i, k, j - 1) + w(i, k, j + 1));
+            acc += P.kCy * (w(i, k - 1, j) + w(i, k + 1, j));
+            acc += P.kCz * sz;
+            acc -= P.kAz * ((pl - m) * (sz + 2.0 * wc));
             acc -= P.kAx * (puw - (u(i + 1, k, j - 1) + u(i, k, j - 1)) * (wc + w(i, k, j - 1)));
             acc -= P.kAy * (pwv - (w(i, k - 1, j) + wc) * (v(i, k - 1, j) + v(i + 1, k - 1, j)));
             hv = acc;
@@ -687,6 +694,7 @@ void setup_plan(NSPlanT<T>& s, int nx, int nz, double x1, double y1, double z1, 
     s.P.kCx = dt / (Re * s.P.dx2); s.P.kCy = dt / (Re * s.P.dy2); s.P.kCz = dt / (Re * s.P.dz2);
     s.P.kAx = dt / (4.0 * s.P.dx); s.P.kAy = dt / (4.0 * s.P.dy); s.P.kAz = dt / (4.0 * s.P.dz);
     s.P.kRx = 1.0 / (s.P.dx * dt); s.P.kRy = 1.0 / (s.P.dy * dt); s.P.kRz = 1.0 / (s.P.dz * dt);
+    s.P.kC0 = 1.0 - 2.0 * (s.P.kCx + s.P.kCy + s.P.kCz);
     s.init();
 }
 }  // namespace
