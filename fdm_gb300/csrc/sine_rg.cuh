@@ -76,7 +76,11 @@ struct RgGeom {
 // to 2.81 ms, the x passes about 1 % faster.  Column passes keep plain
 // layouts: a swizzled column layout at the row stride (3328 -> 2450
 // modelled wavefronts) needed more than 48 registers and ran 3-5 % slower
-// at 4 CTAs per SM than the plain one at 5.
+// at 4 CTAs per SM than the plain one at 5.  What works instead: the FP32
+// column passes of 128 and 256 points hand their lines to the transform in
+// an order that puts a half-warp's two lines 8 lines apart, and use the row
+// masks (y pass 0.61 -> 0.59 ms, FP64-rounding y pass 0.86 -> 0.82 ms per
+// 16 x 255^3 launch; 127^3 solves 3 % faster).
 template <typename T, int N, int AXIS>
 struct RgSwz {
     static constexpr int B0 = 0, B1 = 0, C0 = 0, C1 = 0;
@@ -484,7 +488,22 @@ __device__ __forceinline__ void sine_rg_body(const Tin* in, Tout* out, const Sin
     }
     __syncthreads();
 
-    rg_line_fft<T, N, AXIS>(S + (size_t)l * LS2, g, l, tb);
+    // (not the 256-point combine pass: at its 48 registers the swizzles
+    // spill, and it measured 2 % slower)
+    if constexpr (kCol32 && sizeof(T) == 4 && !(MODE == kCombine && N == 256)) {
+        // the transform takes the lines in an order whose two lines per
+        // half-warp sit 8 lines apart, 8 LS2 = 8 (mod 16) slots, as two
+        // consecutive rows do, so the rows' slot swizzles apply (a bank
+        // model of the transform: 2560 -> 1936 wavefronts per CTA at 256
+        // points); the fold and store phases keep a line per lane
+        static_assert(G == 8 && L == 32 && (8 * LS2) % 16 == 8, "line order for 8 threads per line");
+        static_assert(swz_max(Gm::CS, RgSwz<T, N, 0>::C0 | RgSwz<T, N, 0>::C1) < LS2,
+                      "a swizzled slot stays inside its column line");
+        const int pl = ((l >> 1) & 7) + 8 * (l & 1) + 16 * (l >> 4);
+        rg_line_fft<T, N, 0>(S + (size_t)pl * LS2, g, l, tb);
+    } else {
+        rg_line_fft<T, N, AXIS>(S + (size_t)l * LS2, g, l, tb);
+    }
     __syncthreads();
 
     // ---- store phase: entry i of line l is component i&1 of slot sk(i>>1).
