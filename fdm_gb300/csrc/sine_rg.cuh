@@ -178,7 +178,7 @@ __device__ __forceinline__ int sk(int k) { return k + (k >> 4); }
 // belong to one warp; the phases inside need only warp synchronisation.
 // line: the line's index in the CTA (selects the swizzle of RgSwz; SWZ =
 // false keeps both private layouts plain).
-template <typename T, int N, int AXIS, bool SWZ = true>
+template <typename T, int N, int AXIS, bool SWZ = true, int OOFF = 0>
 __device__ __forceinline__ void rg_line_fft(vec2_t<T>* Ls, int g, int line, const SineTables<T>& tb) {
     using T2 = vec2_t<T>;
     using Gm = RgGeom<N, AXIS>;
@@ -274,6 +274,9 @@ __device__ __forceinline__ void rg_line_fft(vec2_t<T>* Ls, int g, int line, cons
     const T rm = __shfl_sync(0xffffffffu, rmid, 0, G);
     const T exa = inca - ta, exb = incb - tbk;
     const T bbase = s1 + rm + exb;
+    // an odd line's packed output starts OOFF slots later (0: plain)
+    const int mO = (line & 1) ? OOFF : 0;
+    static_assert(Gm::CS + OOFF <= Gm::LS2 || OOFF == 0, "the shifted output stays inside its line");
     __syncwarp();
 #pragma unroll
     for (int t = 0; t < E; t++) {
@@ -281,19 +284,19 @@ __device__ __forceinline__ void rg_line_fft(vec2_t<T>* Ls, int g, int line, cons
         T2 fa;
         fa.x = -ia[t];
         fa.y = exa + pa[t];
-        Ls[sk(k)] = fa;
+        Ls[sk(k) + mO] = fa;
         if (k > 0) {
             T2 fb;
             fb.x = -ib[t];
             fb.y = bbase + pb[t];
-            Ls[sk(M - k)] = fb;
+            Ls[sk(M - k) + mO] = fb;
         }
     }
     if (g == 0) {
         T2 fm;
         fm.x = -imid;
         fm.y = s1 + rmid;
-        Ls[sk(M / 2)] = fm;
+        Ls[sk(M / 2) + mO] = fm;
     }
 }
 
@@ -366,6 +369,12 @@ __device__ __forceinline__ void sine_rg_body(const Tin* in, Tout* out, const Sin
     // ---- load + fold: item (line, j) reads x_j and x_{N-j} and writes
     // y_j = w_j (a+b) + (a-b)/2 and y_{N-j} = w_j (a+b) - (a-b)/2
     constexpr bool kCol32 = AXIS == 1 && L == 32 && NT == 256 && MODE != kResidual;
+    // FP32 column transforms in the row-like line order (below), with the
+    // packed output of odd positions shifted by kColOut slots; not the
+    // 256-point combine pass (at its 48 registers the swizzles spill, and
+    // it measured 2 % slower)
+    constexpr bool kColRemap = kCol32 && sizeof(T) == 4 && !(MODE == kCombine && N == 256);
+    constexpr int kColOut = kColRemap ? (N == 256 ? 4 : 2) : 0;
     const int lane = tid & 31, wid = tid >> 5;
     if constexpr (kCol32) {
         // column pass with one line per lane: warp w takes the items j =
@@ -488,9 +497,7 @@ __device__ __forceinline__ void sine_rg_body(const Tin* in, Tout* out, const Sin
     }
     __syncthreads();
 
-    // (not the 256-point combine pass: at its 48 registers the swizzles
-    // spill, and it measured 2 % slower)
-    if constexpr (kCol32 && sizeof(T) == 4 && !(MODE == kCombine && N == 256)) {
+    if constexpr (kColRemap) {
         // the transform takes the lines in an order whose two lines per
         // half-warp sit 8 lines apart, 8 LS2 = 8 (mod 16) slots, as two
         // consecutive rows do, so the rows' slot swizzles apply (a bank
@@ -500,7 +507,8 @@ __device__ __forceinline__ void sine_rg_body(const Tin* in, Tout* out, const Sin
         static_assert(swz_max(Gm::CS, RgSwz<T, N, 0>::C0 | RgSwz<T, N, 0>::C1) < LS2,
                       "a swizzled slot stays inside its column line");
         const int pl = ((l >> 1) & 7) + 8 * (l & 1) + 16 * (l >> 4);
-        rg_line_fft<T, N, 0>(S + (size_t)pl * LS2, g, l, tb);
+        static_assert(Gm::CS + kColOut <= LS2, "the shifted output stays inside its column line");
+        rg_line_fft<T, N, 0, true, kColOut>(S + (size_t)pl * LS2, g, l, tb);
     } else {
         rg_line_fft<T, N, AXIS>(S + (size_t)l * LS2, g, l, tb);
     }
@@ -532,7 +540,9 @@ __device__ __forceinline__ void sine_rg_body(const Tin* in, Tout* out, const Sin
         // y = 2k-1 and 2k
         constexpr int QS = M / 8;
         const bool act = lane < nact;
-        const T2* src = S + lane * LS2 + wid;
+        // lines at odd transform positions (bit 3 of the line) hold their
+        // packed output kColOut slots later
+        const T2* src = S + lane * LS2 + wid + (kColRemap && (lane & 8) ? kColOut : 0);
         const long long s16 = 16LL * nx;
         const long long base = ((long long)z * ny + 2 * wid - 1) * nx + x0 + lane;  // row 2k-1 at q = 0
         if constexpr (MODE == kCombine) {
