@@ -80,7 +80,8 @@ struct RgGeom {
 // column passes of 128 and 256 points hand their lines to the transform in
 // an order that puts a half-warp's two lines 8 lines apart, and use the row
 // masks (y pass 0.61 -> 0.59 ms, FP64-rounding y pass 0.86 -> 0.82 ms per
-// 16 x 255^3 launch; 127^3 solves 3 % faster).
+// 16 x 255^3 launch; 127^3 solves 3 % faster), and shift the packed output
+// of odd positions (OOFF of rg_line_fft: y pass 0.59 -> 0.56 ms).
 template <typename T, int N, int AXIS>
 struct RgSwz {
     static constexpr int B0 = 0, B1 = 0, C0 = 0, C1 = 0;
